@@ -1,0 +1,299 @@
+"""Benchmark: grid-pt*steps/s of TARA's plain 2D vorticity solver, FP64, RK4.
+
+Workload (one "step" = one classic RK4 step = 4 RHS evaluations): Nx = Ny = 2048,
+2*pi box, nu = 1e-4, dt = 5e-5, seeded random-phase initial vorticity with
+E(k) ~ k^4 exp(-(k/6)^2) normalised to energy 0.5 (seed 20242048).  The working
+set (about 340 MB) is larger than L2, so no flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--n 2048]
+
+Our arm prints one JSON line with value (device-resident state, CUDA events on
+the solver stream), e2e (host buffers through tara2d_set_state / step /
+get_state, copies inside the timed region), the roofline of the dominant kernel,
+clocks sampled during the timed region and a CPU baseline (the oracle's C
+restatement on the host cores, a bounded sample).  ``--impl reference`` times
+the CPU restatement alone (the reference Fortran cannot be built on either
+machine: no Fortran compiler) with all host threads.
+
+Multi-GPU: the path does not shard (one grid is one FFT problem); N ranks run N
+independent replicas, value = all ranks' grid-pt*steps / max-over-ranks time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "grid-pt*steps/s at 2048^2 FP64 (plain 2D vorticity RHS + RK4)"
+UNIT = "grid-pt*steps/s"
+SEED = {512: 20240512, 2048: 20242048}
+NU, DT, K0, ENERGY = 1e-4, 5e-5, 6.0, 0.5
+
+
+def peaks() -> tuple[float, str]:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+        except Exception:
+            pass
+    return 6800.0, "fallback"
+
+
+def traffic_from_profiles(kernel: str, n: int) -> float | None:
+    """DRAM bytes per launch recorded from an ncu capture (profiles/*.txt line
+    'traffic_bytes_per_launch <kernel> <n> <bytes>'), or None."""
+    for f in sorted((ROOT / "profiles").glob("*.txt")):
+        for line in f.read_text().splitlines():
+            parts = line.split()
+            if len(parts) == 4 and parts[0] == "traffic_bytes_per_launch" and parts[1] == kernel \
+                    and parts[2] == str(n):
+                return float(parts[3])
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int = 0):
+        self.index = index
+        self.rows: list[list[str]] = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return self
+
+        def rd():
+            for line in self.proc.stdout:
+                self.rows.append([c.strip() for c in line.split(",")])
+
+        self.thread = threading.Thread(target=rd, daemon=True)
+        self.thread.start()
+        return self
+
+    def stop(self) -> dict:
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        if self.thread is not None:
+            self.thread.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except (ValueError, IndexError):
+                continue
+            for nm, v in zip(names, r[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(n: int, budget_s: float = 15.0, threads: int | None = None) -> dict:
+    """The oracle's C restatement (own FFT, OpenMP over rows/columns) on the
+    host cores: RK4 steps at n^2 until about budget_s of work."""
+    from oracle import oracle as orc
+
+    O = orc.load()
+    O.set_threads(threads or os.cpu_count() or 1)
+    w0 = O.ic_random(n, n, K0, ENERGY, SEED.get(n, 1))
+    steps, elapsed, w = 0, 0.0, w0
+    while elapsed < budget_s and steps < 1000:
+        t0 = time.perf_counter()
+        w, _ = O.run(w, rhs=0, scheme=1, nu=NU, dt=DT, steps=1)
+        elapsed += time.perf_counter() - t0
+        steps += 1
+    return {"value": n * n * steps / elapsed, "unit": UNIT, "cores": O.threads(), "kind": "port",
+            "sample": f"{steps} RK4 step(s) at {n}^2 in {elapsed:.2f} s (oracle C restatement, "
+                      f"own radix-2 FFT, {O.threads()} OpenMP threads)"}
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+
+        backend = "nccl"
+        dist.init_process_group(backend=backend)
+        return rank, ws, dist
+    return 0, 1, None
+
+
+def run_reference(args) -> None:
+    rank, ws, dist = 0, int(os.environ.get("WORLD_SIZE", "1")), None
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from oracle import oracle as orc
+
+    O = orc.load()
+    O.set_threads(os.cpu_count() or 1)
+    n = args.n
+    w = O.ic_random(n, n, K0, ENERGY, SEED.get(n, 1))
+    for _ in range(args.warmup):
+        w, _ = O.run(w, rhs=0, scheme=1, nu=NU, dt=DT, steps=1)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        w, _ = O.run(w, rhs=0, scheme=1, nu=NU, dt=DT, steps=1)
+    el = time.perf_counter() - t0
+    value = n * n * args.steps / el
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded random-phase spectrum)",
+        "config": {"workload": f"2D vorticity plain RHS, RK4, {n}^2, nu={NU}, dt={DT}",
+                   "note": "reference Fortran not buildable (no Fortran compiler); CPU restatement"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": O.threads(), "kind": "port",
+                         "sample": f"{args.steps} timed RK4 steps at {n}^2 after {args.warmup} warm-up"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args) -> None:
+    import numpy as np
+    import torch
+
+    import tara_gb300 as tg
+
+    rank, ws, dist = dist_init()
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    n = args.n
+    s = tg.Solver2D(n, scheme=tg.SCHEME_RK4, nu=NU, dt=DT)
+    s.init_random(K0, ENERGY, SEED.get(n, 1))
+    s.step(args.warmup)
+    s.synchronize()
+
+    # ---- device-resident timed region (CUDA events on the solver's stream)
+    sampler = ClockSampler(local).start() if rank == 0 else None
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    prof = s.step_timed(args.steps)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clocks = sampler.stop() if sampler else None
+    el_ms = prof["total_ms"]
+    if dist:
+        t = torch.tensor([el_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        el_ms = float(t.item())
+    e, z = s.diag()  # also raises on non-finite values
+
+    # ---- end to end through the public API with pinned host buffers
+    nh = n // 2 + 1
+    host_in = torch.empty((n, nh), dtype=torch.complex128, pin_memory=True).numpy()
+    host_out = torch.empty((n, nh), dtype=torch.complex128, pin_memory=True).numpy()
+    host_in[:] = s.get_state()
+    e2e_steps = max(1, min(args.steps, 10))
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        s.set_state(host_in)
+        s.step(1)
+        s.get_state_into(host_out)
+        host_in, host_out = host_out, host_in
+    torch.cuda.synchronize()
+    e2e_el = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([e2e_el], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_el = float(t.item())
+
+    if rank != 0:
+        s.close()
+        return
+
+    # ---- roofline of the dominant kernel (algorithmic bytes / event time)
+    F = 16.0 * nh * n  # one FP64 half spectrum
+    alg_bytes = {  # per launch: what each kernel must read and write at minimum
+        "k_col_inverse": 5 * F,   # read omega_hat, write 4 spectra
+        "k_row_nl": 5 * F,        # read 4 spectra, write the products' spectrum
+        "k_col_forward": 5 * F,   # RK4 stages average (4F, 6F, 6F, 4F + 1F) ~ 5F
+    }
+    ks = prof["kernels"]
+    dom = max(ks, key=lambda k: ks[k]["ms"])
+    avg_ms = ks[dom]["ms"] / max(1, ks[dom]["launches"])
+    peak, peak_kind = peaks()
+    achieved = alg_bytes[dom] / (avg_ms * 1e-3) / 1e9
+    traffic = traffic_from_profiles(dom, n)
+    value = n * n * args.steps * ws / (el_ms * 1e-3)
+    cpu = cpu_baseline(n, budget_s=args.cpu_budget) if not args.no_cpu_baseline else None
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": el_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded random-phase spectrum, Philox4x32-10)",
+        "config": {"workload": f"2D vorticity plain RHS (derive2csh), classic RK4, {n}x{n}, "
+                               f"2pi box, nu={NU}, dt={DT}, k0={K0}, E=0.5, seed {SEED.get(n, 1)}",
+                   "l2": "working set > L2 (no flush)", "parallelism": f"replicas x{ws}"},
+        "e2e": {"value": n * n * e2e_steps * ws / e2e_el, "unit": UNIT,
+                "h2d_bytes_per_step": int(F), "d2h_bytes_per_step": int(F),
+                "path": "tara2d_set_state(pinned host) + tara2d_step(1) + tara2d_get_state"},
+        "gpu_launches": s.launches_per_step * args.steps,
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
+                     "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": traffic, "avg_launch_ms": avg_ms,
+                     "per_kernel_ms": {k: v["ms"] / max(1, v["launches"]) for k, v in ks.items()}},
+        "clocks": clocks,
+        "diag": {"energy": e, "enstrophy": z},
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+    s.close()
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=2048)
+    ap.add_argument("--cpu-budget", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

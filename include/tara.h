@@ -1,0 +1,169 @@
+/* tara.h -- C ABI of libtara, the GB300 (sm_103a) implementation of TARA's 2D
+ * pseudo-spectral right-hand side and explicit time steppers.
+ *
+ * Two layers:
+ *
+ * 1. Drop-in replacements for the reference's Fortran subroutines.  The
+ *    reference declares them as external subroutines with implicit interfaces,
+ *    so gfortran passes every argument by reference and mangles the names to
+ *    lowercase plus one trailing underscore.  Linking libtara.so in place of the
+ *    reference's derive2csh.o / ab2csh.o / derive2css.o / ab2css.o / rk42css.o
+ *    substitutes them without touching the caller.  Arrays are the caller's
+ *    host arrays in Fortran layout: complex(8) a(Nh,Ny) is Nh*Ny interleaved
+ *    (re,im) doubles with the kx index fastest, Nh = Nx/2+1.  Each call copies
+ *    its inputs to the GPU, runs there and copies its outputs back; only the
+ *    outputs the reference writes are written.  The subroutines return nothing
+ *    (as in the reference); a failure is recorded and read back with
+ *    tara_last_error().
+ *
+ * 2. A device-resident solver (tara2d_*) that keeps the state in HBM and runs
+ *    many steps per call, plus batched ensembles (tara_ens_*).  These return an
+ *    int status (TARA_OK = 0).
+ *
+ * Grid sizes: Nx and Ny powers of two from 16 to 2048.
+ */
+#ifndef TARA_H
+#define TARA_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------- */
+#define TARA_OK 0
+#define TARA_ERR_ARGS 1       /* bad sizes, null pointers, unsupported config   */
+#define TARA_ERR_CUDA 2       /* a CUDA runtime call failed                      */
+#define TARA_ERR_NONFINITE 3  /* NaN/Inf found by the energy/enstrophy reduction */
+#define TARA_ERR_NOMEM 4      /* device allocation failed                        */
+#define TARA_ERR_TIMEOUT 5    /* a bounded device-side wait gave up              */
+#define TARA_ERR_INI 6        /* input.ini missing, malformed or missing a key    */
+
+/* Last status recorded on the calling thread by any entry point, and its message. */
+int tara_last_error(void);
+const char* tara_last_error_message(void);
+void tara_clear_error(void);
+
+/* ---- 1. Fortran drop-ins (gfortran mangling) ----------------------------- */
+
+/* Replaces subroutine derive2csh (src/derive2csh.f95:3).  Plain vorticity RHS:
+ * writes dt_omegak_new = -(dealiased u.grad(omega) + nu k^2 omegak).  Reads
+ * omegak; time, omegak_new and dt_omegak_old are unused, as in the reference.
+ * Wavenumbers are the reference's: kx = 2*pi*(i-1)/Lx with pi = 3.1428 (real*4)
+ * and Lx = Ly = 2*pi, i.e. integers. */
+void derive2csh_(const int* Nx, const int* Ny, const int* Nh, const double* nu,
+                 const double* time, double* omegak, double* omegak_new,
+                 double* dt_omegak_old, double* dt_omegak_new);
+
+/* Replaces subroutine ab2csh (src/ab2csh.f95:3):
+ * omegak_new = omegak + (3/2 dt_omegak_new - 1/2 dt_omegak_old) dt. */
+void ab2csh_(const int* Nx, const int* Ny, const int* Nh, const double* nu, const double* time,
+             const double* dt, double* omegak, double* omegak_new, double* dt_omegak_old,
+             double* dt_omegak_new);
+
+/* Replaces subroutine derive2css (src/derive2css.f95:6).  Screened RHS with
+ * psi = omega/(k^2+lambda), derivatives of k^2 psi, NL = alpha(...) + nu k^2 (k^2 psi).
+ * The reference reads Lx, Ly and lambda from uninitialised locals; here they come
+ * from tara_set_css_params (defaults Lx = Ly = 2*3.1428, lambda = 10). */
+void derive2css_(const int* Nx, const int* Ny, const int* Nh, const double* alpha,
+                 const double* nu, const double* time, double* omegak, double* omegak_new,
+                 double* dt_omegak_old, double* dt_omegak_new);
+
+/* Replaces subroutine ab2css (src/ab2css.f95:6); same update as ab2csh_. */
+void ab2css_(const int* Nx, const int* Ny, const int* Nh, const double* alpha, const double* nu,
+             const double* time, const double* dt, double* omegak, double* omegak_new,
+             double* dt_omegak_old, double* dt_omegak_new);
+
+/* Replaces subroutine rk42css (src/rk42css.f95:6) with a working classic RK4 over
+ * the derive2css RHS: writes omegak_new; dt_omegak_old and dt_omegak_new are
+ * unused.  (The reference body reads an uninitialised local and does not
+ * integrate anything.) */
+void rk42css_(const int* Nx, const int* Ny, const int* Nh, const double* alpha, const double* nu,
+              const double* time, const double* dt, double* omegak, double* omegak_new,
+              double* dt_omegak_old, double* dt_omegak_new);
+
+/* Box lengths (true lengths, e.g. 2*pi*Lx_ini) and screening used by
+ * derive2css_ / rk42css_.  The reference driver sets lambda = 10
+ * (src/main2css.f95:87). */
+void tara_set_css_params(double lx, double ly, double lambda);
+
+/* ---- 2. Device-resident solver ------------------------------------------- */
+
+#define TARA_RHS_PLAIN 0   /* derive2csh */
+#define TARA_RHS_SCREEN 1  /* derive2css (defined mode) */
+#define TARA_SCHEME_AB2 0
+#define TARA_SCHEME_RK4 1
+#define TARA_PREC_FP64 0   /* FFTs, products and state in FP64 */
+#define TARA_PREC_FP32 1   /* FP32 FFTs and products; FP64 state and reductions */
+
+typedef struct tara2d_config {
+  int nx, ny;      /* powers of two, 16..2048 */
+  int rhs;         /* TARA_RHS_* */
+  int scheme;      /* TARA_SCHEME_* */
+  int precision;   /* TARA_PREC_* */
+  double nu;       /* viscosity */
+  double dt;       /* time step */
+  double alpha;    /* screened RHS: coefficient of the nonlinear term */
+  double lambda;   /* screened RHS: screening */
+  double lx, ly;   /* box lengths used in kx = 2*kpi*(i-1)/lx */
+  double kpi;      /* the pi in that formula: 3.1428f for the reference's RHS */
+} tara2d_config;
+
+/* Fills cfg with the reference plain RHS defaults (pi = 3.1428f, Lx = Ly = 2*pi,
+ * AB2, FP64). */
+void tara2d_default_config(tara2d_config* cfg, int nx, int ny);
+
+typedef struct tara2d tara2d;
+
+int tara2d_create(const tara2d_config* cfg, tara2d** out);
+int tara2d_destroy(tara2d* h);
+/* Host half spectra in Fortran layout (Nh*Ny complex).  dt_old may be NULL
+ * (the AB2 history is then zero, as the reference's fresh allocation reads). */
+int tara2d_set_state(tara2d* h, const double* omegak, const double* dt_old);
+int tara2d_get_state(tara2d* h, double* omegak, double* dt_old);
+/* Device pointers (dense Nh*Ny complex) on the handle's device. */
+int tara2d_set_state_device(tara2d* h, const void* omegak_dev, const void* dt_old_dev);
+int tara2d_get_state_device(tara2d* h, void* omegak_dev);
+/* Advance nsteps steps on the handle's stream (asynchronous). */
+int tara2d_step(tara2d* h, int nsteps);
+/* As tara2d_step, with a CUDA event recorded on the handle's stream after every
+ * launch; waits for completion and returns, per kernel kind (0 column inverse
+ * pass, 1 row pass, 2 column forward + update pass), the summed milliseconds
+ * and launch counts, and the total milliseconds of the nsteps steps. */
+int tara2d_step_timed(tara2d* h, int nsteps, double* kernel_ms, int* kernel_launches,
+                      double* total_ms);
+/* One RHS evaluation of the current state into a host array (dense Nh*Ny complex). */
+int tara2d_rhs(tara2d* h, double* dt_omegak);
+/* 1/2<|u|^2> and 1/2<omega^2> of the current state in the box (lx, ly) of the
+ * config, from the spectrum by Parseval; TARA_ERR_NONFINITE when NaN/Inf. */
+int tara2d_diag(tara2d* h, double* energy, double* enstrophy);
+int tara2d_synchronize(tara2d* h);
+/* The handle's CUDA stream (cudaStream_t) for callers that order work around it. */
+void* tara2d_stream(tara2d* h);
+/* Number of kernel launches a single step issues (for launch accounting). */
+int tara2d_launches_per_step(const tara2d* h);
+
+/* Seeded random-phase initial spectrum (Philox4x32-10, E(k) ~ k^4 exp(-(k/k0)^2),
+ * Hermitian-projected on the GPU by a c2r/r2c round trip, mean mode zeroed,
+ * rescaled to 1/2<|u|^2> = energy with the handle's wavenumbers). */
+int tara2d_init_random(tara2d* h, double k0, double energy, uint64_t seed);
+
+/* ---- standalone transforms ------------------------------------------------ */
+/* Unnormalised 2D transforms with FFTW's rank-2 r2c/c2r semantics, i.e. what
+ * dfftw_plan_dft_{r2c,c2r}_2d(plan, Nx, Ny, ...) computes in the reference
+ * (src/derive2csh.f95:73-106, lib/fftw/api/f77funcs.h:206-209,300-303): c2r runs
+ * complex DFTs along y and then a 1D c2r along x that reads only the real parts
+ * of the kx = 0 and kx = Nx/2 bins.  Host arrays: real (Nx,Ny) x-fastest,
+ * complex (Nh,Ny) interleaved.  precision TARA_PREC_FP64 or TARA_PREC_FP32 (the
+ * transform arithmetic; inputs and outputs stay double). */
+int tara_fft2d_r2c(int nx, int ny, int precision, const double* in, double* out);
+int tara_fft2d_c2r(int nx, int ny, int precision, const double* in, double* out);
+
+/* Library version string. */
+const char* tara_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,164 @@
+"""ctypes binding of the CPU oracle -- TEST INFRASTRUCTURE ONLY.
+
+Only tests/, ``__graft_entry__.smoke()`` and the CPU-baseline leg of bench.py
+import this module, and only as the checker.  ``load()`` returns the own-FFT
+restatement (liboracle.so, builds anywhere); ``load(fftw=True)`` returns the
+same restatement over FFTW 3.3.9 compiled from the reference's vendored sources
+(oracle/_ref/liboracle_fftw.so), which exists only where the reference tree was
+available at build time.
+"""
+from __future__ import annotations
+
+import ctypes
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+PORT = HERE / "liboracle.so"
+REF = HERE / "_ref" / "liboracle_fftw.so"
+PI_R4 = float(np.float32(3.1428))
+PI_R8 = 3.14159265358979323846
+
+_cache: dict = {}
+
+
+def available(fftw: bool = False) -> bool:
+    return (REF if fftw else PORT).exists()
+
+
+def load(fftw: bool = False) -> "Oracle":
+    key = bool(fftw)
+    if key not in _cache:
+        path = REF if fftw else PORT
+        if not path.exists():
+            raise FileNotFoundError(f"{path} missing (make -C oracle {'ref' if fftw else 'port'})")
+        _cache[key] = Oracle(ctypes.CDLL(str(path)))
+    return _cache[key]
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _i(v):
+    return ctypes.byref(ctypes.c_int(int(v)))
+
+
+def _d(v):
+    return ctypes.byref(ctypes.c_double(float(v)))
+
+
+class Oracle:
+    def __init__(self, L):
+        self.L = L
+        c_int, c_double, vp = ctypes.c_int, ctypes.c_double, ctypes.c_void_p
+        L.oracle_run.argtypes = [c_int, c_int, c_int, c_int, c_double, c_double, c_double, c_int,
+                                 vp, vp]
+        L.oracle_ic_shear.argtypes = [c_int, c_int, c_double, c_double, c_double, c_double,
+                                      c_double, c_int, vp]
+        L.oracle_ic_random.argtypes = [c_int, c_int, c_double, c_double, ctypes.c_uint64, vp]
+        L.oracle_energy_enstrophy.argtypes = [c_int, c_int, c_double, c_double, vp, vp]
+        L.oracle_diag_css.argtypes = [c_int, c_int, c_double, c_double, c_double, vp, vp]
+        L.oracle_set_css_params.argtypes = [c_double, c_double, c_double]
+        L.oracle_r2c_2d.argtypes = [c_int, c_int, vp, vp]
+        L.oracle_c2r_2d.argtypes = [c_int, c_int, vp, vp]
+        L.oracle_set_threads.argtypes = [c_int]
+        self.is_fftw = bool(L.oracle_backend_is_fftw())
+
+    def set_threads(self, n: int) -> None:
+        self.L.oracle_set_threads(int(n))
+
+    def threads(self) -> int:
+        return int(self.L.oracle_get_threads())
+
+    # transforms (unnormalised, FFTW semantics)
+    def r2c(self, x):
+        x = np.ascontiguousarray(x, np.float64)
+        ny, nx = x.shape
+        out = np.zeros((ny, nx // 2 + 1), np.complex128)
+        self.L.oracle_r2c_2d(nx, ny, x.ctypes.data, out.ctypes.data)
+        return out
+
+    def c2r(self, c):
+        c = np.ascontiguousarray(c, np.complex128)
+        ny, nh = c.shape
+        nx = 2 * (nh - 1)
+        out = np.zeros((ny, nx), np.float64)
+        self.L.oracle_c2r_2d(nx, ny, c.ctypes.data, out.ctypes.data)
+        return out
+
+    # reference subroutines
+    def derive2csh(self, w, nu):
+        w = np.ascontiguousarray(w, np.complex128).copy()
+        ny, nh = w.shape
+        out = np.zeros_like(w)
+        self.L.oracle_derive2csh(_i(2 * (nh - 1)), _i(ny), _i(nh), _d(nu), _d(0.0),
+                                 _dp(w.view(np.float64)), None, None, _dp(out.view(np.float64)))
+        return out
+
+    def derive2css(self, w, alpha, nu):
+        w = np.ascontiguousarray(w, np.complex128).copy()
+        ny, nh = w.shape
+        out = np.zeros_like(w)
+        self.L.oracle_derive2css(_i(2 * (nh - 1)), _i(ny), _i(nh), _d(alpha), _d(nu), _d(0.0),
+                                 _dp(w.view(np.float64)), None, None, _dp(out.view(np.float64)))
+        return out
+
+    def ab2(self, w, fo, fn, dt):
+        w, fo, fn = (np.ascontiguousarray(a, np.complex128) for a in (w, fo, fn))
+        ny, nh = w.shape
+        out = np.zeros_like(w)
+        self.L.oracle_ab2csh(_i(2 * (nh - 1)), _i(ny), _i(nh), _d(0.0), _d(0.0), _d(dt),
+                             _dp(w.view(np.float64)), _dp(out.view(np.float64)),
+                             _dp(fo.view(np.float64)), _dp(fn.view(np.float64)))
+        return out
+
+    def rk42css(self, w, alpha, nu, dt):
+        w = np.ascontiguousarray(w, np.complex128).copy()
+        ny, nh = w.shape
+        out = np.zeros_like(w)
+        self.L.oracle_rk42css(_i(2 * (nh - 1)), _i(ny), _i(nh), _d(alpha), _d(nu), _d(0.0), _d(dt),
+                              _dp(w.view(np.float64)), _dp(out.view(np.float64)), None, None)
+        return out
+
+    def set_css_params(self, lx, ly, lam):
+        self.L.oracle_set_css_params(lx, ly, lam)
+
+    def run(self, w, *, rhs=0, scheme=0, alpha=1.0, nu=0.01, dt=1e-4, steps=1, dt_old=None):
+        w = np.ascontiguousarray(w, np.complex128).copy()
+        fo = np.zeros_like(w) if dt_old is None else np.ascontiguousarray(dt_old, np.complex128).copy()
+        ny, nh = w.shape
+        self.L.oracle_run(2 * (nh - 1), ny, rhs, scheme, alpha, nu, dt, int(steps), w.ctypes.data,
+                          fo.ctypes.data)
+        return w, fo
+
+    # initial conditions and diagnostics
+    def ic_shear(self, nx, ny, lx_ini=2.0, ly_ini=2.0, w0=25.0, m0=2.0, d_ini=0.0234375, variant=0):
+        out = np.zeros((ny, nx), np.float64)
+        self.L.oracle_ic_shear(nx, ny, lx_ini, ly_ini, w0, m0, d_ini, variant, out.ctypes.data)
+        return out
+
+    def ic_random(self, nx, ny, k0, energy, seed):
+        out = np.zeros((ny, nx // 2 + 1), np.complex128)
+        self.L.oracle_ic_random(nx, ny, k0, energy, seed, out.ctypes.data)
+        return out
+
+    def energy_enstrophy(self, w, lx=2 * PI_R8, ly=2 * PI_R8):
+        w = np.ascontiguousarray(w, np.complex128)
+        ny, nh = w.shape
+        out = np.zeros(2)
+        self.L.oracle_energy_enstrophy(2 * (nh - 1), ny, lx, ly, w.ctypes.data, out.ctypes.data)
+        return float(out[0]), float(out[1])
+
+    def diag_css(self, w, lx, ly, lam=10.0):
+        w = np.ascontiguousarray(w, np.complex128)
+        ny, nh = w.shape
+        out = np.zeros(6)
+        self.L.oracle_diag_css(2 * (nh - 1), ny, lx, ly, lam, w.ctypes.data, out.ctypes.data)
+        return out
+
+    def philox(self, ctr, key):
+        out = (ctypes.c_uint32 * 4)()
+        self.L.oracle_philox4x32_10((ctypes.c_uint32 * 4)(*ctr), (ctypes.c_uint32 * 2)(*key), out)
+        return [int(v) for v in out]

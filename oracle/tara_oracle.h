@@ -1,0 +1,98 @@
+/* CPU oracle for the TARA 2D pseudo-spectral path -- TEST INFRASTRUCTURE ONLY.
+ *
+ * A plain-C restatement of the reference subroutines on the hot path, used by
+ * the test suite, smoke() and the bench's CPU-baseline leg as the checker.  It
+ * is never linked into the product library.
+ *
+ * Arrays follow the reference's Fortran layout: a half spectrum complex(8)
+ * omegak(Nh,Ny) is Nh*Ny interleaved (re,im) doubles with the kx index fastest;
+ * a real field omega(Nx,Ny) is Nx*Ny doubles with x fastest.
+ *
+ * Two FFT backends share this source: the default build uses the oracle's own
+ * radix-2 FFT (builds anywhere); -DORACLE_USE_FFTW routes every transform
+ * through FFTW 3.3.9 compiled from the reference's vendored sources, planned
+ * with FFTW_ESTIMATE before each transform exactly as the reference does
+ * (src/derive2csh.f95:73-106).  The FFTW build pins the own-FFT build and makes
+ * the golden vectors.
+ */
+#ifndef TARA_ORACLE_H
+#define TARA_ORACLE_H
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* 1 when this build routes transforms through FFTW, 0 for the own FFT */
+int oracle_backend_is_fftw(void);
+/* OpenMP threads used by the own-FFT backend (<=0: all available) */
+void oracle_set_threads(int n);
+int oracle_get_threads(void);
+
+/* Unnormalised 2D transforms with FFTW's r2c/c2r semantics
+ * (dfftw_plan_dft_{r2c,c2r}_2d with Fortran dims (Nx,Ny), see
+ * lib/fftw/api/f77funcs.h:206-209,300-303).  c2r leaves `in` untouched. */
+void oracle_r2c_2d(int nx, int ny, const double* in, double* out);
+void oracle_c2r_2d(int nx, int ny, const double* in, double* out);
+
+/* src/derive2csh.f95:3-149 (plain RHS, faithful: pi=3.1428 real*4, Lx=Ly=2*pi) */
+void oracle_derive2csh(const int* Nx, const int* Ny, const int* Nh, const double* nu,
+                       const double* time, double* omegak, double* omegak_new,
+                       double* dt_omegak_old, double* dt_omegak_new);
+/* src/ab2csh.f95:3-16 */
+void oracle_ab2csh(const int* Nx, const int* Ny, const int* Nh, const double* nu,
+                   const double* time, const double* dt, double* omegak, double* omegak_new,
+                   double* dt_omegak_old, double* dt_omegak_new);
+/* src/derive2css.f95:6-136 in defined mode: Lx, Ly, lambda come from
+ * oracle_set_css_params (defaults 2*3.1428f, 2*3.1428f, 10) */
+void oracle_set_css_params(double lx, double ly, double lambda);
+void oracle_derive2css(const int* Nx, const int* Ny, const int* Nh, const double* alpha,
+                       const double* nu, const double* time, double* omegak, double* omegak_new,
+                       double* dt_omegak_old, double* dt_omegak_new);
+/* src/ab2css.f95:6-22 */
+void oracle_ab2css(const int* Nx, const int* Ny, const int* Nh, const double* alpha,
+                   const double* nu, const double* time, const double* dt, double* omegak,
+                   double* omegak_new, double* dt_omegak_old, double* dt_omegak_new);
+/* Classic RK4 with the signature of src/rk42css.f95:6-13 (the reference body is
+ * non-functional); rhs_kind 0 = derive2csh, 1 = derive2css. */
+void oracle_rk42css(const int* Nx, const int* Ny, const int* Nh, const double* alpha,
+                    const double* nu, const double* time, const double* dt, double* omegak,
+                    double* omegak_new, double* dt_omegak_old, double* dt_omegak_new);
+void oracle_rk4csh(const int* Nx, const int* Ny, const int* Nh, const double* nu,
+                   const double* time, const double* dt, double* omegak, double* omegak_new);
+
+/* Step driver: nsteps of scheme (0 AB2 with the driver's history rotation,
+ * src/main2csh.f95:114-126; 1 classic RK4) over rhs_kind (0 plain, 1 screened).
+ * omegak is updated in place; dt_old holds the AB2 history (zero before the
+ * first step, as the reference's fresh allocation reads). */
+void oracle_run(int nx, int ny, int rhs_kind, int scheme, double alpha, double nu, double dt,
+                int nsteps, double* omegak, double* dt_old);
+
+/* Double-shear-layer initial vorticity in real space (src/main2css.f95:78-104 when
+ * variant 0, src/main2csh.f95:84-106 when variant 1). */
+void oracle_ic_shear(int nx, int ny, double lx_ini, double ly_ini, double w0, double m0,
+                     double d_ini, int variant, double* omega);
+
+/* Philox4x32-10 (Salmon et al., SC'11), one block. */
+void oracle_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+
+/* Seeded random-phase initial spectrum: |w(k)| = sqrt(|k| E(|k|)/pi),
+ * E(k) = k^4 exp(-(k/k0)^2), phase 2*pi*u with u from Philox (counter (i,j,0,0),
+ * key (seed lo, seed hi)), Hermitian-projected by a c2r/r2c round trip and
+ * mean mode set to zero, rescaled to 1/2<|u|^2> = energy.  Box Lx=Ly=2*pi. */
+void oracle_ic_random(int nx, int ny, double k0, double energy, uint64_t seed, double* omegak);
+
+/* Physical-space diagnostics of a half spectrum for a box (lx, ly) (true lengths):
+ * out[0] = 1/2<|u|^2>, out[1] = 1/2<omega^2>; velocity from psi = omega/k^2. */
+void oracle_energy_enstrophy(int nx, int ny, double lx, double ly, const double* omegak,
+                             double* out);
+
+/* Reference diagnostic of the screened driver (src/main2css.f95:206-275):
+ * out[0] = Energy = sum(ux^2+uy^2), out[1] = sum(uy^2), out[2..5] = C0..C3, with
+ * lambda applied to ky >= 0 rows only, as the reference does. */
+void oracle_diag_css(int nx, int ny, double lx, double ly, double lambda, const double* omegak,
+                     double* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,320 @@
+"""tara_gb300: GB300-native pseudo-spectral RHS and time steppers of TARA.
+
+This module is a thin ctypes binding of ``libtara.so`` (the C ABI in
+``include/tara.h``).  All compute runs in the library's CUDA kernels; there is
+no Python or CPU fallback: importing the module without the built library, or
+calling it without a GPU, raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from pathlib import Path
+
+import numpy as np
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "libtara.so"
+
+TARA_OK = 0
+TARA_ERR_ARGS = 1
+TARA_ERR_CUDA = 2
+TARA_ERR_NONFINITE = 3
+TARA_ERR_NOMEM = 4
+TARA_ERR_TIMEOUT = 5
+TARA_ERR_INI = 6
+
+RHS_PLAIN, RHS_SCREEN = 0, 1
+SCHEME_AB2, SCHEME_RK4 = 0, 1
+PREC_FP64, PREC_FP32 = 0, 1
+
+PI_R4 = float(np.float32(3.1428))  # real(8), parameter :: pi = 3.1428 (default-real literal)
+
+
+class TaraError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"tara error {code}: {msg}")
+        self.code = code
+
+
+class Config2D(ctypes.Structure):
+    _fields_ = [
+        ("nx", ctypes.c_int), ("ny", ctypes.c_int), ("rhs", ctypes.c_int),
+        ("scheme", ctypes.c_int), ("precision", ctypes.c_int),
+        ("nu", ctypes.c_double), ("dt", ctypes.c_double), ("alpha", ctypes.c_double),
+        ("lam", ctypes.c_double), ("lx", ctypes.c_double), ("ly", ctypes.c_double),
+        ("kpi", ctypes.c_double),
+    ]
+
+
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    """Load libtara.so (built in-tree by ``__graft_entry__.build()``)."""
+    global _lib
+    if _lib is None:
+        path = Path(os.environ.get("TARA_LIB", LIB_PATH))
+        if not path.exists():
+            raise ImportError(f"{path} is missing: build it with __graft_entry__.build()")
+        L = ctypes.CDLL(str(path))
+        _declare(L)
+        _lib = L
+    return _lib
+
+
+def _declare(L: ctypes.CDLL) -> None:
+    ip, dp, vp = ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double), ctypes.c_void_p
+    c_int, c_double = ctypes.c_int, ctypes.c_double
+    L.tara_last_error.restype = c_int
+    L.tara_last_error_message.restype = ctypes.c_char_p
+    L.tara_version.restype = ctypes.c_char_p
+    for name in ("derive2csh_",):
+        getattr(L, name).argtypes = [ip, ip, ip, dp, dp, dp, dp, dp, dp]
+    L.ab2csh_.argtypes = [ip, ip, ip, dp, dp, dp, dp, dp, dp, dp]
+    L.derive2css_.argtypes = [ip, ip, ip, dp, dp, dp, dp, dp, dp, dp]
+    L.ab2css_.argtypes = [ip, ip, ip, dp, dp, dp, dp, dp, dp, dp, dp]
+    L.rk42css_.argtypes = [ip, ip, ip, dp, dp, dp, dp, dp, dp, dp, dp]
+    for name in ("derive2csh_", "ab2csh_", "derive2css_", "ab2css_", "rk42css_"):
+        getattr(L, name).restype = None
+    L.tara_set_css_params.argtypes = [c_double, c_double, c_double]
+    L.tara_set_css_params.restype = None
+    cfgp = ctypes.POINTER(Config2D)
+    L.tara2d_default_config.argtypes = [cfgp, c_int, c_int]
+    L.tara2d_default_config.restype = None
+    L.tara2d_create.argtypes = [cfgp, ctypes.POINTER(vp)]
+    L.tara2d_destroy.argtypes = [vp]
+    L.tara2d_set_state.argtypes = [vp, dp, dp]
+    L.tara2d_get_state.argtypes = [vp, dp, dp]
+    L.tara2d_set_state_device.argtypes = [vp, vp, vp]
+    L.tara2d_get_state_device.argtypes = [vp, vp]
+    L.tara2d_step.argtypes = [vp, c_int]
+    L.tara2d_step_timed.argtypes = [vp, c_int, dp, ip, dp]
+    L.tara2d_rhs.argtypes = [vp, dp]
+    L.tara2d_diag.argtypes = [vp, dp, dp]
+    L.tara2d_synchronize.argtypes = [vp]
+    L.tara2d_stream.argtypes = [vp]
+    L.tara2d_stream.restype = vp
+    L.tara2d_launches_per_step.argtypes = [vp]
+    L.tara2d_init_random.argtypes = [vp, c_double, c_double, ctypes.c_uint64]
+    L.tara_fft2d_r2c.argtypes = [c_int, c_int, c_int, dp, dp]
+    L.tara_fft2d_c2r.argtypes = [c_int, c_int, c_int, dp, dp]
+
+
+def _check(rc: int) -> None:
+    if rc != TARA_OK:
+        raise TaraError(rc, lib().tara_last_error_message().decode())
+
+
+def last_error() -> tuple[int, str]:
+    L = lib()
+    return L.tara_last_error(), L.tara_last_error_message().decode()
+
+
+def _dp(a: np.ndarray):
+    assert a.flags.c_contiguous
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _as_spectrum(a: np.ndarray, nh: int, ny: int) -> np.ndarray:
+    a = np.ascontiguousarray(a, dtype=np.complex128)
+    if a.shape != (ny, nh):
+        raise ValueError(f"expected a ({ny}, {nh}) half spectrum, got {a.shape}")
+    return a
+
+
+# ---------------------------------------------------------------------------
+# Fortran drop-ins, called exactly as the reference's callers call them
+# ---------------------------------------------------------------------------
+def _ints(*v):
+    return [ctypes.byref(ctypes.c_int(int(x))) for x in v]
+
+
+def _dbls(*v):
+    return [ctypes.byref(ctypes.c_double(float(x))) for x in v]
+
+
+def derive2csh(omegak: np.ndarray, nu: float, time: float = 0.0) -> np.ndarray:
+    """subroutine derive2csh (src/derive2csh.f95:3): returns dt_omegak_new.
+    ``omegak`` is (Ny, Nh) complex: row ky, column kx (Fortran omegak(Nh,Ny))."""
+    ny, nh = omegak.shape
+    nx = 2 * (nh - 1)
+    w = _as_spectrum(omegak, nh, ny).copy()
+    out = np.zeros_like(w)
+    dummy = np.zeros_like(w)
+    lib().derive2csh_(*_ints(nx, ny, nh), *_dbls(nu, time), _dp(w.view(np.float64)),
+                      _dp(dummy.view(np.float64)), _dp(dummy.view(np.float64)),
+                      _dp(out.view(np.float64)))
+    _check(lib().tara_last_error())
+    return out
+
+
+def derive2css(omegak: np.ndarray, alpha: float, nu: float, time: float = 0.0) -> np.ndarray:
+    """subroutine derive2css (src/derive2css.f95:6), defined mode."""
+    ny, nh = omegak.shape
+    nx = 2 * (nh - 1)
+    w = _as_spectrum(omegak, nh, ny).copy()
+    out = np.zeros_like(w)
+    dummy = np.zeros_like(w)
+    lib().derive2css_(*_ints(nx, ny, nh), *_dbls(alpha, nu, time), _dp(w.view(np.float64)),
+                      _dp(dummy.view(np.float64)), _dp(dummy.view(np.float64)),
+                      _dp(out.view(np.float64)))
+    _check(lib().tara_last_error())
+    return out
+
+
+def ab2csh(omegak, dt_omegak_old, dt_omegak_new, dt: float, nu: float = 0.0, time: float = 0.0):
+    """subroutine ab2csh (src/ab2csh.f95:3): returns omegak_new."""
+    ny, nh = omegak.shape
+    nx = 2 * (nh - 1)
+    w = _as_spectrum(omegak, nh, ny)
+    fo = _as_spectrum(dt_omegak_old, nh, ny)
+    fn = _as_spectrum(dt_omegak_new, nh, ny)
+    out = np.zeros_like(w)
+    lib().ab2csh_(*_ints(nx, ny, nh), *_dbls(nu, time, dt), _dp(w.view(np.float64)),
+                  _dp(out.view(np.float64)), _dp(fo.view(np.float64)), _dp(fn.view(np.float64)))
+    _check(lib().tara_last_error())
+    return out
+
+
+def rk42css(omegak, alpha: float, nu: float, dt: float, time: float = 0.0):
+    """subroutine rk42css (src/rk42css.f95:6) as a working classic RK4 step."""
+    ny, nh = omegak.shape
+    nx = 2 * (nh - 1)
+    w = _as_spectrum(omegak, nh, ny).copy()
+    out = np.zeros_like(w)
+    dummy = np.zeros_like(w)
+    lib().rk42css_(*_ints(nx, ny, nh), *_dbls(alpha, nu, time, dt), _dp(w.view(np.float64)),
+                   _dp(out.view(np.float64)), _dp(dummy.view(np.float64)),
+                   _dp(dummy.view(np.float64)))
+    _check(lib().tara_last_error())
+    return out
+
+
+def set_css_params(lx: float, ly: float, lam: float) -> None:
+    lib().tara_set_css_params(lx, ly, lam)
+
+
+def fft2d_r2c(x: np.ndarray, precision: int = PREC_FP64) -> np.ndarray:
+    """Unnormalised r2c of a real (Ny, Nx) field -> (Ny, Nh) complex (FFTW semantics)."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    ny, nx = x.shape
+    out = np.zeros((ny, nx // 2 + 1), np.complex128)
+    _check(lib().tara_fft2d_r2c(nx, ny, precision, _dp(x), _dp(out.view(np.float64))))
+    return out
+
+
+def fft2d_c2r(c: np.ndarray, precision: int = PREC_FP64) -> np.ndarray:
+    """Unnormalised c2r of a (Ny, Nh) half spectrum -> real (Ny, Nx) (FFTW semantics)."""
+    c = np.ascontiguousarray(c, dtype=np.complex128)
+    ny, nh = c.shape
+    nx = 2 * (nh - 1)
+    out = np.zeros((ny, nx), np.float64)
+    _check(lib().tara_fft2d_c2r(nx, ny, precision, _dp(c.view(np.float64)), _dp(out)))
+    return out
+
+
+# ---------------------------------------------------------------------------
+# Device-resident solver
+# ---------------------------------------------------------------------------
+class Solver2D:
+    """Owns a tara2d handle: state in HBM, steps on the library's CUDA stream."""
+
+    def __init__(self, nx: int, ny: int | None = None, *, rhs: int = RHS_PLAIN,
+                 scheme: int = SCHEME_AB2, precision: int = PREC_FP64, nu: float = 0.01,
+                 dt: float = 1e-4, alpha: float = 1.0, lam: float = 10.0,
+                 lx: float | None = None, ly: float | None = None, kpi: float = PI_R4):
+        ny = nx if ny is None else ny
+        cfg = Config2D()
+        lib().tara2d_default_config(ctypes.byref(cfg), nx, ny)
+        cfg.rhs, cfg.scheme, cfg.precision = rhs, scheme, precision
+        cfg.nu, cfg.dt, cfg.alpha, cfg.lam = nu, dt, alpha, lam
+        cfg.kpi = kpi
+        cfg.lx = 2.0 * kpi if lx is None else lx
+        cfg.ly = 2.0 * kpi if ly is None else ly
+        h = ctypes.c_void_p()
+        _check(lib().tara2d_create(ctypes.byref(cfg), ctypes.byref(h)))
+        self._h = h
+        self.nx, self.ny, self.nh = nx, ny, nx // 2 + 1
+        self.cfg = cfg
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            lib().tara2d_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def launches_per_step(self) -> int:
+        return lib().tara2d_launches_per_step(self._h)
+
+    def set_state(self, omegak: np.ndarray, dt_old: np.ndarray | None = None) -> None:
+        w = _as_spectrum(omegak, self.nh, self.ny)
+        fo = None if dt_old is None else _as_spectrum(dt_old, self.nh, self.ny)
+        _check(lib().tara2d_set_state(self._h, _dp(w.view(np.float64)),
+                                      None if fo is None else _dp(fo.view(np.float64))))
+
+    def get_state(self, with_history: bool = False):
+        w = np.zeros((self.ny, self.nh), np.complex128)
+        fo = np.zeros_like(w) if with_history else None
+        _check(lib().tara2d_get_state(self._h, _dp(w.view(np.float64)),
+                                      None if fo is None else _dp(fo.view(np.float64))))
+        return (w, fo) if with_history else w
+
+    def get_state_into(self, out: np.ndarray) -> None:
+        """Copy the state into a caller-owned (Ny, Nh) complex128 array (e.g. pinned)."""
+        if out.shape != (self.ny, self.nh) or out.dtype != np.complex128 or not out.flags.c_contiguous:
+            raise ValueError("out must be a C-contiguous (Ny, Nh) complex128 array")
+        _check(lib().tara2d_get_state(self._h, _dp(out.view(np.float64)), None))
+
+    def set_state_device(self, ptr: int, dt_old_ptr: int | None = None) -> None:
+        _check(lib().tara2d_set_state_device(self._h, ctypes.c_void_p(ptr),
+                                             ctypes.c_void_p(dt_old_ptr) if dt_old_ptr else None))
+
+    def get_state_device(self, ptr: int) -> None:
+        _check(lib().tara2d_get_state_device(self._h, ctypes.c_void_p(ptr)))
+
+    def step(self, n: int = 1) -> None:
+        _check(lib().tara2d_step(self._h, int(n)))
+
+    KERNELS = ("k_col_inverse", "k_row_nl", "k_col_forward")
+
+    def step_timed(self, n: int) -> dict:
+        """Run n steps with CUDA events between launches; per-kernel-kind totals."""
+        ms = (ctypes.c_double * 3)()
+        cnt = (ctypes.c_int * 3)()
+        tot = ctypes.c_double()
+        _check(lib().tara2d_step_timed(self._h, int(n), ms, cnt, ctypes.byref(tot)))
+        return {"total_ms": tot.value,
+                "kernels": {k: {"ms": ms[i], "launches": cnt[i]} for i, k in enumerate(self.KERNELS)}}
+
+    def rhs(self) -> np.ndarray:
+        out = np.zeros((self.ny, self.nh), np.complex128)
+        _check(lib().tara2d_rhs(self._h, _dp(out.view(np.float64))))
+        return out
+
+    def diag(self) -> tuple[float, float]:
+        e, z = ctypes.c_double(), ctypes.c_double()
+        _check(lib().tara2d_diag(self._h, ctypes.byref(e), ctypes.byref(z)))
+        return e.value, z.value
+
+    def synchronize(self) -> None:
+        _check(lib().tara2d_synchronize(self._h))
+
+    @property
+    def stream(self) -> int:
+        return lib().tara2d_stream(self._h) or 0
+
+    def init_random(self, k0: float, energy: float, seed: int) -> None:
+        _check(lib().tara2d_init_random(self._h, k0, energy, seed))

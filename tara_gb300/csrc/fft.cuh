@@ -1,0 +1,165 @@
+// Shared-memory Stockham FFT building blocks for sm_103a.
+//
+// One "slot" is a length-N complex vector in shared memory, transformed by a
+// group of G = N/16 threads (16 elements per thread: four radix-4 butterflies
+// per stage, or eight radix-2 butterflies in the final odd stage).  Every thread
+// of the CTA calls the same transform so that the stage barriers line up;
+// `active` masks threads whose slot holds nothing.
+//
+// Stockham autosort form (Govindaraju et al., SC'08): at a stage with
+// sub-transform length Ns and radix R, butterfly j reads in[j + r*N/R],
+// multiplies input r by W^(r*k*N/(R*Ns)) with k = j mod Ns, and writes the R
+// outputs to out[(j-k)*R + k + r*Ns].  Results come out in natural order, so no
+// bit reversal is needed.  Reads and writes of a stage touch different slots,
+// so each thread stages its inputs in registers between two barriers and the
+// transform runs in place.
+//
+// Arithmetic: the twiddled radix-4 butterfly is written with the two-sided FMA
+// form a = v0 + w*v2, b = 2*v0 - a, which costs 3 FMA-pipe instructions per
+// output pair component instead of a separate multiply and two adds; a full
+// twiddled radix-4 butterfly is 24 FP64 instructions for 4 points over 2
+// stages.  The first stage has unit twiddles and uses 16 adds.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace tara {
+
+template <typename T> struct cplx_of;
+template <> struct cplx_of<double> { typedef double2 type; };
+template <> struct cplx_of<float> { typedef float2 type; };
+
+template <typename T>
+__device__ __forceinline__ typename cplx_of<T>::type mkc(T x, T y) {
+  typename cplx_of<T>::type c;
+  c.x = x;
+  c.y = y;
+  return c;
+}
+
+__host__ __device__ constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c(n >> 1); }
+
+// threads per transform of length N
+__host__ __device__ constexpr int fft_group(int n) { return n >= 16 ? n / 16 : 1; }
+
+// Untwiddled radix-4 DFT (first stage).  Forward: y1 = a1 - i a3, y3 = a1 + i a3.
+template <bool INV, typename C>
+__device__ __forceinline__ void dft4(C& v0, C& v1, C& v2, C& v3) {
+  const auto a0r = v0.x + v2.x, a0i = v0.y + v2.y;
+  const auto a1r = v0.x - v2.x, a1i = v0.y - v2.y;
+  const auto a2r = v1.x + v3.x, a2i = v1.y + v3.y;
+  const auto a3r = v1.x - v3.x, a3i = v1.y - v3.y;
+  v0.x = a0r + a2r; v0.y = a0i + a2i;
+  v2.x = a0r - a2r; v2.y = a0i - a2i;
+  if (!INV) {
+    v1.x = a1r + a3i; v1.y = a1i - a3r;
+    v3.x = a1r - a3i; v3.y = a1i + a3r;
+  } else {
+    v1.x = a1r - a3i; v1.y = a1i + a3r;
+    v3.x = a1r + a3i; v3.y = a1i - a3r;
+  }
+}
+
+// Twiddled radix-4 butterfly; w1..w3 are already conjugated for the inverse.
+template <bool INV, typename C>
+__device__ __forceinline__ void dft4_tw(C& v0, C& v1, C& v2, C& v3, const C w1, const C w2,
+                                        const C w3) {
+  typedef decltype(v0.x) T;
+  const T two = T(2);
+  // a0 = v0 + w2 v2, a1 = v0 - w2 v2
+  const T a0r = fma(v2.x, w2.x, fma(-v2.y, w2.y, v0.x));
+  const T a0i = fma(v2.x, w2.y, fma(v2.y, w2.x, v0.y));
+  const T a1r = fma(two, v0.x, -a0r);
+  const T a1i = fma(two, v0.y, -a0i);
+  // t1 = w1 v1; a2 = t1 + w3 v3, a3 = t1 - w3 v3
+  const T t1r = fma(v1.x, w1.x, -v1.y * w1.y);
+  const T t1i = fma(v1.x, w1.y, v1.y * w1.x);
+  const T a2r = fma(v3.x, w3.x, fma(-v3.y, w3.y, t1r));
+  const T a2i = fma(v3.x, w3.y, fma(v3.y, w3.x, t1i));
+  const T a3r = fma(two, t1r, -a2r);
+  const T a3i = fma(two, t1i, -a2i);
+  v0.x = a0r + a2r; v0.y = a0i + a2i;
+  v2.x = a0r - a2r; v2.y = a0i - a2i;
+  if (!INV) {
+    v1.x = a1r + a3i; v1.y = a1i - a3r;
+    v3.x = a1r - a3i; v3.y = a1i + a3r;
+  } else {
+    v1.x = a1r - a3i; v1.y = a1i + a3r;
+    v3.x = a1r + a3i; v3.y = a1i - a3r;
+  }
+}
+
+template <bool INV, typename C>
+__device__ __forceinline__ C load_tw(const C* __restrict__ tw, int m) {
+  C w = __ldg(tw + m);
+  if (INV) w.y = -w.y;
+  return w;
+}
+
+// In-place length-N transform of buf (unnormalised).  tw[m] = exp(-2 pi i m/N).
+// Forward: X[k] = sum x[n] e^{-2 pi i nk/N}; inverse uses e^{+...}.
+template <typename T, int N, bool INV>
+__device__ __forceinline__ void fft_slot(typename cplx_of<T>::type* buf, int lane, bool active,
+                                         const typename cplx_of<T>::type* __restrict__ tw) {
+  typedef typename cplx_of<T>::type C;
+  constexpr int G = fft_group(N);
+  constexpr int Q = N / 4;
+  constexpr int LG = ilog2c(N);
+  constexpr int NR4 = LG / 2;
+  static_assert((1 << LG) == N && N >= 16, "power-of-two length >= 16");
+  static_assert(Q % G == 0, "group must divide the butterfly count");
+  constexpr int BPT = Q / G;
+#pragma unroll
+  for (int s = 0; s < NR4; ++s) {
+    const int Ns = 1 << (2 * s);
+    C v[BPT][4];
+    if (active) {
+#pragma unroll
+      for (int b = 0; b < BPT; ++b) {
+        const int j = lane + b * G;
+#pragma unroll
+        for (int r = 0; r < 4; ++r) v[b][r] = buf[j + r * Q];
+      }
+    }
+    __syncthreads();
+    if (active) {
+#pragma unroll
+      for (int b = 0; b < BPT; ++b) {
+        const int j = lane + b * G;
+        const int k = j & (Ns - 1);
+        if (s == 0) {
+          dft4<INV>(v[b][0], v[b][1], v[b][2], v[b][3]);
+        } else {
+          const int step = k * (N / (4 * Ns));
+          const C w1 = load_tw<INV>(tw, step);
+          const C w2 = load_tw<INV>(tw, 2 * step);
+          const C w3 = load_tw<INV>(tw, 3 * step);
+          dft4_tw<INV>(v[b][0], v[b][1], v[b][2], v[b][3], w1, w2, w3);
+        }
+        const int base = ((j - k) << 2) + k;
+#pragma unroll
+        for (int r = 0; r < 4; ++r) buf[base + r * Ns] = v[b][r];
+      }
+    }
+    __syncthreads();
+  }
+  if (LG & 1) {
+    // final radix-2 stage, Ns = N/2: out[j] = a + w^j b, out[j + N/2] = a - w^j b
+    constexpr int H = N / 2;
+    constexpr int B2 = H / G;
+    if (active) {
+#pragma unroll
+      for (int b = 0; b < B2; ++b) {
+        const int j = lane + b * G;
+        const C a = buf[j], c = buf[j + H];
+        const C w = load_tw<INV>(tw, j);
+        const T xr = fma(c.x, w.x, fma(-c.y, w.y, a.x));
+        const T xi = fma(c.x, w.y, fma(c.y, w.x, a.y));
+        buf[j] = mkc<T>(xr, xi);
+        buf[j + H] = mkc<T>(fma(T(2), a.x, -xr), fma(T(2), a.y, -xi));
+      }
+    }
+    __syncthreads();
+  }
+}
+
+}  // namespace tara

@@ -1,0 +1,79 @@
+// Internal host-side declarations shared by the translation units of libtara.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "../../include/tara.h"
+#include "kernels2d.cuh"
+
+namespace tara {
+
+// thread-local status (tara_last_error)
+int set_error(int code, const std::string& msg);
+int set_ok();
+int cuda_fail(cudaError_t e, const char* what);
+
+#define TARA_CK(call)                                   \
+  do {                                                  \
+    cudaError_t e_ = (call);                            \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+  } while (0)
+
+// Largest transform length: one FP64 row pass of 2048 points fills 128 KB of
+// shared memory with four slots; longer rows would need a split transform.
+constexpr int kMaxN = 2048;
+inline bool is_pow2_in_range(int n) { return n >= 16 && n <= kMaxN && (n & (n - 1)) == 0; }
+inline int round_up(int v, int m) { return (v + m - 1) / m * m; }
+
+// Host tables shared with the oracle's arithmetic: kx = 2*kpi*i/lx etc.
+void make_wavenumbers(int nx, int ny, double kpi, double lx, double ly, double* kx, double* ky,
+                      int* i0);
+
+// Precision-dispatched launchers (one translation unit per precision).
+template <typename T>
+struct Launch2D {
+  static int col_inverse(int ny, int nh, const double2* win, void* u, const Grid2D& g,
+                         const RhsParams& p, const void* twy, cudaStream_t s);
+  static int row_nl(int nx, int ny, const void* u, void* nl, const Grid2D& g, const void* twx,
+                    cudaStream_t s);
+  static int col_forward(int ny, int nh, const void* nl, const StepBufs& sb, const Grid2D& g,
+                         const RhsParams& p, int mode, const void* twy, cudaStream_t s);
+  static int col_fft(int ny, int nh, int pitch, const void* in, void* out, bool inverse,
+                     const void* twy, cudaStream_t s);
+  static int row_c2r(int nx, int ny, int pitch, int rpitch, const void* in, void* out,
+                     const void* twx, cudaStream_t s);
+  static int row_r2c(int nx, int ny, int rpitch, int pitch, const void* in, void* out,
+                     const void* twx, cudaStream_t s);
+};
+
+// Twiddle table exp(-2 pi i m/n), m < n, in precision T, uploaded to device.
+int make_twiddles(int n, bool fp32, void** dev);
+
+}  // namespace tara
+
+struct tara2d {
+  tara2d_config cfg;
+  int dev = 0;
+  int nx = 0, ny = 0, nh = 0, pitch = 0;
+  cudaStream_t stream = nullptr;
+  double2 *w0 = nullptr, *ws = nullptr, *acc = nullptr, *fold = nullptr, *fout = nullptr;
+  void* u = nullptr;   // 4 fields of the y-inverse pass, precision of cfg
+  void* nl = nullptr;  // x-r2c output of the products
+  double *kx = nullptr, *ky = nullptr;
+  int* i0 = nullptr;
+  void *twx = nullptr, *twy = nullptr;
+  double *diag_part = nullptr, *diag_out = nullptr;
+  unsigned int* flag = nullptr;
+  tara::Grid2D grid;
+  tara::RhsParams rp;
+};
+
+namespace tara {
+// One RHS evaluation of `win` followed by the update of `mode`; when ev is not
+// null, ev[0..2] are recorded on the handle's stream after the three launches.
+int rhs_and_update(tara2d* h, const double2* win, int mode, cudaEvent_t* ev);
+int copy_in_dense(tara2d* h, double2* dst, const double* host);
+int copy_out_dense(tara2d* h, double* host, const double2* src);
+int refresh_tables(tara2d* h);
+}  // namespace tara

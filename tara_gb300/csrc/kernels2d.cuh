@@ -1,0 +1,409 @@
+// 2D pseudo-spectral kernels: the reference's derive2csh / derive2css RHS and the
+// AB2 / RK4 updates, split into three passes over HBM per RHS evaluation.
+//
+// Layout in HBM: every spectral field is a half spectrum stored row by row,
+// field[y * pitch + x] for ky row y in [0, Ny) and kx column x in [0, Nh),
+// Nh = Nx/2 + 1, pitch = Nh rounded up to 8 elements (128 B rows for FP64).
+// This is the reference's complex(8) a(Nh,Ny) layout with padded rows.
+//
+// Pass A  k_col_inverse   per tile of kx columns: read omega_hat, form
+//         u_x = i ky psi, u_y = -i kx psi, i kx w, i ky w (w = omega_hat for the
+//         plain RHS, w = k^2 psi for the screened one) and inverse-transform
+//         each along y.  (src/derive2csh.f95:29-71, src/derive2css.f95:22-55)
+// Pass B  k_row_nl        per pair of ky rows: the x-direction c2r of the four
+//         fields as two complex transforms (u_x + i u_y, w_x + i w_y), the
+//         product u.grad(w), and the x-direction r2c of the two rows' products
+//         as one complex transform.  (src/derive2csh.f95:73-106)
+// Pass C  k_col_forward   per tile of kx columns: forward transform along y,
+//         2/3 truncation, scaling, nu k^2 term, and the stage update of the
+//         chosen scheme.  (src/derive2csh.f95:108-145, src/ab2csh.f95:10-14)
+//
+// The c2r follows FFTW's rank-2 c2r semantics: complex DFTs along y for all
+// Nh columns first, then a 1D c2r along x that reads only the real parts of the
+// kx = 0 and kx = Nx/2 bins (lib/fftw/rdft/rank-geq2-rdft2.c).  The reference
+// feeds it non-Hermitian spectra (e.g. i ky w on the ky = -Ny/2 row), so the
+// order and the discard rule are kept exactly.
+#pragma once
+#include "fft.cuh"
+
+namespace tara {
+
+struct Grid2D {
+  int nx, ny, nh, pitch;
+  const double* __restrict__ kx;  // [nh]
+  const double* __restrict__ ky;  // [ny]
+  const int* __restrict__ i0;     // [ny]: first kx index removed by the 2/3 rule
+};
+
+enum StepMode {
+  MODE_DERIVE = 0,  // write F = dt_omegak_new
+  MODE_AB2 = 1,     // w0 += (3/2 F - 1/2 Fold) dt ; Fold = F
+  MODE_RK1 = 2,     // S = F ; ws = w0 + F dt/2
+  MODE_RK2 = 3,     // S += 2F ; ws = w0 + F dt/2
+  MODE_RK3 = 4,     // S += 2F ; ws = w0 + F dt
+  MODE_RK4 = 5      // w0 += dt/6 (S + F)
+};
+
+struct RhsParams {
+  int rhs;          // 0 plain (derive2csh), 1 screened (derive2css)
+  double nu, alpha, lambda;
+  double nl_scale;  // 1/2 (pair split) * 1/(Nx Ny)^2 (two unnormalised c2r)
+  double dt;
+};
+
+// Largest power-of-two column tile with tile smem <= 100 KB and <= 512 threads.
+__host__ __device__ constexpr int pick_tc(int bytes_per_col, int threads_per_col) {
+  int tc = 32;
+  while (tc > 1 && (tc * bytes_per_col > 100 * 1024 || tc * threads_per_col > 512)) tc >>= 1;
+  return tc;
+}
+
+// Row pairs per CTA for the row pass: <= 512 threads, <= 64 KB (at least 1).
+__host__ __device__ constexpr int pick_rp(int n, int csize) {
+  int rp = 32;
+  while (rp > 1 && (4 * rp * fft_group(n) > 512 || rp * 4 * n * csize > 64 * 1024)) rp >>= 1;
+  return rp;
+}
+
+template <typename T, int N> struct ColCfg {
+  typedef typename cplx_of<T>::type C;
+  static constexpr int G = fft_group(N);
+  static constexpr int S = N + 1;  // smem column stride (one element of padding)
+  static constexpr int TCA = pick_tc(2 * S * (int)sizeof(C), 2 * G);  // pass A: 2 slots/column
+  static constexpr int TCC = pick_tc(S * (int)sizeof(C), G);          // pass C: 1 slot/column
+  static constexpr int THREADS_A = 2 * TCA * G;
+  static constexpr int THREADS_C = TCC * G;
+  static constexpr int SMEM_A = 2 * TCA * S * (int)sizeof(C);
+  static constexpr int SMEM_C = TCC * S * (int)sizeof(C);
+};
+
+template <typename T, int N> struct RowCfg {
+  typedef typename cplx_of<T>::type C;
+  static constexpr int G = fft_group(N);
+  static constexpr int RP = pick_rp(N, (int)sizeof(C));
+  static constexpr int THREADS = 4 * RP * G;
+  static constexpr int SMEM = RP * 4 * N * (int)sizeof(C);
+};
+
+// ---------------------------------------------------------------------------
+// Pass A
+// ---------------------------------------------------------------------------
+template <typename T, int N>
+__global__ void __launch_bounds__(ColCfg<T, N>::THREADS_A)
+    k_col_inverse(const double2* __restrict__ win, typename cplx_of<T>::type* __restrict__ u,
+                  Grid2D g, RhsParams p, const typename cplx_of<T>::type* __restrict__ tw) {
+  typedef typename cplx_of<T>::type C;
+  typedef ColCfg<T, N> CF;
+  constexpr int TC = CF::TCA, S = CF::S, G = CF::G;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C* sm = reinterpret_cast<C*>(smraw);  // [2][TC][S]
+  const int x0 = blockIdx.x * TC;
+  const int tid = threadIdx.x;
+  const size_t fsz = (size_t)g.ny * g.pitch;
+  const int slot = tid / G, lane = tid % G;
+  for (int round = 0; round < 2; ++round) {
+    for (int e = tid; e < N * TC; e += CF::THREADS_A) {
+      const int y = e / TC, c = e % TC, x = x0 + c;
+      C fa = mkc<T>(T(0), T(0)), fb = fa;
+      if (x < g.nh) {
+        const double2 w = win[(size_t)y * g.pitch + x];
+        const double kx = g.kx[x], ky = g.ky[y];
+        const bool origin = (x == 0 && y == 0);
+        const double k2 = kx * kx + ky * ky;
+        double pr = 0.0, pim = 0.0;
+        if (!origin) {
+          const double den = p.rhs ? k2 + p.lambda : k2;
+          pr = w.x / den;
+          pim = w.y / den;
+        }
+        if (round == 0) {
+          // u_x = (0,1) ky psi, u_y = -(0,1) kx psi
+          fa = mkc<T>(T(-ky * pim), T(ky * pr));
+          fb = mkc<T>(T(kx * pim), T(-(kx * pr)));
+        } else {
+          // i kx w, i ky w with w = omega_hat (plain) or k^2 psi (screened)
+          const double dr = p.rhs ? k2 * pr : w.x;
+          const double di = p.rhs ? k2 * pim : w.y;
+          fa = mkc<T>(T(-kx * di), T(kx * dr));
+          fb = mkc<T>(T(-ky * di), T(ky * dr));
+        }
+      }
+      sm[c * S + y] = fa;
+      sm[(TC + c) * S + y] = fb;
+    }
+    __syncthreads();
+    fft_slot<T, N, true>(sm + slot * S, lane, true, tw);
+    for (int e = tid; e < N * TC; e += CF::THREADS_A) {
+      const int y = e / TC, c = e % TC, x = x0 + c;
+      if (x < g.nh) {
+        const size_t q = (size_t)y * g.pitch + x;
+        u[(size_t)(2 * round) * fsz + q] = sm[c * S + y];
+        u[(size_t)(2 * round + 1) * fsz + q] = sm[(TC + c) * S + y];
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Pass B
+// ---------------------------------------------------------------------------
+// Slot s of row pair p: s = 0 (u_x + i u_y, row a), 1 (w_x + i w_y, row a),
+// 2 and 3 the same for row b = a + 1.  Hermitian extension of a half row A:
+// Z[k] = A[k] + i B[k] (k <= N/2), Z[N-k] = conj(A[k]) + i conj(B[k]), with the
+// imaginary parts of the k = 0 and k = N/2 bins dropped first.
+template <typename T, int N>
+__global__ void __launch_bounds__(RowCfg<T, N>::THREADS)
+    k_row_nl(const typename cplx_of<T>::type* __restrict__ u,
+             typename cplx_of<T>::type* __restrict__ nl, Grid2D g,
+             const typename cplx_of<T>::type* __restrict__ tw) {
+  typedef typename cplx_of<T>::type C;
+  typedef RowCfg<T, N> RC;
+  constexpr int G = RC::G, H = N / 2, RP = RC::RP;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C* sm = reinterpret_cast<C*>(smraw);  // [RP][4][N]
+  const int tid = threadIdx.x;
+  const int slot = tid / G, lane = tid % G;
+  const int y_base = blockIdx.x * (2 * RP);
+  const size_t fsz = (size_t)g.ny * g.pitch;
+  for (int e = tid; e < RP * 4 * N; e += RC::THREADS) {
+    const int k = e % N, sl = e / N;
+    const int pp = sl >> 2, s = sl & 3;
+    const int y = y_base + 2 * pp + (s >> 1);
+    C z = mkc<T>(T(0), T(0));
+    if (y < g.ny) {
+      const C* fa = u + (size_t)(2 * (s & 1)) * fsz + (size_t)y * g.pitch;
+      const C* fb = fa + fsz;
+      const int kk = k <= H ? k : N - k;
+      C A = fa[kk], B = fb[kk];
+      if (kk == 0 || kk == H) {
+        A.y = T(0);
+        B.y = T(0);
+      }
+      z = (k <= H) ? mkc<T>(A.x - B.y, A.y + B.x) : mkc<T>(A.x + B.y, -A.y + B.x);
+    }
+    sm[sl * N + k] = z;
+  }
+  __syncthreads();
+  fft_slot<T, N, true>(sm + slot * N, lane, true, tw);
+  // products u_x w_x + u_y w_y for rows a and b, packed as a + i b
+  for (int e = tid; e < RP * N; e += RC::THREADS) {
+    const int x = e % N, pp = e / N;
+    C* b = sm + (size_t)pp * 4 * N;
+    const C c1a = b[x], c2a = b[N + x], c1b = b[2 * N + x], c2b = b[3 * N + x];
+    const T na = fma(c1a.x, c2a.x, c1a.y * c2a.y);
+    const T nb = fma(c1b.x, c2b.x, c1b.y * c2b.y);
+    b[x] = mkc<T>(na, nb);
+  }
+  __syncthreads();
+  fft_slot<T, N, false>(sm + slot * N, lane, (slot & 3) == 0, tw);
+  // split: 2 X_a[k] = Z[k] + conj Z[N-k], 2 X_b[k] = -i (Z[k] - conj Z[N-k])
+  for (int e = tid; e < RP * (H + 1); e += RC::THREADS) {
+    const int k = e % (H + 1), pp = e / (H + 1);
+    const int ya = y_base + 2 * pp;
+    if (ya < g.ny) {
+      const C* b = sm + (size_t)pp * 4 * N;
+      const C z = b[k], m = b[(N - k) & (N - 1)];
+      nl[(size_t)ya * g.pitch + k] = mkc<T>(z.x + m.x, z.y - m.y);
+      nl[(size_t)(ya + 1) * g.pitch + k] = mkc<T>(z.y + m.y, -(z.x - m.x));
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Pass C
+// ---------------------------------------------------------------------------
+struct StepBufs {
+  const double2* win;  // RHS input (w0 or ws); may alias ws
+  double2* w0;         // state
+  double2* ws;         // RK stage input
+  double2* acc;        // RK sum k1 + 2k2 + 2k3
+  double2* fold;       // AB2 history
+  double2* fout;       // MODE_DERIVE output
+  unsigned int* flag;  // bit 0: a non-finite value was produced
+};
+
+template <typename T, int N>
+__global__ void __launch_bounds__(ColCfg<T, N>::THREADS_C)
+    k_col_forward(const typename cplx_of<T>::type* __restrict__ nl, StepBufs sb, Grid2D g,
+                  RhsParams p, int mode, const typename cplx_of<T>::type* __restrict__ tw) {
+  typedef typename cplx_of<T>::type C;
+  typedef ColCfg<T, N> CF;
+  constexpr int TC = CF::TCC, S = CF::S, G = CF::G;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C* sm = reinterpret_cast<C*>(smraw);  // [TC][S]
+  const int x0 = blockIdx.x * TC;
+  const int tid = threadIdx.x;
+  for (int e = tid; e < N * TC; e += CF::THREADS_C) {
+    const int y = e / TC, c = e % TC, x = x0 + c;
+    sm[c * S + y] = (x < g.nh) ? nl[(size_t)y * g.pitch + x] : mkc<T>(T(0), T(0));
+  }
+  __syncthreads();
+  fft_slot<T, N, false>(sm + (tid / G) * S, tid % G, true, tw);
+  bool bad = false;
+  for (int e = tid; e < N * TC; e += CF::THREADS_C) {
+    const int y = e / TC, c = e % TC, x = x0 + c;
+    if (x >= g.nh) continue;
+    const size_t q = (size_t)y * g.pitch + x;
+    const C v = sm[c * S + y];
+    double nr = (double)v.x * p.nl_scale, ni = (double)v.y * p.nl_scale;
+    if (x >= g.i0[y]) nr = ni = 0.0;  // 2/3 truncation of the nonlinear term only
+    const double kx = g.kx[x], ky = g.ky[y];
+    const double k2 = kx * kx + ky * ky;
+    const double vk2 = p.nu * k2;
+    const double2 w = sb.win[q];
+    double fr, fi;
+    if (p.rhs == 0) {
+      fr = -(nr + vk2 * w.x);
+      fi = -(ni + vk2 * w.y);
+    } else {
+      double dr = 0.0, di = 0.0;
+      if (!(x == 0 && y == 0)) {
+        const double den = k2 + p.lambda;
+        dr = k2 * (w.x / den);
+        di = k2 * (w.y / den);
+      }
+      fr = -(p.alpha * nr + vk2 * dr);
+      fi = -(p.alpha * ni + vk2 * di);
+    }
+    bad |= !(isfinite(fr) && isfinite(fi));
+    const double dt = p.dt;
+    switch (mode) {
+      case MODE_DERIVE:
+        sb.fout[q] = make_double2(fr, fi);
+        break;
+      case MODE_AB2: {
+        const double2 fo = sb.fold[q];
+        const double2 s = sb.w0[q];
+        sb.w0[q] = make_double2(s.x + (1.5 * fr - 0.5 * fo.x) * dt, s.y + (1.5 * fi - 0.5 * fo.y) * dt);
+        sb.fold[q] = make_double2(fr, fi);
+        break;
+      }
+      case MODE_RK1: {
+        const double2 s = sb.w0[q];
+        sb.acc[q] = make_double2(fr, fi);
+        sb.ws[q] = make_double2(s.x + fr * dt / 2.0, s.y + fi * dt / 2.0);
+        break;
+      }
+      case MODE_RK2:
+      case MODE_RK3: {
+        const double2 s = sb.w0[q];
+        const double2 a = sb.acc[q];
+        const double h = (mode == MODE_RK2) ? dt / 2.0 : dt;
+        sb.acc[q] = make_double2(a.x + 2.0 * fr, a.y + 2.0 * fi);
+        sb.ws[q] = make_double2(s.x + fr * h, s.y + fi * h);
+        break;
+      }
+      default: {  // MODE_RK4
+        const double2 s = sb.w0[q];
+        const double2 a = sb.acc[q];
+        sb.w0[q] = make_double2(s.x + dt / 6.0 * (a.x + fr), s.y + dt / 6.0 * (a.y + fi));
+        break;
+      }
+    }
+  }
+  if (bad) atomicOr(sb.flag, 1u);
+}
+
+// ---------------------------------------------------------------------------
+// Plain transforms (initial conditions, diagnostics and the transform API)
+// ---------------------------------------------------------------------------
+// Column transform of a half spectrum along y, in place or out of place.
+template <typename T, int N, bool INV>
+__global__ void __launch_bounds__(ColCfg<T, N>::THREADS_C)
+    k_col_fft(const typename cplx_of<T>::type* in, typename cplx_of<T>::type* out, int nh,
+              int pitch, const typename cplx_of<T>::type* __restrict__ tw) {
+  typedef typename cplx_of<T>::type C;
+  typedef ColCfg<T, N> CF;
+  constexpr int TC = CF::TCC, S = CF::S, G = CF::G;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C* sm = reinterpret_cast<C*>(smraw);
+  const int x0 = blockIdx.x * TC, tid = threadIdx.x;
+  for (int e = tid; e < N * TC; e += CF::THREADS_C) {
+    const int y = e / TC, c = e % TC, x = x0 + c;
+    sm[c * S + y] = (x < nh) ? in[(size_t)y * pitch + x] : mkc<T>(T(0), T(0));
+  }
+  __syncthreads();
+  fft_slot<T, N, INV>(sm + (tid / G) * S, tid % G, true, tw);
+  for (int e = tid; e < N * TC; e += CF::THREADS_C) {
+    const int y = e / TC, c = e % TC, x = x0 + c;
+    if (x < nh) out[(size_t)y * pitch + x] = sm[c * S + y];
+  }
+}
+
+// 1D c2r along x for pairs of rows (after the y pass): out rows are real with
+// row pitch rpitch.  Unnormalised.
+template <typename T, int N>
+__global__ void __launch_bounds__(RowCfg<T, N>::THREADS)
+    k_row_c2r(const typename cplx_of<T>::type* __restrict__ in, T* __restrict__ out, int ny,
+              int pitch, int rpitch, const typename cplx_of<T>::type* __restrict__ tw) {
+  typedef typename cplx_of<T>::type C;
+  typedef RowCfg<T, N> RC;
+  constexpr int G = RC::G, H = N / 2, NP = 4 * RC::RP;  // NP row pairs per CTA
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C* sm = reinterpret_cast<C*>(smraw);  // [NP][N]
+  const int tid = threadIdx.x, y_base = blockIdx.x * (2 * NP);
+  for (int e = tid; e < NP * N; e += RC::THREADS) {
+    const int k = e % N, pp = e / N, ya = y_base + 2 * pp;
+    C z = mkc<T>(T(0), T(0));
+    if (ya < ny) {
+      const int kk = k <= H ? k : N - k;
+      C A = in[(size_t)ya * pitch + kk], B = in[(size_t)(ya + 1) * pitch + kk];
+      if (kk == 0 || kk == H) {
+        A.y = T(0);
+        B.y = T(0);
+      }
+      z = (k <= H) ? mkc<T>(A.x - B.y, A.y + B.x) : mkc<T>(A.x + B.y, -A.y + B.x);
+    }
+    sm[pp * N + k] = z;
+  }
+  __syncthreads();
+  fft_slot<T, N, true>(sm + (tid / G) * N, tid % G, true, tw);
+  for (int e = tid; e < NP * N; e += RC::THREADS) {
+    const int x = e % N, pp = e / N, ya = y_base + 2 * pp;
+    if (ya < ny) {
+      const C z = sm[pp * N + x];
+      out[(size_t)ya * rpitch + x] = z.x;
+      out[(size_t)(ya + 1) * rpitch + x] = z.y;
+    }
+  }
+}
+
+// 1D r2c along x for pairs of real rows (before the y pass).  Unnormalised.
+template <typename T, int N>
+__global__ void __launch_bounds__(RowCfg<T, N>::THREADS)
+    k_row_r2c(const T* __restrict__ in, typename cplx_of<T>::type* __restrict__ out, int ny,
+              int rpitch, int pitch, const typename cplx_of<T>::type* __restrict__ tw) {
+  typedef typename cplx_of<T>::type C;
+  typedef RowCfg<T, N> RC;
+  constexpr int G = RC::G, H = N / 2, NP = 4 * RC::RP;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  C* sm = reinterpret_cast<C*>(smraw);
+  const int tid = threadIdx.x, y_base = blockIdx.x * (2 * NP);
+  for (int e = tid; e < NP * N; e += RC::THREADS) {
+    const int x = e % N, pp = e / N, ya = y_base + 2 * pp;
+    sm[pp * N + x] = (ya < ny) ? mkc<T>(in[(size_t)ya * rpitch + x], in[(size_t)(ya + 1) * rpitch + x])
+                               : mkc<T>(T(0), T(0));
+  }
+  __syncthreads();
+  fft_slot<T, N, false>(sm + (tid / G) * N, tid % G, true, tw);
+  for (int e = tid; e < NP * (H + 1); e += RC::THREADS) {
+    const int k = e % (H + 1), pp = e / (H + 1), ya = y_base + 2 * pp;
+    if (ya < ny) {
+      const C z = sm[pp * N + k], m = sm[pp * N + ((N - k) & (N - 1))];
+      out[(size_t)ya * pitch + k] = mkc<T>(T(0.5) * (z.x + m.x), T(0.5) * (z.y - m.y));
+      out[(size_t)(ya + 1) * pitch + k] = mkc<T>(T(0.5) * (z.y + m.y), T(-0.5) * (z.x - m.x));
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Diagnostics: 1/2<|u|^2> and 1/2<omega^2> by Parseval over the half spectrum
+// (weight 1 on the kx = 0 and kx = Nx/2 columns, 2 elsewhere).
+// ---------------------------------------------------------------------------
+__global__ void k_diag_partial(const double2* __restrict__ w, Grid2D g, double* __restrict__ part);
+__global__ void k_diag_final(const double* __restrict__ part, int nparts, double inv,
+                             double* __restrict__ out, unsigned int* flag);
+__global__ void k_mul(double2* __restrict__ w, size_t n, double s);
+
+}  // namespace tara

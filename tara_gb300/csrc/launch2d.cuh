@@ -1,0 +1,157 @@
+// Launchers for the 2D kernels: runtime grid size -> compile-time transform
+// length.  Included once per precision (launch_fp64.cu, launch_fp32.cu) so the
+// two instantiation sets compile in parallel.
+#pragma once
+#include "internal.h"
+
+namespace tara {
+
+// Opt a kernel into more than 48 KB of dynamic shared memory (once per process).
+template <typename K>
+static cudaError_t allow_smem(K kernel, int bytes) {
+  if (bytes <= 48 * 1024) return cudaSuccess;
+  return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
+#define TARA_SWITCH_N(n, CALL)         \
+  switch (n) {                         \
+    case 16: { constexpr int N = 16; CALL; } break;     \
+    case 32: { constexpr int N = 32; CALL; } break;     \
+    case 64: { constexpr int N = 64; CALL; } break;     \
+    case 128: { constexpr int N = 128; CALL; } break;   \
+    case 256: { constexpr int N = 256; CALL; } break;   \
+    case 512: { constexpr int N = 512; CALL; } break;   \
+    case 1024: { constexpr int N = 1024; CALL; } break; \
+    case 2048: { constexpr int N = 2048; CALL; } break; \
+    default: return set_error(TARA_ERR_ARGS, "grid size must be a power of two in [16, 2048]"); \
+  }
+
+template <typename T, int N>
+static int launch_col_inverse(int nh, const double2* win, void* u, const Grid2D& g,
+                              const RhsParams& p, const void* tw, cudaStream_t s) {
+  typedef typename cplx_of<T>::type C;
+  typedef ColCfg<T, N> CF;
+  static cudaError_t attr = allow_smem(k_col_inverse<T, N>, CF::SMEM_A);
+  TARA_CK(attr);
+  const int blocks = (nh + CF::TCA - 1) / CF::TCA;
+  k_col_inverse<T, N><<<blocks, CF::THREADS_A, CF::SMEM_A, s>>>(win, (C*)u, g, p, (const C*)tw);
+  TARA_CK(cudaGetLastError());
+  return TARA_OK;
+}
+
+template <typename T, int N>
+static int launch_row_nl(int ny, const void* u, void* nl, const Grid2D& g, const void* tw,
+                         cudaStream_t s) {
+  typedef typename cplx_of<T>::type C;
+  typedef RowCfg<T, N> RC;
+  static cudaError_t attr = allow_smem(k_row_nl<T, N>, RC::SMEM);
+  TARA_CK(attr);
+  const int blocks = (ny + 2 * RC::RP - 1) / (2 * RC::RP);
+  k_row_nl<T, N><<<blocks, RC::THREADS, RC::SMEM, s>>>((const C*)u, (C*)nl, g, (const C*)tw);
+  TARA_CK(cudaGetLastError());
+  return TARA_OK;
+}
+
+template <typename T, int N>
+static int launch_col_forward(int nh, const void* nl, const StepBufs& sb, const Grid2D& g,
+                              const RhsParams& p, int mode, const void* tw, cudaStream_t s) {
+  typedef typename cplx_of<T>::type C;
+  typedef ColCfg<T, N> CF;
+  static cudaError_t attr = allow_smem(k_col_forward<T, N>, CF::SMEM_C);
+  TARA_CK(attr);
+  const int blocks = (nh + CF::TCC - 1) / CF::TCC;
+  k_col_forward<T, N><<<blocks, CF::THREADS_C, CF::SMEM_C, s>>>((const C*)nl, sb, g, p, mode,
+                                                                 (const C*)tw);
+  TARA_CK(cudaGetLastError());
+  return TARA_OK;
+}
+
+template <typename T, int N, bool INV>
+static int launch_col_fft(int nh, int pitch, const void* in, void* out, const void* tw,
+                          cudaStream_t s) {
+  typedef typename cplx_of<T>::type C;
+  typedef ColCfg<T, N> CF;
+  static cudaError_t attr = allow_smem(k_col_fft<T, N, INV>, CF::SMEM_C);
+  TARA_CK(attr);
+  const int blocks = (nh + CF::TCC - 1) / CF::TCC;
+  k_col_fft<T, N, INV><<<blocks, CF::THREADS_C, CF::SMEM_C, s>>>((const C*)in, (C*)out, nh, pitch,
+                                                                  (const C*)tw);
+  TARA_CK(cudaGetLastError());
+  return TARA_OK;
+}
+
+template <typename T, int N>
+static int launch_row_c2r(int ny, int pitch, int rpitch, const void* in, void* out, const void* tw,
+                          cudaStream_t s) {
+  typedef typename cplx_of<T>::type C;
+  typedef RowCfg<T, N> RC;
+  static cudaError_t attr = allow_smem(k_row_c2r<T, N>, RC::SMEM);
+  TARA_CK(attr);
+  const int per = 2 * 4 * RC::RP;
+  k_row_c2r<T, N><<<(ny + per - 1) / per, RC::THREADS, RC::SMEM, s>>>((const C*)in, (T*)out, ny,
+                                                                      pitch, rpitch, (const C*)tw);
+  TARA_CK(cudaGetLastError());
+  return TARA_OK;
+}
+
+template <typename T, int N>
+static int launch_row_r2c(int ny, int rpitch, int pitch, const void* in, void* out, const void* tw,
+                          cudaStream_t s) {
+  typedef typename cplx_of<T>::type C;
+  typedef RowCfg<T, N> RC;
+  static cudaError_t attr = allow_smem(k_row_r2c<T, N>, RC::SMEM);
+  TARA_CK(attr);
+  const int per = 2 * 4 * RC::RP;
+  k_row_r2c<T, N><<<(ny + per - 1) / per, RC::THREADS, RC::SMEM, s>>>((const T*)in, (C*)out, ny,
+                                                                      rpitch, pitch, (const C*)tw);
+  TARA_CK(cudaGetLastError());
+  return TARA_OK;
+}
+
+template <typename T>
+int Launch2D<T>::col_inverse(int ny, int nh, const double2* win, void* u, const Grid2D& g,
+                             const RhsParams& p, const void* twy, cudaStream_t s) {
+  TARA_SWITCH_N(ny, return (launch_col_inverse<T, N>(nh, win, u, g, p, twy, s)));
+  return TARA_OK;
+}
+
+template <typename T>
+int Launch2D<T>::row_nl(int nx, int ny, const void* u, void* nl, const Grid2D& g, const void* twx,
+                        cudaStream_t s) {
+  TARA_SWITCH_N(nx, return (launch_row_nl<T, N>(ny, u, nl, g, twx, s)));
+  return TARA_OK;
+}
+
+template <typename T>
+int Launch2D<T>::col_forward(int ny, int nh, const void* nl, const StepBufs& sb, const Grid2D& g,
+                             const RhsParams& p, int mode, const void* twy, cudaStream_t s) {
+  TARA_SWITCH_N(ny, return (launch_col_forward<T, N>(nh, nl, sb, g, p, mode, twy, s)));
+  return TARA_OK;
+}
+
+template <typename T>
+int Launch2D<T>::col_fft(int ny, int nh, int pitch, const void* in, void* out, bool inverse,
+                         const void* twy, cudaStream_t s) {
+  if (inverse) {
+    TARA_SWITCH_N(ny, return (launch_col_fft<T, N, true>(nh, pitch, in, out, twy, s)));
+  } else {
+    TARA_SWITCH_N(ny, return (launch_col_fft<T, N, false>(nh, pitch, in, out, twy, s)));
+  }
+  return TARA_OK;
+}
+
+template <typename T>
+int Launch2D<T>::row_c2r(int nx, int ny, int pitch, int rpitch, const void* in, void* out,
+                         const void* twx, cudaStream_t s) {
+  TARA_SWITCH_N(nx, return (launch_row_c2r<T, N>(ny, pitch, rpitch, in, out, twx, s)));
+  return TARA_OK;
+}
+
+template <typename T>
+int Launch2D<T>::row_r2c(int nx, int ny, int rpitch, int pitch, const void* in, void* out,
+                         const void* twx, cudaStream_t s) {
+  TARA_SWITCH_N(nx, return (launch_row_r2c<T, N>(ny, rpitch, pitch, in, out, twx, s)));
+  return TARA_OK;
+}
+
+}  // namespace tara

@@ -1,0 +1,581 @@
+// Device-resident 2D solver (tara2d_*), status handling, tables and the
+// diagnostics reduction.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "internal.h"
+
+namespace tara {
+
+// ---------------------------------------------------------------------------
+// status
+// ---------------------------------------------------------------------------
+static thread_local int g_err = TARA_OK;
+static thread_local std::string g_msg;
+
+int set_error(int code, const std::string& msg) {
+  g_err = code;
+  g_msg = msg;
+  return code;
+}
+int set_ok() {
+  g_err = TARA_OK;
+  g_msg.clear();
+  return TARA_OK;
+}
+int cuda_fail(cudaError_t e, const char* what) {
+  const int code = (e == cudaErrorMemoryAllocation) ? TARA_ERR_NOMEM : TARA_ERR_CUDA;
+  return set_error(code, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+// ---------------------------------------------------------------------------
+// tables
+// ---------------------------------------------------------------------------
+// kx = 2.0d0*pi*dfloat(i-1)/Lx and ky = 2.0d0*pi*(dfloat(j-1)-Ny)/Ly above
+// Ny/2 (src/derive2csh.f95:30,32,48); the 2/3 rule removes the nonlinear term
+// where dsqrt(kx*kx+ky*ky) >= (dfloat(Nx+Ny)/2.0)/3.0 (src/derive2csh.f95:113).
+// Evaluated on the host with the same expressions (no FMA contraction), so the
+// tables equal the reference's values bit for bit; because kx grows with i, the
+// removed set of row j is {i >= i0[j]}.
+void make_wavenumbers(int nx, int ny, double kpi, double lx, double ly, double* kx, double* ky,
+                      int* i0) {
+  const int nh = nx / 2 + 1;
+  for (int i = 0; i < nh; ++i) kx[i] = 2.0 * kpi * (double)i / lx;
+  for (int j = 0; j < ny; ++j)
+    ky[j] = (j < ny / 2) ? 2.0 * kpi * (double)j / ly : 2.0 * kpi * ((double)j - (double)ny) / ly;
+  const double cut = ((double)(nx + ny) / 2.0) / 3.0;
+  for (int j = 0; j < ny; ++j) {
+    int first = nh;
+    for (int i = nh - 1; i >= 0; --i) {
+      if (std::sqrt(kx[i] * kx[i] + ky[j] * ky[j]) >= cut)
+        first = i;
+      else
+        break;
+    }
+    i0[j] = first;
+  }
+}
+
+int make_twiddles(int n, bool fp32, void** dev) {
+  const long double tp = 6.283185307179586476925286766559005768L;
+  if (fp32) {
+    std::vector<float2> w(n);
+    for (int m = 0; m < n; ++m) {
+      const long double a = tp * (long double)m / (long double)n;
+      w[m] = make_float2((float)std::cos(a), (float)-std::sin(a));
+    }
+    TARA_CK(cudaMalloc(dev, n * sizeof(float2)));
+    TARA_CK(cudaMemcpy(*dev, w.data(), n * sizeof(float2), cudaMemcpyHostToDevice));
+  } else {
+    std::vector<double2> w(n);
+    for (int m = 0; m < n; ++m) {
+      const long double a = tp * (long double)m / (long double)n;
+      w[m] = make_double2((double)std::cos(a), (double)-std::sin(a));
+    }
+    TARA_CK(cudaMalloc(dev, n * sizeof(double2)));
+    TARA_CK(cudaMemcpy(*dev, w.data(), n * sizeof(double2), cudaMemcpyHostToDevice));
+  }
+  return TARA_OK;
+}
+
+// ---------------------------------------------------------------------------
+// diagnostics
+// ---------------------------------------------------------------------------
+constexpr int kDiagBlocks = 304, kDiagThreads = 256;
+
+__global__ void __launch_bounds__(kDiagThreads)
+    k_diag_partial(const double2* __restrict__ w, Grid2D g, double* __restrict__ part) {
+  double e = 0.0, z = 0.0;
+  const size_t total = (size_t)g.ny * g.nh;
+  for (size_t t = (size_t)blockIdx.x * kDiagThreads + threadIdx.x; t < total;
+       t += (size_t)gridDim.x * kDiagThreads) {
+    const int y = (int)(t / g.nh), x = (int)(t % g.nh);
+    const double2 v = w[(size_t)y * g.pitch + x];
+    const double wt = (x == 0 || 2 * (x) == g.nx) ? 1.0 : 2.0;
+    const double a2 = v.x * v.x + v.y * v.y;
+    z += wt * a2;
+    if (x != 0 || y != 0) {
+      const double kx = g.kx[x], ky = g.ky[y];
+      e += wt * a2 / (kx * kx + ky * ky);
+    }
+  }
+  __shared__ double se[kDiagThreads / 32], sz[kDiagThreads / 32];
+  for (int o = 16; o > 0; o >>= 1) {
+    e += __shfl_down_sync(0xffffffffu, e, o);
+    z += __shfl_down_sync(0xffffffffu, z, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    se[threadIdx.x >> 5] = e;
+    sz[threadIdx.x >> 5] = z;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double te = 0.0, tz = 0.0;
+    for (int i = 0; i < kDiagThreads / 32; ++i) {
+      te += se[i];
+      tz += sz[i];
+    }
+    part[2 * blockIdx.x] = te;
+    part[2 * blockIdx.x + 1] = tz;
+  }
+}
+
+__global__ void k_diag_final(const double* __restrict__ part, int nparts, double inv,
+                             double* __restrict__ out, unsigned int* flag) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double e = 0.0, z = 0.0;
+  for (int i = 0; i < nparts; ++i) {
+    e += part[2 * i];
+    z += part[2 * i + 1];
+  }
+  out[0] = e * inv;
+  out[1] = z * inv;
+  if (!(isfinite(e) && isfinite(z))) atomicOr(flag, 2u);
+}
+
+// w *= s
+__global__ void k_mul(double2* __restrict__ w, size_t n, double s) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const double2 v = w[i];
+    w[i] = make_double2(v.x * s, v.y * s);
+  }
+}
+
+// pointwise AB2 on dense arrays: out = w + (3/2 fn - 1/2 fo) dt  (src/ab2csh.f95:12)
+__global__ void k_ab2_dense(const double2* w, double2* out, const double2* __restrict__ fo,
+                            const double2* __restrict__ fn, size_t n, double dt) {
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const double2 a = w[i], b = fo[i], c = fn[i];
+    out[i] = make_double2(a.x + ((3.0 / 2.0) * c.x - (1.0 / 2.0) * b.x) * dt,
+                          a.y + ((3.0 / 2.0) * c.y - (1.0 / 2.0) * b.y) * dt);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// solver internals
+// ---------------------------------------------------------------------------
+template <typename T>
+static int rhs_update_t(tara2d* h, const double2* win, int mode, cudaEvent_t* ev) {
+  StepBufs sb;
+  sb.win = win;
+  sb.w0 = h->w0;
+  sb.ws = h->ws;
+  sb.acc = h->acc;
+  sb.fold = h->fold;
+  sb.fout = h->fout;
+  sb.flag = h->flag;
+  int rc;
+  if ((rc = Launch2D<T>::col_inverse(h->ny, h->nh, win, h->u, h->grid, h->rp, h->twy, h->stream)))
+    return rc;
+  if (ev) TARA_CK(cudaEventRecord(ev[0], h->stream));
+  if ((rc = Launch2D<T>::row_nl(h->nx, h->ny, h->u, h->nl, h->grid, h->twx, h->stream))) return rc;
+  if (ev) TARA_CK(cudaEventRecord(ev[1], h->stream));
+  if ((rc = Launch2D<T>::col_forward(h->ny, h->nh, h->nl, sb, h->grid, h->rp, mode, h->twy,
+                                     h->stream)))
+    return rc;
+  if (ev) TARA_CK(cudaEventRecord(ev[2], h->stream));
+  return TARA_OK;
+}
+
+// One RHS evaluation of `win` followed by the update of `mode`; when ev is not
+// null, ev[0..2] are recorded after the three launches.
+int rhs_and_update(tara2d* h, const double2* win, int mode, cudaEvent_t* ev) {
+  return h->cfg.precision == TARA_PREC_FP32 ? rhs_update_t<float>(h, win, mode, ev)
+                                            : rhs_update_t<double>(h, win, mode, ev);
+}
+
+int copy_in_dense(tara2d* h, double2* dst, const double* host) {
+  TARA_CK(cudaMemcpy2DAsync(dst, h->pitch * sizeof(double2), host, h->nh * sizeof(double2),
+                            h->nh * sizeof(double2), h->ny, cudaMemcpyHostToDevice, h->stream));
+  return TARA_OK;
+}
+
+int copy_out_dense(tara2d* h, double* host, const double2* src) {
+  TARA_CK(cudaMemcpy2DAsync(host, h->nh * sizeof(double2), src, h->pitch * sizeof(double2),
+                            h->nh * sizeof(double2), h->ny, cudaMemcpyDeviceToHost, h->stream));
+  return TARA_OK;
+}
+
+int refresh_tables(tara2d* h) {
+  std::vector<double> kx(h->nh), ky(h->ny);
+  std::vector<int> i0(h->ny);
+  make_wavenumbers(h->nx, h->ny, h->cfg.kpi, h->cfg.lx, h->cfg.ly, kx.data(), ky.data(), i0.data());
+  TARA_CK(cudaMemcpyAsync(h->kx, kx.data(), h->nh * sizeof(double), cudaMemcpyHostToDevice,
+                          h->stream));
+  TARA_CK(cudaMemcpyAsync(h->ky, ky.data(), h->ny * sizeof(double), cudaMemcpyHostToDevice,
+                          h->stream));
+  TARA_CK(cudaMemcpyAsync(h->i0, i0.data(), h->ny * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+  TARA_CK(cudaStreamSynchronize(h->stream));  // host vectors go out of scope
+  h->rp.rhs = h->cfg.rhs;
+  h->rp.nu = h->cfg.nu;
+  h->rp.alpha = h->cfg.alpha;
+  h->rp.lambda = h->cfg.lambda;
+  h->rp.dt = h->cfg.dt;
+  const double nn = (double)h->nx * (double)h->ny;
+  h->rp.nl_scale = 0.5 / (nn * nn);
+  return TARA_OK;
+}
+
+static int check_flag(tara2d* h) {
+  unsigned int f = 0;
+  TARA_CK(cudaMemcpyAsync(&f, h->flag, sizeof(f), cudaMemcpyDeviceToHost, h->stream));
+  TARA_CK(cudaStreamSynchronize(h->stream));
+  if (f) return set_error(TARA_ERR_NONFINITE, "non-finite value in the vorticity update");
+  return TARA_OK;
+}
+
+}  // namespace tara
+
+using namespace tara;
+
+// ---------------------------------------------------------------------------
+// public API
+// ---------------------------------------------------------------------------
+extern "C" {
+
+int tara_last_error(void) { return g_err; }
+const char* tara_last_error_message(void) { return g_msg.c_str(); }
+void tara_clear_error(void) { set_ok(); }
+const char* tara_version(void) { return "tara-gb300 0.1 (sm_103a)"; }
+
+void tara2d_default_config(tara2d_config* c, int nx, int ny) {
+  std::memset(c, 0, sizeof(*c));
+  c->nx = nx;
+  c->ny = ny;
+  c->rhs = TARA_RHS_PLAIN;
+  c->scheme = TARA_SCHEME_AB2;
+  c->precision = TARA_PREC_FP64;
+  c->nu = 0.01;
+  c->dt = 1e-4;
+  c->alpha = 1.0;
+  c->lambda = 10.0;
+  c->kpi = (double)3.1428f;
+  c->lx = 2.0 * c->kpi;
+  c->ly = 2.0 * c->kpi;
+}
+
+int tara2d_destroy(tara2d* h) {
+  if (!h) return set_ok();
+  cudaSetDevice(h->dev);
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  void* ptrs[] = {h->w0, h->ws, h->acc, h->fold, h->fout, h->u, h->nl, h->kx, h->ky, h->i0,
+                  h->twx, h->twy, h->diag_part, h->diag_out, h->flag};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return set_ok();
+}
+
+int tara2d_create(const tara2d_config* cfg, tara2d** out) {
+  if (!cfg || !out) return set_error(TARA_ERR_ARGS, "null argument");
+  *out = nullptr;
+  if (!is_pow2_in_range(cfg->nx) || !is_pow2_in_range(cfg->ny))
+    return set_error(TARA_ERR_ARGS, "nx and ny must be powers of two in [16, 2048]");
+  if (cfg->rhs != TARA_RHS_PLAIN && cfg->rhs != TARA_RHS_SCREEN)
+    return set_error(TARA_ERR_ARGS, "unknown rhs kind");
+  if (cfg->scheme != TARA_SCHEME_AB2 && cfg->scheme != TARA_SCHEME_RK4)
+    return set_error(TARA_ERR_ARGS, "unknown scheme");
+  if (cfg->precision != TARA_PREC_FP64 && cfg->precision != TARA_PREC_FP32)
+    return set_error(TARA_ERR_ARGS, "unknown precision");
+  if (!(cfg->lx > 0.0) || !(cfg->ly > 0.0) || !(cfg->kpi > 0.0))
+    return set_error(TARA_ERR_ARGS, "box lengths and kpi must be positive");
+  tara2d* h = new tara2d();
+  h->cfg = *cfg;
+  h->nx = cfg->nx;
+  h->ny = cfg->ny;
+  h->nh = cfg->nx / 2 + 1;
+  h->pitch = round_up(h->nh, 8);
+  int rc = TARA_OK;
+  auto fail = [&](int code) {
+    tara2d_destroy(h);
+    return code;
+  };
+#define CKC(call)                                              \
+  do {                                                         \
+    cudaError_t e_ = (call);                                   \
+    if (e_ != cudaSuccess) return fail(cuda_fail(e_, #call)); \
+  } while (0)
+  CKC(cudaGetDevice(&h->dev));
+  CKC(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+  const size_t fbytes = (size_t)h->ny * h->pitch * sizeof(double2);
+  const size_t csize = cfg->precision == TARA_PREC_FP32 ? sizeof(float2) : sizeof(double2);
+  const size_t wbytes = (size_t)h->ny * h->pitch * csize;
+  CKC(cudaMalloc(&h->w0, fbytes));
+  CKC(cudaMalloc(&h->fold, fbytes));
+  CKC(cudaMalloc(&h->fout, fbytes));
+  if (cfg->scheme == TARA_SCHEME_RK4) {
+    CKC(cudaMalloc(&h->ws, fbytes));
+    CKC(cudaMalloc(&h->acc, fbytes));
+  }
+  CKC(cudaMalloc(&h->u, 4 * wbytes));
+  CKC(cudaMalloc(&h->nl, wbytes));
+  CKC(cudaMalloc(&h->kx, h->nh * sizeof(double)));
+  CKC(cudaMalloc(&h->ky, h->ny * sizeof(double)));
+  CKC(cudaMalloc(&h->i0, h->ny * sizeof(int)));
+  CKC(cudaMalloc(&h->diag_part, 2 * kDiagBlocks * sizeof(double)));
+  CKC(cudaMalloc(&h->diag_out, 4 * sizeof(double)));
+  CKC(cudaMalloc(&h->flag, sizeof(unsigned int)));
+  CKC(cudaMemsetAsync(h->w0, 0, fbytes, h->stream));
+  CKC(cudaMemsetAsync(h->fold, 0, fbytes, h->stream));
+  CKC(cudaMemsetAsync(h->fout, 0, fbytes, h->stream));
+  if (h->ws) CKC(cudaMemsetAsync(h->ws, 0, fbytes, h->stream));
+  if (h->acc) CKC(cudaMemsetAsync(h->acc, 0, fbytes, h->stream));
+  CKC(cudaMemsetAsync(h->u, 0, 4 * wbytes, h->stream));
+  CKC(cudaMemsetAsync(h->nl, 0, wbytes, h->stream));
+  CKC(cudaMemsetAsync(h->flag, 0, sizeof(unsigned int), h->stream));
+#undef CKC
+  const bool f32 = cfg->precision == TARA_PREC_FP32;
+  if ((rc = make_twiddles(h->nx, f32, &h->twx))) return fail(rc);
+  if ((rc = make_twiddles(h->ny, f32, &h->twy))) return fail(rc);
+  h->grid.nx = h->nx;
+  h->grid.ny = h->ny;
+  h->grid.nh = h->nh;
+  h->grid.pitch = h->pitch;
+  h->grid.kx = h->kx;
+  h->grid.ky = h->ky;
+  h->grid.i0 = h->i0;
+  if ((rc = refresh_tables(h))) return fail(rc);
+  *out = h;
+  return set_ok();
+}
+
+int tara2d_set_state(tara2d* h, const double* omegak, const double* dt_old) {
+  if (!h || !omegak) return set_error(TARA_ERR_ARGS, "null argument");
+  TARA_CK(cudaSetDevice(h->dev));
+  int rc;
+  if ((rc = copy_in_dense(h, h->w0, omegak))) return rc;
+  if (dt_old) {
+    if ((rc = copy_in_dense(h, h->fold, dt_old))) return rc;
+  } else {
+    TARA_CK(cudaMemsetAsync(h->fold, 0, (size_t)h->ny * h->pitch * sizeof(double2), h->stream));
+  }
+  TARA_CK(cudaStreamSynchronize(h->stream));
+  return set_ok();
+}
+
+int tara2d_get_state(tara2d* h, double* omegak, double* dt_old) {
+  if (!h || !omegak) return set_error(TARA_ERR_ARGS, "null argument");
+  TARA_CK(cudaSetDevice(h->dev));
+  int rc;
+  if ((rc = copy_out_dense(h, omegak, h->w0))) return rc;
+  if (dt_old && (rc = copy_out_dense(h, dt_old, h->fold))) return rc;
+  TARA_CK(cudaStreamSynchronize(h->stream));
+  return set_ok();
+}
+
+int tara2d_set_state_device(tara2d* h, const void* omegak, const void* dt_old) {
+  if (!h || !omegak) return set_error(TARA_ERR_ARGS, "null argument");
+  TARA_CK(cudaSetDevice(h->dev));
+  const size_t row = h->nh * sizeof(double2), dp = h->pitch * sizeof(double2);
+  TARA_CK(cudaMemcpy2DAsync(h->w0, dp, omegak, row, row, h->ny, cudaMemcpyDeviceToDevice, h->stream));
+  if (dt_old)
+    TARA_CK(cudaMemcpy2DAsync(h->fold, dp, dt_old, row, row, h->ny, cudaMemcpyDeviceToDevice,
+                              h->stream));
+  else
+    TARA_CK(cudaMemsetAsync(h->fold, 0, (size_t)h->ny * dp, h->stream));
+  return set_ok();
+}
+
+int tara2d_get_state_device(tara2d* h, void* omegak) {
+  if (!h || !omegak) return set_error(TARA_ERR_ARGS, "null argument");
+  TARA_CK(cudaSetDevice(h->dev));
+  const size_t row = h->nh * sizeof(double2), dp = h->pitch * sizeof(double2);
+  TARA_CK(cudaMemcpy2DAsync(omegak, row, h->w0, dp, row, h->ny, cudaMemcpyDeviceToDevice, h->stream));
+  return set_ok();
+}
+
+int tara2d_launches_per_step(const tara2d* h) {
+  if (!h) return 0;
+  return h->cfg.scheme == TARA_SCHEME_RK4 ? 12 : 3;
+}
+
+static int step_impl(tara2d* h, int nsteps, cudaEvent_t* ev) {
+  int rc;
+  const int per = h->cfg.scheme == TARA_SCHEME_RK4 ? 12 : 3;
+  for (int s = 0; s < nsteps; ++s) {
+    cudaEvent_t* e = ev ? ev + (size_t)s * per : nullptr;
+    if (h->cfg.scheme == TARA_SCHEME_AB2) {
+      if ((rc = rhs_and_update(h, h->w0, MODE_AB2, e))) return rc;
+    } else {
+      if ((rc = rhs_and_update(h, h->w0, MODE_RK1, e))) return rc;
+      if ((rc = rhs_and_update(h, h->ws, MODE_RK2, e ? e + 3 : nullptr))) return rc;
+      if ((rc = rhs_and_update(h, h->ws, MODE_RK3, e ? e + 6 : nullptr))) return rc;
+      if ((rc = rhs_and_update(h, h->ws, MODE_RK4, e ? e + 9 : nullptr))) return rc;
+    }
+  }
+  return TARA_OK;
+}
+
+int tara2d_step(tara2d* h, int nsteps) {
+  if (!h || nsteps < 0) return set_error(TARA_ERR_ARGS, "bad handle or step count");
+  TARA_CK(cudaSetDevice(h->dev));
+  int rc;
+  if ((rc = step_impl(h, nsteps, nullptr))) return rc;
+  return set_ok();
+}
+
+int tara2d_step_timed(tara2d* h, int nsteps, double* kernel_ms, int* kernel_launches,
+                      double* total_ms) {
+  if (!h || nsteps <= 0 || !kernel_ms || !kernel_launches)
+    return set_error(TARA_ERR_ARGS, "bad arguments");
+  TARA_CK(cudaSetDevice(h->dev));
+  const int per = h->cfg.scheme == TARA_SCHEME_RK4 ? 12 : 3;
+  const size_t nev = (size_t)nsteps * per + 1;
+  std::vector<cudaEvent_t> ev(nev, nullptr);
+  int rc = TARA_OK;
+  for (size_t i = 0; i < nev && !rc; ++i)
+    if (cudaEventCreate(&ev[i]) != cudaSuccess) rc = set_error(TARA_ERR_CUDA, "cudaEventCreate");
+  if (!rc && cudaEventRecord(ev[0], h->stream) != cudaSuccess)
+    rc = set_error(TARA_ERR_CUDA, "cudaEventRecord");
+  if (!rc) rc = step_impl(h, nsteps, ev.data() + 1);
+  if (!rc && cudaEventSynchronize(ev[nev - 1]) != cudaSuccess)
+    rc = set_error(TARA_ERR_CUDA, "cudaEventSynchronize");
+  if (!rc) {
+    for (int k = 0; k < 3; ++k) {
+      kernel_ms[k] = 0.0;
+      kernel_launches[k] = 0;
+    }
+    for (size_t i = 1; i < nev; ++i) {
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, ev[i - 1], ev[i]);
+      const int kind = (int)((i - 1) % 3);  // col_inverse, row_nl, col_forward
+      kernel_ms[kind] += ms;
+      kernel_launches[kind] += 1;
+    }
+    if (total_ms) {
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, ev[0], ev[nev - 1]);
+      *total_ms = ms;
+    }
+  }
+  for (cudaEvent_t e : ev)
+    if (e) cudaEventDestroy(e);
+  return rc ? rc : set_ok();
+}
+
+int tara2d_rhs(tara2d* h, double* dt_omegak) {
+  if (!h || !dt_omegak) return set_error(TARA_ERR_ARGS, "null argument");
+  TARA_CK(cudaSetDevice(h->dev));
+  int rc;
+  if ((rc = rhs_and_update(h, h->w0, MODE_DERIVE, nullptr))) return rc;
+  if ((rc = copy_out_dense(h, dt_omegak, h->fout))) return rc;
+  TARA_CK(cudaStreamSynchronize(h->stream));
+  return set_ok();
+}
+
+int tara2d_diag(tara2d* h, double* energy, double* enstrophy) {
+  if (!h) return set_error(TARA_ERR_ARGS, "null handle");
+  TARA_CK(cudaSetDevice(h->dev));
+  k_diag_partial<<<kDiagBlocks, kDiagThreads, 0, h->stream>>>(h->w0, h->grid, h->diag_part);
+  TARA_CK(cudaGetLastError());
+  const double nn = (double)h->nx * (double)h->ny;
+  k_diag_final<<<1, 32, 0, h->stream>>>(h->diag_part, kDiagBlocks, 0.5 / (nn * nn), h->diag_out,
+                                        h->flag);
+  TARA_CK(cudaGetLastError());
+  double out[2];
+  TARA_CK(cudaMemcpyAsync(out, h->diag_out, sizeof(out), cudaMemcpyDeviceToHost, h->stream));
+  TARA_CK(cudaStreamSynchronize(h->stream));
+  if (energy) *energy = out[0];
+  if (enstrophy) *enstrophy = out[1];
+  int rc;
+  if ((rc = check_flag(h))) return rc;
+  return set_ok();
+}
+
+int tara2d_synchronize(tara2d* h) {
+  if (!h) return set_error(TARA_ERR_ARGS, "null handle");
+  TARA_CK(cudaSetDevice(h->dev));
+  TARA_CK(cudaStreamSynchronize(h->stream));
+  return check_flag(h) ? g_err : set_ok();
+}
+
+void* tara2d_stream(tara2d* h) { return h ? (void*)h->stream : nullptr; }
+
+// Philox4x32-10 on the host (Salmon et al., SC'11), for the seeded phases.
+static void philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
+  uint32_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3], k0 = key[0], k1 = key[1];
+  for (int r = 0; r < 10; ++r) {
+    const uint64_t p0 = (uint64_t)0xD2511F53u * c0, p1 = (uint64_t)0xCD9E8D57u * c2;
+    const uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+    const uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+    c0 = hi1 ^ c1 ^ k0;
+    c1 = lo1;
+    c2 = hi0 ^ c3 ^ k1;
+    c3 = lo0;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+int tara2d_init_random(tara2d* h, double k0, double energy, uint64_t seed) {
+  if (!h || !(k0 > 0.0) || !(energy > 0.0)) return set_error(TARA_ERR_ARGS, "bad arguments");
+  TARA_CK(cudaSetDevice(h->dev));
+  const int nx = h->nx, ny = h->ny, nh = h->nh;
+  const double pi = 3.14159265358979323846;
+  std::vector<double2> spec((size_t)nh * ny);
+  const uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+  for (int j = 0; j < ny; ++j) {
+    const double ky = (j < ny / 2) ? (double)j : (double)(j - ny);
+    for (int i = 0; i < nh; ++i) {
+      const double kx = (double)i;
+      double2 v = make_double2(0.0, 0.0);
+      if (i || j) {
+        const uint32_t ctr[4] = {(uint32_t)i, (uint32_t)j, 0u, 0u};
+        uint32_t r[4];
+        philox4x32_10(ctr, key, r);
+        const double theta = 2.0 * pi * ((double)r[0] * (1.0 / 4294967296.0));
+        const double k = std::sqrt(kx * kx + ky * ky);
+        const double ek = k * k * k * k * std::exp(-(k / k0) * (k / k0));
+        const double amp = std::sqrt(k * ek / pi);
+        v = make_double2(amp * std::cos(theta), amp * std::sin(theta));
+      }
+      spec[(size_t)j * nh + i] = v;
+    }
+  }
+  int rc;
+  if ((rc = copy_in_dense(h, h->w0, (const double*)spec.data()))) return rc;
+  // Hermitian projection: c2r then r2c (FP64 transforms), scaled by 1/(Nx Ny)
+  const int rpitch = round_up(nx, 8);
+  double* real = nullptr;
+  void *tx = nullptr, *ty = nullptr;
+  if ((rc = make_twiddles(nx, false, &tx)) || (rc = make_twiddles(ny, false, &ty))) {
+    cudaFree(tx);
+    cudaFree(ty);
+    return rc;
+  }
+  TARA_CK(cudaMalloc(&real, (size_t)ny * rpitch * sizeof(double)));
+  TARA_CK(cudaMemcpyAsync(h->fout, h->w0, (size_t)ny * h->pitch * sizeof(double2),
+                          cudaMemcpyDeviceToDevice, h->stream));
+  rc = Launch2D<double>::col_fft(ny, nh, h->pitch, h->fout, h->fout, true, ty, h->stream);
+  if (!rc) rc = Launch2D<double>::row_c2r(nx, ny, h->pitch, rpitch, h->fout, real, tx, h->stream);
+  if (!rc) rc = Launch2D<double>::row_r2c(nx, ny, rpitch, h->pitch, real, h->w0, tx, h->stream);
+  if (!rc) rc = Launch2D<double>::col_fft(ny, nh, h->pitch, h->w0, h->w0, false, ty, h->stream);
+  if (!rc) {
+    const double nn = (double)nx * (double)ny;
+    TARA_CK(cudaMemsetAsync(h->w0, 0, sizeof(double2), h->stream));  // zero mean vorticity
+    k_mul<<<304, 256, 0, h->stream>>>(h->w0, (size_t)ny * h->pitch, 1.0 / nn);
+    TARA_CK(cudaGetLastError());
+    double e0 = 0.0;
+    rc = tara2d_diag(h, &e0, nullptr);
+    if (!rc) {
+      k_mul<<<304, 256, 0, h->stream>>>(h->w0, (size_t)ny * h->pitch,
+                                        e0 > 0.0 ? std::sqrt(energy / e0) : 1.0);
+      TARA_CK(cudaGetLastError());
+      TARA_CK(cudaMemsetAsync(h->fold, 0, (size_t)ny * h->pitch * sizeof(double2), h->stream));
+    }
+  }
+  TARA_CK(cudaStreamSynchronize(h->stream));
+  cudaFree(real);
+  cudaFree(tx);
+  cudaFree(ty);
+  return rc ? rc : set_ok();
+}
+
+}  // extern "C"

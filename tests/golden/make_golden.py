@@ -1,0 +1,72 @@
+"""Generate tests/golden/golden64.npz from the FFTW-backed oracle.
+
+The oracle restates the reference's 2D path in C; this build of it routes every
+transform through FFTW 3.3.9 compiled from the reference's own vendored sources
+(oracle/_ref, made by ``make -C oracle ref``), planned FFTW_ESTIMATE per
+transform as src/derive2csh.f95:73-106 does.  The fixtures pin the portable
+own-FFT oracle (tests/test_oracle.py) and the GPU path (tests/test_gpu_*.py).
+
+Run from the repository root:  python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import sys
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+from oracle import oracle as orc  # noqa: E402
+
+OUT = Path(__file__).resolve().parent / "golden64.npz"
+
+
+def main() -> None:
+    O = orc.load(fftw=True)
+    assert O.is_fftw
+    rng = np.random.default_rng(20240512)
+    g: dict[str, np.ndarray] = {}
+    n = 64
+    # FFT vectors: rectangular real field, and a non-Hermitian half spectrum
+    x = rng.standard_normal((32, 64))
+    g["fft_r2c_in"] = x
+    g["fft_r2c_out"] = O.r2c(x)
+    c = rng.standard_normal((64, 17)) + 1j * rng.standard_normal((64, 17))
+    g["fft_c2r_in"] = c
+    g["fft_c2r_out"] = O.c2r(c)
+    # configuration-1 initial condition (src/main2css.f95:78-110): 64^2, Lx=Ly=2 (x pi),
+    # W0=25, m0=2, d=3/128 written as 0.0234375
+    w_real = O.ic_shear(n, n, 2.0, 2.0, 25.0, 2.0, 0.0234375, variant=0)
+    g["ic_real"] = w_real
+    w0 = O.r2c(w_real)
+    g["ic_spec"] = w0
+    # one RHS evaluation of each kind
+    g["rhs_plain"] = O.derive2csh(w0, 0.01)
+    O.set_css_params(2 * orc.PI_R4, 2 * orc.PI_R4, 10.0)
+    g["rhs_screen"] = O.derive2css(w0, 1.0, 0.01)
+    O.set_css_params(2.0 * orc.PI_R8, 2.0 * orc.PI_R8, 10.0)
+    g["rhs_screen_driverL"] = O.derive2css(w0, 1.0, 0.01)
+    O.set_css_params(2 * orc.PI_R4, 2 * orc.PI_R4, 10.0)
+    # AB2 runs with the driver's history rotation (zero history before step 1)
+    for steps in (1, 10, 2000):
+        w, fo = O.run(w0, rhs=0, scheme=0, nu=0.01, dt=1e-4, steps=steps)
+        g[f"ab2_plain_{steps}"] = w
+        g[f"ab2_plain_{steps}_hist"] = fo
+    w, _ = O.run(w0, rhs=1, scheme=0, alpha=1.0, nu=0.01, dt=1e-4, steps=2000)
+    g["ab2_screen_2000"] = w
+    # RK4: plain RHS from a seeded random-phase spectrum, and one rk42css step
+    wr = O.ic_random(n, n, 6.0, 0.5, 20240512)
+    g["ic_random"] = wr
+    w, _ = O.run(wr, rhs=0, scheme=1, nu=1e-4, dt=5e-5, steps=10)
+    g["rk4_plain_10"] = w
+    g["rk42css_1"] = O.rk42css(w0, 1.0, 0.01, 1e-4)
+    # diagnostics
+    g["energy_enstrophy_ic"] = np.array(O.energy_enstrophy(w0))
+    g["diag_css_ic"] = O.diag_css(w0, 2.0 * orc.PI_R8, 2.0 * orc.PI_R8, 10.0)
+    np.savez_compressed(OUT, **g)
+    print(f"wrote {OUT} ({OUT.stat().st_size} bytes, {len(g)} arrays)")
+
+
+if __name__ == "__main__":
+    main()

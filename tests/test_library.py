@@ -1,0 +1,95 @@
+"""CPU tests of libtara's C ABI: the library loads, exports every function that
+include/tara.h declares, and rejects bad arguments before touching a GPU."""
+from __future__ import annotations
+
+import ctypes
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import tara_gb300 as tg
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def declared_functions() -> list[str]:
+    names = []
+    for hdr in sorted((ROOT / "include").glob("*.h")):
+        text = re.sub(r"/\*.*?\*/", "", hdr.read_text(), flags=re.S)
+        names += re.findall(r"\b([a-z_][a-z0-9_]*)\s*\([^;{]*\)\s*;", text)
+    return sorted(set(n for n in names if n not in {"sizeof"}))
+
+
+def test_every_declared_symbol_is_exported():
+    L = tg.lib()
+    names = declared_functions()
+    assert "derive2csh_" in names and "tara2d_step" in names
+    missing = [n for n in names if not hasattr(L, n)]
+    assert not missing, f"declared but not exported: {missing}"
+
+
+def test_fortran_symbols_use_gfortran_mangling():
+    L = tg.lib()
+    for n in ("derive2csh_", "ab2csh_", "derive2css_", "ab2css_", "rk42css_"):
+        assert hasattr(L, n)
+
+
+def test_version():
+    assert b"sm_103a" in tg.lib().tara_version()
+
+
+def _cfg(nx, ny):
+    c = tg.Config2D()
+    tg.lib().tara2d_default_config(ctypes.byref(c), nx, ny)
+    return c
+
+
+@pytest.mark.parametrize("nx,ny", [(100, 64), (64, 8), (4096, 64), (0, 0), (64, 3)])
+def test_create_rejects_bad_sizes(nx, ny):
+    h = ctypes.c_void_p()
+    rc = tg.lib().tara2d_create(ctypes.byref(_cfg(nx, ny)), ctypes.byref(h))
+    assert rc == tg.TARA_ERR_ARGS
+    assert not h.value
+    assert tg.last_error()[0] == tg.TARA_ERR_ARGS
+
+
+def test_create_rejects_bad_kinds():
+    for field, val in (("rhs", 7), ("scheme", 5), ("precision", 9), ("lx", -1.0)):
+        c = _cfg(64, 64)
+        setattr(c, field, val)
+        h = ctypes.c_void_p()
+        assert tg.lib().tara2d_create(ctypes.byref(c), ctypes.byref(h)) == tg.TARA_ERR_ARGS
+
+
+def test_dropin_bad_dims_records_error():
+    w = np.zeros((64, 10), np.complex128)  # Nh inconsistent with Nx = 64
+    L = tg.lib()
+    ints = [ctypes.byref(ctypes.c_int(v)) for v in (64, 64, 10)]
+    dbl = [ctypes.byref(ctypes.c_double(v)) for v in (0.01, 0.0)]
+    p = w.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    L.derive2csh_(*ints, *dbl, p, p, p, p)
+    assert tg.last_error()[0] == tg.TARA_ERR_ARGS
+
+
+def test_python_wrapper_raises_on_bad_args():
+    with pytest.raises(tg.TaraError) as e:
+        tg.fft2d_r2c(np.zeros((24, 24)))
+    assert e.value.code == tg.TARA_ERR_ARGS
+
+
+def test_no_silent_fallback_without_gpu():
+    """With no usable GPU a valid request fails loudly (CUDA error), never
+    computes on the CPU."""
+    try:
+        import torch
+
+        has_gpu = torch.cuda.is_available()
+    except Exception:
+        has_gpu = False
+    if has_gpu:
+        pytest.skip("a GPU is present")
+    with pytest.raises(tg.TaraError) as e:
+        tg.Solver2D(64)
+    assert e.value.code in (tg.TARA_ERR_CUDA, tg.TARA_ERR_NOMEM)
