@@ -86,6 +86,12 @@ int make_twiddles(int n, bool fp32, void** dev) {
 // ---------------------------------------------------------------------------
 constexpr int kDiagBlocks = 304, kDiagThreads = 256;
 
+// Energy as the reference measures it: u from c2r of i ky psi and -i kx psi,
+// psi = omega/k^2, summed over grid points.  The c2r keeps only real parts in the
+// kx = 0 and kx = Nx/2 columns, which removes u_y of the whole kx = Nx/2 column
+// and u_x of the ky = -Ny/2 row in those two columns (their derivatives vanish
+// on the grid); every other mode counts by Parseval with weight 1 on the two
+// edge columns and 2 elsewhere.
 __global__ void __launch_bounds__(kDiagThreads)
     k_diag_partial(const double2* __restrict__ w, Grid2D g, double* __restrict__ part) {
   double e = 0.0, z = 0.0;
@@ -94,12 +100,16 @@ __global__ void __launch_bounds__(kDiagThreads)
        t += (size_t)gridDim.x * kDiagThreads) {
     const int y = (int)(t / g.nh), x = (int)(t % g.nh);
     const double2 v = w[(size_t)y * g.pitch + x];
-    const double wt = (x == 0 || 2 * (x) == g.nx) ? 1.0 : 2.0;
+    const bool edge_x = (x == 0 || 2 * x == g.nx);
+    const double wt = edge_x ? 1.0 : 2.0;
     const double a2 = v.x * v.x + v.y * v.y;
     z += wt * a2;
     if (x != 0 || y != 0) {
       const double kx = g.kx[x], ky = g.ky[y];
-      e += wt * a2 / (kx * kx + ky * ky);
+      const double k2 = kx * kx + ky * ky;
+      const double keep_ux = (edge_x && 2 * y == g.ny) ? 0.0 : ky * ky;
+      const double keep_uy = (2 * x == g.nx) ? 0.0 : kx * kx;
+      e += wt * a2 * (keep_ux + keep_uy) / (k2 * k2);
     }
   }
   __shared__ double se[kDiagThreads / 32], sz[kDiagThreads / 32];

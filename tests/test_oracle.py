@@ -122,3 +122,30 @@ def test_parseval_energy(oracle, golden):
     e_spec = 0.5 * np.sum(wt * np.abs(w) ** 2 / k2s * (k2 != 0)) / n**4
     z_spec = 0.5 * np.sum(wt * np.abs(w) ** 2) / n**4
     assert abs(e - e_spec) < 1e-12 * e and abs(z - z_spec) < 1e-12 * z
+
+
+def grid_energy_rule(w):
+    """Parseval with the c2r discard rule of the reference's transforms (the rule
+    libtara's reduction implements): u_y of the kx = Nx/2 column and u_x of the
+    ky = -Ny/2 row in the kx = 0 and kx = Nx/2 columns vanish on the grid."""
+    ny, nh = w.shape
+    nx = 2 * (nh - 1)
+    ky = np.fft.fftfreq(ny, 1.0 / ny)[:, None]
+    kx = np.arange(nh)[None, :].astype(float)
+    k2 = kx**2 + ky**2
+    edge = (kx == 0) | (kx == nx // 2)
+    wt = np.where(edge, 1.0, 2.0)
+    keep_ux = np.where(edge & (ky == -ny // 2), 0.0, ky**2)
+    keep_uy = np.where(kx == nx // 2, 0.0, kx**2)
+    k2s = np.where(k2 == 0, 1.0, k2)
+    e = 0.5 * np.sum(wt * np.abs(w) ** 2 * (keep_ux + keep_uy) / k2s**2 * (k2 != 0)) / (nx * ny) ** 2
+    z = 0.5 * np.sum(wt * np.abs(w) ** 2) / (nx * ny) ** 2
+    return e, z
+
+
+@pytest.mark.parametrize("n,seed", [(64, 20240512), (128, 3), (32, 9)])
+def test_grid_energy_rule_matches_physical_space(oracle, n, seed):
+    w = oracle.ic_random(n, n, 6.0 if n > 32 else 12.0, 0.5, seed)
+    e, z = oracle.energy_enstrophy(w)
+    er, zr = grid_energy_rule(w)
+    assert abs(er - e) < 1e-14 * e and abs(zr - z) < 1e-14 * z
