@@ -160,6 +160,24 @@ int tara2d_init_random(tara2d* h, double k0, double energy, uint64_t seed);
 int tara_fft2d_r2c(int nx, int ny, int precision, const double* in, double* out);
 int tara_fft2d_c2r(int nx, int ny, int precision, const double* in, double* out);
 
+/* ---- allocation-free RHS ------------------------------------------------- */
+/* No counterpart in the reference.  The plain RHS of derive2csh_ (same
+ * arithmetic, same kernels) on caller-owned device arrays -- omegak_dev in,
+ * dt_omegak_dev out, each a dense (Nh,Ny) complex(8) array, 16-byte aligned --
+ * enqueued on `stream` (a cudaStream_t; NULL for the legacy default stream).
+ * It performs no device allocation at all, for callers that cannot call
+ * cudaMalloc: programs whose device memory is owned by another allocator or
+ * reserved up front, and time loops that must not trigger the device-wide
+ * synchronisation cudaMalloc/cudaFree can cause.  Its scratch is one
+ * file-scope static device array of about 2.7 MB that every GPU loading the
+ * library holds until exit, so grids are limited to Nx, Ny <= 256 (powers of
+ * two); larger ones return TARA_ERR_ARGS.  The first call on a device resolves
+ * the array's address and uploads twiddle tables synchronously, so make it
+ * before any stream capture.  All calls on a device share the array: calls
+ * whose GPU work overlaps race and must be serialised by the caller. */
+int tara_derive2csh_noalloc(int nx, int ny, double nu, const void* omegak_dev,
+                            void* dt_omegak_dev, void* stream);
+
 /* Library version string. */
 const char* tara_version(void);
 

@@ -97,6 +97,7 @@ def _declare(L: ctypes.CDLL) -> None:
     L.tara2d_stream.restype = vp
     L.tara2d_launches_per_step.argtypes = [vp]
     L.tara2d_init_random.argtypes = [vp, c_double, c_double, ctypes.c_uint64]
+    L.tara_derive2csh_noalloc.argtypes = [c_int, c_int, c_double, vp, vp, vp]
     L.tara_fft2d_r2c.argtypes = [c_int, c_int, c_int, dp, dp]
     L.tara_fft2d_c2r.argtypes = [c_int, c_int, c_int, dp, dp]
 
