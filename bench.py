@@ -49,20 +49,19 @@ def peaks() -> tuple[float, str]:
     return 6800.0, "fallback"
 
 
-def traffic_from_profiles(kernel: str, n: int) -> float | None:
-    """DRAM bytes per launch recorded from an ncu capture (profiles/*.txt line
-    'traffic_bytes_per_launch <kernel> <n> <bytes>'), or None."""
+def from_profiles(key: str, kernel: str, n: int) -> float | None:
+    """A per-kernel figure recorded from an ncu capture: a profiles/*.txt line
+    '<key> <kernel> <n> <value>' (e.g. traffic_bytes_per_launch), or None."""
     for f in sorted((ROOT / "profiles").glob("*.txt")):
         for line in f.read_text().splitlines():
             parts = line.split()
-            if len(parts) == 4 and parts[0] == "traffic_bytes_per_launch" and parts[1] == kernel \
-                    and parts[2] == str(n):
+            if len(parts) == 4 and parts[0] == key and parts[1] == kernel and parts[2] == str(n):
                 return float(parts[3])
     return None
 
 
 class ClockSampler:
-    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    """nvidia-smi clocks and throttle reasons sampled every 50 ms."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -78,7 +77,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except Exception:
             self.proc = None
@@ -86,13 +85,17 @@ class ClockSampler:
 
         def rd():
             for line in self.proc.stdout:
-                self.rows.append([c.strip() for c in line.split(",")])
+                self.rows.append((time.time(), [c.strip() for c in line.split(",")]))
 
         self.thread = threading.Thread(target=rd, daemon=True)
         self.thread.start()
         return self
 
+    def mark(self, which: str) -> None:
+        setattr(self, "t_" + which, time.time())
+
     def stop(self) -> dict:
+        time.sleep(0.1)
         if self.proc is not None:
             self.proc.terminate()
             try:
@@ -103,7 +106,11 @@ class ClockSampler:
             self.thread.join(timeout=2)
         sm, mx, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for r in self.rows:
+        t0, t1 = getattr(self, "t_start", 0.0), getattr(self, "t_end", float("inf"))
+        window = [r for t, r in self.rows if t0 <= t <= t1 + 0.05]
+        if not window:  # a timed region shorter than the sampling period: nearest samples
+            window = [r for t, r in self.rows if t >= t0][:2]
+        for r in window:
             try:
                 sm.append(float(r[1]))
                 mx.append(float(r[2]))
@@ -197,11 +204,17 @@ def run_ours(args) -> None:
 
     # ---- device-resident timed region (CUDA events on the solver's stream)
     sampler = ClockSampler(local).start() if rank == 0 else None
+    if sampler:
+        time.sleep(0.5)  # let nvidia-smi start before the timed region
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
+    if sampler:
+        sampler.mark("start")
     prof = s.step_timed(args.steps)
     torch.cuda.synchronize()
+    if sampler:
+        sampler.mark("end")
     if dist:
         dist.barrier()
     clocks = sampler.stop() if sampler else None
@@ -250,7 +263,7 @@ def run_ours(args) -> None:
     avg_ms = ks[dom]["ms"] / max(1, ks[dom]["launches"])
     peak, peak_kind = peaks()
     achieved = alg_bytes[dom] / (avg_ms * 1e-3) / 1e9
-    traffic = traffic_from_profiles(dom, n)
+    traffic = from_profiles("traffic_bytes_per_launch", dom, n)
     value = n * n * args.steps * ws / (el_ms * 1e-3)
     cpu = cpu_baseline(n, budget_s=args.cpu_budget) if not args.no_cpu_baseline else None
     line = {
@@ -268,6 +281,8 @@ def run_ours(args) -> None:
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "avg_launch_ms": avg_ms,
+                     "limiter": "FP64 pipe (GB300: 2 FP64 thread-instructions per SM per cycle)",
+                     "fp64_pipe_busy_pct_ncu": from_profiles("fp64_pipe_busy_pct", dom, n),
                      "per_kernel_ms": {k: v["ms"] / max(1, v["launches"]) for k, v in ks.items()}},
         "clocks": clocks,
         "diag": {"energy": e, "enstrophy": z},

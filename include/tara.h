@@ -169,7 +169,7 @@ int tara_fft2d_c2r(int nx, int ny, int precision, const double* in, double* out)
  * cudaMalloc: programs whose device memory is owned by another allocator or
  * reserved up front, and time loops that must not trigger the device-wide
  * synchronisation cudaMalloc/cudaFree can cause.  Its scratch is one
- * file-scope static device array of about 2.7 MB that every GPU loading the
+ * file-scope static device array of about 2.9 MB that every GPU loading the
  * library holds until exit, so grids are limited to Nx, Ny <= 256 (powers of
  * two); larger ones return TARA_ERR_ARGS.  The first call on a device resolves
  * the array's address and uploads twiddle tables synchronously, so make it

@@ -29,6 +29,10 @@ inline int round_up(int v, int m) { return (v + m - 1) / m * m; }
 // Host tables shared with the oracle's arithmetic: kx = 2*kpi*i/lx etc.
 void make_wavenumbers(int nx, int ny, double kpi, double lx, double ly, double* kx, double* ky,
                       int* i0);
+// inv[j*nh+i] = 1/(kx^2+ky^2 [+lambda]) (0 at the origin), same operation order as
+// the RHS's denominators.
+void make_inverse_table(int nx, int ny, const double* kx, const double* ky, bool screened,
+                        double lambda, double* inv);
 
 // Precision-dispatched launchers (one translation unit per precision).
 template <typename T>
@@ -60,7 +64,7 @@ struct tara2d {
   double2 *w0 = nullptr, *ws = nullptr, *acc = nullptr, *fold = nullptr, *fout = nullptr;
   void* u = nullptr;   // 4 fields of the y-inverse pass, precision of cfg
   void* nl = nullptr;  // x-r2c output of the products
-  double *kx = nullptr, *ky = nullptr;
+  double *kx = nullptr, *ky = nullptr, *inv = nullptr;
   int* i0 = nullptr;
   void *twx = nullptr, *twy = nullptr;
   double *diag_part = nullptr, *diag_out = nullptr;

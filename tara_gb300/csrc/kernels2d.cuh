@@ -30,9 +30,11 @@ namespace tara {
 
 struct Grid2D {
   int nx, ny, nh, pitch;
-  const double* __restrict__ kx;  // [nh]
-  const double* __restrict__ ky;  // [ny]
-  const int* __restrict__ i0;     // [ny]: first kx index removed by the 2/3 rule
+  const double* __restrict__ kx;   // [nh]
+  const double* __restrict__ ky;   // [ny]
+  const int* __restrict__ i0;      // [ny]: first kx index removed by the 2/3 rule
+  const double* __restrict__ inv;  // [ny][nh]: 1/(kx^2+ky^2) (+lambda when screened), 0 at k = 0
+  int i0max;                       // columns x >= i0max lose the whole nonlinear term
 };
 
 enum StepMode {
@@ -51,10 +53,11 @@ struct RhsParams {
   double dt;
 };
 
-// Largest power-of-two column tile with tile smem <= 100 KB and <= 512 threads.
-__host__ __device__ constexpr int pick_tc(int bytes_per_col, int threads_per_col) {
+// Largest power-of-two column tile with tile smem <= budget and <= 512 threads.
+__host__ __device__ constexpr int pick_tc(int bytes_per_col, int threads_per_col,
+                                          int budget = 100 * 1024) {
   int tc = 32;
-  while (tc > 1 && (tc * bytes_per_col > 100 * 1024 || tc * threads_per_col > 512)) tc >>= 1;
+  while (tc > 1 && (tc * bytes_per_col > budget || tc * threads_per_col > 512)) tc >>= 1;
   return tc;
 }
 
@@ -70,7 +73,9 @@ template <typename T, int N> struct ColCfg {
   static constexpr int G = fft_group(N);
   static constexpr int S = N + 1;  // smem column stride (one element of padding)
   static constexpr int TCA = pick_tc(2 * S * (int)sizeof(C), 2 * G);  // pass A: 2 slots/column
-  static constexpr int TCC = pick_tc(S * (int)sizeof(C), G);          // pass C: 1 slot/column
+  // pass C: 1 slot/column; a small tile keeps the live (not fully truncated)
+  // columns spread evenly over the SMs
+  static constexpr int TCC = pick_tc(S * (int)sizeof(C), G, 48 * 1024);
   static constexpr int THREADS_A = 2 * TCA * G;
   static constexpr int THREADS_C = TCC * G;
   static constexpr int SMEM_A = 2 * TCA * S * (int)sizeof(C);
@@ -88,6 +93,8 @@ template <typename T, int N> struct RowCfg {
 // ---------------------------------------------------------------------------
 // Pass A
 // ---------------------------------------------------------------------------
+// blockIdx.y = 0: (u_x, u_y); blockIdx.y = 1: (i kx w, i ky w).  Splitting the
+// two field pairs over the grid halves the tail of the last wave.
 template <typename T, int N>
 __global__ void __launch_bounds__(ColCfg<T, N>::THREADS_A)
     k_col_inverse(const double2* __restrict__ win, typename cplx_of<T>::type* __restrict__ u,
@@ -98,50 +105,46 @@ __global__ void __launch_bounds__(ColCfg<T, N>::THREADS_A)
   extern __shared__ __align__(16) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);  // [2][TC][S]
   const int x0 = blockIdx.x * TC;
+  const int pair = blockIdx.y;
   const int tid = threadIdx.x;
   const size_t fsz = (size_t)g.ny * g.pitch;
   const int slot = tid / G, lane = tid % G;
-  for (int round = 0; round < 2; ++round) {
-    for (int e = tid; e < N * TC; e += CF::THREADS_A) {
-      const int y = e / TC, c = e % TC, x = x0 + c;
-      C fa = mkc<T>(T(0), T(0)), fb = fa;
-      if (x < g.nh) {
-        const double2 w = win[(size_t)y * g.pitch + x];
-        const double kx = g.kx[x], ky = g.ky[y];
-        const bool origin = (x == 0 && y == 0);
-        const double k2 = kx * kx + ky * ky;
-        double pr = 0.0, pim = 0.0;
-        if (!origin) {
-          const double den = p.rhs ? k2 + p.lambda : k2;
-          pr = w.x / den;
-          pim = w.y / den;
+  for (int e = tid; e < N * TC; e += CF::THREADS_A) {
+    const int y = e / TC, c = e % TC, x = x0 + c;
+    C fa = mkc<T>(T(0), T(0)), fb = fa;
+    if (x < g.nh) {
+      const double2 w = win[(size_t)y * g.pitch + x];
+      const double kx = g.kx[x], ky = g.ky[y];
+      const double inv = g.inv[(size_t)y * g.nh + x];  // 1/k^2 or 1/(k^2+lambda); 0 at k = 0
+      if (pair == 0) {
+        // psi = omega/(k^2 [+lambda]); u_x = (0,1) ky psi, u_y = -(0,1) kx psi
+        const double pr = w.x * inv, pim = w.y * inv;
+        fa = mkc<T>(T(-ky * pim), T(ky * pr));
+        fb = mkc<T>(T(kx * pim), T(-(kx * pr)));
+      } else {
+        // i kx w, i ky w with w = omega_hat (plain) or k^2 psi (screened)
+        double dr = w.x, di = w.y;
+        if (p.rhs) {
+          const double k2 = kx * kx + ky * ky;
+          dr = k2 * (w.x * inv);
+          di = k2 * (w.y * inv);
         }
-        if (round == 0) {
-          // u_x = (0,1) ky psi, u_y = -(0,1) kx psi
-          fa = mkc<T>(T(-ky * pim), T(ky * pr));
-          fb = mkc<T>(T(kx * pim), T(-(kx * pr)));
-        } else {
-          // i kx w, i ky w with w = omega_hat (plain) or k^2 psi (screened)
-          const double dr = p.rhs ? k2 * pr : w.x;
-          const double di = p.rhs ? k2 * pim : w.y;
-          fa = mkc<T>(T(-kx * di), T(kx * dr));
-          fb = mkc<T>(T(-ky * di), T(ky * dr));
-        }
-      }
-      sm[c * S + y] = fa;
-      sm[(TC + c) * S + y] = fb;
-    }
-    __syncthreads();
-    fft_slot<T, N, true>(sm + slot * S, lane, true, tw);
-    for (int e = tid; e < N * TC; e += CF::THREADS_A) {
-      const int y = e / TC, c = e % TC, x = x0 + c;
-      if (x < g.nh) {
-        const size_t q = (size_t)y * g.pitch + x;
-        u[(size_t)(2 * round) * fsz + q] = sm[c * S + y];
-        u[(size_t)(2 * round + 1) * fsz + q] = sm[(TC + c) * S + y];
+        fa = mkc<T>(T(-kx * di), T(kx * dr));
+        fb = mkc<T>(T(-ky * di), T(ky * dr));
       }
     }
-    __syncthreads();
+    sm[c * S + y] = fa;
+    sm[(TC + c) * S + y] = fb;
+  }
+  __syncthreads();
+  fft_slot<T, N, true>(sm + slot * S, lane, true, tw);
+  for (int e = tid; e < N * TC; e += CF::THREADS_A) {
+    const int y = e / TC, c = e % TC, x = x0 + c;
+    if (x < g.nh) {
+      const size_t q = (size_t)y * g.pitch + x;
+      u[(size_t)(2 * pair) * fsz + q] = sm[c * S + y];
+      u[(size_t)(2 * pair + 1) * fsz + q] = sm[(TC + c) * S + y];
+    }
   }
 }
 
@@ -234,20 +237,29 @@ __global__ void __launch_bounds__(ColCfg<T, N>::THREADS_C)
   C* sm = reinterpret_cast<C*>(smraw);  // [TC][S]
   const int x0 = blockIdx.x * TC;
   const int tid = threadIdx.x;
-  for (int e = tid; e < N * TC; e += CF::THREADS_C) {
-    const int y = e / TC, c = e % TC, x = x0 + c;
-    sm[c * S + y] = (x < g.nh) ? nl[(size_t)y * g.pitch + x] : mkc<T>(T(0), T(0));
+  // Tiles whose columns all lie at kx >= i0max lose the whole nonlinear term to
+  // the 2/3 rule: their transform is skipped (uniform per CTA, so the barriers
+  // inside fft_slot stay matched).
+  const bool live = x0 < g.i0max;
+  if (live) {
+    for (int e = tid; e < N * TC; e += CF::THREADS_C) {
+      const int y = e / TC, c = e % TC, x = x0 + c;
+      sm[c * S + y] = (x < g.nh) ? nl[(size_t)y * g.pitch + x] : mkc<T>(T(0), T(0));
+    }
+    __syncthreads();
+    fft_slot<T, N, false>(sm + (tid / G) * S, tid % G, true, tw);
   }
-  __syncthreads();
-  fft_slot<T, N, false>(sm + (tid / G) * S, tid % G, true, tw);
   bool bad = false;
   for (int e = tid; e < N * TC; e += CF::THREADS_C) {
     const int y = e / TC, c = e % TC, x = x0 + c;
     if (x >= g.nh) continue;
     const size_t q = (size_t)y * g.pitch + x;
-    const C v = sm[c * S + y];
-    double nr = (double)v.x * p.nl_scale, ni = (double)v.y * p.nl_scale;
-    if (x >= g.i0[y]) nr = ni = 0.0;  // 2/3 truncation of the nonlinear term only
+    double nr = 0.0, ni = 0.0;
+    if (x < g.i0[y]) {  // 2/3 truncation of the nonlinear term only
+      const C v = sm[c * S + y];
+      nr = (double)v.x * p.nl_scale;
+      ni = (double)v.y * p.nl_scale;
+    }
     const double kx = g.kx[x], ky = g.ky[y];
     const double k2 = kx * kx + ky * ky;
     const double vk2 = p.nu * k2;
@@ -257,12 +269,8 @@ __global__ void __launch_bounds__(ColCfg<T, N>::THREADS_C)
       fr = -(nr + vk2 * w.x);
       fi = -(ni + vk2 * w.y);
     } else {
-      double dr = 0.0, di = 0.0;
-      if (!(x == 0 && y == 0)) {
-        const double den = k2 + p.lambda;
-        dr = k2 * (w.x / den);
-        di = k2 * (w.y / den);
-      }
+      const double inv = g.inv[(size_t)y * g.nh + x];  // 1/(k^2+lambda), 0 at k = 0
+      const double dr = k2 * (w.x * inv), di = k2 * (w.y * inv);
       fr = -(p.alpha * nr + vk2 * dr);
       fi = -(p.alpha * ni + vk2 * di);
     }

@@ -33,7 +33,7 @@ static int launch_col_inverse(int nh, const double2* win, void* u, const Grid2D&
   typedef ColCfg<T, N> CF;
   static cudaError_t attr = allow_smem(k_col_inverse<T, N>, CF::SMEM_A);
   TARA_CK(attr);
-  const int blocks = (nh + CF::TCA - 1) / CF::TCA;
+  const dim3 blocks((nh + CF::TCA - 1) / CF::TCA, 2);
   k_col_inverse<T, N><<<blocks, CF::THREADS_A, CF::SMEM_A, s>>>(win, (C*)u, g, p, (const C*)tw);
   TARA_CK(cudaGetLastError());
   return TARA_OK;

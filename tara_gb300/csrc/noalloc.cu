@@ -10,10 +10,11 @@
 // on first use; this one never does.
 //
 // Where its scratch lives: one file-scope `static __device__` array,
-// g_noalloc_scratch, of fixed size (kScratchBytes, about 2.7 MB) that every GPU
+// g_noalloc_scratch, of fixed size (kScratchBytes, about 2.9 MB) that every GPU
 // which loads libtara holds until the process exits.  It carries the four
 // y-inverse spectra, the products' spectrum, the twiddle tables, the
-// wavenumber tables and an error flag for grids up to kNoAllocMaxN^2 = 256^2;
+// wavenumber and 1/k^2 tables and an error flag for grids up to
+// kNoAllocMaxN^2 = 256^2;
 // larger grids are rejected with TARA_ERR_ARGS.
 //
 // Host code cannot use the name g_noalloc_scratch as a device address (on the
@@ -49,7 +50,8 @@ constexpr size_t kOffTw = kOffNL + align256(kFieldElems * sizeof(double2));
 constexpr size_t kOffKx = kOffTw + align256(kTwElems * sizeof(double2));
 constexpr size_t kOffKy = kOffKx + align256(kNhMax * sizeof(double));
 constexpr size_t kOffI0 = kOffKy + align256(kNoAllocMaxN * sizeof(double));
-constexpr size_t kOffFlag = kOffI0 + align256(kNoAllocMaxN * sizeof(int));
+constexpr size_t kOffInv = kOffI0 + align256(kNoAllocMaxN * sizeof(int));
+constexpr size_t kOffFlag = kOffInv + align256(kFieldElems * sizeof(double));
 constexpr size_t kScratchBytes = kOffFlag + 256;
 
 // offset of the length-n twiddle table inside the twiddle region
@@ -68,7 +70,7 @@ namespace tara {
 // Wavenumbers and the 2/3-rule index of derive2csh in IEEE double with the
 // host's operation order and no contraction (explicit _rn intrinsics), so the
 // tables equal make_wavenumbers()'s bit for bit.
-__global__ void k_noalloc_tables(int nx, int ny, double* kx, double* ky, int* i0,
+__global__ void k_noalloc_tables(int nx, int ny, double* kx, double* ky, int* i0, double* inv,
                                  unsigned int* flag) {
   const double kpi = (double)3.1428f;
   const double l = __dmul_rn(2.0, kpi);
@@ -91,6 +93,11 @@ __global__ void k_noalloc_tables(int nx, int ny, double* kx, double* ky, int* i0
         break;
     }
     i0[j] = first;
+  }
+  for (int q = t; q < ny * nh; q += blockDim.x) {
+    const int j = q / nh, i = q % nh;
+    const double k2 = __dadd_rn(__dmul_rn(kx[i], kx[i]), __dmul_rn(ky[j], ky[j]));
+    inv[q] = (i == 0 && j == 0) ? 0.0 : __ddiv_rn(1.0, k2);
   }
 }
 
@@ -139,11 +146,12 @@ extern "C" int tara_derive2csh_noalloc(int nx, int ny, double nu, const void* om
   double* kx = (double*)(base + kOffKx);
   double* ky = (double*)(base + kOffKy);
   int* i0 = (int*)(base + kOffI0);
+  double* inv = (double*)(base + kOffInv);
   unsigned int* flag = (unsigned int*)(base + kOffFlag);
   double2* u = (double2*)(base + kOffU);
   double2* nl = (double2*)(base + kOffNL);
   const double2* tw = (const double2*)(base + kOffTw);
-  k_noalloc_tables<<<1, 256, 0, s>>>(nx, ny, kx, ky, i0, flag);
+  k_noalloc_tables<<<1, 256, 0, s>>>(nx, ny, kx, ky, i0, inv, flag);
   TARA_CK(cudaGetLastError());
   Grid2D g;
   g.nx = nx;
@@ -153,6 +161,15 @@ extern "C" int tara_derive2csh_noalloc(int nx, int ny, double nu, const void* om
   g.kx = kx;
   g.ky = ky;
   g.i0 = i0;
+  g.inv = inv;
+  {  // the same tables on the host (stack arrays) give the last column the 2/3 rule keeps
+    double hkx[kNhMax], hky[kNoAllocMaxN];
+    int hi0[kNoAllocMaxN];
+    make_wavenumbers(nx, ny, (double)3.1428f, 2.0 * (double)3.1428f, 2.0 * (double)3.1428f, hkx,
+                     hky, hi0);
+    g.i0max = 0;
+    for (int j = 0; j < ny; ++j) g.i0max = hi0[j] > g.i0max ? hi0[j] : g.i0max;
+  }
   RhsParams p;
   p.rhs = TARA_RHS_PLAIN;
   p.nu = nu;

@@ -59,6 +59,16 @@ void make_wavenumbers(int nx, int ny, double kpi, double lx, double ly, double* 
   }
 }
 
+void make_inverse_table(int nx, int ny, const double* kx, const double* ky, bool screened,
+                        double lambda, double* inv) {
+  const int nh = nx / 2 + 1;
+  for (int j = 0; j < ny; ++j)
+    for (int i = 0; i < nh; ++i) {
+      const double k2 = kx[i] * kx[i] + ky[j] * ky[j];
+      inv[(size_t)j * nh + i] = (i == 0 && j == 0) ? 0.0 : 1.0 / (screened ? k2 + lambda : k2);
+    }
+}
+
 int make_twiddles(int n, bool fp32, void** dev) {
   const long double tp = 6.283185307179586476925286766559005768L;
   if (fp32) {
@@ -212,9 +222,16 @@ int copy_out_dense(tara2d* h, double* host, const double2* src) {
 }
 
 int refresh_tables(tara2d* h) {
-  std::vector<double> kx(h->nh), ky(h->ny);
+  std::vector<double> kx(h->nh), ky(h->ny), inv((size_t)h->nh * h->ny);
   std::vector<int> i0(h->ny);
   make_wavenumbers(h->nx, h->ny, h->cfg.kpi, h->cfg.lx, h->cfg.ly, kx.data(), ky.data(), i0.data());
+  make_inverse_table(h->nx, h->ny, kx.data(), ky.data(), h->cfg.rhs == TARA_RHS_SCREEN,
+                     h->cfg.lambda, inv.data());
+  int i0max = 0;
+  for (int j = 0; j < h->ny; ++j) i0max = i0[j] > i0max ? i0[j] : i0max;
+  h->grid.i0max = i0max;
+  TARA_CK(cudaMemcpyAsync(h->inv, inv.data(), inv.size() * sizeof(double), cudaMemcpyHostToDevice,
+                          h->stream));
   TARA_CK(cudaMemcpyAsync(h->kx, kx.data(), h->nh * sizeof(double), cudaMemcpyHostToDevice,
                           h->stream));
   TARA_CK(cudaMemcpyAsync(h->ky, ky.data(), h->ny * sizeof(double), cudaMemcpyHostToDevice,
@@ -273,7 +290,7 @@ int tara2d_destroy(tara2d* h) {
   if (!h) return set_ok();
   cudaSetDevice(h->dev);
   if (h->stream) cudaStreamSynchronize(h->stream);
-  void* ptrs[] = {h->w0, h->ws, h->acc, h->fold, h->fout, h->u, h->nl, h->kx, h->ky, h->i0,
+  void* ptrs[] = {h->w0, h->ws, h->acc, h->fold, h->fout, h->u, h->nl, h->kx, h->ky, h->i0, h->inv,
                   h->twx, h->twy, h->diag_part, h->diag_out, h->flag};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -328,6 +345,7 @@ int tara2d_create(const tara2d_config* cfg, tara2d** out) {
   CKC(cudaMalloc(&h->kx, h->nh * sizeof(double)));
   CKC(cudaMalloc(&h->ky, h->ny * sizeof(double)));
   CKC(cudaMalloc(&h->i0, h->ny * sizeof(int)));
+  CKC(cudaMalloc(&h->inv, (size_t)h->ny * h->nh * sizeof(double)));
   CKC(cudaMalloc(&h->diag_part, 2 * kDiagBlocks * sizeof(double)));
   CKC(cudaMalloc(&h->diag_out, 4 * sizeof(double)));
   CKC(cudaMalloc(&h->flag, sizeof(unsigned int)));
@@ -350,6 +368,7 @@ int tara2d_create(const tara2d_config* cfg, tara2d** out) {
   h->grid.kx = h->kx;
   h->grid.ky = h->ky;
   h->grid.i0 = h->i0;
+  h->grid.inv = h->inv;
   if ((rc = refresh_tables(h))) return fail(rc);
   *out = h;
   return set_ok();
