@@ -149,6 +149,70 @@ int tara2d_launches_per_step(const tara2d* h);
  * rescaled to 1/2<|u|^2> = energy with the handle's wavenumbers). */
 int tara2d_init_random(tara2d* h, double k0, double energy, uint64_t seed);
 
+/* ---- 3D compressible MHD (derive3com / ab3com) --------------------------- */
+
+/* Replaces subroutine derive3com (src/derive3com.f95:6): writes the eight
+ * d_*_k_dt_new arrays (rho, rho ux, rho uy, rho uz, E, Bx, By, Bz) from the eight
+ * state spectra; the *_old arrays and time are unused.  Arrays are complex(8)
+ * (Nh,Ny,Nz).  Lx, Ly, Lz, mu, eta, CS are read from the caller's common block
+ * /comm/ (comm_), wavenumbers use the pi argument; viscosity and resistivity are
+ * the reference's hard-coded 1/450.  The forcing the reference transforms but
+ * never uses is not computed.  Sizes: powers of two in [16, 256]. */
+void derive3com_(const int* Nx, const int* Ny, const int* Nz, const int* Nh, const double* pi,
+                 const double* time, const double* rho_k, const double* rho_ux_k,
+                 const double* rho_uy_k, const double* rho_uz_k, const double* E_k,
+                 const double* Bx_k, const double* By_k, const double* Bz_k, double* d_rho_k_dt_old,
+                 double* d_rho_k_dt_new, double* d_rho_ux_k_dt_old, double* d_rho_ux_k_dt_new,
+                 double* d_rho_uy_k_dt_old, double* d_rho_uy_k_dt_new, double* d_rho_uz_k_dt_old,
+                 double* d_rho_uz_k_dt_new, double* d_E_k_dt_old, double* d_E_k_dt_new,
+                 double* d_Bx_k_dt_old, double* d_Bx_k_dt_new, double* d_By_k_dt_old,
+                 double* d_By_k_dt_new, double* d_Bz_k_dt_old, double* d_Bz_k_dt_new);
+
+/* Replaces subroutine ab3com (src/ab3com.f95:6): AB2 into the *_new state arrays
+ * with dt from /comm/; E is carried over unchanged, as the reference leaves it. */
+void ab3com_(const int* Nx, const int* Ny, const int* Nz, const int* Nh, const double* pi,
+             const double* time, const double* rho_k, const double* rho_ux_k,
+             const double* rho_uy_k, const double* rho_uz_k, const double* E_k, const double* Bx_k,
+             const double* By_k, const double* Bz_k, double* rho_k_new, double* rho_ux_k_new,
+             double* rho_uy_k_new, double* rho_uz_k_new, double* E_k_new, double* Bx_k_new,
+             double* By_k_new, double* Bz_k_new, const double* d_rho_k_dt_old,
+             const double* d_rho_k_dt_new, const double* d_rho_ux_k_dt_old,
+             const double* d_rho_ux_k_dt_new, const double* d_rho_uy_k_dt_old,
+             const double* d_rho_uy_k_dt_new, const double* d_rho_uz_k_dt_old,
+             const double* d_rho_uz_k_dt_new, const double* d_E_k_dt_old, const double* d_E_k_dt_new,
+             const double* d_Bx_k_dt_old, const double* d_Bx_k_dt_new, const double* d_By_k_dt_old,
+             const double* d_By_k_dt_new, const double* d_Bz_k_dt_old, const double* d_Bz_k_dt_new);
+
+typedef struct tara3d_config {
+  int nx, ny, nz;      /* powers of two, 16..256 */
+  int defined;         /* 0: k^2 f / 450 as the reference; 1: nu_u k^2 u and eta_b k^2 B */
+  double kpi;          /* the pi of kx = 2*pi*(i-1)/Lx */
+  double lx, ly, lz;   /* box lengths (the reference driver uses Lx = Lx_ini * pi) */
+  double mu;           /* coefficient of E_Visc in the energy equation (ini nu) */
+  double eta;          /* resistivity in the energy flux (0.005 in the reference) */
+  double cs;           /* sound speed, P = CS^2 rho (10 in the reference) */
+  double nu_u, eta_b;  /* defined-mode viscosity and resistivity */
+  double dt;
+} tara3d_config;
+
+typedef struct tara3d tara3d;
+
+/* Reference defaults: 2*pi box, mu = 0.01, eta = 0.005, CS = 10, faithful 1/450. */
+void tara3d_default_config(tara3d_config* cfg, int nx, int ny, int nz);
+int tara3d_create(const tara3d_config* cfg, tara3d** out);
+int tara3d_destroy(tara3d* h);
+/* eight dense (Nh,Ny,Nz) complex spectra in the order rho, rho ux, rho uy, rho uz,
+ * E, Bx, By, Bz; hist8 (the AB2 history) may be NULL for zero history. */
+int tara3d_set_state(tara3d* h, const double* state8, const double* hist8);
+int tara3d_get_state(tara3d* h, double* state8, double* hist8);
+/* eight real (Nx,Ny,Nz) fields in the same order, transformed on the GPU */
+int tara3d_set_state_real(tara3d* h, const double* real8);
+/* nsteps of derive3com + ab3com + the driver's history rotation (E frozen) */
+int tara3d_step(tara3d* h, int nsteps);
+/* all eight derivatives of the current state (dense spectra), as derive3com */
+int tara3d_rhs(tara3d* h, double* d8);
+int tara3d_synchronize(tara3d* h);
+
 /* ---- standalone transforms ------------------------------------------------ */
 /* Unnormalised 2D transforms with FFTW's rank-2 r2c/c2r semantics, i.e. what
  * dfftw_plan_dft_{r2c,c2r}_2d(plan, Nx, Ny, ...) computes in the reference

@@ -49,6 +49,18 @@ def _d(v):
     return ctypes.byref(ctypes.c_double(float(v)))
 
 
+class MhdParams(ctypes.Structure):
+    """oracle_mhd_params (oracle/tara_oracle.h)."""
+    _fields_ = [("lx", ctypes.c_double), ("ly", ctypes.c_double), ("lz", ctypes.c_double),
+                ("mu", ctypes.c_double), ("eta", ctypes.c_double), ("cs", ctypes.c_double),
+                ("defined", ctypes.c_int), ("nu_u", ctypes.c_double), ("eta_b", ctypes.c_double)]
+
+
+def mhd_params(lx=2 * PI_R8, ly=2 * PI_R8, lz=2 * PI_R8, mu=0.01, eta=0.005, cs=10.0,
+               defined=0, nu_u=0.0, eta_b=0.0) -> MhdParams:
+    return MhdParams(lx, ly, lz, mu, eta, cs, defined, nu_u, eta_b)
+
+
 class Oracle:
     def __init__(self, L):
         self.L = L
@@ -64,6 +76,12 @@ class Oracle:
         L.oracle_r2c_2d.argtypes = [c_int, c_int, vp, vp]
         L.oracle_c2r_2d.argtypes = [c_int, c_int, vp, vp]
         L.oracle_set_threads.argtypes = [c_int]
+        L.oracle_r2c_3d.argtypes = [c_int, c_int, c_int, vp, vp]
+        L.oracle_c2r_3d.argtypes = [c_int, c_int, c_int, vp, vp]
+        L.oracle_derive3com.argtypes = [c_int, c_int, c_int, vp, vp, vp]
+        L.oracle_ab3com.argtypes = [c_int, c_int, c_int, c_double, vp, vp, vp, vp]
+        L.oracle_run3d.argtypes = [c_int, c_int, c_int, vp, c_double, c_int, vp, vp]
+        L.oracle_ic3d_abc.argtypes = [c_int, c_int, c_int, c_double, c_double, c_double, vp]
         self.is_fftw = bool(L.oracle_backend_is_fftw())
 
     def set_threads(self, n: int) -> None:
@@ -157,6 +175,54 @@ class Oracle:
         out = np.zeros(6)
         self.L.oracle_diag_css(2 * (nh - 1), ny, lx, ly, lam, w.ctypes.data, out.ctypes.data)
         return out
+
+    # 3D MHD: arrays are (Nz, Ny, Nh) complex / (Nz, Ny, Nx) real; a state is (8, Nz, Ny, Nh)
+    def r2c3(self, x):
+        x = np.ascontiguousarray(x, np.float64)
+        nz, ny, nx = x.shape
+        out = np.zeros((nz, ny, nx // 2 + 1), np.complex128)
+        self.L.oracle_r2c_3d(nx, ny, nz, x.ctypes.data, out.ctypes.data)
+        return out
+
+    def c2r3(self, c):
+        c = np.ascontiguousarray(c, np.complex128)
+        nz, ny, nh = c.shape
+        nx = 2 * (nh - 1)
+        out = np.zeros((nz, ny, nx), np.float64)
+        self.L.oracle_c2r_3d(nx, ny, nz, c.ctypes.data, out.ctypes.data)
+        return out
+
+    def derive3com(self, state, params):
+        state = np.ascontiguousarray(state, np.complex128)
+        _, nz, ny, nh = state.shape
+        out = np.zeros_like(state)
+        self.L.oracle_derive3com(2 * (nh - 1), ny, nz, ctypes.addressof(params), state.ctypes.data,
+                                 out.ctypes.data)
+        return out
+
+    def ab3com(self, state, d_old, d_new, dt):
+        state, d_old, d_new = (np.ascontiguousarray(a, np.complex128) for a in (state, d_old, d_new))
+        _, nz, ny, nh = state.shape
+        out = np.zeros_like(state)
+        self.L.oracle_ab3com(2 * (nh - 1), ny, nz, dt, state.ctypes.data, out.ctypes.data,
+                             d_old.ctypes.data, d_new.ctypes.data)
+        return out
+
+    def run3d(self, state, params, dt, steps, hist=None):
+        st = np.ascontiguousarray(state, np.complex128).copy()
+        h = np.zeros_like(st) if hist is None else np.ascontiguousarray(hist, np.complex128).copy()
+        _, nz, ny, nh = st.shape
+        self.L.oracle_run3d(2 * (nh - 1), ny, nz, ctypes.addressof(params), dt, int(steps),
+                            st.ctypes.data, h.ctypes.data)
+        return st, h
+
+    def ic3d_abc(self, nx, ny, nz, l_ini=2.0):
+        out = np.zeros((8, nz, ny, nx), np.float64)
+        self.L.oracle_ic3d_abc(nx, ny, nz, l_ini, l_ini, l_ini, out.ctypes.data)
+        return out
+
+    def state_from_real(self, real8):
+        return np.stack([self.r2c3(f) for f in real8])
 
     def philox(self, ctr, key):
         out = (ctypes.c_uint32 * 4)()

@@ -76,6 +76,22 @@ void oracle_c2r_2d(int nx, int ny, const double* in, double* out) {
   fftw_destroy_plan(p);
   free(tmp);
 }
+/* dfftw_plan_dft_{r2c,c2r}_3d_(plan, Nx, Ny, Nz, ...) -> dims (Nz, Ny, Nx) in C order */
+void oracle_r2c_3d(int nx, int ny, int nz, const double* in, double* out) {
+  fftw_plan p = fftw_plan_dft_r2c_3d(nz, ny, nx, (double*)in, (fftw_complex*)out, FFTW_ESTIMATE);
+  fftw_execute(p);
+  fftw_destroy_plan(p);
+}
+
+void oracle_c2r_3d(int nx, int ny, int nz, const double* in, double* out) {
+  const size_t ns = (size_t)(nx / 2 + 1) * ny * nz;
+  double* tmp = (double*)xcalloc(2 * ns, sizeof(double));
+  memcpy(tmp, in, 2 * ns * sizeof(double));
+  fftw_plan p = fftw_plan_dft_c2r_3d(nz, ny, nx, (fftw_complex*)tmp, out, FFTW_ESTIMATE);
+  fftw_execute(p);
+  fftw_destroy_plan(p);
+  free(tmp);
+}
 #else
 int oracle_backend_is_fftw(void) { return 0; }
 
@@ -242,6 +258,107 @@ void oracle_r2c_2d(int nx, int ny, const double* in, double* out) {
     }
     free(col);
   }
+}
+
+/* strided complex transforms of all lines along one axis of a (nh, ny, nz) array */
+static void lines_fft(double* a, int nlines_outer, int nlines_inner, size_t outer_stride,
+                      size_t inner_stride, int n, size_t point_stride, int sign) {
+  const fft_plan* p = get_plan(n);
+#pragma omp parallel num_threads(oracle_get_threads())
+  {
+    double* col = (double*)xcalloc(2 * (size_t)n, sizeof(double));
+#pragma omp for collapse(2) schedule(static)
+    for (int o = 0; o < nlines_outer; ++o)
+      for (int i = 0; i < nlines_inner; ++i) {
+        double* base = a + 2 * ((size_t)o * outer_stride + (size_t)i * inner_stride);
+        for (int q = 0; q < n; ++q) {
+          col[2 * q] = base[2 * q * point_stride];
+          col[2 * q + 1] = base[2 * q * point_stride + 1];
+        }
+        fft1d(col, n, sign, p);
+        for (int q = 0; q < n; ++q) {
+          base[2 * q * point_stride] = col[2 * q];
+          base[2 * q * point_stride + 1] = col[2 * q + 1];
+        }
+      }
+    free(col);
+  }
+}
+
+/* rank-3 c2r: complex DFTs along z and y for all Nh columns, then the 1D c2r
+ * along x reading only the real parts of the kx = 0 and kx = Nx/2 bins. */
+void oracle_c2r_3d(int nx, int ny, int nz, const double* in, double* out) {
+  const int nh = nx / 2 + 1;
+  const size_t ns = (size_t)nh * ny * nz;
+  double* tmp = (double*)xcalloc(2 * ns, sizeof(double));
+  memcpy(tmp, in, 2 * ns * sizeof(double));
+  lines_fft(tmp, ny, nh, nh, 1, nz, (size_t)nh * ny, +1);       /* z */
+  lines_fft(tmp, nz, nh, (size_t)nh * ny, 1, ny, (size_t)nh, +1); /* y */
+  /* x rows as pairs through the 2D row code: rows r = k*ny + j */
+  const int rows = ny * nz;
+  const fft_plan* px = get_plan(nx);
+#pragma omp parallel num_threads(oracle_get_threads())
+  {
+    double* z = (double*)xcalloc(2 * (size_t)nx, sizeof(double));
+#pragma omp for schedule(static)
+    for (int r = 0; r < rows; r += 2) {
+      const double* a = tmp + 2 * (size_t)r * nh;
+      const double* b = (r + 1 < rows) ? tmp + 2 * (size_t)(r + 1) * nh : NULL;
+      for (int k = 0; k <= nx / 2; ++k) {
+        const int edge = (k == 0 || k == nx / 2);
+        const double ar = a[2 * k], ai = edge ? 0.0 : a[2 * k + 1];
+        const double br = b ? b[2 * k] : 0.0, bi = (b && !edge) ? b[2 * k + 1] : 0.0;
+        z[2 * k] = ar - bi;
+        z[2 * k + 1] = ai + br;
+        if (k > 0 && k < nx / 2) {
+          z[2 * (nx - k)] = ar + bi;
+          z[2 * (nx - k) + 1] = -ai + br;
+        }
+      }
+      fft1d(z, nx, +1, px);
+      for (int x = 0; x < nx; ++x) {
+        out[(size_t)r * nx + x] = z[2 * x];
+        if (b) out[(size_t)(r + 1) * nx + x] = z[2 * x + 1];
+      }
+    }
+    free(z);
+  }
+  free(tmp);
+}
+
+void oracle_r2c_3d(int nx, int ny, int nz, const double* in, double* out) {
+  const int nh = nx / 2 + 1;
+  const int rows = ny * nz;
+  const fft_plan* px = get_plan(nx);
+#pragma omp parallel num_threads(oracle_get_threads())
+  {
+    double* z = (double*)xcalloc(2 * (size_t)nx, sizeof(double));
+#pragma omp for schedule(static)
+    for (int r = 0; r < rows; r += 2) {
+      const int two = (r + 1 < rows);
+      for (int x = 0; x < nx; ++x) {
+        z[2 * x] = in[(size_t)r * nx + x];
+        z[2 * x + 1] = two ? in[(size_t)(r + 1) * nx + x] : 0.0;
+      }
+      fft1d(z, nx, -1, px);
+      double* a = out + 2 * (size_t)r * nh;
+      double* b = two ? out + 2 * (size_t)(r + 1) * nh : NULL;
+      for (int k = 0; k <= nx / 2; ++k) {
+        const int m = (nx - k) % nx;
+        const double zr = z[2 * k], zi = z[2 * k + 1];
+        const double mr = z[2 * m], mi = -z[2 * m + 1];
+        a[2 * k] = 0.5 * (zr + mr);
+        a[2 * k + 1] = 0.5 * (zi + mi);
+        if (b) {
+          b[2 * k] = 0.5 * (zi - mi);
+          b[2 * k + 1] = -0.5 * (zr - mr);
+        }
+      }
+    }
+    free(z);
+  }
+  lines_fft(out, nz, nh, (size_t)nh * ny, 1, ny, (size_t)nh, -1); /* y */
+  lines_fft(out, ny, nh, nh, 1, nz, (size_t)nh * ny, -1);         /* z */
 }
 #endif
 
@@ -718,4 +835,239 @@ void oracle_diag_css(int nx, int ny, double lx, double ly, double lambda, const 
   }
   out[0] = e; out[1] = ye; out[2] = c0; out[3] = c1; out[4] = c2; out[5] = c3;
   free(wd); free(ukx); free(uky); free(om); free(ux); free(uy);
+}
+
+/* ------------------------------------------------------------------------- */
+/* 3D compressible MHD -- src/derive3com.f95, src/ab3com.f95                  */
+/* ------------------------------------------------------------------------- */
+enum { F_RHO = 0, F_RUX, F_RUY, F_RUZ, F_E, F_BX, F_BY, F_BZ, NF3 };
+
+/* kx = 2.0d0*pi*dfloat(i-1)/Lx, ky/kz with (j-1)-Ny above Ny/2 (derive3com.f95:213-215) */
+static double k3_of(int i0, int n, double pi, double l, int signed_) {
+  if (!signed_ || i0 < n / 2) return 2.0 * pi * (double)i0 / l;
+  return 2.0 * pi * (double)(i0 - n) / l;
+}
+
+void oracle_derive3com(int nx, int ny, int nz, const oracle_mhd_params* p, const double* state,
+                       double* dstate) {
+  const int nh = nx / 2 + 1;
+  const size_t ns = (size_t)nh * ny * nz, nr = (size_t)nx * ny * nz;
+  const double pi = PI_R8;
+  const double nn = (double)nx * (double)ny * (double)nz;
+  const double* sk[NF3];
+  for (int f = 0; f < NF3; ++f) sk[f] = state + 2 * ns * f;
+  /* eight c2r of the state (:73-135), normalised (:147-159) */
+  double* rl[NF3];
+  for (int f = 0; f < NF3; ++f) {
+    rl[f] = (double*)xcalloc(nr, sizeof(double));
+    oracle_c2r_3d(nx, ny, nz, sk[f], rl[f]);
+    for (size_t r = 0; r < nr; ++r) rl[f][r] = rl[f][r] / nn;
+  }
+  double *ux = (double*)xcalloc(nr, sizeof(double)), *uy = (double*)xcalloc(nr, sizeof(double)),
+         *uz = (double*)xcalloc(nr, sizeof(double)), *b2 = (double*)xcalloc(nr, sizeof(double));
+  for (size_t r = 0; r < nr; ++r) { /* :162-175 */
+    const double rho = rl[F_RHO][r];
+    ux[r] = rl[F_RUX][r] / rho;
+    uy[r] = rl[F_RUY][r] / rho;
+    uz[r] = rl[F_RUZ][r] / rho;
+    b2[r] = rl[F_BX][r] * rl[F_BX][r] + rl[F_BY][r] * rl[F_BY][r] + rl[F_BZ][r] * rl[F_BZ][r];
+  }
+  /* velocity spectra (:201-217) */
+  double* uk[3];
+  double* ur[3] = {ux, uy, uz};
+  for (int c = 0; c < 3; ++c) {
+    uk[c] = (double*)xcalloc(2 * ns, sizeof(double));
+    oracle_r2c_3d(nx, ny, nz, ur[c], uk[c]);
+  }
+  /* first derivatives (:224-298): i kx ux, i ky uy, i kz uz, i ky Bx, i kz Bx,
+   * i kx By, i kz By, i kx Bz, i ky Bz */
+  enum { D_UXX, D_UYY, D_UZZ, D_BXY, D_BXZ, D_BYX, D_BYZ, D_BZX, D_BZY, ND };
+  double* dk[ND];
+  for (int d = 0; d < ND; ++d) dk[d] = (double*)xcalloc(2 * ns, sizeof(double));
+  for (int k = 0; k < nz; ++k) {
+    const double kz = k3_of(k, nz, pi, p->lz, 1);
+    for (int j = 0; j < ny; ++j) {
+      const double ky = k3_of(j, ny, pi, p->ly, 1);
+      for (int i = 0; i < nh; ++i) {
+        const double kx = k3_of(i, nx, pi, p->lx, 0);
+        const size_t q = 2 * (((size_t)k * ny + j) * nh + i);
+#define IK(dst, kk, src) do { dk[dst][q] = -(kk) * (src)[q + 1]; dk[dst][q + 1] = (kk) * (src)[q]; } while (0)
+        IK(D_UXX, kx, uk[0]); IK(D_UYY, ky, uk[1]); IK(D_UZZ, kz, uk[2]);
+        IK(D_BXY, ky, sk[F_BX]); IK(D_BXZ, kz, sk[F_BX]);
+        IK(D_BYX, kx, sk[F_BY]); IK(D_BYZ, kz, sk[F_BY]);
+        IK(D_BZX, kx, sk[F_BZ]); IK(D_BZY, ky, sk[F_BZ]);
+#undef IK
+      }
+    }
+  }
+  double* dr[ND];
+  for (int d = 0; d < ND; ++d) {
+    dr[d] = (double*)xcalloc(nr, sizeof(double));
+    oracle_c2r_3d(nx, ny, nz, dk[d], dr[d]); /* :300-352 */
+    for (size_t r = 0; r < nr; ++r) dr[d][r] = dr[d][r] / nn;
+  }
+  /* fluxes (:363-436) */
+  enum { M_X1, M_X2, M_X3, M_Y1, M_Y2, M_Y3, M_Z1, M_Z2, M_Z3, EN_X, EN_Y, EN_Z, E_VISC,
+         MG_X1, MG_X2, MG_Y1, MG_Y2, MG_Z1, MG_Z2, NFL };
+  double* fl[NFL];
+  for (int f = 0; f < NFL; ++f) fl[f] = (double*)xcalloc(nr, sizeof(double));
+  const double eta = p->eta, cs = p->cs;
+  for (size_t r = 0; r < nr; ++r) {
+    const double rho = rl[F_RHO][r], rux = rl[F_RUX][r], ruy = rl[F_RUY][r], ruz = rl[F_RUZ][r];
+    const double E = rl[F_E][r], bx = rl[F_BX][r], by = rl[F_BY][r], bz = rl[F_BZ][r];
+    const double vx = ux[r], vy = uy[r], vz = uz[r], B2 = b2[r];
+    const double cx = dr[D_BZY][r] - dr[D_BYZ][r]; /* curl_x_B */
+    const double cy = dr[D_BZX][r] - dr[D_BXZ][r]; /* curl_y_B as the reference defines it */
+    const double cz = dr[D_BYX][r] - dr[D_BXY][r]; /* curl_z_B */
+    const double P = cs * cs * rho;
+    fl[M_X1][r] = rux * vx + P + B2 / 2.0 - bx * bx;
+    fl[M_X2][r] = rux * vy - bx * by;
+    fl[M_X3][r] = rux * vz - bx * bz;
+    fl[M_Y1][r] = rux * vy - bx * by;
+    fl[M_Y2][r] = ruy * vy + P + B2 / 2.0 - by * by;
+    fl[M_Y3][r] = ruy * vz - by * bz;
+    fl[M_Z1][r] = ruz * vx - bz * bx;
+    fl[M_Z2][r] = ruz * vy - bz * by;
+    fl[M_Z3][r] = ruz * vz + P + B2 / 2.0 - bz * bz;
+    fl[EN_X][r] = (E + P + B2 / 2.0) * vx - vx * bx * bx - vy * bx * by - vz * bx * bz -
+                  eta * (by * cz + bz * cy);
+    fl[EN_Y][r] = (E + P + B2 / 2.0) * vy - vx * bx * by - vy * by * by - vz * by * bz +
+                  eta * (bx * cz - bz * cx);
+    fl[EN_Z][r] = (E + P + B2 / 2.0) * vz - vx * bz * bx - vy * bz * by - vz * bz * bz +
+                  eta * (bx * cy + by * cx);
+    const double dv = dr[D_UXX][r] + dr[D_UYY][r] + dr[D_UZZ][r];
+    fl[E_VISC][r] = dv * dv;
+    fl[MG_X1][r] = vx * by - vy * bx;
+    fl[MG_X2][r] = vx * bz - vz * bx;
+    fl[MG_Y1][r] = vx * by - vy * bx;
+    fl[MG_Y2][r] = vy * bz - vz * by;
+    fl[MG_Z1][r] = vx * bz - vz * bx;
+    fl[MG_Z2][r] = vy * bz - vz * by;
+  }
+  double* fk[NFL];
+  for (int f = 0; f < NFL; ++f) {
+    fk[f] = (double*)xcalloc(2 * ns, sizeof(double));
+    oracle_r2c_3d(nx, ny, nz, fl[f], fk[f]); /* :444-556 */
+  }
+  /* spectral derivatives, the |k| >= (Nx+Ny+Nz)/9 sphere and the assembly
+   * (:561-1043) */
+  const double cut = ((double)(nx + ny + nz) / 3.0) / 3.0 + 0;
+  for (int k = 0; k < nz; ++k) {
+    const double kz = k3_of(k, nz, pi, p->lz, 1);
+    for (int j = 0; j < ny; ++j) {
+      const double ky = k3_of(j, ny, pi, p->ly, 1);
+      for (int i = 0; i < nh; ++i) {
+        const double kx = k3_of(i, nx, pi, p->lx, 0);
+        const size_t q = 2 * (((size_t)k * ny + j) * nh + i);
+        const int keep = !(sqrt(kx * kx + ky * ky + kz * kz) >= cut);
+        double out[NF3][2];
+        for (int c = 0; c < 2; ++c) { /* c = 0 real part, 1 imaginary part */
+          /* i k f: real = -k*Im f, imag = k*Re f */
+#define IKC(kk, f) ((c == 0) ? -(kk) * (f)[q + 1] : (kk) * (f)[q])
+#define K2(kk, f) ((kk) * (kk) * (f)[q + c])
+          if (!keep) {
+            for (int f = 0; f < NF3; ++f) out[f][c] = 0.0;
+            continue;
+          }
+          const double drho = -(IKC(kx, sk[F_RUX]) + IKC(ky, sk[F_RUY]) + IKC(kz, sk[F_RUZ]));
+          const double lux = K2(kx, uk[0]) + K2(ky, uk[0]) + K2(kz, uk[0]);
+          const double luy = K2(kx, uk[1]) + K2(ky, uk[1]) + K2(kz, uk[1]);
+          const double luz = K2(kx, uk[2]) + K2(ky, uk[2]) + K2(kz, uk[2]);
+          const double lbx = K2(kx, sk[F_BX]) + K2(ky, sk[F_BX]) + K2(kz, sk[F_BX]);
+          const double lby = K2(kx, sk[F_BY]) + K2(ky, sk[F_BY]) + K2(kz, sk[F_BY]);
+          const double lbz = K2(kx, sk[F_BZ]) + K2(ky, sk[F_BZ]) + K2(kz, sk[F_BZ]);
+          const double vux = p->defined ? p->nu_u * lux : lux / 450.0;
+          const double vuy = p->defined ? p->nu_u * luy : luy / 450.0;
+          const double vuz = p->defined ? p->nu_u * luz : luz / 450.0;
+          const double vbx = p->defined ? p->eta_b * lbx : lbx / 450.0;
+          const double vby = p->defined ? p->eta_b * lby : lby / 450.0;
+          const double vbz = p->defined ? p->eta_b * lbz : lbz / 450.0;
+          out[F_RHO][c] = drho;
+          out[F_RUX][c] = -(IKC(kx, fk[M_X1]) + IKC(ky, fk[M_X2]) + IKC(kz, fk[M_X3])) - vux;
+          out[F_RUY][c] = -(IKC(kx, fk[M_Y1]) + IKC(ky, fk[M_Y2]) + IKC(kz, fk[M_Y3])) - vuy;
+          out[F_RUZ][c] = -(IKC(kx, fk[M_Z1]) + IKC(ky, fk[M_Z2]) + IKC(kz, fk[M_Z3])) - vuz;
+          out[F_E][c] = -(IKC(kx, fk[EN_X]) + IKC(ky, fk[EN_Y]) + IKC(kz, fk[EN_Z])) +
+                        p->mu * fk[E_VISC][q + c];
+          out[F_BX][c] = +(IKC(ky, fk[MG_X1]) + IKC(kz, fk[MG_X2])) - vbx;
+          out[F_BY][c] = -(IKC(kx, fk[MG_Y1]) - IKC(kz, fk[MG_Y2])) - vby;
+          out[F_BZ][c] = -(IKC(kx, fk[MG_Z1]) + IKC(ky, fk[MG_Z2])) - vbz;
+#undef IKC
+#undef K2
+        }
+        for (int f = 0; f < NF3; ++f) {
+          dstate[2 * ns * f + q] = out[f][0];
+          dstate[2 * ns * f + q + 1] = out[f][1];
+        }
+      }
+    }
+  }
+  for (int f = 0; f < NF3; ++f) free(rl[f]);
+  free(ux); free(uy); free(uz); free(b2);
+  for (int c = 0; c < 3; ++c) free(uk[c]);
+  for (int d = 0; d < ND; ++d) { free(dk[d]); free(dr[d]); }
+  for (int f = 0; f < NFL; ++f) { free(fl[f]); free(fk[f]); }
+}
+
+void oracle_ab3com(int nx, int ny, int nz, double dt, const double* state, double* state_new,
+                   const double* d_old, const double* d_new) {
+  const size_t n2 = 2 * (size_t)(nx / 2 + 1) * ny * nz;
+  for (int f = 0; f < NF3; ++f) {
+    const size_t o = n2 * f;
+    for (size_t q = 0; q < n2; ++q)
+      state_new[o + q] = (f == F_E) ? state[o + q] /* E_k_new = E_k (:51) */
+                                    : state[o + q] + ((3.0 / 2.0) * d_new[o + q] -
+                                                      (1.0 / 2.0) * d_old[o + q]) * dt;
+  }
+}
+
+void oracle_run3d(int nx, int ny, int nz, const oracle_mhd_params* p, double dt, int nsteps,
+                  double* state, double* hist) {
+  const size_t n = 2 * (size_t)(nx / 2 + 1) * ny * nz * NF3;
+  double* dn = (double*)xcalloc(n, sizeof(double));
+  double* sn = (double*)xcalloc(n, sizeof(double));
+  for (int s = 0; s < nsteps; ++s) {
+    oracle_derive3com(nx, ny, nz, p, state, dn);
+    oracle_ab3com(nx, ny, nz, dt, state, sn, hist, dn);
+    memcpy(hist, dn, n * sizeof(double));
+    memcpy(state, sn, n * sizeof(double));
+  }
+  free(dn); free(sn);
+}
+
+/* src/main3com.f95:202-347 with U0 = 0.1, A = B = C = kf = 1, B0 = 0.1, P0 = 1 */
+void oracle_ic3d_abc(int nx, int ny, int nz, double lx_ini, double ly_ini, double lz_ini,
+                     double* real8) {
+  const double pi = PI_R8;
+  const double lx = lx_ini * pi, ly = ly_ini * pi, lz = lz_ini * pi;
+  const double dx = lx / (double)nx, dy = ly / (double)ny, dz = lz / (double)nz;
+  const double U0 = 0.10, A = 1.0, B = 1.0, C = 1.0, kf = 1.0, M = 0.10, MA = 1.0;
+  const double rho0 = 1.0, P0 = 1.0, mu_0 = 1.0;
+  (void)M;
+  const double VA = U0 / MA, B0 = VA * sqrt(mu_0 * rho0);
+  const size_t nr = (size_t)nx * ny * nz;
+  for (int i = 0; i < nx; ++i) {
+    const double x = 0.0 + (double)(float)i * dx;
+    for (int j = 0; j < ny; ++j) {
+      const double y = 0.0 + (double)(float)j * dy;
+      for (int k = 0; k < nz; ++k) {
+        const double z = 0.0 + (double)(float)k * dz;
+        const size_t r = ((size_t)k * ny + j) * nx + i;
+        const double rho = rho0;
+        const double vx = U0 * (A * sin(kf * z) + C * cos(kf * y));
+        const double vy = U0 * (B * sin(kf * x) + A * cos(kf * z));
+        const double vz = U0 * (C * sin(kf * y) + B * cos(kf * x));
+        const double P = P0, bx = B0, by = B0, bz = B0;
+        const double E = P + 0.50 * rho * (vx * vx + vy * vy + vz * vz) +
+                         0.50 * (bx * bx + by * by + bz * bz);
+        real8[nr * F_RHO + r] = rho;
+        real8[nr * F_RUX + r] = rho * vx;
+        real8[nr * F_RUY + r] = rho * vy;
+        real8[nr * F_RUZ + r] = rho * vz;
+        real8[nr * F_E + r] = E;
+        real8[nr * F_BX + r] = bx;
+        real8[nr * F_BY + r] = by;
+        real8[nr * F_BZ + r] = bz;
+      }
+    }
+  }
 }

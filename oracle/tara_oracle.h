@@ -92,6 +92,37 @@ void oracle_energy_enstrophy(int nx, int ny, double lx, double ly, const double*
 void oracle_diag_css(int nx, int ny, double lx, double ly, double lambda, const double* omegak,
                      double* out);
 
+/* ---- 3D compressible MHD (src/derive3com.f95, src/ab3com.f95) ---------- */
+/* Half spectra are (Nh,Ny,Nz) complex(8), x fastest; real fields (Nx,Ny,Nz).
+ * The state is 8 consecutive half spectra in the order of the reference's
+ * arguments: rho, rho_ux, rho_uy, rho_uz, E, Bx, By, Bz. */
+typedef struct oracle_mhd_params {
+  double lx, ly, lz; /* true box lengths (Lx = Lx_ini*pi, src/main3com.f95) */
+  double mu;         /* coefficient of E_Visc in the energy equation (ini nu) */
+  double eta;        /* resistivity in the energy flux (0.005 in the reference) */
+  double cs;         /* sound speed, P = CS^2 rho (CS = 1/M = 10) */
+  int defined;       /* 0: viscous/resistive terms k^2 f / 450 (faithful);
+                        1: nu_u k^2 u and eta_b k^2 B (defined mode) */
+  double nu_u, eta_b;
+} oracle_mhd_params;
+
+void oracle_r2c_3d(int nx, int ny, int nz, const double* in, double* out);
+void oracle_c2r_3d(int nx, int ny, int nz, const double* in, double* out);
+/* src/derive3com.f95:6-1047 (the forcing, computed but unused there, is left out) */
+void oracle_derive3com(int nx, int ny, int nz, const oracle_mhd_params* p, const double* state,
+                       double* dstate);
+/* src/ab3com.f95:6-66: AB2 for all fields except E, which stays frozen (:51) */
+void oracle_ab3com(int nx, int ny, int nz, double dt, const double* state, double* state_new,
+                   const double* d_old, const double* d_new);
+/* derive3com + ab3com + the rotation of src/main3com.f95:560-614, nsteps times */
+void oracle_run3d(int nx, int ny, int nz, const oracle_mhd_params* p, double dt, int nsteps,
+                  double* state, double* hist);
+/* Reference initial condition (src/main3com.f95:292-347): rho=1, ABC flow of
+ * amplitude U0=0.1 (A=B=C=kf=1), uniform B = B0 = 0.1, P = 1, E from them; real
+ * fields in the state order. */
+void oracle_ic3d_abc(int nx, int ny, int nz, double lx_ini, double ly_ini, double lz_ini,
+                     double* real8);
+
 #ifdef __cplusplus
 }
 #endif

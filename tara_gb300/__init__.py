@@ -47,6 +47,23 @@ class Config2D(ctypes.Structure):
     ]
 
 
+class Config3D(ctypes.Structure):
+    _fields_ = [
+        ("nx", ctypes.c_int), ("ny", ctypes.c_int), ("nz", ctypes.c_int), ("defined", ctypes.c_int),
+        ("kpi", ctypes.c_double), ("lx", ctypes.c_double), ("ly", ctypes.c_double),
+        ("lz", ctypes.c_double), ("mu", ctypes.c_double), ("eta", ctypes.c_double),
+        ("cs", ctypes.c_double), ("nu_u", ctypes.c_double), ("eta_b", ctypes.c_double),
+        ("dt", ctypes.c_double),
+    ]
+
+
+class MhdCommon(ctypes.Structure):
+    """The reference's common block /comm/ (src/derive3com.f95:62) as libtara sees it."""
+    _fields_ = [("iret", ctypes.c_int32), ("thread_num", ctypes.c_int32)] + [
+        (n, ctypes.c_double) for n in ("time_max", "Lx", "Ly", "Lz", "dx", "dy", "dz", "spheat",
+                                       "mu", "ms", "CS", "mu_0", "eta", "dt", "kf")]
+
+
 _lib = None
 
 
@@ -98,6 +115,21 @@ def _declare(L: ctypes.CDLL) -> None:
     L.tara2d_launches_per_step.argtypes = [vp]
     L.tara2d_init_random.argtypes = [vp, c_double, c_double, ctypes.c_uint64]
     L.tara_derive2csh_noalloc.argtypes = [c_int, c_int, c_double, vp, vp, vp]
+    c3p = ctypes.POINTER(Config3D)
+    L.tara3d_default_config.argtypes = [c3p, c_int, c_int, c_int]
+    L.tara3d_default_config.restype = None
+    L.tara3d_create.argtypes = [c3p, ctypes.POINTER(vp)]
+    L.tara3d_destroy.argtypes = [vp]
+    L.tara3d_set_state.argtypes = [vp, vp, vp]
+    L.tara3d_get_state.argtypes = [vp, vp, vp]
+    L.tara3d_set_state_real.argtypes = [vp, vp]
+    L.tara3d_step.argtypes = [vp, c_int]
+    L.tara3d_rhs.argtypes = [vp, vp]
+    L.tara3d_synchronize.argtypes = [vp]
+    L.derive3com_.argtypes = [ip] * 4 + [dp] * 2 + [vp] * 24
+    L.derive3com_.restype = None
+    L.ab3com_.argtypes = [ip] * 4 + [dp] * 2 + [vp] * 32
+    L.ab3com_.restype = None
     L.tara_fft2d_r2c.argtypes = [c_int, c_int, c_int, dp, dp]
     L.tara_fft2d_c2r.argtypes = [c_int, c_int, c_int, dp, dp]
 
@@ -319,3 +351,108 @@ class Solver2D:
 
     def init_random(self, k0: float, energy: float, seed: int) -> None:
         _check(lib().tara2d_init_random(self._h, k0, energy, seed))
+
+
+# ---------------------------------------------------------------------------
+# 3D compressible MHD
+# ---------------------------------------------------------------------------
+def mhd_common() -> MhdCommon:
+    """libtara's view of the Fortran common block /comm/ (read by derive3com_/ab3com_)."""
+    return MhdCommon.in_dll(lib(), "comm_")
+
+
+def _state8(a) -> np.ndarray:
+    a = np.ascontiguousarray(a, dtype=np.complex128)
+    if a.ndim != 4 or a.shape[0] != 8:
+        raise ValueError("expected an (8, Nz, Ny, Nh) state")
+    return a
+
+
+def derive3com(state, pi: float = 3.14159265358979323846, time: float = 0.0) -> np.ndarray:
+    """subroutine derive3com (src/derive3com.f95:6): the eight d_*_k_dt_new arrays."""
+    st = _state8(state)
+    _, nz, ny, nh = st.shape
+    out = np.zeros_like(st)
+    old = np.zeros_like(st[0])
+    args = []
+    for f in range(8):
+        args += [old.ctypes.data, out[f].ctypes.data]
+    lib().derive3com_(*_ints(2 * (nh - 1), ny, nz, nh), *_dbls(pi, time),
+                      *[st[f].ctypes.data for f in range(8)], *args)
+    _check(lib().tara_last_error())
+    return out
+
+
+def ab3com(state, d_old, d_new, pi: float = 3.14159265358979323846, time: float = 0.0):
+    """subroutine ab3com (src/ab3com.f95:6): the eight *_k_new arrays (dt from /comm/)."""
+    st, do, dn = _state8(state), _state8(d_old), _state8(d_new)
+    _, nz, ny, nh = st.shape
+    out = np.zeros_like(st)
+    pairs = []
+    for f in range(8):
+        pairs += [do[f].ctypes.data, dn[f].ctypes.data]
+    lib().ab3com_(*_ints(2 * (nh - 1), ny, nz, nh), *_dbls(pi, time),
+                  *[st[f].ctypes.data for f in range(8)], *[out[f].ctypes.data for f in range(8)],
+                  *pairs)
+    _check(lib().tara_last_error())
+    return out
+
+
+class Solver3D:
+    """Device-resident 3D MHD state (tara3d handle)."""
+
+    def __init__(self, nx: int, ny: int | None = None, nz: int | None = None, **kw):
+        ny = nx if ny is None else ny
+        nz = nx if nz is None else nz
+        cfg = Config3D()
+        lib().tara3d_default_config(ctypes.byref(cfg), nx, ny, nz)
+        for k, v in kw.items():
+            setattr(cfg, k, v)
+        h = ctypes.c_void_p()
+        _check(lib().tara3d_create(ctypes.byref(cfg), ctypes.byref(h)))
+        self._h = h
+        self.shape = (nz, ny, nx // 2 + 1)
+        self.cfg = cfg
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().tara3d_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def set_state(self, state, hist=None):
+        st = _state8(state)
+        h = None if hist is None else _state8(hist)
+        _check(lib().tara3d_set_state(self._h, st.ctypes.data, None if h is None else h.ctypes.data))
+
+    def set_state_real(self, real8):
+        r = np.ascontiguousarray(real8, dtype=np.float64)
+        _check(lib().tara3d_set_state_real(self._h, r.ctypes.data))
+
+    def get_state(self, with_history: bool = False):
+        st = np.zeros((8,) + self.shape, np.complex128)
+        h = np.zeros_like(st) if with_history else None
+        _check(lib().tara3d_get_state(self._h, st.ctypes.data, None if h is None else h.ctypes.data))
+        return (st, h) if with_history else st
+
+    def step(self, n: int = 1):
+        _check(lib().tara3d_step(self._h, int(n)))
+
+    def rhs(self):
+        out = np.zeros((8,) + self.shape, np.complex128)
+        _check(lib().tara3d_rhs(self._h, out.ctypes.data))
+        return out
+
+    def synchronize(self):
+        _check(lib().tara3d_synchronize(self._h))

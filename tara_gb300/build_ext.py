@@ -21,7 +21,7 @@ LIB = PKG / "libtara.so"
 ORACLE = ROOT / "oracle"
 REFERENCE = Path(os.environ.get("TARA_REFERENCE", "/root/reference"))
 
-SOURCES = ["launch_fp64.cu", "launch_fp32.cu", "solver2d.cu", "capi.cu", "noalloc.cu"]
+SOURCES = ["launch_fp64.cu", "launch_fp32.cu", "solver2d.cu", "capi.cu", "noalloc.cu", "mhd3d.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + [
     "-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",

@@ -68,5 +68,23 @@ def main() -> None:
     print(f"wrote {OUT} ({OUT.stat().st_size} bytes, {len(g)} arrays)")
 
 
+
+
+def main3d() -> None:
+    """tests/golden/golden3d.npz: the 3D MHD path at 16^3 from the FFTW oracle
+    (reference initial condition of src/main3com.f95:292-347, faithful 1/450)."""
+    O = orc.load(fftw=True)
+    out = Path(__file__).resolve().parent / "golden3d.npz"
+    real = O.ic3d_abc(16, 16, 16)
+    state = O.state_from_real(real)
+    p = orc.mhd_params()
+    g = {"state0": state, "derive_faithful": O.derive3com(state, p)}
+    st, h = O.run3d(state, p, 1e-3, 5)
+    g["ab2_5"] = st
+    np.savez_compressed(out, **g)
+    print(f"wrote {out} ({out.stat().st_size} bytes)")
+
+
 if __name__ == "__main__":
     main()
+    main3d()
