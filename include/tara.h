@@ -144,6 +144,22 @@ void* tara2d_stream(tara2d* h);
 /* Number of kernel launches a single step issues (for launch accounting). */
 int tara2d_launches_per_step(const tara2d* h);
 
+/* Driver diagnostics in the reference's form.  Wavenumbers kx = 2*kpi*i/lx
+ * (the drivers use the true pi and Lx = Lx_ini*pi); screened != 0 applies the
+ * screened driver's psi = omega/(k^2+lambda) on the ky >= 0 half only
+ * (src/main2css.f95:215 vs :226), screened = 0 the plain driver's psi = omega/k^2. */
+typedef struct tara2d_diag_params {
+  double kpi, lx, ly, lambda;
+  int screened;
+} tara2d_diag_params;
+/* usq = sum over the grid of ux^2+uy^2 and uysq = sum of uy^2, with u from c2r
+ * divided by Nx*Ny (src/main2css.f95:253-259 "Energy" and its uy part). */
+int tara2d_diag_reference(tara2d* h, const tara2d_diag_params* dp, double* usq, double* uysq);
+/* Real (Nx,Ny) fields psi, omega (k^2 psi when screened), ux, uy of the current
+ * state, normalised as the drivers normalise them; any pointer may be NULL. */
+int tara2d_real_fields(tara2d* h, const tara2d_diag_params* dp, double* psi, double* omega,
+                       double* ux, double* uy);
+
 /* Seeded random-phase initial spectrum (Philox4x32-10, E(k) ~ k^4 exp(-(k/k0)^2),
  * Hermitian-projected on the GPU by a c2r/r2c round trip, mean mode zeroed,
  * rescaled to 1/2<|u|^2> = energy with the handle's wavenumbers). */
@@ -212,6 +228,32 @@ int tara3d_step(tara3d* h, int nsteps);
 /* all eight derivatives of the current state (dense spectra), as derive3com */
 int tara3d_rhs(tara3d* h, double* d8);
 int tara3d_synchronize(tara3d* h);
+/* The first columns of the reference's 3D Energy.dat (src/main3com.f95:1024-1070)
+ * for the current state: out4 = {Pressure = <CS^2 rho>, Energy = <|u|^2>/2,
+ * T_Energy = <E>, B_Field = <|B|^2>/2}, u = (rho u)/rho in real space. */
+int tara3d_diag(tara3d* h, double* out4);
+
+/* ---- input.ini driver ----------------------------------------------------- */
+
+/* Runs the solver an input.ini selects, as the reference's program TARA2D does
+ * (src/main.f95:24-89): dim=2 serial bare -> the plain vorticity loop of
+ * tara2dHydSer (src/main2csh.f95), dim=2 serial screen -> tara2dScrSer
+ * (src/main2css.f95), dim=3 openmp mhd -> tara3dMHDOMP (src/main3com.f95);
+ * arch cpu and single-gpu both run on the GPU.  Output files go to out_dir
+ * (the reference writes ./output).  max_steps > 0 caps the number of steps
+ * (0: the full time_min..time_max loop).  Returns TARA_ERR_INI for a missing or
+ * malformed ini key, TARA_ERR_ARGS for a solver outside this build. */
+int tara_run_ini(const char* ini_path, const char* out_dir, int max_steps);
+
+/* cfg%gets of the reference's ini parser: the value of section/key with the
+ * DEFAULTS fallback, quotes stripped and ${sec:key} interpolated. */
+int tara_ini_get(const char* path, const char* section, const char* key, char* buf, int buflen);
+/* Fortran list-directed read of one REAL(8) / INTEGER from a string, e.g.
+ * "0.010d0" -> 0.01 and "3.0d0/128.0d0" -> 3.0 (the slash ends the read). */
+int tara_fortran_read_double(const char* s, double* out);
+int tara_fortran_read_int(const char* s, long long* out);
+/* One list-directed output record of n REAL(8) values, gfortran style. */
+int tara_fortran_list_record(const double* v, int n, char* buf, int buflen);
 
 /* ---- standalone transforms ------------------------------------------------ */
 /* Unnormalised 2D transforms with FFTW's rank-2 r2c/c2r semantics, i.e. what

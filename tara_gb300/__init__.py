@@ -130,6 +130,14 @@ def _declare(L: ctypes.CDLL) -> None:
     L.derive3com_.restype = None
     L.ab3com_.argtypes = [ip] * 4 + [dp] * 2 + [vp] * 32
     L.ab3com_.restype = None
+    L.tara_fortran_read_double.argtypes = [ctypes.c_char_p, dp]
+    L.tara_fortran_read_int.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_longlong)]
+    L.tara_ini_get.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, c_int]
+    L.tara_fortran_list_record.argtypes = [dp, c_int, ctypes.c_char_p, c_int]
+    L.tara_run_ini.argtypes = [ctypes.c_char_p, ctypes.c_char_p, c_int]
+    L.tara3d_diag.argtypes = [vp, dp]
+    L.tara2d_diag_reference.argtypes = [vp, vp, dp, dp]
+    L.tara2d_real_fields.argtypes = [vp, vp, dp, dp, dp, dp]
     L.tara_fft2d_r2c.argtypes = [c_int, c_int, c_int, dp, dp]
     L.tara_fft2d_c2r.argtypes = [c_int, c_int, c_int, dp, dp]
 

@@ -21,7 +21,9 @@ LIB = PKG / "libtara.so"
 ORACLE = ROOT / "oracle"
 REFERENCE = Path(os.environ.get("TARA_REFERENCE", "/root/reference"))
 
-SOURCES = ["launch_fp64.cu", "launch_fp32.cu", "solver2d.cu", "capi.cu", "noalloc.cu", "mhd3d.cu"]
+SOURCES = ["launch_fp64.cu", "launch_fp32.cu", "solver2d.cu", "capi.cu", "noalloc.cu", "mhd3d.cu",
+           "ini.cpp", "driver.cpp"]
+EXE = PKG / "tara"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + [
     "-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
@@ -55,14 +57,15 @@ def _compile(src: Path, obj: Path) -> None:
 
 
 def build_lib(force: bool = False, verbose: bool = False) -> Path:
-    deps = list(CSRC.glob("*.cu")) + list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h"))
+    deps = (list(CSRC.glob("*.cu")) + list(CSRC.glob("*.cuh")) + list(CSRC.glob("*.h")) +
+            list(CSRC.glob("*.cpp")))
     deps.append(ROOT / "include" / "tara.h")
     stamp = _stamp(deps)
     stamp_file = BUILD / "stamp"
     if not force and LIB.exists() and stamp_file.exists() and stamp_file.read_text() == stamp:
         return LIB
     BUILD.mkdir(exist_ok=True)
-    objs = [BUILD / (s.replace(".cu", ".o")) for s in SOURCES]
+    objs = [BUILD / (s.rsplit(".", 1)[0] + ".o") for s in SOURCES]
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         futs = [ex.submit(_compile, CSRC / s, o) for s, o in zip(SOURCES, objs)]
         for f in futs:
@@ -73,6 +76,12 @@ def build_lib(force: bool = False, verbose: bool = False) -> Path:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    # the `tara` executable (input.ini driver) links the library by relative rpath
+    cmd = [nvcc(), *ARCH, "-o", str(EXE), str(CSRC / "tara_main.cpp"), f"-L{PKG}", "-ltara",
+           "-Xlinker", "-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"tara executable link failed:\n{r.stdout}\n{r.stderr}")
     stamp_file.write_text(stamp)
     if verbose:
         print(f"built {LIB}")

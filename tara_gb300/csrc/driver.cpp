@@ -1,0 +1,316 @@
+// input.ini driver: the reference program's dispatch (src/main.f95) and the
+// time loops of the solvers on the path (src/main2css.f95, src/main2csh.f95,
+// src/main3com.f95), with their output files.  Host code over the C ABI; every
+// transform and update runs in libtara's kernels.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <sys/stat.h>
+#include <vector>
+
+#include "../../include/tara.h"
+#include "ini.h"
+
+namespace tara {
+int set_error(int code, const std::string& msg);
+int set_ok();
+}  // namespace tara
+
+using namespace tara;
+
+namespace {
+
+const double kPi = 3.14159265358979323846;  // real(kind=8), parameter :: pi (main2css.f95:9)
+
+struct Reader {
+  IniFile ini;
+  std::string err;
+  bool ok = true;
+
+  void str(const char* sec, const char* key, std::string& v) {
+    if (!ok) return;
+    ok = ini_get(ini, sec, key, v, err);
+    if (ok) {  // character(len=90) variables, compared without trailing blanks
+      if (v.size() > 90) v.resize(90);
+      while (!v.empty() && v.back() == ' ') v.pop_back();
+    }
+  }
+  void i(const char* sec, const char* key, int& v) {
+    std::string s;
+    str(sec, key, s);
+    if (!ok) return;
+    long long x = 0;
+    ok = fortran_read_int(s, x, err);
+    if (!ok) err = std::string(sec) + ":" + key + ": " + err;
+    v = (int)x;
+  }
+  void d(const char* sec, const char* key, double& v) {
+    std::string s;
+    str(sec, key, s);
+    if (!ok) return;
+    ok = fortran_read_double(s, v, err);
+    if (!ok) err = std::string(sec) + ":" + key + ": " + err;
+  }
+};
+
+struct Out {
+  FILE* f = nullptr;
+  explicit Out(const std::string& path) { f = std::fopen(path.c_str(), "w"); }
+  ~Out() {
+    if (f) std::fclose(f);
+  }
+  void rec(std::initializer_list<double> v) {
+    std::vector<double> a(v);
+    const std::string r = fortran_list_record(a.data(), (int)a.size());
+    std::fprintf(f, "%s\n", r.c_str());
+  }
+};
+
+// Fortran real DO loop `do time = t0, t1, dt`: the trip count is
+// max(int((t1 - t0 + dt)/dt), 0) in the loop variable's type, and the variable
+// advances by dt each iteration.
+long trip_count(double t0, double t1, double dt) {
+  const double n = (t1 - t0 + dt) / dt;
+  return n > 0 ? (long)n : 0;
+}
+
+long nint(double x) { return (long)std::llround(x); }
+
+std::string fort_name(const std::string& dir, long unit) {
+  char buf[64];
+  std::snprintf(buf, sizeof buf, "/fort.%08ld", unit);  // '("output/fort.",I8.8)'
+  return dir + buf;
+}
+
+int fail_rc() { return tara_last_error() ? tara_last_error() : TARA_ERR_CUDA; }
+
+// ---------------------------------------------------------------------------
+// tara2dScrSer (src/main2css.f95) and tara2dHydSer (src/main2csh.f95)
+// ---------------------------------------------------------------------------
+int run_2d(Reader& R, const std::string& out, int max_steps, bool screened) {
+  int np = 0, nx = 0, ny = 0;
+  double lx = 0, ly = 0, nu = 0, tmin = 0, tmax = 0, dt = 0, w0 = 0, m0 = 0, d = 0;
+  R.i("particle", "Np", np);
+  R.i("grid", "Nx", nx);
+  R.i("grid", "Ny", ny);
+  R.d("length", "Lx", lx);
+  R.d("length", "Ly", ly);
+  R.d("resistivity", "nu", nu);
+  R.d("time", "time_min", tmin);
+  R.d("time", "time_max", tmax);
+  R.d("time", "dt", dt);
+  R.d("initialProfile", "W0", w0);
+  R.d("initialProfile", "m0", m0);
+  R.d("initialProfile", "d", d);
+  if (!R.ok) return set_error(TARA_ERR_INI, R.err);
+  (void)np;  // Lagrangian particles (src/main2csh.f95:187-273) are not part of this build
+  lx = lx * kPi;
+  ly = ly * kPi;
+  const double dx = lx / (double)nx, dy = ly / (double)ny;
+  d = d * kPi;
+  const double alpha = 1.0, lambda = 10.0;  // src/main2css.f95:86-87
+  const int nh = nx / 2 + 1;
+  // initial vorticity (src/main2css.f95:89-104, src/main2csh.f95:98-106)
+  std::vector<double> xs(nx), ys(ny), omega((size_t)nx * ny);
+  for (int i = 0; i < nx; ++i) xs[i] = screened ? 0.0 + (double)(float)i * dx : (double)i * dx;
+  for (int j = 0; j < ny; ++j) ys[j] = screened ? (double)0.0f + (double)(float)j * dy : (double)j * dy;
+  for (int i = 0; i < nx; ++i)
+    for (int j = 0; j < ny; ++j) {
+      const double y = ys[j];
+      const double c1 = std::cosh((y + 0.5 * kPi) / d), c2 = std::cosh((y - 0.5 * kPi) / d);
+      const double c3 = std::cosh((y + 1.5 * kPi) / d), c4 = std::cosh((y - 1.5 * kPi) / d);
+      double w = w0 / (c1 * c1) - w0 / (c2 * c2);
+      w = w - w0 / (c3 * c3) + w0 / (c4 * c4);
+      w = w + (screened ? (double)0.01f : 0.10) * std::cos(m0 * xs[i]);
+      omega[(size_t)j * nx + i] = w;
+    }
+  mkdir(out.c_str(), 0755);
+  if (screened) {
+    Out f15(out + "/Initial_Condition_Velocity.dat");
+    for (int i = 0; i < nx; ++i)
+      for (int j = 0; j < ny; ++j) f15.rec({xs[i], ys[j], omega[(size_t)j * nx + i], 0.0, 0.0});
+  }
+  std::vector<double> wk(2 * (size_t)nh * ny);
+  if (tara_fft2d_r2c(nx, ny, TARA_PREC_FP64, omega.data(), wk.data())) return fail_rc();
+  tara2d_config cfg;
+  tara2d_default_config(&cfg, nx, ny);
+  cfg.nu = nu;
+  cfg.dt = dt;
+  if (screened) {  // derive2css in defined mode: its pi = 3.1428 with the driver's box
+    cfg.rhs = TARA_RHS_SCREEN;
+    cfg.alpha = alpha;
+    cfg.lambda = lambda;
+    cfg.lx = lx;
+    cfg.ly = ly;
+  }
+  tara2d* h = nullptr;
+  if (tara2d_create(&cfg, &h)) return fail_rc();
+  struct Guard {
+    tara2d* h;
+    ~Guard() { tara2d_destroy(h); }
+  } guard{h};
+  if (tara2d_set_state(h, wk.data(), nullptr)) return fail_rc();
+  const size_t nr = (size_t)nx * ny;
+  std::vector<double> psi(nr), om(nr), ux(nr), uy(nr);
+  if (screened) {  // initial diagnostics use psi = omega/k^2 (src/main2css.f95:112-179)
+    tara2d_diag_params p0 = {kPi, lx, ly, 0.0, 0};
+    if (tara2d_real_fields(h, &p0, psi.data(), om.data(), ux.data(), uy.data())) return fail_rc();
+    Out f10(out + "/Initial_Condition_Omega_REP.dat");
+    for (int i = 0; i < nx; ++i)
+      for (int j = 0; j < ny; ++j) {
+        const size_t r = (size_t)j * nx + i;
+        f10.rec({xs[i], ys[j], om[r], psi[r], ux[r], uy[r]});
+      }
+  }
+  Out energy(out + "/Energy.dat");  // written every step by the screened driver only
+  const tara2d_diag_params dp = {kPi, lx, ly, screened ? lambda : 0.0, screened ? 1 : 0};
+  const long n = trip_count(tmin, tmax, dt);
+  const long steps = (max_steps > 0 && max_steps < n) ? max_steps : n;
+  const long every = screened ? 100 : 1000;
+  double time = tmin, y_energy = 0.0;
+  for (long it = 0; it < steps; ++it) {
+    const long t = nint(time / dt) - (long)(tmin / dt);
+    if (tara2d_step(h, 1)) return fail_rc();  // derive + ab2 + history rotation
+    if (screened) {
+      double usq = 0.0, uysq = 0.0;
+      if (tara2d_diag_reference(h, &dp, &usq, &uysq)) return fail_rc();
+      y_energy += uysq;  // never reset by the reference (src/main2css.f95:259)
+      if (t % every == 0) {
+        if (tara2d_real_fields(h, &dp, nullptr, om.data(), ux.data(), uy.data())) return fail_rc();
+        Out snap(fort_name(out, t + 100));
+        for (int i = 0; i < nx; ++i)
+          for (int j = 0; j < ny; ++j) {
+            const size_t r = (size_t)j * nx + i;
+            snap.rec({xs[i], ys[j], ux[r], uy[r], om[r]});
+          }
+      }
+      energy.rec({time, usq, y_energy});
+    } else if (t % every == 0) {
+      if (tara2d_real_fields(h, &dp, nullptr, om.data(), ux.data(), uy.data())) return fail_rc();
+      Out snap(fort_name(out, t + 100));
+      for (int i = 0; i < nx; ++i)
+        for (int j = 0; j < ny; ++j) {
+          const size_t r = (size_t)j * nx + i;
+          snap.rec({xs[i], ys[j], om[r], ux[r], uy[r]});
+        }
+    }
+    time = time + dt;
+  }
+  if (tara2d_synchronize(h)) return fail_rc();
+  return set_ok();
+}
+
+// ---------------------------------------------------------------------------
+// tara3dMHDOMP (src/main3com.f95)
+// ---------------------------------------------------------------------------
+int run_3d(Reader& R, const std::string& out, int max_steps) {
+  int nx = 0, ny = 0, nz = 0;
+  double lx = 0, ly = 0, lz = 0, tmin = 0, tmax = 0, dt = 0, mu = 0;
+  R.i("grid", "Nx", nx);
+  R.i("grid", "Ny", ny);
+  R.i("grid", "Nz", nz);
+  R.d("length", "Lx", lx);
+  R.d("length", "Ly", ly);
+  R.d("length", "Lz", lz);
+  R.d("time", "time_min", tmin);
+  R.d("time", "time_max", tmax);
+  R.d("time", "dt", dt);
+  R.d("resistivity", "nu", mu);
+  if (!R.ok) return set_error(TARA_ERR_INI, R.err);
+  lx = lx * kPi;
+  ly = ly * kPi;
+  lz = lz * kPi;
+  const double dx = lx / (double)nx, dy = ly / (double)ny, dz = lz / (double)nz;
+  // src/main3com.f95:216-262: eta = 0.005, M = 0.1 -> CS = 10, U0 = 0.1, B0 = U0/MA
+  const double eta = 0.005, U0 = 0.10, cs = 1.0 / 0.10, B0 = U0 / 1.0 * std::sqrt(1.0 * 1.0);
+  const double A = 1.0, B = 1.0, C = 1.0, kf = 1.0, P0 = 1.0, rho0 = 1.0;
+  const size_t nr = (size_t)nx * ny * nz;
+  std::vector<double> real(8 * nr);
+  for (int i = 0; i < nx; ++i) {
+    const double x = 0.0 + (double)(float)i * dx;
+    for (int j = 0; j < ny; ++j) {
+      const double y = 0.0 + (double)(float)j * dy;
+      for (int k = 0; k < nz; ++k) {
+        const double z = 0.0 + (double)(float)k * dz;
+        const size_t r = ((size_t)k * ny + j) * nx + i;
+        const double vx = U0 * (A * std::sin(kf * z) + C * std::cos(kf * y));
+        const double vy = U0 * (B * std::sin(kf * x) + A * std::cos(kf * z));
+        const double vz = U0 * (C * std::sin(kf * y) + B * std::cos(kf * x));
+        const double E = P0 + 0.50 * rho0 * (vx * vx + vy * vy + vz * vz) +
+                         0.50 * (B0 * B0 + B0 * B0 + B0 * B0);
+        const double f[8] = {rho0, rho0 * vx, rho0 * vy, rho0 * vz, E, B0, B0, B0};
+        for (int q = 0; q < 8; ++q) real[q * nr + r] = f[q];
+      }
+    }
+  }
+  tara3d_config cfg;
+  tara3d_default_config(&cfg, nx, ny, nz);
+  cfg.kpi = kPi;
+  cfg.lx = lx;
+  cfg.ly = ly;
+  cfg.lz = lz;
+  cfg.mu = mu;
+  cfg.eta = eta;
+  cfg.cs = cs;
+  cfg.dt = dt;
+  cfg.defined = 0;
+  tara3d* h = nullptr;
+  if (tara3d_create(&cfg, &h)) return fail_rc();
+  struct Guard {
+    tara3d* h;
+    ~Guard() { tara3d_destroy(h); }
+  } guard{h};
+  if (tara3d_set_state_real(h, real.data())) return fail_rc();
+  mkdir(out.c_str(), 0755);
+  Out energy(out + "/Energy.dat");
+  const long n = trip_count(tmin, tmax, dt);
+  const long steps = (max_steps > 0 && max_steps < n) ? max_steps : n;
+  double time = tmin;
+  for (long it = 0; it < steps; ++it) {
+    if (tara3d_step(h, 1)) return fail_rc();
+    double dg[4];
+    if (tara3d_diag(h, dg)) return fail_rc();
+    energy.rec({time, dg[0], dg[1], dg[2], dg[3]});
+    time = time + dt;
+  }
+  return set_ok();
+}
+
+}  // namespace
+
+extern "C" int tara_run_ini(const char* ini_path, const char* out_dir, int max_steps) {
+  Reader R;
+  if (!ini_path) return set_error(TARA_ERR_ARGS, "null ini path");
+  if (!ini_parse_file(ini_path, R.ini, R.err)) return set_error(TARA_ERR_INI, R.err);
+  const std::string out = out_dir ? out_dir : "output";
+  int dim = 0;
+  std::string arch, mode, domain, hydrotype;
+  R.i("dimension", "dim", dim);  // src/main.f95:26-30
+  R.str("architecture", "arch", arch);
+  R.str("parallel", "mode", mode);
+  R.str("type", "domain", domain);
+  R.str("problem", "hydrotype", hydrotype);
+  if (!R.ok) return set_error(TARA_ERR_INI, R.err);
+  const bool here = (arch == "cpu" || arch == "single-gpu");
+  if (dim == 2 && here && mode == "serial" && hydrotype == "bare") {
+    std::printf(" tara-gb300: 2D serial hydrodynamic vorticity solver on the GPU\n");
+    return run_2d(R, out, max_steps, false);
+  }
+  if (dim == 2 && here && mode == "serial" && hydrotype == "screen") {
+    std::printf(" tara-gb300: 2D serial screened hydrodynamic vorticity solver on the GPU\n");
+    return run_2d(R, out, max_steps, true);
+  }
+  if (dim == 3 && here && mode == "openmp" && domain == "mhd") {
+    std::printf(" tara-gb300: 3D compressible MHD solver on the GPU\n");
+    return run_3d(R, out, max_steps);
+  }
+  if (mode == "mpi" || arch == "multi-gpu" || (dim == 3 && mode == "serial")) {
+    std::printf(" Under preparation. Please wait!\n");  // src/main.f95:40-85
+    return set_ok();
+  }
+  if (dim == 1 || (dim == 2 && mode == "openmp"))
+    return set_error(TARA_ERR_ARGS, "the 1D Burgers and 2D compressible solvers are outside this build");
+  std::printf(" Incompatible Input file. Please check TARA user-manual.\n");
+  return set_error(TARA_ERR_INI, "incompatible input file");
+}

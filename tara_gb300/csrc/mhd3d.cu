@@ -194,6 +194,36 @@ __global__ void k3_assemble(double2* __restrict__ st, const double2* __restrict_
   if (bad) atomicOr(flag, 1u);
 }
 
+// Grid sums of the reference's 3D diagnostics (src/main3com.f95:1024-1043):
+// part[4*b + 0..3] = sum rho, sum |u|^2, sum E, sum |B|^2 over this block's points.
+__global__ void k3_diag_partial(const double* __restrict__ rl, const double* __restrict__ pr,
+                                Grid3D g, double inv_n, double* __restrict__ part) {
+  const size_t total = (size_t)g.nz * g.ny * g.nx;
+  double a[4] = {0.0, 0.0, 0.0, 0.0};
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += (size_t)gridDim.x * blockDim.x) {
+    const size_t r = (t / g.nx) * g.rpitch + (t % g.nx);
+    const double ux = pr[P_UX * g.rfs + r], uy = pr[P_UY * g.rfs + r], uz = pr[P_UZ * g.rfs + r];
+    const double bx = rl[S_BX * g.rfs + r] * inv_n, by = rl[S_BY * g.rfs + r] * inv_n,
+                 bz = rl[S_BZ * g.rfs + r] * inv_n;
+    a[0] += rl[S_RHO * g.rfs + r] * inv_n;
+    a[1] += ux * ux + uy * uy + uz * uz;
+    a[2] += rl[S_E * g.rfs + r] * inv_n;
+    a[3] += bx * bx + by * by + bz * bz;
+  }
+  __shared__ double sh[4][8];
+  for (int k = 0; k < 4; ++k) {
+    for (int o = 16; o > 0; o >>= 1) a[k] += __shfl_down_sync(0xffffffffu, a[k], o);
+    if ((threadIdx.x & 31) == 0) sh[k][threadIdx.x >> 5] = a[k];
+  }
+  __syncthreads();
+  if (threadIdx.x < 4) {
+    double s = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += sh[threadIdx.x][w];
+    part[4 * blockIdx.x + threadIdx.x] = s;
+  }
+}
+
 // dense AB2 of ab3com on 8 fields: out = s + (3/2 dn - 1/2 do) dt, E copied
 __global__ void k3_ab2_dense(const double2* __restrict__ s, double2* __restrict__ out,
                              const double2* __restrict__ dold, const double2* __restrict__ dnew,
@@ -596,6 +626,36 @@ int tara3d_rhs(tara3d* h, double* d8) {
     if ((rc = copy3(h, h->dout + f * h->fs, nullptr, cudaMemcpyDeviceToHost, d8 + f * dense)))
       return rc;
   TARA_CK(cudaStreamSynchronize(h->stream));
+  return set_ok();
+}
+
+int tara3d_diag(tara3d* h, double* out4) {
+  if (!h || !out4) return set_error(TARA_ERR_ARGS, "null argument");
+  TARA_CK(cudaSetDevice(h->dev));
+  int rc;
+  if ((rc = c2r3(h, h->st, h->rl, S_N))) return rc;
+  k3_prim<<<kPwBlocks, kPwThreads, 0, h->stream>>>(h->rl, h->pr, h->g, h->p);
+  TARA_CK(cudaGetLastError());
+  double* part = nullptr;
+  TARA_CK(cudaMalloc(&part, 4 * kPwBlocks * sizeof(double)));
+  k3_diag_partial<<<kPwBlocks, kPwThreads, 0, h->stream>>>(h->rl, h->pr, h->g, h->p.inv_n, part);
+  std::vector<double> hp(4 * kPwBlocks);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(hp.data(), part, hp.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  cudaFree(part);
+  if (e != cudaSuccess) return cuda_fail(e, "tara3d_diag");
+  double a[4] = {0, 0, 0, 0};
+  for (int b = 0; b < kPwBlocks; ++b)
+    for (int k = 0; k < 4; ++k) a[k] += hp[4 * b + k];
+  const double n = (double)h->nx * (double)h->ny * (double)h->nz;
+  out4[0] = h->cfg.cs * h->cfg.cs * a[0] / n;  // Pressure = <CS^2 rho>
+  out4[1] = a[1] / (2.0 * n);                  // Energy = <|u|^2>/2
+  out4[2] = a[2] / n;                          // T_Energy = <E>
+  out4[3] = a[3] / (2.0 * n);                  // B_Field = <|B|^2>/(2 mu_0), mu_0 = 1
+  for (int k = 0; k < 4; ++k)
+    if (!std::isfinite(out4[k])) return set_error(TARA_ERR_NONFINITE, "non-finite 3D diagnostics");
   return set_ok();
 }
 

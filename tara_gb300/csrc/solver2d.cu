@@ -177,6 +177,83 @@ __global__ void k_ab2_dense(const double2* w, double2* out, const double2* __res
 }
 
 // ---------------------------------------------------------------------------
+// driver diagnostics in the reference's form (src/main2css.f95:206-275,
+// src/main2csh.f95:128-168): spectra of psi, omega_dum, u_x, u_y with the
+// driver's wavenumbers, and the grid sums of u^2 through the c2r discard rule
+// ---------------------------------------------------------------------------
+// psi = omega/(k^2 + lam_row) with lam_row = lambda for j < Ny/2 and 0 above (the
+// screened driver applies lambda to one half only, :215 vs :226; the plain
+// driver passes lambda = 0); out[0..3] = psi, k^2 psi (screened) or omega
+// (plain), (0,1) ky psi, -(0,1) kx psi.
+__global__ void k_diag_spectra(const double2* __restrict__ w, Grid2D g, double lambda, int screened,
+                               double2* __restrict__ out) {
+  const size_t total = (size_t)g.ny * g.nh, fsz = (size_t)g.ny * g.pitch;
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += (size_t)gridDim.x * blockDim.x) {
+    const int y = (int)(t / g.nh), x = (int)(t % g.nh);
+    const size_t q = (size_t)y * g.pitch + x;
+    const double2 v = w[q];
+    const double kx = g.kx[x], ky = g.ky[y];
+    const double k2 = kx * kx + ky * ky;
+    double pr = 0.0, pim = 0.0;
+    if (x != 0 || y != 0) {
+      const double den = (screened && 2 * y < g.ny) ? k2 + lambda : k2;
+      pr = v.x / den;
+      pim = v.y / den;
+    }
+    out[q] = make_double2(pr, pim);
+    out[fsz + q] = screened ? make_double2(k2 * pr, k2 * pim) : v;
+    out[2 * fsz + q] = make_double2(-ky * pim, ky * pr);
+    out[3 * fsz + q] = make_double2(kx * pim, -(kx * pr));
+  }
+}
+
+// Grid sums of u_x^2 + u_y^2 and of u_y^2 over the N^2 points after c2r and
+// division by NxNy: (1/(NxNy)) * sum over the full spectrum of |U|^2, where on
+// the kx = 0 and kx = Nx/2 columns the c2r keeps only the Hermitian part
+// (U(ky) + conj U(-ky))/2 of each column.
+__global__ void k_diag_usq(const double2* __restrict__ sp, Grid2D g, double* __restrict__ part) {
+  const size_t total = (size_t)g.ny * g.nh, fsz = (size_t)g.ny * g.pitch;
+  double sx = 0.0, sy = 0.0;
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += (size_t)gridDim.x * blockDim.x) {
+    const int y = (int)(t / g.nh), x = (int)(t % g.nh);
+    const size_t q = (size_t)y * g.pitch + x;
+    const double2 a = sp[2 * fsz + q], b = sp[3 * fsz + q];
+    if (x == 0 || 2 * x == g.nx) {
+      const size_t qm = (size_t)((g.ny - y) % g.ny) * g.pitch + x;
+      const double2 am = sp[2 * fsz + qm], bm = sp[3 * fsz + qm];
+      const double hax = 0.5 * (a.x + am.x), hay = 0.5 * (a.y - am.y);
+      const double hbx = 0.5 * (b.x + bm.x), hby = 0.5 * (b.y - bm.y);
+      sx += hax * hax + hay * hay;
+      sy += hbx * hbx + hby * hby;
+    } else {
+      sx += 2.0 * (a.x * a.x + a.y * a.y);
+      sy += 2.0 * (b.x * b.x + b.y * b.y);
+    }
+  }
+  __shared__ double s1[8], s2[8];
+  for (int o = 16; o > 0; o >>= 1) {
+    sx += __shfl_down_sync(0xffffffffu, sx, o);
+    sy += __shfl_down_sync(0xffffffffu, sy, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    s1[threadIdx.x >> 5] = sx;
+    s2[threadIdx.x >> 5] = sy;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double a = 0.0, b = 0.0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) {
+      a += s1[i];
+      b += s2[i];
+    }
+    part[2 * blockIdx.x] = a;
+    part[2 * blockIdx.x + 1] = b;
+  }
+}
+
+// ---------------------------------------------------------------------------
 // solver internals
 // ---------------------------------------------------------------------------
 template <typename T>
@@ -525,6 +602,113 @@ int tara2d_synchronize(tara2d* h) {
 }
 
 void* tara2d_stream(tara2d* h) { return h ? (void*)h->stream : nullptr; }
+
+// Diagnostic spectra with the driver's wavenumbers (true pi, ini box), into
+// four consecutive pitched fields at `sp`.
+static int diag_spectra(tara2d* h, const tara2d_diag_params* dp, double2* sp, Grid2D* gout,
+                        double** kbuf) {
+  std::vector<double> kx(h->nh), ky(h->ny);
+  std::vector<int> i0(h->ny);
+  make_wavenumbers(h->nx, h->ny, dp->kpi, dp->lx, dp->ly, kx.data(), ky.data(), i0.data());
+  double* dk = nullptr;
+  TARA_CK(cudaMalloc(&dk, (h->nh + h->ny) * sizeof(double)));
+  *kbuf = dk;
+  TARA_CK(cudaMemcpyAsync(dk, kx.data(), h->nh * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  TARA_CK(cudaMemcpyAsync(dk + h->nh, ky.data(), h->ny * sizeof(double), cudaMemcpyHostToDevice,
+                          h->stream));
+  Grid2D g = h->grid;
+  g.kx = dk;
+  g.ky = dk + h->nh;
+  *gout = g;
+  k_diag_spectra<<<304, 256, 0, h->stream>>>(h->w0, g, dp->lambda, dp->screened, sp);
+  TARA_CK(cudaGetLastError());
+  TARA_CK(cudaStreamSynchronize(h->stream));  // host tables go out of scope
+  return TARA_OK;
+}
+
+int tara2d_diag_reference(tara2d* h, const tara2d_diag_params* dp, double* usq, double* uysq) {
+  if (!h || !dp) return set_error(TARA_ERR_ARGS, "null argument");
+  TARA_CK(cudaSetDevice(h->dev));
+  double2* sp = nullptr;
+  double* part = nullptr;
+  double* kbuf = nullptr;
+  const size_t fsz = (size_t)h->ny * h->pitch;
+  int rc = TARA_OK;
+  if (cudaMalloc(&sp, 4 * fsz * sizeof(double2)) != cudaSuccess ||
+      cudaMalloc(&part, 2 * kDiagBlocks * sizeof(double)) != cudaSuccess)
+    rc = set_error(TARA_ERR_NOMEM, "cudaMalloc");
+  Grid2D g;
+  if (!rc) rc = diag_spectra(h, dp, sp, &g, &kbuf);
+  std::vector<double> hp(2 * kDiagBlocks);
+  if (!rc) {
+    k_diag_usq<<<kDiagBlocks, kDiagThreads, 0, h->stream>>>(sp, g, part);
+    if (cudaGetLastError() != cudaSuccess ||
+        cudaMemcpyAsync(hp.data(), part, hp.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                        h->stream) != cudaSuccess ||
+        cudaStreamSynchronize(h->stream) != cudaSuccess)
+      rc = set_error(TARA_ERR_CUDA, "diag reduction");
+  }
+  if (!rc) {
+    double a = 0.0, b = 0.0;
+    for (int i = 0; i < kDiagBlocks; ++i) {
+      a += hp[2 * i];
+      b += hp[2 * i + 1];
+    }
+    const double nn = (double)h->nx * (double)h->ny;
+    if (usq) *usq = (a + b) / nn;
+    if (uysq) *uysq = b / nn;
+    if (!(std::isfinite(a) && std::isfinite(b)))
+      rc = set_error(TARA_ERR_NONFINITE, "non-finite energy");
+  }
+  cudaFree(sp);
+  cudaFree(part);
+  cudaFree(kbuf);
+  return rc ? rc : set_ok();
+}
+
+int tara2d_real_fields(tara2d* h, const tara2d_diag_params* dp, double* psi, double* omega,
+                       double* ux, double* uy) {
+  if (!h || !dp) return set_error(TARA_ERR_ARGS, "null argument");
+  TARA_CK(cudaSetDevice(h->dev));
+  const size_t fsz = (size_t)h->ny * h->pitch;
+  const int rpitch = round_up(h->nx, 8);
+  double2* sp = nullptr;
+  double* real = nullptr;
+  double* kbuf = nullptr;
+  void *tx = nullptr, *ty = nullptr;
+  int rc = TARA_OK;
+  if (cudaMalloc(&sp, 4 * fsz * sizeof(double2)) != cudaSuccess ||
+      cudaMalloc(&real, (size_t)h->ny * rpitch * sizeof(double)) != cudaSuccess)
+    rc = set_error(TARA_ERR_NOMEM, "cudaMalloc");
+  Grid2D g;
+  if (!rc) rc = diag_spectra(h, dp, sp, &g, &kbuf);
+  // the diagnostic transforms run in FP64 whatever the solver's precision
+  if (!rc) rc = make_twiddles(h->nx, false, &tx);
+  if (!rc) rc = make_twiddles(h->ny, false, &ty);
+  double* outs[4] = {psi, omega, ux, uy};
+  std::vector<double> host((size_t)h->ny * rpitch);
+  const double nn = (double)h->nx * (double)h->ny;
+  for (int f = 0; f < 4 && !rc; ++f) {
+    if (!outs[f]) continue;
+    double2* in = sp + f * fsz;
+    rc = Launch2D<double>::col_fft(h->ny, h->nh, h->pitch, in, in, true, ty, h->stream);
+    if (!rc) rc = Launch2D<double>::row_c2r(h->nx, h->ny, h->pitch, rpitch, in, real, tx, h->stream);
+    if (!rc && (cudaMemcpyAsync(host.data(), real, host.size() * sizeof(double),
+                                cudaMemcpyDeviceToHost, h->stream) != cudaSuccess ||
+                cudaStreamSynchronize(h->stream) != cudaSuccess))
+      rc = set_error(TARA_ERR_CUDA, "real field copy");
+    if (!rc)
+      for (int j = 0; j < h->ny; ++j)
+        for (int i = 0; i < h->nx; ++i)
+          outs[f][(size_t)j * h->nx + i] = host[(size_t)j * rpitch + i] / nn;
+  }
+  cudaFree(sp);
+  cudaFree(real);
+  cudaFree(kbuf);
+  cudaFree(tx);
+  cudaFree(ty);
+  return rc ? rc : set_ok();
+}
 
 // Philox4x32-10 on the host (Salmon et al., SC'11), for the seeded phases.
 static void philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {

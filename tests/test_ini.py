@@ -1,0 +1,149 @@
+"""CPU tests of the input.ini layer: the reference parser's semantics
+(lib/iniparser/cfgio_mod.f90), Fortran list-directed reads
+(lib/iniparser/string_conv_mod.f90:95-99) and list-directed output records."""
+from __future__ import annotations
+
+import ctypes
+import math
+
+import pytest
+
+import tara_gb300 as tg
+
+
+def read_d(s: str):
+    v = ctypes.c_double()
+    rc = tg.lib().tara_fortran_read_double(s.encode(), ctypes.byref(v))
+    return rc, v.value
+
+
+def read_i(s: str):
+    v = ctypes.c_longlong()
+    rc = tg.lib().tara_fortran_read_int(s.encode(), ctypes.byref(v))
+    return rc, v.value
+
+
+@pytest.mark.parametrize("text,value", [
+    ("0.010d0", 0.01), ("2.0d0", 2.0), ("2.0D0", 2.0), ("0.00010d0", 1e-4), ("1e-4", 1e-4),
+    ("25.0d0", 25.0), ("  7 ", 7.0), (".5", 0.5), ("5.", 5.0), ("-1.5q0", -1.5),
+    ("1.0+05", 1.0e5), ("1.0-2", 1.0e-2), ("2*3.5", 3.5), ("1.0d0 # comment", 1.0),
+    ("4.0,5.0", 4.0),
+    # a slash ends list-directed input: the reference's "d = 3.0d0/128.0d0" reads 3.0
+    ("3.0d0/128.0d0", 3.0),
+])
+def test_fortran_read_double(text, value):
+    rc, v = read_d(text)
+    assert rc == tg.TARA_OK
+    assert v == value
+
+
+@pytest.mark.parametrize("text", ["abc", "", "   ", ",1.0", "/", "1.0x", "1.0d", "--1"])
+def test_fortran_read_double_rejects(text):
+    rc, _ = read_d(text)
+    assert rc == tg.TARA_ERR_INI
+
+
+def test_fortran_read_double_special():
+    assert math.isinf(read_d("Infinity")[1]) and math.isnan(read_d("NaN")[1])
+
+
+@pytest.mark.parametrize("text,value", [("64", 64), (" 64 ! c", 64), ("+3", 3), ("-12,", -12),
+                                        ("2*8", 8)])
+def test_fortran_read_int(text, value):
+    assert read_i(text) == (tg.TARA_OK, value)
+
+
+@pytest.mark.parametrize("text", ["6.4e1", "64.0", "x", "", "12y"])
+def test_fortran_read_int_rejects(text):
+    assert read_i(text)[0] == tg.TARA_ERR_INI
+
+
+INI = """# test input (the reference's keys)
+[dimension]
+dim = 2
+; semicolon comment
+[grid]
+Nx = 64
+Ny = ${Nx}
+Nz = ${grid:Nx}
+[length]
+Lx = 2.0d0
+Lx = 9.0d0
+[initialProfile]
+d = 3.0d0/128.0d0
+[problem]
+hydrotype = "screen"
+[dimension]
+extra = 5
+[DEFAULTS]
+nu = 0.010d0
+"""
+
+
+@pytest.fixture
+def ini_path(tmp_path):
+    p = tmp_path / "in.ini"
+    p.write_text(INI)
+    return p
+
+
+def ini_get(path, sec, key):
+    buf = ctypes.create_string_buffer(512)
+    rc = tg.lib().tara_ini_get(str(path).encode(), sec.encode(), key.encode(), buf, 512)
+    return rc, buf.value.decode()
+
+
+def test_ini_sections_keys_and_interpolation(ini_path):
+    assert ini_get(ini_path, "dimension", "dim") == (tg.TARA_OK, "2")
+    assert ini_get(ini_path, "grid", "Ny") == (tg.TARA_OK, "64")      # ${key}
+    assert ini_get(ini_path, "grid", "Nz") == (tg.TARA_OK, "64")      # ${sec:key}
+    assert ini_get(ini_path, "length", "Lx") == (tg.TARA_OK, "2.0d0")  # first match wins
+    assert ini_get(ini_path, "problem", "hydrotype") == (tg.TARA_OK, "screen")  # unquoted
+    assert ini_get(ini_path, "dimension", "extra") == (tg.TARA_OK, "5")  # reopened section
+    # DEFAULTS fallback for a missing key and for a missing section
+    assert ini_get(ini_path, "resistivity", "nu") == (tg.TARA_OK, "0.010d0")
+    assert ini_get(ini_path, "grid", "nu") == (tg.TARA_OK, "0.010d0")
+    rc, _ = ini_get(ini_path, "grid", "missing")
+    assert rc == tg.TARA_ERR_INI
+    assert "Cannot find the key" in tg.last_error()[1]
+
+
+def test_ini_bad_section_title(tmp_path):
+    p = tmp_path / "bad.ini"
+    p.write_text("[grid\nNx = 4\n")
+    assert ini_get(p, "grid", "Nx")[0] == tg.TARA_ERR_INI
+
+
+def record(*v):
+    arr = (ctypes.c_double * len(v))(*v)
+    buf = ctypes.create_string_buffer(4096)
+    assert tg.lib().tara_fortran_list_record(arr, len(v), buf, 4096) == tg.TARA_OK
+    return buf.value.decode()
+
+
+def test_list_directed_output_style():
+    assert record(1.0) == "   1.0000000000000000     "
+    assert record(12.5) == "   12.500000000000000     "
+    assert record(0.1) == "  0.10000000000000001     "
+    assert record(1e-4) == "   1.0000000000000000E-004"
+    assert record(0.0) == "   0.0000000000000000     "
+    assert record(-2.5) == "  -2.5000000000000000     "
+    assert record(1e20) == "   1.0000000000000000E+020"
+    two = record(1.0, 2.0)
+    assert two.split() == ["1.0000000000000000", "2.0000000000000000"]
+
+
+def test_run_ini_dispatch_without_gpu(tmp_path):
+    L = tg.lib()
+    p = tmp_path / "a.ini"
+    base = ("[dimension]\ndim = {dim}\n[architecture]\narch = cpu\n[parallel]\nmode = {mode}\n"
+            "[type]\ndomain = hydro\n[problem]\nhydrotype = bare\n")
+    p.write_text(base.format(dim=1, mode="serial"))
+    assert L.tara_run_ini(str(p).encode(), str(tmp_path / "o").encode(), 0) == tg.TARA_ERR_ARGS
+    p.write_text(base.format(dim=2, mode="mpi"))
+    assert L.tara_run_ini(str(p).encode(), str(tmp_path / "o").encode(), 0) == tg.TARA_OK
+    p.write_text("[dimension]\ndim = 2\n")  # arch missing
+    assert L.tara_run_ini(str(p).encode(), str(tmp_path / "o").encode(), 0) == tg.TARA_ERR_INI
+    p.write_text(base.format(dim=2, mode="serial").replace("[grid]", ""))  # no grid keys
+    rc = L.tara_run_ini(str(p).encode(), str(tmp_path / "o").encode(), 0)
+    assert rc == tg.TARA_ERR_INI and "Np" in tg.last_error()[1] + "particle"
