@@ -252,10 +252,11 @@ bool fortran_read_int(const std::string& s, long long& v, std::string& err) {
 }
 
 std::string fortran_list_record(const double* v, int n) {
-  std::string rec = " ";
+  std::string rec;
   char buf[64];
   for (int k = 0; k < n; ++k) {
     const double x = v[k];
+    rec += ' ';  // value separator: a 20-character F field must not touch its neighbour
     if (!std::isfinite(x)) {
       std::snprintf(buf, sizeof buf, "%25s", std::isnan(x) ? "NaN" : (x > 0 ? "Infinity" : "-Infinity"));
       rec += buf;

@@ -36,7 +36,7 @@ bool fortran_read_int(const std::string& s, long long& v, std::string& err);
 
 // One list-directed output record of REAL(8) values in gfortran's style
 // (G25.17 per item: F form for 0.1 <= |x| < 1e17, otherwise 1P E form with a
-// three-digit exponent), with the leading blank of the record.
+// three-digit exponent), each item preceded by one separating blank.
 std::string fortran_list_record(const double* v, int n);
 
 }  // namespace tara

@@ -131,6 +131,9 @@ def test_list_directed_output_style():
     assert record(1e20) == "   1.0000000000000000E+020"
     two = record(1.0, 2.0)
     assert two.split() == ["1.0000000000000000", "2.0000000000000000"]
+    # a negative value with a 20-character F field stays separated from an E field
+    assert record(0.098, -0.10000341643993921).split() == ["9.8000000000000004E-002",
+                                                            "-0.10000341643993921"]
 
 
 def test_run_ini_dispatch_without_gpu(tmp_path):
