@@ -292,6 +292,122 @@ def run_ours(args) -> None:
     s.close()
 
 
+def timed_on_stream(stream_ptr: int, fn):
+    """CUDA-event time (ms) of fn() on the library stream stream_ptr."""
+    import torch
+
+    st = torch.cuda.ExternalStream(stream_ptr)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    a.record(st)
+    fn()
+    b.record(st)
+    b.synchronize()
+    return a.elapsed_time(b)
+
+
+def run_ensemble(args) -> None:
+    """Config 4: 384 independent 2D runs (128 each at 128^2, 256^2, 512^2), RK4,
+    nu = 1e-3, dt = 1e-4, FP32 transforms and products with FP64 state,
+    k0 ~ U[4,10] (numpy default_rng(4000)), seed 4000 + r.  One CUDA-graph launch
+    per ensemble step; tile variants picked by the autotuner first."""
+    import numpy as np
+    import torch
+
+    import tara_gb300 as tg
+
+    torch.cuda.set_device(0)
+    k0 = np.random.default_rng(4000).uniform(4.0, 10.0, 384)
+    runs = [(n, float(k0[r]), 4000 + r) for r, n in enumerate([128] * 128 + [256] * 128 + [512] * 128)]
+    e = tg.Ensemble(runs, precision=tg.PREC_FP32, nu=1e-3, dt=1e-4)
+    e.autotune(3)
+    e.step(args.warmup)
+    e.synchronize()
+    ms = timed_on_stream(e.stream, lambda: e.step(args.steps))
+    e.synchronize()
+    pts = sum(n * n for n, _, _ in runs)
+    line = {"metric": "ensemble grid-pt*steps/s (384 runs: 128 each at 128^2, 256^2, 512^2; RK4)",
+            "value": pts * args.steps / (ms * 1e-3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "dtype": "f32 transforms / f64 state", "data": "synthetic (seeded random-phase spectra)",
+            "config": {"workload": "config 4 ensemble", "graph": "one cudaGraphLaunch per step",
+                       "l2": "working set > L2 (no flush)"},
+            "gpu_launches": e.launches_per_step * args.steps, "autotune": e.groups()}
+    if args.ens_error_steps:
+        e64 = tg.Ensemble(runs, precision=tg.PREC_FP64, nu=1e-3, dt=1e-4)
+        e.step(args.ens_error_steps - args.steps - args.warmup)
+        e64.step(args.ens_error_steps)
+        e.synchronize()
+        e64.synchronize()
+        errs = []
+        for r in range(len(runs)):
+            a, b = e.get_state(r), e64.get_state(r)
+            errs.append(float(np.linalg.norm(a - b) / np.linalg.norm(b)))
+        line["error_vs_fp64"] = {"steps": args.ens_error_steps, "max": max(errs),
+                                 "median": float(np.median(errs)),
+                                 "per_size_max": {str(n): max(x for (m, _, _), x in zip(runs, errs) if m == n)
+                                                  for n in (128, 256, 512)}}
+        e64.close()
+    print(json.dumps(line), flush=True)
+    e.close()
+
+
+def mhd3d_initial_state(n: int, seed: int = 3):
+    """Config 3 initial condition as real fields (rho, rho u, E, B): u = (-sin y,
+    sin x, 0), B = (-sin y, sin 2x, 0), rho = 1, plus a seeded 1 % random-phase
+    solenoidal perturbation of u and B at |k| <= 4; E = 1 + |u|^2/2 + |B|^2/2."""
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    g = np.arange(n) * (2 * np.pi / n)
+    z, y, x = np.meshgrid(g, g, g, indexing="ij")
+    kz, ky, kx = np.meshgrid(np.fft.fftfreq(n, 1 / n), np.fft.fftfreq(n, 1 / n),
+                             np.arange(n // 2 + 1), indexing="ij")
+    k2 = kx**2 + ky**2 + kz**2
+    shell = (k2 > 0) & (k2 <= 16)
+
+    def solenoidal(base):
+        a = [np.where(shell, np.exp(2j * np.pi * rng.random(k2.shape)), 0) for _ in range(3)]
+        kd = (kx * a[0] + ky * a[1] + kz * a[2]) / np.where(k2 > 0, k2, 1)
+        a = [a[0] - kx * kd, a[1] - ky * kd, a[2] - kz * kd]
+        f = [np.fft.irfftn(c, s=(n, n, n), axes=(0, 1, 2)) for c in a]
+        rms = np.sqrt(sum((v**2).mean() for v in f))
+        brms = np.sqrt(sum((v**2).mean() for v in base))
+        return [b + 0.01 * brms / rms * v for b, v in zip(base, f)]
+
+    u = solenoidal([-np.sin(y), np.sin(x), 0 * x])
+    b = solenoidal([-np.sin(y), np.sin(2 * x), 0 * x])
+    rho = np.ones_like(x)
+    e = 1.0 + 0.5 * sum(v**2 for v in u) + 0.5 * sum(v**2 for v in b)
+    return np.stack([rho, u[0], u[1], u[2], e, b[0], b[1], b[2]])
+
+
+def run_mhd3d(args) -> None:
+    """Config 3: 128^3 compressible MHD, FP64, AB2, nu = eta = 0.01, dt = 1e-3."""
+    import torch
+
+    import tara_gb300 as tg
+
+    torch.cuda.set_device(0)
+    n = 128
+    s = tg.Solver3D(n, defined=1, nu_u=0.01, eta_b=0.01, dt=1e-3)
+    s.set_state_real(mhd3d_initial_state(n))
+    s.step(args.warmup)
+    s.synchronize()
+    ms = timed_on_stream(s.stream, lambda: s.step(args.steps))
+    s.synchronize()
+    d = s.diag()
+    line = {"metric": "grid-pt*steps/s at 128^3 FP64 (3D compressible MHD, AB2)",
+            "value": n**3 * args.steps / (ms * 1e-3), "unit": UNIT, "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "dtype": "f64", "data": "synthetic (config 3 profile)",
+            "config": {"workload": "config 3: 128^3, nu=eta=0.01, dt=1e-3, AB2, 20 transforms/step"},
+            "gpu_launches": None, "diag": {"pressure": d[0], "kinetic": d[1], "total_E": d[2],
+                                           "magnetic": d[3]}}
+    print(json.dumps(line), flush=True)
+    s.close()
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -301,11 +417,19 @@ def main() -> None:
     ap.add_argument("--n", type=int, default=2048)
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="rk4-2048", choices=["rk4-2048", "ensemble", "mhd3d"],
+                    help="rk4-2048 is the headline; the others measure configs 4 and 3")
+    ap.add_argument("--ens-error-steps", type=int, default=0,
+                    help="ensemble: also report the per-run error vs FP64 after this many steps")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "ensemble":
+        run_ensemble(args)
+    elif args.workload == "mhd3d":
+        run_mhd3d(args)
     else:
         run_ours(args)
 

@@ -108,6 +108,7 @@ typedef struct tara2d_config {
   double lambda;   /* screened RHS: screening */
   double lx, ly;   /* box lengths used in kx = 2*kpi*(i-1)/lx */
   double kpi;      /* the pi in that formula: 3.1428f for the reference's RHS */
+  int batch;       /* independent runs of this shape advanced together (>= 1) */
 } tara2d_config;
 
 /* Fills cfg with the reference plain RHS defaults (pi = 3.1428f, Lx = Ly = 2*pi,
@@ -122,6 +123,9 @@ int tara2d_destroy(tara2d* h);
  * (the AB2 history is then zero, as the reference's fresh allocation reads). */
 int tara2d_set_state(tara2d* h, const double* omegak, const double* dt_old);
 int tara2d_get_state(tara2d* h, double* omegak, double* dt_old);
+/* The same for run `run` of a batched handle (the calls above address run 0). */
+int tara2d_set_state_run(tara2d* h, int run, const double* omegak, const double* dt_old);
+int tara2d_get_state_run(tara2d* h, int run, double* omegak, double* dt_old);
 /* Device pointers (dense Nh*Ny complex) on the handle's device. */
 int tara2d_set_state_device(tara2d* h, const void* omegak_dev, const void* dt_old_dev);
 int tara2d_get_state_device(tara2d* h, void* omegak_dev);
@@ -138,6 +142,7 @@ int tara2d_rhs(tara2d* h, double* dt_omegak);
 /* 1/2<|u|^2> and 1/2<omega^2> of the current state in the box (lx, ly) of the
  * config, from the spectrum by Parseval; TARA_ERR_NONFINITE when NaN/Inf. */
 int tara2d_diag(tara2d* h, double* energy, double* enstrophy);
+int tara2d_diag_run(tara2d* h, int run, double* energy, double* enstrophy);
 int tara2d_synchronize(tara2d* h);
 /* The handle's CUDA stream (cudaStream_t) for callers that order work around it. */
 void* tara2d_stream(tara2d* h);
@@ -164,6 +169,45 @@ int tara2d_real_fields(tara2d* h, const tara2d_diag_params* dp, double* psi, dou
  * Hermitian-projected on the GPU by a c2r/r2c round trip, mean mode zeroed,
  * rescaled to 1/2<|u|^2> = energy with the handle's wavenumbers). */
 int tara2d_init_random(tara2d* h, double k0, double energy, uint64_t seed);
+int tara2d_init_random_run(tara2d* h, int run, double k0, double energy, uint64_t seed);
+
+/* ---- ensembles of runs of uneven sizes ------------------------------------ */
+
+/* One run: grid n x n (power of two in [16, 2048]) with a seeded random-phase
+ * initial spectrum (tara2d_init_random's recipe with this k0 and seed). */
+typedef struct tara_ens_run {
+  int n;
+  double k0;
+  uint64_t seed;
+} tara_ens_run;
+
+typedef struct tara_ens tara_ens;
+
+/* Runs of one size are advanced by the same launches (a batched handle per size);
+ * all sizes share nu, dt, scheme and precision (TARA_PREC_FP32: FP32 transforms
+ * and products, FP64 state and reductions).  Plain RHS, 2*pi box. */
+int tara_ens_create(int nruns, const tara_ens_run* runs, int precision, int scheme, double nu,
+                    double dt, double energy, tara_ens** out);
+int tara_ens_destroy(tara_ens* e);
+/* Times both tile variants of each kernel on trial_steps steps per size and keeps
+ * the faster per kernel and size; the state is saved and restored around it. */
+int tara_ens_autotune(tara_ens* e, int trial_steps);
+/* Advances every run nsteps steps: one CUDA-graph launch per step (the graph,
+ * one parallel branch per size, is captured on first use).  Asynchronous. */
+int tara_ens_step(tara_ens* e, int nsteps);
+int tara_ens_synchronize(tara_ens* e);
+/* The stream the graph launches on (cudaStream_t). */
+void* tara_ens_stream(tara_ens* e);
+int tara_ens_get_state(tara_ens* e, int run, double* omegak);
+int tara_ens_set_state(tara_ens* e, int run, const double* omegak);
+int tara_ens_diag(tara_ens* e, int run, double* energy, double* enstrophy);
+int tara_ens_groups(tara_ens* e);
+/* Size group info: n, number of runs, chosen variants of the three kernels, and
+ * the autotuner's per-launch milliseconds (variant 0 then 1, three kernels each). */
+int tara_ens_group_info(tara_ens* e, int group, int* n, int* runs, int* variants3,
+                        double* tuned_ms6);
+/* Kernel launches one ensemble step contains (inside its graph). */
+int tara_ens_launches_per_step(tara_ens* e);
 
 /* ---- 3D compressible MHD (derive3com / ab3com) --------------------------- */
 
@@ -228,6 +272,8 @@ int tara3d_step(tara3d* h, int nsteps);
 /* all eight derivatives of the current state (dense spectra), as derive3com */
 int tara3d_rhs(tara3d* h, double* d8);
 int tara3d_synchronize(tara3d* h);
+/* The handle's CUDA stream (cudaStream_t). */
+void* tara3d_stream(tara3d* h);
 /* The first columns of the reference's 3D Energy.dat (src/main3com.f95:1024-1070)
  * for the current state: out4 = {Pressure = <CS^2 rho>, Energy = <|u|^2>/2,
  * T_Energy = <E>, B_Field = <|B|^2>/2}, u = (rho u)/rho in real space. */

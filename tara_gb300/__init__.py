@@ -43,7 +43,7 @@ class Config2D(ctypes.Structure):
         ("scheme", ctypes.c_int), ("precision", ctypes.c_int),
         ("nu", ctypes.c_double), ("dt", ctypes.c_double), ("alpha", ctypes.c_double),
         ("lam", ctypes.c_double), ("lx", ctypes.c_double), ("ly", ctypes.c_double),
-        ("kpi", ctypes.c_double),
+        ("kpi", ctypes.c_double), ("batch", ctypes.c_int),
     ]
 
 
@@ -136,6 +136,26 @@ def _declare(L: ctypes.CDLL) -> None:
     L.tara_fortran_list_record.argtypes = [dp, c_int, ctypes.c_char_p, c_int]
     L.tara_run_ini.argtypes = [ctypes.c_char_p, ctypes.c_char_p, c_int]
     L.tara3d_diag.argtypes = [vp, dp]
+    L.tara3d_stream.argtypes = [vp]
+    L.tara3d_stream.restype = vp
+    L.tara2d_set_state_run.argtypes = [vp, c_int, dp, dp]
+    L.tara2d_get_state_run.argtypes = [vp, c_int, dp, dp]
+    L.tara2d_diag_run.argtypes = [vp, c_int, dp, dp]
+    L.tara2d_init_random_run.argtypes = [vp, c_int, c_double, c_double, ctypes.c_uint64]
+    L.tara_ens_create.argtypes = [c_int, vp, c_int, c_int, c_double, c_double, c_double,
+                                  ctypes.POINTER(vp)]
+    L.tara_ens_destroy.argtypes = [vp]
+    L.tara_ens_autotune.argtypes = [vp, c_int]
+    L.tara_ens_step.argtypes = [vp, c_int]
+    L.tara_ens_synchronize.argtypes = [vp]
+    L.tara_ens_stream.argtypes = [vp]
+    L.tara_ens_stream.restype = vp
+    L.tara_ens_get_state.argtypes = [vp, c_int, dp]
+    L.tara_ens_set_state.argtypes = [vp, c_int, dp]
+    L.tara_ens_diag.argtypes = [vp, c_int, dp, dp]
+    L.tara_ens_groups.argtypes = [vp]
+    L.tara_ens_group_info.argtypes = [vp, c_int, ip, ip, ip, dp]
+    L.tara_ens_launches_per_step.argtypes = [vp]
     L.tara2d_diag_reference.argtypes = [vp, vp, dp, dp]
     L.tara2d_real_fields.argtypes = [vp, vp, dp, dp, dp, dp]
     L.tara_fft2d_r2c.argtypes = [c_int, c_int, c_int, dp, dp]
@@ -464,3 +484,92 @@ class Solver3D:
 
     def synchronize(self):
         _check(lib().tara3d_synchronize(self._h))
+
+    @property
+    def stream(self) -> int:
+        return lib().tara3d_stream(self._h) or 0
+
+    def diag(self):
+        out = (ctypes.c_double * 4)()
+        _check(lib().tara3d_diag(self._h, out))
+        return list(out)
+
+
+# ---------------------------------------------------------------------------
+# Ensembles of runs of uneven sizes
+# ---------------------------------------------------------------------------
+class EnsRun(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int), ("k0", ctypes.c_double), ("seed", ctypes.c_uint64)]
+
+
+class Ensemble:
+    """tara_ens handle: runs grouped by size, one CUDA-graph launch per step."""
+
+    def __init__(self, runs, *, precision=PREC_FP32, scheme=SCHEME_RK4, nu=1e-3, dt=1e-4,
+                 energy=0.5):
+        arr = (EnsRun * len(runs))(*[EnsRun(int(n), float(k0), int(seed)) for n, k0, seed in runs])
+        h = ctypes.c_void_p()
+        _check(lib().tara_ens_create(len(runs), ctypes.cast(arr, ctypes.c_void_p), precision, scheme,
+                                     nu, dt, energy, ctypes.byref(h)))
+        self._h = h
+        self.runs = list(runs)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().tara_ens_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def autotune(self, trial_steps: int = 3):
+        _check(lib().tara_ens_autotune(self._h, int(trial_steps)))
+
+    def step(self, n: int = 1):
+        _check(lib().tara_ens_step(self._h, int(n)))
+
+    def synchronize(self):
+        _check(lib().tara_ens_synchronize(self._h))
+
+    @property
+    def stream(self) -> int:
+        return lib().tara_ens_stream(self._h) or 0
+
+    @property
+    def launches_per_step(self) -> int:
+        return lib().tara_ens_launches_per_step(self._h)
+
+    def get_state(self, run: int) -> np.ndarray:
+        n = self.runs[run][0]
+        out = np.zeros((n, n // 2 + 1), np.complex128)
+        _check(lib().tara_ens_get_state(self._h, run, _dp(out.view(np.float64))))
+        return out
+
+    def set_state(self, run: int, w: np.ndarray) -> None:
+        n = self.runs[run][0]
+        w = _as_spectrum(w, n // 2 + 1, n)
+        _check(lib().tara_ens_set_state(self._h, run, _dp(w.view(np.float64))))
+
+    def diag(self, run: int):
+        e, z = ctypes.c_double(), ctypes.c_double()
+        _check(lib().tara_ens_diag(self._h, run, ctypes.byref(e), ctypes.byref(z)))
+        return e.value, z.value
+
+    def groups(self):
+        out = []
+        for g in range(lib().tara_ens_groups(self._h)):
+            n, r = ctypes.c_int(), ctypes.c_int()
+            v = (ctypes.c_int * 3)()
+            ms = (ctypes.c_double * 6)()
+            _check(lib().tara_ens_group_info(self._h, g, ctypes.byref(n), ctypes.byref(r), v, ms))
+            out.append({"n": n.value, "runs": r.value, "variants": list(v), "tuned_ms": list(ms)})
+        return out

@@ -37,12 +37,15 @@ void make_inverse_table(int nx, int ny, const double* kx, const double* ky, bool
 // Precision-dispatched launchers (one translation unit per precision).
 template <typename T>
 struct Launch2D {
+  // nb: runs in the batch (grid dimension); v: tile variant (0 default, 1 half tile)
   static int col_inverse(int ny, int nh, const double2* win, void* u, const Grid2D& g,
-                         const RhsParams& p, const void* twy, cudaStream_t s);
+                         const RhsParams& p, const void* twy, cudaStream_t s, int nb = 1,
+                         int v = 0);
   static int row_nl(int nx, int ny, const void* u, void* nl, const Grid2D& g, const void* twx,
-                    cudaStream_t s);
+                    cudaStream_t s, int nb = 1, int v = 0);
   static int col_forward(int ny, int nh, const void* nl, const StepBufs& sb, const Grid2D& g,
-                         const RhsParams& p, int mode, const void* twy, cudaStream_t s);
+                         const RhsParams& p, int mode, const void* twy, cudaStream_t s,
+                         int nb = 1, int v = 0);
   static int col_fft(int ny, int nh, int pitch, const void* in, void* out, bool inverse,
                      const void* twy, cudaStream_t s);
   static int row_c2r(int nx, int ny, int pitch, int rpitch, const void* in, void* out,
@@ -58,6 +61,8 @@ int make_twiddles(int n, bool fp32, void** dev);
 
 struct tara2d {
   tara2d_config cfg;
+  int batch = 1;          // runs advanced together (config 4 ensembles)
+  int var[3] = {0, 0, 0};  // tile variants of the three kernels (autotuner)
   int dev = 0;
   int nx = 0, ny = 0, nh = 0, pitch = 0;
   cudaStream_t stream = nullptr;

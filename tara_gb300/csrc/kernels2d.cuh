@@ -68,24 +68,28 @@ __host__ __device__ constexpr int pick_rp(int n, int csize) {
   return rp;
 }
 
-template <typename T, int N> struct ColCfg {
+// V selects a tile variant for the autotuner: 0 the default tile, 1 half of it.
+template <typename T, int N, int V = 0> struct ColCfg {
   typedef typename cplx_of<T>::type C;
   static constexpr int G = fft_group(N);
   static constexpr int S = N + 1;  // smem column stride (one element of padding)
-  static constexpr int TCA = pick_tc(2 * S * (int)sizeof(C), 2 * G);  // pass A: 2 slots/column
+  static constexpr int TCA0 = pick_tc(2 * S * (int)sizeof(C), 2 * G);  // pass A: 2 slots/column
   // pass C: 1 slot/column; a small tile keeps the live (not fully truncated)
   // columns spread evenly over the SMs
-  static constexpr int TCC = pick_tc(S * (int)sizeof(C), G, 48 * 1024);
+  static constexpr int TCC0 = pick_tc(S * (int)sizeof(C), G, 48 * 1024);
+  static constexpr int TCA = (V == 1 && TCA0 > 1) ? TCA0 / 2 : TCA0;
+  static constexpr int TCC = (V == 1 && TCC0 > 1) ? TCC0 / 2 : TCC0;
   static constexpr int THREADS_A = 2 * TCA * G;
   static constexpr int THREADS_C = TCC * G;
   static constexpr int SMEM_A = 2 * TCA * S * (int)sizeof(C);
   static constexpr int SMEM_C = TCC * S * (int)sizeof(C);
 };
 
-template <typename T, int N> struct RowCfg {
+template <typename T, int N, int V = 0> struct RowCfg {
   typedef typename cplx_of<T>::type C;
   static constexpr int G = fft_group(N);
-  static constexpr int RP = pick_rp(N, (int)sizeof(C));
+  static constexpr int RP0 = pick_rp(N, (int)sizeof(C));
+  static constexpr int RP = (V == 1 && RP0 > 1) ? RP0 / 2 : RP0;
   static constexpr int THREADS = 4 * RP * G;
   static constexpr int SMEM = RP * 4 * N * (int)sizeof(C);
 };
@@ -95,12 +99,13 @@ template <typename T, int N> struct RowCfg {
 // ---------------------------------------------------------------------------
 // blockIdx.y = 0: (u_x, u_y); blockIdx.y = 1: (i kx w, i ky w).  Splitting the
 // two field pairs over the grid halves the tail of the last wave.
-template <typename T, int N>
-__global__ void __launch_bounds__(ColCfg<T, N>::THREADS_A)
+// blockIdx.z = run of a batch (runs are ny*pitch apart in every field).
+template <typename T, int N, int V>
+__global__ void __launch_bounds__(ColCfg<T, N, V>::THREADS_A)
     k_col_inverse(const double2* __restrict__ win, typename cplx_of<T>::type* __restrict__ u,
                   Grid2D g, RhsParams p, const typename cplx_of<T>::type* __restrict__ tw) {
   typedef typename cplx_of<T>::type C;
-  typedef ColCfg<T, N> CF;
+  typedef ColCfg<T, N, V> CF;
   constexpr int TC = CF::TCA, S = CF::S, G = CF::G;
   extern __shared__ __align__(16) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);  // [2][TC][S]
@@ -108,6 +113,8 @@ __global__ void __launch_bounds__(ColCfg<T, N>::THREADS_A)
   const int pair = blockIdx.y;
   const int tid = threadIdx.x;
   const size_t fsz = (size_t)g.ny * g.pitch;
+  win += blockIdx.z * fsz;
+  u += blockIdx.z * 4 * fsz;
   const int slot = tid / G, lane = tid % G;
   for (int e = tid; e < N * TC; e += CF::THREADS_A) {
     const int y = e / TC, c = e % TC, x = x0 + c;
@@ -155,13 +162,14 @@ __global__ void __launch_bounds__(ColCfg<T, N>::THREADS_A)
 // 2 and 3 the same for row b = a + 1.  Hermitian extension of a half row A:
 // Z[k] = A[k] + i B[k] (k <= N/2), Z[N-k] = conj(A[k]) + i conj(B[k]), with the
 // imaginary parts of the k = 0 and k = N/2 bins dropped first.
-template <typename T, int N>
-__global__ void __launch_bounds__(RowCfg<T, N>::THREADS)
+// blockIdx.y = run of a batch.
+template <typename T, int N, int V>
+__global__ void __launch_bounds__(RowCfg<T, N, V>::THREADS)
     k_row_nl(const typename cplx_of<T>::type* __restrict__ u,
              typename cplx_of<T>::type* __restrict__ nl, Grid2D g,
              const typename cplx_of<T>::type* __restrict__ tw) {
   typedef typename cplx_of<T>::type C;
-  typedef RowCfg<T, N> RC;
+  typedef RowCfg<T, N, V> RC;
   constexpr int G = RC::G, H = N / 2, RP = RC::RP;
   extern __shared__ __align__(16) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);  // [RP][4][N]
@@ -169,6 +177,8 @@ __global__ void __launch_bounds__(RowCfg<T, N>::THREADS)
   const int slot = tid / G, lane = tid % G;
   const int y_base = blockIdx.x * (2 * RP);
   const size_t fsz = (size_t)g.ny * g.pitch;
+  u += blockIdx.y * 4 * fsz;
+  nl += blockIdx.y * fsz;
   for (int e = tid; e < RP * 4 * N; e += RC::THREADS) {
     const int k = e % N, sl = e / N;
     const int pp = sl >> 2, s = sl & 3;
@@ -226,17 +236,28 @@ struct StepBufs {
   unsigned int* flag;  // bit 0: a non-finite value was produced
 };
 
-template <typename T, int N>
-__global__ void __launch_bounds__(ColCfg<T, N>::THREADS_C)
+// blockIdx.y = run of a batch.
+template <typename T, int N, int V>
+__global__ void __launch_bounds__(ColCfg<T, N, V>::THREADS_C)
     k_col_forward(const typename cplx_of<T>::type* __restrict__ nl, StepBufs sb, Grid2D g,
                   RhsParams p, int mode, const typename cplx_of<T>::type* __restrict__ tw) {
   typedef typename cplx_of<T>::type C;
-  typedef ColCfg<T, N> CF;
+  typedef ColCfg<T, N, V> CF;
   constexpr int TC = CF::TCC, S = CF::S, G = CF::G;
   extern __shared__ __align__(16) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);  // [TC][S]
   const int x0 = blockIdx.x * TC;
   const int tid = threadIdx.x;
+  {
+    const size_t off = blockIdx.y * (size_t)g.ny * g.pitch;
+    nl += off;
+    sb.win += off;
+    if (sb.w0) sb.w0 += off;
+    if (sb.ws) sb.ws += off;
+    if (sb.acc) sb.acc += off;
+    if (sb.fold) sb.fold += off;
+    if (sb.fout) sb.fout += off;
+  }
   // Tiles whose columns all lie at kx >= i0max lose the whole nonlinear term to
   // the 2/3 rule: their transform is skipped (uniform per CTA, so the barriers
   // inside fft_slot stay matched).

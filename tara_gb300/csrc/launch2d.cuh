@@ -26,42 +26,42 @@ static cudaError_t allow_smem(K kernel, int bytes) {
     default: return set_error(TARA_ERR_ARGS, "grid size must be a power of two in [16, 2048]"); \
   }
 
-template <typename T, int N>
+template <typename T, int N, int V>
 static int launch_col_inverse(int nh, const double2* win, void* u, const Grid2D& g,
-                              const RhsParams& p, const void* tw, cudaStream_t s) {
+                              const RhsParams& p, const void* tw, cudaStream_t s, int nb) {
   typedef typename cplx_of<T>::type C;
-  typedef ColCfg<T, N> CF;
-  static cudaError_t attr = allow_smem(k_col_inverse<T, N>, CF::SMEM_A);
+  typedef ColCfg<T, N, V> CF;
+  static cudaError_t attr = allow_smem(k_col_inverse<T, N, V>, CF::SMEM_A);
   TARA_CK(attr);
-  const dim3 blocks((nh + CF::TCA - 1) / CF::TCA, 2);
-  k_col_inverse<T, N><<<blocks, CF::THREADS_A, CF::SMEM_A, s>>>(win, (C*)u, g, p, (const C*)tw);
+  const dim3 blocks((nh + CF::TCA - 1) / CF::TCA, 2, nb);
+  k_col_inverse<T, N, V><<<blocks, CF::THREADS_A, CF::SMEM_A, s>>>(win, (C*)u, g, p, (const C*)tw);
   TARA_CK(cudaGetLastError());
   return TARA_OK;
 }
 
-template <typename T, int N>
+template <typename T, int N, int V>
 static int launch_row_nl(int ny, const void* u, void* nl, const Grid2D& g, const void* tw,
-                         cudaStream_t s) {
+                         cudaStream_t s, int nb) {
   typedef typename cplx_of<T>::type C;
-  typedef RowCfg<T, N> RC;
-  static cudaError_t attr = allow_smem(k_row_nl<T, N>, RC::SMEM);
+  typedef RowCfg<T, N, V> RC;
+  static cudaError_t attr = allow_smem(k_row_nl<T, N, V>, RC::SMEM);
   TARA_CK(attr);
-  const int blocks = (ny + 2 * RC::RP - 1) / (2 * RC::RP);
-  k_row_nl<T, N><<<blocks, RC::THREADS, RC::SMEM, s>>>((const C*)u, (C*)nl, g, (const C*)tw);
+  const dim3 blocks((ny + 2 * RC::RP - 1) / (2 * RC::RP), nb);
+  k_row_nl<T, N, V><<<blocks, RC::THREADS, RC::SMEM, s>>>((const C*)u, (C*)nl, g, (const C*)tw);
   TARA_CK(cudaGetLastError());
   return TARA_OK;
 }
 
-template <typename T, int N>
+template <typename T, int N, int V>
 static int launch_col_forward(int nh, const void* nl, const StepBufs& sb, const Grid2D& g,
-                              const RhsParams& p, int mode, const void* tw, cudaStream_t s) {
+                              const RhsParams& p, int mode, const void* tw, cudaStream_t s, int nb) {
   typedef typename cplx_of<T>::type C;
-  typedef ColCfg<T, N> CF;
-  static cudaError_t attr = allow_smem(k_col_forward<T, N>, CF::SMEM_C);
+  typedef ColCfg<T, N, V> CF;
+  static cudaError_t attr = allow_smem(k_col_forward<T, N, V>, CF::SMEM_C);
   TARA_CK(attr);
-  const int blocks = (nh + CF::TCC - 1) / CF::TCC;
-  k_col_forward<T, N><<<blocks, CF::THREADS_C, CF::SMEM_C, s>>>((const C*)nl, sb, g, p, mode,
-                                                                 (const C*)tw);
+  const dim3 blocks((nh + CF::TCC - 1) / CF::TCC, nb);
+  k_col_forward<T, N, V><<<blocks, CF::THREADS_C, CF::SMEM_C, s>>>((const C*)nl, sb, g, p, mode,
+                                                                    (const C*)tw);
   TARA_CK(cudaGetLastError());
   return TARA_OK;
 }
@@ -110,22 +110,35 @@ static int launch_row_r2c(int ny, int rpitch, int pitch, const void* in, void* o
 
 template <typename T>
 int Launch2D<T>::col_inverse(int ny, int nh, const double2* win, void* u, const Grid2D& g,
-                             const RhsParams& p, const void* twy, cudaStream_t s) {
-  TARA_SWITCH_N(ny, return (launch_col_inverse<T, N>(nh, win, u, g, p, twy, s)));
+                             const RhsParams& p, const void* twy, cudaStream_t s, int nb, int v) {
+  if (v) {
+    TARA_SWITCH_N(ny, return (launch_col_inverse<T, N, 1>(nh, win, u, g, p, twy, s, nb)));
+  } else {
+    TARA_SWITCH_N(ny, return (launch_col_inverse<T, N, 0>(nh, win, u, g, p, twy, s, nb)));
+  }
   return TARA_OK;
 }
 
 template <typename T>
 int Launch2D<T>::row_nl(int nx, int ny, const void* u, void* nl, const Grid2D& g, const void* twx,
-                        cudaStream_t s) {
-  TARA_SWITCH_N(nx, return (launch_row_nl<T, N>(ny, u, nl, g, twx, s)));
+                        cudaStream_t s, int nb, int v) {
+  if (v) {
+    TARA_SWITCH_N(nx, return (launch_row_nl<T, N, 1>(ny, u, nl, g, twx, s, nb)));
+  } else {
+    TARA_SWITCH_N(nx, return (launch_row_nl<T, N, 0>(ny, u, nl, g, twx, s, nb)));
+  }
   return TARA_OK;
 }
 
 template <typename T>
 int Launch2D<T>::col_forward(int ny, int nh, const void* nl, const StepBufs& sb, const Grid2D& g,
-                             const RhsParams& p, int mode, const void* twy, cudaStream_t s) {
-  TARA_SWITCH_N(ny, return (launch_col_forward<T, N>(nh, nl, sb, g, p, mode, twy, s)));
+                             const RhsParams& p, int mode, const void* twy, cudaStream_t s, int nb,
+                             int v) {
+  if (v) {
+    TARA_SWITCH_N(ny, return (launch_col_forward<T, N, 1>(nh, nl, sb, g, p, mode, twy, s, nb)));
+  } else {
+    TARA_SWITCH_N(ny, return (launch_col_forward<T, N, 0>(nh, nl, sb, g, p, mode, twy, s, nb)));
+  }
   return TARA_OK;
 }
 

@@ -629,6 +629,8 @@ int tara3d_rhs(tara3d* h, double* d8) {
   return set_ok();
 }
 
+void* tara3d_stream(tara3d* h) { return h ? (void*)h->stream : nullptr; }
+
 int tara3d_diag(tara3d* h, double* out4) {
   if (!h || !out4) return set_error(TARA_ERR_ARGS, "null argument");
   TARA_CK(cudaSetDevice(h->dev));

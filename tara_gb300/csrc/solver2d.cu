@@ -267,13 +267,17 @@ static int rhs_update_t(tara2d* h, const double2* win, int mode, cudaEvent_t* ev
   sb.fout = h->fout;
   sb.flag = h->flag;
   int rc;
-  if ((rc = Launch2D<T>::col_inverse(h->ny, h->nh, win, h->u, h->grid, h->rp, h->twy, h->stream)))
+  const int nb = h->batch;
+  if ((rc = Launch2D<T>::col_inverse(h->ny, h->nh, win, h->u, h->grid, h->rp, h->twy, h->stream, nb,
+                                     h->var[0])))
     return rc;
   if (ev) TARA_CK(cudaEventRecord(ev[0], h->stream));
-  if ((rc = Launch2D<T>::row_nl(h->nx, h->ny, h->u, h->nl, h->grid, h->twx, h->stream))) return rc;
+  if ((rc = Launch2D<T>::row_nl(h->nx, h->ny, h->u, h->nl, h->grid, h->twx, h->stream, nb,
+                                h->var[1])))
+    return rc;
   if (ev) TARA_CK(cudaEventRecord(ev[1], h->stream));
   if ((rc = Launch2D<T>::col_forward(h->ny, h->nh, h->nl, sb, h->grid, h->rp, mode, h->twy,
-                                     h->stream)))
+                                     h->stream, nb, h->var[2])))
     return rc;
   if (ev) TARA_CK(cudaEventRecord(ev[2], h->stream));
   return TARA_OK;
@@ -361,6 +365,7 @@ void tara2d_default_config(tara2d_config* c, int nx, int ny) {
   c->kpi = (double)3.1428f;
   c->lx = 2.0 * c->kpi;
   c->ly = 2.0 * c->kpi;
+  c->batch = 1;
 }
 
 int tara2d_destroy(tara2d* h) {
@@ -389,8 +394,10 @@ int tara2d_create(const tara2d_config* cfg, tara2d** out) {
     return set_error(TARA_ERR_ARGS, "unknown precision");
   if (!(cfg->lx > 0.0) || !(cfg->ly > 0.0) || !(cfg->kpi > 0.0))
     return set_error(TARA_ERR_ARGS, "box lengths and kpi must be positive");
+  if (cfg->batch < 1 || cfg->batch > 65535) return set_error(TARA_ERR_ARGS, "batch must be in [1, 65535]");
   tara2d* h = new tara2d();
   h->cfg = *cfg;
+  h->batch = cfg->batch;
   h->nx = cfg->nx;
   h->ny = cfg->ny;
   h->nh = cfg->nx / 2 + 1;
@@ -407,9 +414,9 @@ int tara2d_create(const tara2d_config* cfg, tara2d** out) {
   } while (0)
   CKC(cudaGetDevice(&h->dev));
   CKC(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
-  const size_t fbytes = (size_t)h->ny * h->pitch * sizeof(double2);
+  const size_t fbytes = (size_t)h->batch * h->ny * h->pitch * sizeof(double2);
   const size_t csize = cfg->precision == TARA_PREC_FP32 ? sizeof(float2) : sizeof(double2);
-  const size_t wbytes = (size_t)h->ny * h->pitch * csize;
+  const size_t wbytes = (size_t)h->batch * h->ny * h->pitch * csize;
   CKC(cudaMalloc(&h->w0, fbytes));
   CKC(cudaMalloc(&h->fold, fbytes));
   CKC(cudaMalloc(&h->fout, fbytes));
@@ -451,28 +458,38 @@ int tara2d_create(const tara2d_config* cfg, tara2d** out) {
   return set_ok();
 }
 
-int tara2d_set_state(tara2d* h, const double* omegak, const double* dt_old) {
-  if (!h || !omegak) return set_error(TARA_ERR_ARGS, "null argument");
+int tara2d_set_state_run(tara2d* h, int run, const double* omegak, const double* dt_old) {
+  if (!h || !omegak || run < 0 || run >= h->batch) return set_error(TARA_ERR_ARGS, "bad argument");
   TARA_CK(cudaSetDevice(h->dev));
+  const size_t off = (size_t)run * h->ny * h->pitch;
   int rc;
-  if ((rc = copy_in_dense(h, h->w0, omegak))) return rc;
+  if ((rc = copy_in_dense(h, h->w0 + off, omegak))) return rc;
   if (dt_old) {
-    if ((rc = copy_in_dense(h, h->fold, dt_old))) return rc;
+    if ((rc = copy_in_dense(h, h->fold + off, dt_old))) return rc;
   } else {
-    TARA_CK(cudaMemsetAsync(h->fold, 0, (size_t)h->ny * h->pitch * sizeof(double2), h->stream));
+    TARA_CK(cudaMemsetAsync(h->fold + off, 0, (size_t)h->ny * h->pitch * sizeof(double2), h->stream));
   }
   TARA_CK(cudaStreamSynchronize(h->stream));
   return set_ok();
 }
 
-int tara2d_get_state(tara2d* h, double* omegak, double* dt_old) {
-  if (!h || !omegak) return set_error(TARA_ERR_ARGS, "null argument");
+int tara2d_get_state_run(tara2d* h, int run, double* omegak, double* dt_old) {
+  if (!h || !omegak || run < 0 || run >= h->batch) return set_error(TARA_ERR_ARGS, "bad argument");
   TARA_CK(cudaSetDevice(h->dev));
+  const size_t off = (size_t)run * h->ny * h->pitch;
   int rc;
-  if ((rc = copy_out_dense(h, omegak, h->w0))) return rc;
-  if (dt_old && (rc = copy_out_dense(h, dt_old, h->fold))) return rc;
+  if ((rc = copy_out_dense(h, omegak, h->w0 + off))) return rc;
+  if (dt_old && (rc = copy_out_dense(h, dt_old, h->fold + off))) return rc;
   TARA_CK(cudaStreamSynchronize(h->stream));
   return set_ok();
+}
+
+int tara2d_set_state(tara2d* h, const double* omegak, const double* dt_old) {
+  return tara2d_set_state_run(h, 0, omegak, dt_old);
+}
+
+int tara2d_get_state(tara2d* h, double* omegak, double* dt_old) {
+  return tara2d_get_state_run(h, 0, omegak, dt_old);
 }
 
 int tara2d_set_state_device(tara2d* h, const void* omegak, const void* dt_old) {
@@ -575,10 +592,11 @@ int tara2d_rhs(tara2d* h, double* dt_omegak) {
   return set_ok();
 }
 
-int tara2d_diag(tara2d* h, double* energy, double* enstrophy) {
-  if (!h) return set_error(TARA_ERR_ARGS, "null handle");
+int tara2d_diag_run(tara2d* h, int run, double* energy, double* enstrophy) {
+  if (!h || run < 0 || run >= h->batch) return set_error(TARA_ERR_ARGS, "bad argument");
   TARA_CK(cudaSetDevice(h->dev));
-  k_diag_partial<<<kDiagBlocks, kDiagThreads, 0, h->stream>>>(h->w0, h->grid, h->diag_part);
+  k_diag_partial<<<kDiagBlocks, kDiagThreads, 0, h->stream>>>(
+      h->w0 + (size_t)run * h->ny * h->pitch, h->grid, h->diag_part);
   TARA_CK(cudaGetLastError());
   const double nn = (double)h->nx * (double)h->ny;
   k_diag_final<<<1, 32, 0, h->stream>>>(h->diag_part, kDiagBlocks, 0.5 / (nn * nn), h->diag_out,
@@ -592,6 +610,10 @@ int tara2d_diag(tara2d* h, double* energy, double* enstrophy) {
   int rc;
   if ((rc = check_flag(h))) return rc;
   return set_ok();
+}
+
+int tara2d_diag(tara2d* h, double* energy, double* enstrophy) {
+  return tara2d_diag_run(h, 0, energy, enstrophy);
 }
 
 int tara2d_synchronize(tara2d* h) {
@@ -728,7 +750,12 @@ static void philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t
 }
 
 int tara2d_init_random(tara2d* h, double k0, double energy, uint64_t seed) {
-  if (!h || !(k0 > 0.0) || !(energy > 0.0)) return set_error(TARA_ERR_ARGS, "bad arguments");
+  return tara2d_init_random_run(h, 0, k0, energy, seed);
+}
+
+int tara2d_init_random_run(tara2d* h, int run, double k0, double energy, uint64_t seed) {
+  if (!h || !(k0 > 0.0) || !(energy > 0.0) || run < 0 || run >= h->batch)
+    return set_error(TARA_ERR_ARGS, "bad arguments");
   TARA_CK(cudaSetDevice(h->dev));
   const int nx = h->nx, ny = h->ny, nh = h->nh;
   const double pi = 3.14159265358979323846;
@@ -753,7 +780,10 @@ int tara2d_init_random(tara2d* h, double k0, double energy, uint64_t seed) {
     }
   }
   int rc;
-  if ((rc = copy_in_dense(h, h->w0, (const double*)spec.data()))) return rc;
+  const size_t off = (size_t)run * ny * h->pitch;
+  double2* w0 = h->w0 + off;
+  double2* tmp = h->fout + off;
+  if ((rc = copy_in_dense(h, w0, (const double*)spec.data()))) return rc;
   // Hermitian projection: c2r then r2c (FP64 transforms), scaled by 1/(Nx Ny)
   const int rpitch = round_up(nx, 8);
   double* real = nullptr;
@@ -764,24 +794,24 @@ int tara2d_init_random(tara2d* h, double k0, double energy, uint64_t seed) {
     return rc;
   }
   TARA_CK(cudaMalloc(&real, (size_t)ny * rpitch * sizeof(double)));
-  TARA_CK(cudaMemcpyAsync(h->fout, h->w0, (size_t)ny * h->pitch * sizeof(double2),
+  TARA_CK(cudaMemcpyAsync(tmp, w0, (size_t)ny * h->pitch * sizeof(double2),
                           cudaMemcpyDeviceToDevice, h->stream));
-  rc = Launch2D<double>::col_fft(ny, nh, h->pitch, h->fout, h->fout, true, ty, h->stream);
-  if (!rc) rc = Launch2D<double>::row_c2r(nx, ny, h->pitch, rpitch, h->fout, real, tx, h->stream);
-  if (!rc) rc = Launch2D<double>::row_r2c(nx, ny, rpitch, h->pitch, real, h->w0, tx, h->stream);
-  if (!rc) rc = Launch2D<double>::col_fft(ny, nh, h->pitch, h->w0, h->w0, false, ty, h->stream);
+  rc = Launch2D<double>::col_fft(ny, nh, h->pitch, tmp, tmp, true, ty, h->stream);
+  if (!rc) rc = Launch2D<double>::row_c2r(nx, ny, h->pitch, rpitch, tmp, real, tx, h->stream);
+  if (!rc) rc = Launch2D<double>::row_r2c(nx, ny, rpitch, h->pitch, real, w0, tx, h->stream);
+  if (!rc) rc = Launch2D<double>::col_fft(ny, nh, h->pitch, w0, w0, false, ty, h->stream);
   if (!rc) {
     const double nn = (double)nx * (double)ny;
-    TARA_CK(cudaMemsetAsync(h->w0, 0, sizeof(double2), h->stream));  // zero mean vorticity
-    k_mul<<<304, 256, 0, h->stream>>>(h->w0, (size_t)ny * h->pitch, 1.0 / nn);
+    TARA_CK(cudaMemsetAsync(w0, 0, sizeof(double2), h->stream));  // zero mean vorticity
+    k_mul<<<304, 256, 0, h->stream>>>(w0, (size_t)ny * h->pitch, 1.0 / nn);
     TARA_CK(cudaGetLastError());
     double e0 = 0.0;
-    rc = tara2d_diag(h, &e0, nullptr);
+    rc = tara2d_diag_run(h, run, &e0, nullptr);
     if (!rc) {
-      k_mul<<<304, 256, 0, h->stream>>>(h->w0, (size_t)ny * h->pitch,
+      k_mul<<<304, 256, 0, h->stream>>>(w0, (size_t)ny * h->pitch,
                                         e0 > 0.0 ? std::sqrt(energy / e0) : 1.0);
       TARA_CK(cudaGetLastError());
-      TARA_CK(cudaMemsetAsync(h->fold, 0, (size_t)ny * h->pitch * sizeof(double2), h->stream));
+      TARA_CK(cudaMemsetAsync(h->fold + off, 0, (size_t)ny * h->pitch * sizeof(double2), h->stream));
     }
   }
   TARA_CK(cudaStreamSynchronize(h->stream));
