@@ -317,8 +317,9 @@ def run_ensemble(args) -> None:
     import tara_gb300 as tg
 
     torch.cuda.set_device(0)
-    k0 = np.random.default_rng(4000).uniform(4.0, 10.0, 384)
-    runs = [(n, float(k0[r]), 4000 + r) for r, n in enumerate([128] * 128 + [256] * 128 + [512] * 128)]
+    per = args.ens_runs_per_size
+    k0 = np.random.default_rng(4000).uniform(4.0, 10.0, 3 * per)
+    runs = [(n, float(k0[r]), 4000 + r) for r, n in enumerate([128] * per + [256] * per + [512] * per)]
     e = tg.Ensemble(runs, precision=tg.PREC_FP32, nu=1e-3, dt=1e-4)
     e.autotune(3)
     e.step(args.warmup)
@@ -326,7 +327,7 @@ def run_ensemble(args) -> None:
     ms = timed_on_stream(e.stream, lambda: e.step(args.steps))
     e.synchronize()
     pts = sum(n * n for n, _, _ in runs)
-    line = {"metric": "ensemble grid-pt*steps/s (384 runs: 128 each at 128^2, 256^2, 512^2; RK4)",
+    line = {"metric": f"ensemble grid-pt*steps/s ({3 * per} runs: {per} each at 128^2, 256^2, 512^2; RK4)",
             "value": pts * args.steps / (ms * 1e-3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
             "dtype": "f32 transforms / f64 state", "data": "synthetic (seeded random-phase spectra)",
@@ -419,6 +420,8 @@ def main() -> None:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="rk4-2048", choices=["rk4-2048", "ensemble", "mhd3d"],
                     help="rk4-2048 is the headline; the others measure configs 4 and 3")
+    ap.add_argument("--ens-runs-per-size", type=int, default=128,
+                    help="ensemble: runs of each size (config 4 uses 128)")
     ap.add_argument("--ens-error-steps", type=int, default=0,
                     help="ensemble: also report the per-run error vs FP64 after this many steps")
     args = ap.parse_args()

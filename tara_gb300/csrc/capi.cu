@@ -86,6 +86,8 @@ void derive_common(int rhs, const int* Nx, const int* Ny, const int* Nh, double 
   if (rhs == TARA_RHS_SCREEN && sync_css(h)) return;
   h->rp.nu = nu;
   h->rp.alpha = alpha;
+  h->rp.nu_f = (float)nu;
+  h->rp.alpha_f = (float)alpha;
   if (copy_in_dense(h, h->w0, omegak)) return;
   if (rhs_and_update(h, h->w0, MODE_DERIVE, nullptr)) return;
   if (copy_out_dense(h, dt_omegak_new, h->fout)) return;
@@ -189,6 +191,8 @@ void rk42css_(const int* Nx, const int* Ny, const int* Nh, const double* alpha, 
   if (sync_css(h)) return;
   h->rp.nu = *nu;
   h->rp.alpha = *alpha;
+  h->rp.nu_f = (float)*nu;
+  h->rp.alpha_f = (float)*alpha;
   h->rp.dt = *dt;
   h->cfg.dt = *dt;
   if (copy_in_dense(h, h->w0, omegak)) return;

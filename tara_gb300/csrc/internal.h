@@ -70,6 +70,7 @@ struct tara2d {
   void* u = nullptr;   // 4 fields of the y-inverse pass, precision of cfg
   void* nl = nullptr;  // x-r2c output of the products
   double *kx = nullptr, *ky = nullptr, *inv = nullptr;
+  float* tabf = nullptr;  // kx, ky, inv in FP32 (nh + ny + nh*ny floats)
   int* i0 = nullptr;
   void *twx = nullptr, *twy = nullptr;
   double *diag_part = nullptr, *diag_out = nullptr;

@@ -35,6 +35,11 @@ struct Grid2D {
   const int* __restrict__ i0;      // [ny]: first kx index removed by the 2/3 rule
   const double* __restrict__ inv;  // [ny][nh]: 1/(kx^2+ky^2) (+lambda when screened), 0 at k = 0
   int i0max;                       // columns x >= i0max lose the whole nonlinear term
+  // FP32 copies of kx, ky, inv for the FP32-transform mode, whose spectral
+  // products run in FP32 (only the state update stays FP64)
+  const float* __restrict__ kxf;
+  const float* __restrict__ kyf;
+  const float* __restrict__ invf;
 };
 
 enum StepMode {
@@ -51,6 +56,7 @@ struct RhsParams {
   double nu, alpha, lambda;
   double nl_scale;  // 1/2 (pair split) * 1/(Nx Ny)^2 (two unnormalised c2r)
   double dt;
+  float nu_f, alpha_f, nl_scale_f;  // the same in FP32 for the FP32-transform mode
 };
 
 // Largest power-of-two column tile with tile smem <= budget and <= 512 threads.
@@ -91,7 +97,8 @@ template <typename T, int N, int V = 0> struct RowCfg {
   static constexpr int RP0 = pick_rp(N, (int)sizeof(C));
   static constexpr int RP = (V == 1 && RP0 > 1) ? RP0 / 2 : RP0;
   static constexpr int THREADS = 4 * RP * G;
-  static constexpr int SMEM = RP * 4 * N * (int)sizeof(C);
+  static constexpr int SL = N;  // smem stride between row slots
+  static constexpr int SMEM = RP * 4 * SL * (int)sizeof(C);
 };
 
 // ---------------------------------------------------------------------------
@@ -119,7 +126,27 @@ __global__ void __launch_bounds__(ColCfg<T, N, V>::THREADS_A)
   for (int e = tid; e < N * TC; e += CF::THREADS_A) {
     const int y = e / TC, c = e % TC, x = x0 + c;
     C fa = mkc<T>(T(0), T(0)), fb = fa;
-    if (x < g.nh) {
+    if constexpr (sizeof(T) == 4) {
+      if (x < g.nh) {  // FP32 products from the FP64 state
+        const double2 wd = win[(size_t)y * g.pitch + x];
+        const float wx = (float)wd.x, wy = (float)wd.y;
+        const float kx = g.kxf[x], ky = g.kyf[y], inv = g.invf[(size_t)y * g.nh + x];
+        if (pair == 0) {
+          const float pr = wx * inv, pim = wy * inv;
+          fa = mkc<T>(-ky * pim, ky * pr);
+          fb = mkc<T>(kx * pim, -(kx * pr));
+        } else {
+          float dr = wx, di = wy;
+          if (p.rhs) {
+            const float k2 = kx * kx + ky * ky;
+            dr = k2 * (wx * inv);
+            di = k2 * (wy * inv);
+          }
+          fa = mkc<T>(-kx * di, kx * dr);
+          fb = mkc<T>(-ky * di, ky * dr);
+        }
+      }
+    } else if (x < g.nh) {
       const double2 w = win[(size_t)y * g.pitch + x];
       const double kx = g.kx[x], ky = g.ky[y];
       const double inv = g.inv[(size_t)y * g.nh + x];  // 1/k^2 or 1/(k^2+lambda); 0 at k = 0
@@ -170,7 +197,7 @@ __global__ void __launch_bounds__(RowCfg<T, N, V>::THREADS)
              const typename cplx_of<T>::type* __restrict__ tw) {
   typedef typename cplx_of<T>::type C;
   typedef RowCfg<T, N, V> RC;
-  constexpr int G = RC::G, H = N / 2, RP = RC::RP;
+  constexpr int G = RC::G, H = N / 2, RP = RC::RP, SL = RC::SL;
   extern __shared__ __align__(16) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);  // [RP][4][N]
   const int tid = threadIdx.x;
@@ -195,27 +222,27 @@ __global__ void __launch_bounds__(RowCfg<T, N, V>::THREADS)
       }
       z = (k <= H) ? mkc<T>(A.x - B.y, A.y + B.x) : mkc<T>(A.x + B.y, -A.y + B.x);
     }
-    sm[sl * N + k] = z;
+    sm[sl * SL + k] = z;
   }
   __syncthreads();
-  fft_slot<T, N, true>(sm + slot * N, lane, true, tw);
+  fft_slot<T, N, true>(sm + slot * SL, lane, true, tw);
   // products u_x w_x + u_y w_y for rows a and b, packed as a + i b
   for (int e = tid; e < RP * N; e += RC::THREADS) {
     const int x = e % N, pp = e / N;
-    C* b = sm + (size_t)pp * 4 * N;
-    const C c1a = b[x], c2a = b[N + x], c1b = b[2 * N + x], c2b = b[3 * N + x];
+    C* b = sm + (size_t)pp * 4 * SL;
+    const C c1a = b[x], c2a = b[SL + x], c1b = b[2 * SL + x], c2b = b[3 * SL + x];
     const T na = fma(c1a.x, c2a.x, c1a.y * c2a.y);
     const T nb = fma(c1b.x, c2b.x, c1b.y * c2b.y);
     b[x] = mkc<T>(na, nb);
   }
   __syncthreads();
-  fft_slot<T, N, false>(sm + slot * N, lane, (slot & 3) == 0, tw);
+  fft_slot<T, N, false>(sm + slot * SL, lane, (slot & 3) == 0, tw);
   // split: 2 X_a[k] = Z[k] + conj Z[N-k], 2 X_b[k] = -i (Z[k] - conj Z[N-k])
   for (int e = tid; e < RP * (H + 1); e += RC::THREADS) {
     const int k = e % (H + 1), pp = e / (H + 1);
     const int ya = y_base + 2 * pp;
     if (ya < g.ny) {
-      const C* b = sm + (size_t)pp * 4 * N;
+      const C* b = sm + (size_t)pp * 4 * SL;
       const C z = b[k], m = b[(N - k) & (N - 1)];
       nl[(size_t)ya * g.pitch + k] = mkc<T>(z.x + m.x, z.y - m.y);
       nl[(size_t)(ya + 1) * g.pitch + k] = mkc<T>(z.y + m.y, -(z.x - m.x));
@@ -275,25 +302,47 @@ __global__ void __launch_bounds__(ColCfg<T, N, V>::THREADS_C)
     const int y = e / TC, c = e % TC, x = x0 + c;
     if (x >= g.nh) continue;
     const size_t q = (size_t)y * g.pitch + x;
-    double nr = 0.0, ni = 0.0;
-    if (x < g.i0[y]) {  // 2/3 truncation of the nonlinear term only
-      const C v = sm[c * S + y];
-      nr = (double)v.x * p.nl_scale;
-      ni = (double)v.y * p.nl_scale;
-    }
-    const double kx = g.kx[x], ky = g.ky[y];
-    const double k2 = kx * kx + ky * ky;
-    const double vk2 = p.nu * k2;
-    const double2 w = sb.win[q];
     double fr, fi;
-    if (p.rhs == 0) {
-      fr = -(nr + vk2 * w.x);
-      fi = -(ni + vk2 * w.y);
+    if constexpr (sizeof(T) == 4) {  // FP32 right-hand side, FP64 update below
+      float nr = 0.f, ni = 0.f;
+      if (x < g.i0[y]) {
+        const C v = sm[c * S + y];
+        nr = v.x * p.nl_scale_f;
+        ni = v.y * p.nl_scale_f;
+      }
+      const float kx = g.kxf[x], ky = g.kyf[y];
+      const float k2 = kx * kx + ky * ky;
+      const float vk2 = p.nu_f * k2;
+      const double2 wd = sb.win[q];
+      const float wx = (float)wd.x, wy = (float)wd.y;
+      if (p.rhs == 0) {
+        fr = (double)(-(nr + vk2 * wx));
+        fi = (double)(-(ni + vk2 * wy));
+      } else {
+        const float inv = g.invf[(size_t)y * g.nh + x];
+        fr = (double)(-(p.alpha_f * nr + vk2 * (k2 * (wx * inv))));
+        fi = (double)(-(p.alpha_f * ni + vk2 * (k2 * (wy * inv))));
+      }
     } else {
-      const double inv = g.inv[(size_t)y * g.nh + x];  // 1/(k^2+lambda), 0 at k = 0
-      const double dr = k2 * (w.x * inv), di = k2 * (w.y * inv);
-      fr = -(p.alpha * nr + vk2 * dr);
-      fi = -(p.alpha * ni + vk2 * di);
+      double nr = 0.0, ni = 0.0;
+      if (x < g.i0[y]) {  // 2/3 truncation of the nonlinear term only
+        const C v = sm[c * S + y];
+        nr = (double)v.x * p.nl_scale;
+        ni = (double)v.y * p.nl_scale;
+      }
+      const double kx = g.kx[x], ky = g.ky[y];
+      const double k2 = kx * kx + ky * ky;
+      const double vk2 = p.nu * k2;
+      const double2 w = sb.win[q];
+      if (p.rhs == 0) {
+        fr = -(nr + vk2 * w.x);
+        fi = -(ni + vk2 * w.y);
+      } else {
+        const double inv = g.inv[(size_t)y * g.nh + x];  // 1/(k^2+lambda), 0 at k = 0
+        const double dr = k2 * (w.x * inv), di = k2 * (w.y * inv);
+        fr = -(p.alpha * nr + vk2 * dr);
+        fi = -(p.alpha * ni + vk2 * di);
+      }
     }
     bad |= !(isfinite(fr) && isfinite(fi));
     const double dt = p.dt;
@@ -368,7 +417,7 @@ __global__ void __launch_bounds__(RowCfg<T, N>::THREADS)
               int pitch, int rpitch, const typename cplx_of<T>::type* __restrict__ tw) {
   typedef typename cplx_of<T>::type C;
   typedef RowCfg<T, N> RC;
-  constexpr int G = RC::G, H = N / 2, NP = 4 * RC::RP;  // NP row pairs per CTA
+  constexpr int G = RC::G, H = N / 2, NP = 4 * RC::RP, SL = RC::SL;  // NP row pairs per CTA
   extern __shared__ __align__(16) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);  // [NP][N]
   const int tid = threadIdx.x, y_base = blockIdx.x * (2 * NP);
@@ -384,14 +433,14 @@ __global__ void __launch_bounds__(RowCfg<T, N>::THREADS)
       }
       z = (k <= H) ? mkc<T>(A.x - B.y, A.y + B.x) : mkc<T>(A.x + B.y, -A.y + B.x);
     }
-    sm[pp * N + k] = z;
+    sm[pp * SL + k] = z;
   }
   __syncthreads();
-  fft_slot<T, N, true>(sm + (tid / G) * N, tid % G, true, tw);
+  fft_slot<T, N, true>(sm + (tid / G) * SL, tid % G, true, tw);
   for (int e = tid; e < NP * N; e += RC::THREADS) {
     const int x = e % N, pp = e / N, ya = y_base + 2 * pp;
     if (ya < ny) {
-      const C z = sm[pp * N + x];
+      const C z = sm[pp * SL + x];
       out[(size_t)ya * rpitch + x] = z.x;
       out[(size_t)(ya + 1) * rpitch + x] = z.y;
     }
@@ -405,21 +454,21 @@ __global__ void __launch_bounds__(RowCfg<T, N>::THREADS)
               int rpitch, int pitch, const typename cplx_of<T>::type* __restrict__ tw) {
   typedef typename cplx_of<T>::type C;
   typedef RowCfg<T, N> RC;
-  constexpr int G = RC::G, H = N / 2, NP = 4 * RC::RP;
+  constexpr int G = RC::G, H = N / 2, NP = 4 * RC::RP, SL = RC::SL;
   extern __shared__ __align__(16) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);
   const int tid = threadIdx.x, y_base = blockIdx.x * (2 * NP);
   for (int e = tid; e < NP * N; e += RC::THREADS) {
     const int x = e % N, pp = e / N, ya = y_base + 2 * pp;
-    sm[pp * N + x] = (ya < ny) ? mkc<T>(in[(size_t)ya * rpitch + x], in[(size_t)(ya + 1) * rpitch + x])
+    sm[pp * SL + x] = (ya < ny) ? mkc<T>(in[(size_t)ya * rpitch + x], in[(size_t)(ya + 1) * rpitch + x])
                                : mkc<T>(T(0), T(0));
   }
   __syncthreads();
-  fft_slot<T, N, false>(sm + (tid / G) * N, tid % G, true, tw);
+  fft_slot<T, N, false>(sm + (tid / G) * SL, tid % G, true, tw);
   for (int e = tid; e < NP * (H + 1); e += RC::THREADS) {
     const int k = e % (H + 1), pp = e / (H + 1), ya = y_base + 2 * pp;
     if (ya < ny) {
-      const C z = sm[pp * N + k], m = sm[pp * N + ((N - k) & (N - 1))];
+      const C z = sm[pp * SL + k], m = sm[pp * SL + ((N - k) & (N - 1))];
       out[(size_t)ya * pitch + k] = mkc<T>(T(0.5) * (z.x + m.x), T(0.5) * (z.y - m.y));
       out[(size_t)(ya + 1) * pitch + k] = mkc<T>(T(0.5) * (z.y + m.y), T(-0.5) * (z.x - m.x));
     }

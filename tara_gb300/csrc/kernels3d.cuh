@@ -54,7 +54,7 @@ __global__ void __launch_bounds__(RowCfg<T, N>::THREADS)
                const typename cplx_of<T>::type* __restrict__ tw) {
   typedef typename cplx_of<T>::type C;
   typedef RowCfg<T, N> RC;
-  constexpr int G = RC::G, H = N / 2, NP = 4 * RC::RP;
+  constexpr int G = RC::G, H = N / 2, NP = 4 * RC::RP, SL = RC::SL;
   extern __shared__ __align__(16) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);
   const int tid = threadIdx.x, y_base = blockIdx.x * (2 * NP);
@@ -72,14 +72,14 @@ __global__ void __launch_bounds__(RowCfg<T, N>::THREADS)
       }
       z = (k <= H) ? mkc<T>(A.x - B.y, A.y + B.x) : mkc<T>(A.x + B.y, -A.y + B.x);
     }
-    sm[pp * N + k] = z;
+    sm[pp * SL + k] = z;
   }
   __syncthreads();
-  fft_slot<T, N, true>(sm + (tid / G) * N, tid % G, true, tw);
+  fft_slot<T, N, true>(sm + (tid / G) * SL, tid % G, true, tw);
   for (int e = tid; e < NP * N; e += RC::THREADS) {
     const int x = e % N, pp = e / N, ya = y_base + 2 * pp;
     if (ya < rows) {
-      const C z = sm[pp * N + x];
+      const C z = sm[pp * SL + x];
       fout[(size_t)ya * rpitch + x] = z.x;
       fout[(size_t)(ya + 1) * rpitch + x] = z.y;
     }
@@ -94,7 +94,7 @@ __global__ void __launch_bounds__(RowCfg<T, N>::THREADS)
                const typename cplx_of<T>::type* __restrict__ tw) {
   typedef typename cplx_of<T>::type C;
   typedef RowCfg<T, N> RC;
-  constexpr int G = RC::G, H = N / 2, NP = 4 * RC::RP;
+  constexpr int G = RC::G, H = N / 2, NP = 4 * RC::RP, SL = RC::SL;
   extern __shared__ __align__(16) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);
   const int tid = threadIdx.x, y_base = blockIdx.x * (2 * NP);
@@ -102,15 +102,15 @@ __global__ void __launch_bounds__(RowCfg<T, N>::THREADS)
   C* fout = out + (size_t)blockIdx.y * fs_out;
   for (int e = tid; e < NP * N; e += RC::THREADS) {
     const int x = e % N, pp = e / N, ya = y_base + 2 * pp;
-    sm[pp * N + x] = (ya < rows) ? mkc<T>(fin[(size_t)ya * rpitch + x], fin[(size_t)(ya + 1) * rpitch + x])
+    sm[pp * SL + x] = (ya < rows) ? mkc<T>(fin[(size_t)ya * rpitch + x], fin[(size_t)(ya + 1) * rpitch + x])
                                  : mkc<T>(T(0), T(0));
   }
   __syncthreads();
-  fft_slot<T, N, false>(sm + (tid / G) * N, tid % G, true, tw);
+  fft_slot<T, N, false>(sm + (tid / G) * SL, tid % G, true, tw);
   for (int e = tid; e < NP * (H + 1); e += RC::THREADS) {
     const int k = e % (H + 1), pp = e / (H + 1), ya = y_base + 2 * pp;
     if (ya < rows) {
-      const C z = sm[pp * N + k], m = sm[pp * N + ((N - k) & (N - 1))];
+      const C z = sm[pp * SL + k], m = sm[pp * SL + ((N - k) & (N - 1))];
       fout[(size_t)ya * pitch + k] = mkc<T>(T(0.5) * (z.x + m.x), T(0.5) * (z.y - m.y));
       fout[(size_t)(ya + 1) * pitch + k] = mkc<T>(T(0.5) * (z.y + m.y), T(-0.5) * (z.x - m.x));
     }

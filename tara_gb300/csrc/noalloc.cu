@@ -178,6 +178,10 @@ extern "C" int tara_derive2csh_noalloc(int nx, int ny, double nu, const void* om
   p.dt = 0.0;
   const double nn = (double)nx * (double)ny;
   p.nl_scale = 0.5 / (nn * nn);
+  p.nu_f = (float)nu;
+  p.alpha_f = 1.0f;
+  p.nl_scale_f = (float)p.nl_scale;
+  g.kxf = g.kyf = g.invf = nullptr;  // FP64 kernels only
   StepBufs sb = {};
   sb.win = (const double2*)omegak_dev;
   sb.fout = (double2*)dt_omegak_dev;

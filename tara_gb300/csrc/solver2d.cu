@@ -313,12 +313,21 @@ int refresh_tables(tara2d* h) {
   h->grid.i0max = i0max;
   TARA_CK(cudaMemcpyAsync(h->inv, inv.data(), inv.size() * sizeof(double), cudaMemcpyHostToDevice,
                           h->stream));
+  std::vector<float> tf(h->nh + h->ny + inv.size());
+  for (int i = 0; i < h->nh; ++i) tf[i] = (float)kx[i];
+  for (int j = 0; j < h->ny; ++j) tf[h->nh + j] = (float)ky[j];
+  for (size_t q = 0; q < inv.size(); ++q) tf[h->nh + h->ny + q] = (float)inv[q];
+  TARA_CK(cudaMemcpyAsync(h->tabf, tf.data(), tf.size() * sizeof(float), cudaMemcpyHostToDevice,
+                          h->stream));
   TARA_CK(cudaMemcpyAsync(h->kx, kx.data(), h->nh * sizeof(double), cudaMemcpyHostToDevice,
                           h->stream));
   TARA_CK(cudaMemcpyAsync(h->ky, ky.data(), h->ny * sizeof(double), cudaMemcpyHostToDevice,
                           h->stream));
   TARA_CK(cudaMemcpyAsync(h->i0, i0.data(), h->ny * sizeof(int), cudaMemcpyHostToDevice, h->stream));
   TARA_CK(cudaStreamSynchronize(h->stream));  // host vectors go out of scope
+  h->grid.kxf = h->tabf;
+  h->grid.kyf = h->tabf + h->nh;
+  h->grid.invf = h->tabf + h->nh + h->ny;
   h->rp.rhs = h->cfg.rhs;
   h->rp.nu = h->cfg.nu;
   h->rp.alpha = h->cfg.alpha;
@@ -326,6 +335,9 @@ int refresh_tables(tara2d* h) {
   h->rp.dt = h->cfg.dt;
   const double nn = (double)h->nx * (double)h->ny;
   h->rp.nl_scale = 0.5 / (nn * nn);
+  h->rp.nu_f = (float)h->rp.nu;
+  h->rp.alpha_f = (float)h->rp.alpha;
+  h->rp.nl_scale_f = (float)h->rp.nl_scale;
   return TARA_OK;
 }
 
@@ -372,7 +384,7 @@ int tara2d_destroy(tara2d* h) {
   if (!h) return set_ok();
   cudaSetDevice(h->dev);
   if (h->stream) cudaStreamSynchronize(h->stream);
-  void* ptrs[] = {h->w0, h->ws, h->acc, h->fold, h->fout, h->u, h->nl, h->kx, h->ky, h->i0, h->inv,
+  void* ptrs[] = {h->w0, h->ws, h->acc, h->fold, h->fout, h->u, h->nl, h->kx, h->ky, h->i0, h->inv, h->tabf,
                   h->twx, h->twy, h->diag_part, h->diag_out, h->flag};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -430,6 +442,7 @@ int tara2d_create(const tara2d_config* cfg, tara2d** out) {
   CKC(cudaMalloc(&h->ky, h->ny * sizeof(double)));
   CKC(cudaMalloc(&h->i0, h->ny * sizeof(int)));
   CKC(cudaMalloc(&h->inv, (size_t)h->ny * h->nh * sizeof(double)));
+  CKC(cudaMalloc(&h->tabf, ((size_t)h->ny * h->nh + h->nh + h->ny) * sizeof(float)));
   CKC(cudaMalloc(&h->diag_part, 2 * kDiagBlocks * sizeof(double)));
   CKC(cudaMalloc(&h->diag_out, 4 * sizeof(double)));
   CKC(cudaMalloc(&h->flag, sizeof(unsigned int)));
