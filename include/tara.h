@@ -148,6 +148,14 @@ int tara2d_synchronize(tara2d* h);
 void* tara2d_stream(tara2d* h);
 /* Number of kernel launches a single step issues (for launch accounting). */
 int tara2d_launches_per_step(const tara2d* h);
+/* Tile variants of the three step kernels (column inverse pass, row pass,
+ * column forward pass): 0 the default tile, 1 half of it, 2 one column / one
+ * row pair per CTA (small grids, whose FP64 work would otherwise sit on a few
+ * SMs).  tara2d_autotune times each variant over trial_steps steps, keeps the
+ * fastest per kernel and restores the state; variants3 and ms9 (per-launch ms,
+ * variant-major) may be NULL. */
+int tara2d_autotune(tara2d* h, int trial_steps, int* variants3, double* ms9);
+int tara2d_set_variants(tara2d* h, const int* variants3);
 
 /* Driver diagnostics in the reference's form.  Wavenumbers kx = 2*kpi*i/lx
  * (the drivers use the true pi and Lx = Lx_ini*pi); screened != 0 applies the
@@ -203,9 +211,9 @@ int tara_ens_set_state(tara_ens* e, int run, const double* omegak);
 int tara_ens_diag(tara_ens* e, int run, double* energy, double* enstrophy);
 int tara_ens_groups(tara_ens* e);
 /* Size group info: n, number of runs, chosen variants of the three kernels, and
- * the autotuner's per-launch milliseconds (variant 0 then 1, three kernels each). */
+ * the autotuner's per-launch milliseconds (variants 0, 1, 2, three kernels each). */
 int tara_ens_group_info(tara_ens* e, int group, int* n, int* runs, int* variants3,
-                        double* tuned_ms6);
+                        double* tuned_ms9);
 /* Kernel launches one ensemble step contains (inside its graph). */
 int tara_ens_launches_per_step(tara_ens* e);
 
@@ -311,6 +319,89 @@ int tara_fortran_list_record(const double* v, int n, char* buf, int buflen);
  * transform arithmetic; inputs and outputs stay double). */
 int tara_fft2d_r2c(int nx, int ny, int precision, const double* in, double* out);
 int tara_fft2d_c2r(int nx, int ny, int precision, const double* in, double* out);
+
+/* ---- learned subgrid closure ---------------------------------------------- */
+/* No counterpart in the reference: a coarse-grid run of the plain vorticity
+ * solver corrected by a Fourier neural operator (FNO) that predicts the
+ * subgrid vorticity flux from the filtered vorticity.  The network is trained
+ * on the GPU by the library's own forward/backward kernels on filtered
+ * fine-grid snapshots that the plain solver generates (tara2d_filter).
+ *
+ * Network (per sample, activations H x W x channels, FP32):
+ *   v0 = x Pw + Pb;  v_l = GELU(S_l(v_{l-1}) + v_{l-1} W_l + b_l), l = 1..L
+ *   (no GELU after the last layer);  y = GELU(v_L Q1 + q1) Q2 + q2.
+ * S_l keeps the Fourier modes kx in [0, mx), ky in [-my/2, my/2) of rfft2(v),
+ * multiplies each by a complex c x c matrix and returns irfft2 of the result.
+ * Flat parameter vector order: Pw (ci x c), Pb (c), then per layer R_l
+ * (my x mx x c x c complex, ky index j = ky mod my, interleaved re/im), W_l
+ * (c x c), b_l (c); then Q1 (c x p), q1 (p), Q2 (p x co), q2 (co).  Matrices
+ * are row-major (input index first).  Grids are powers of two, c a multiple of
+ * 8, p and co <= 256.  The handle works on its own non-blocking stream, which
+ * does not wait for other streams: device inputs must be complete before a call
+ * (as for the tara2d_* device-pointer entry points). */
+typedef struct tara_fno tara_fno;
+#define TARA_FNO_BF16 0  /* channel mixing on BF16 tensor cores, FP32 accumulators */
+#define TARA_FNO_FP32 1  /* the same GEMMs on FP32 CUDA cores (gradient checks)    */
+typedef struct tara_fno_config {
+  int h, w;           /* grid (rows, columns) */
+  int ci, c, co;      /* input, hidden and output channels */
+  int mx, my;         /* retained modes: mx <= w/2, my even <= h */
+  int layers, p;      /* Fourier layers (1..8), projection width */
+  int max_batch;      /* samples per call */
+  int mode;           /* TARA_FNO_* */
+  uint64_t seed;      /* initial parameters: uniform(+-1/sqrt(fan_in)), R uniform(+-1/c^2) */
+} tara_fno_config;
+/* 128 x 128, ci 1, c 32, co 2, mx 16, my 32, 4 layers, p 128, batch 32, BF16. */
+void tara_fno_default_config(tara_fno_config* c);
+int tara_fno_create(const tara_fno_config* cfg, tara_fno** out);
+int tara_fno_destroy(tara_fno* f);
+size_t tara_fno_num_params(const tara_fno* f);
+int tara_fno_get_params(tara_fno* f, float* host);
+int tara_fno_set_params(tara_fno* f, const float* host);
+/* Gradients of the last tara_fno_train_step (same layout as the parameters). */
+int tara_fno_get_grads(tara_fno* f, float* host);
+int tara_fno_set_mode(tara_fno* f, int mode);
+/* y_dev (B,H,W,co) = FNO(x_dev (B,H,W,ci)); device FP32 arrays; synchronous. */
+int tara_fno_forward(tara_fno* f, const float* x_dev, float* y_dev, int B);
+/* Forward, loss = mean((y - t)^2), backward, then one Adam step (beta 0.9,
+ * 0.999, eps 1e-8, bias-corrected) when lr > 0.  With idx_dev (B int32 sample
+ * indices, device) the batch is gathered from datasets x_dev / t_dev of
+ * n_samples samples (an index outside them returns TARA_ERR_ARGS); with idx_dev
+ * NULL, x_dev / t_dev hold the batch itself (n_samples >= B). */
+int tara_fno_train_step(tara_fno* f, const float* x_dev, const float* t_dev, const int* idx_dev,
+                        int n_samples, int B, float lr, double* loss);
+/* Adam steps taken so far; setting it restarts the bias correction count. */
+long long tara_fno_adam_steps(const tara_fno* f);
+void* tara_fno_stream(tara_fno* f);
+
+/* Box filter of run `run` of a plain-solver handle onto the grid coarsened by
+ * `factor` (block means of factor x factor cells; Nx, Ny divisible by it).
+ * Device outputs, any may be NULL: omega_bar (Ny/f, Nx/f) FP32, flux
+ * (Ny/f, Nx/f, 2) FP32 = the subgrid vorticity flux bar(u w) - bar(u) bar(w),
+ * bar(v w) - bar(v) bar(w), omega_bar64 (Ny/f, Nx/f) FP64.  Velocities come
+ * from the state with the solver's wavenumbers, in FP64. */
+int tara2d_filter(tara2d* h, int run, int factor, float* omega_bar, float* flux,
+                  double* omega_bar64);
+/* Set run `run` to the r2c of a real vorticity field on the device (Nx x Ny,
+ * x fastest, FP64); the AB2 history is zeroed. */
+int tara2d_set_state_real_device(tara2d* h, int run, const double* omega_dev);
+/* Shell energy spectrum of run `run`: E[k], k = 0..kmax, sums 1/2 |u_hat|^2 / (NxNy)^2
+ * over the modes with round(|k|) = k (|k| in the solver's integer wavenumbers),
+ * so that sum_k E[k] is the energy when kmax covers the grid. */
+int tara2d_spectrum(tara2d* h, int run, int kmax, double* E);
+
+/* A coarse plain-solver handle advanced with the FNO's subgrid flux: every
+ * step evaluates y = FNO(in_scale * omega) on the runs' real vorticity, takes
+ * flux = out_scale * y and adds -div(flux) (2/3-truncated) to the right-hand
+ * side of every stage of the step.  The handle and the network stay owned by
+ * the caller and must outlive the closure; the network's batch must hold the
+ * handle's runs and its grid must be the handle's. */
+typedef struct tara_closure tara_closure;
+int tara_closure_create(tara2d* coarse, tara_fno* fno, double in_scale, double out_scale,
+                        tara_closure** out);
+int tara_closure_destroy(tara_closure* c);
+/* Advance nsteps closure steps (enqueued on the handle's stream). */
+int tara_closure_step(tara_closure* c, int nsteps);
 
 /* ---- allocation-free RHS ------------------------------------------------- */
 /* No counterpart in the reference.  The plain RHS of derive2csh_ (same

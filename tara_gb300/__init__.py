@@ -64,6 +64,13 @@ class MhdCommon(ctypes.Structure):
                                        "mu", "ms", "CS", "mu_0", "eta", "dt", "kf")]
 
 
+class FnoConfig(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int) for n in ("h", "w", "ci", "c", "co", "mx", "my", "layers", "p",
+                                            "max_batch", "mode")] + [("seed", ctypes.c_uint64)]
+
+
+FNO_BF16, FNO_FP32 = 0, 1
+
 _lib = None
 
 
@@ -160,6 +167,32 @@ def _declare(L: ctypes.CDLL) -> None:
     L.tara2d_real_fields.argtypes = [vp, vp, dp, dp, dp, dp]
     L.tara_fft2d_r2c.argtypes = [c_int, c_int, c_int, dp, dp]
     L.tara_fft2d_c2r.argtypes = [c_int, c_int, c_int, dp, dp]
+    fcp = ctypes.POINTER(FnoConfig)
+    L.tara_fno_default_config.argtypes = [fcp]
+    L.tara_fno_default_config.restype = None
+    L.tara_fno_create.argtypes = [fcp, ctypes.POINTER(vp)]
+    L.tara_fno_destroy.argtypes = [vp]
+    L.tara_fno_num_params.argtypes = [vp]
+    L.tara_fno_num_params.restype = ctypes.c_size_t
+    fp = ctypes.POINTER(ctypes.c_float)
+    L.tara_fno_get_params.argtypes = [vp, fp]
+    L.tara_fno_set_params.argtypes = [vp, fp]
+    L.tara_fno_get_grads.argtypes = [vp, fp]
+    L.tara_fno_set_mode.argtypes = [vp, c_int]
+    L.tara_fno_forward.argtypes = [vp, vp, vp, c_int]
+    L.tara_fno_train_step.argtypes = [vp, vp, vp, vp, c_int, c_int, ctypes.c_float, dp]
+    L.tara_fno_adam_steps.argtypes = [vp]
+    L.tara_fno_adam_steps.restype = ctypes.c_longlong
+    L.tara_fno_stream.argtypes = [vp]
+    L.tara_fno_stream.restype = vp
+    L.tara2d_filter.argtypes = [vp, c_int, c_int, vp, vp, vp]
+    L.tara2d_autotune.argtypes = [vp, c_int, ip, dp]
+    L.tara2d_set_variants.argtypes = [vp, ip]
+    L.tara2d_set_state_real_device.argtypes = [vp, c_int, vp]
+    L.tara2d_spectrum.argtypes = [vp, c_int, c_int, dp]
+    L.tara_closure_create.argtypes = [vp, vp, c_double, c_double, ctypes.POINTER(vp)]
+    L.tara_closure_destroy.argtypes = [vp]
+    L.tara_closure_step.argtypes = [vp, c_int]
 
 
 def _check(rc: int) -> None:
@@ -284,11 +317,13 @@ class Solver2D:
     def __init__(self, nx: int, ny: int | None = None, *, rhs: int = RHS_PLAIN,
                  scheme: int = SCHEME_AB2, precision: int = PREC_FP64, nu: float = 0.01,
                  dt: float = 1e-4, alpha: float = 1.0, lam: float = 10.0,
-                 lx: float | None = None, ly: float | None = None, kpi: float = PI_R4):
+                 lx: float | None = None, ly: float | None = None, kpi: float = PI_R4,
+                 batch: int = 1):
         ny = nx if ny is None else ny
         cfg = Config2D()
         lib().tara2d_default_config(ctypes.byref(cfg), nx, ny)
         cfg.rhs, cfg.scheme, cfg.precision = rhs, scheme, precision
+        cfg.batch = batch
         cfg.nu, cfg.dt, cfg.alpha, cfg.lam = nu, dt, alpha, lam
         cfg.kpi = kpi
         cfg.lx = 2.0 * kpi if lx is None else lx
@@ -377,8 +412,48 @@ class Solver2D:
     def stream(self) -> int:
         return lib().tara2d_stream(self._h) or 0
 
-    def init_random(self, k0: float, energy: float, seed: int) -> None:
-        _check(lib().tara2d_init_random(self._h, k0, energy, seed))
+    def init_random(self, k0: float, energy: float, seed: int, run: int = 0) -> None:
+        _check(lib().tara2d_init_random_run(self._h, run, k0, energy, seed))
+
+    def autotune(self, trial_steps: int = 3) -> dict:
+        """Pick the fastest tile variant per step kernel (state restored)."""
+        v = (ctypes.c_int * 3)()
+        ms = (ctypes.c_double * 9)()
+        _check(lib().tara2d_autotune(self._h, int(trial_steps), v, ms))
+        return {"variants": list(v), "ms": [list(ms[3 * i:3 * i + 3]) for i in range(3)]}
+
+    def set_variants(self, variants) -> None:
+        v = (ctypes.c_int * 3)(*[int(x) for x in variants])
+        _check(lib().tara2d_set_variants(self._h, v))
+
+    def get_state_run(self, run: int) -> np.ndarray:
+        w = np.zeros((self.ny, self.nh), np.complex128)
+        _check(lib().tara2d_get_state_run(self._h, run, _dp(w.view(np.float64)), None))
+        return w
+
+    def set_state_run(self, run: int, omegak: np.ndarray) -> None:
+        w = _as_spectrum(omegak, self.nh, self.ny)
+        _check(lib().tara2d_set_state_run(self._h, run, _dp(w.view(np.float64)), None))
+
+    def diag_run(self, run: int) -> tuple[float, float]:
+        e, z = ctypes.c_double(), ctypes.c_double()
+        _check(lib().tara2d_diag_run(self._h, run, ctypes.byref(e), ctypes.byref(z)))
+        return e.value, z.value
+
+    def filter(self, run: int, factor: int, omega_bar=0, flux=0, omega_bar64=0) -> None:
+        """Box filter onto the grid coarsened by ``factor``; device pointers
+        (FP32 omega_bar, FP32 (.., 2) flux, FP64 omega_bar64), 0 to skip."""
+        _check(lib().tara2d_filter(self._h, run, factor, ctypes.c_void_p(omega_bar or None),
+                                   ctypes.c_void_p(flux or None), ctypes.c_void_p(omega_bar64 or None)))
+
+    def set_state_real_device(self, run: int, ptr: int) -> None:
+        _check(lib().tara2d_set_state_real_device(self._h, run, ctypes.c_void_p(ptr)))
+
+    def spectrum(self, run: int = 0, kmax: int | None = None) -> np.ndarray:
+        kmax = self.nx // 2 if kmax is None else kmax
+        out = np.zeros(kmax + 1)
+        _check(lib().tara2d_spectrum(self._h, run, kmax, _dp(out)))
+        return out
 
 
 # ---------------------------------------------------------------------------
@@ -569,7 +644,120 @@ class Ensemble:
         for g in range(lib().tara_ens_groups(self._h)):
             n, r = ctypes.c_int(), ctypes.c_int()
             v = (ctypes.c_int * 3)()
-            ms = (ctypes.c_double * 6)()
+            ms = (ctypes.c_double * 9)()
             _check(lib().tara_ens_group_info(self._h, g, ctypes.byref(n), ctypes.byref(r), v, ms))
             out.append({"n": n.value, "runs": r.value, "variants": list(v), "tuned_ms": list(ms)})
         return out
+
+
+# ---------------------------------------------------------------------------
+# Learned subgrid closure
+# ---------------------------------------------------------------------------
+def fno_default_config(**kw) -> FnoConfig:
+    c = FnoConfig()
+    lib().tara_fno_default_config(ctypes.byref(c))
+    for k, v in kw.items():
+        setattr(c, k, v)
+    return c
+
+
+class FNO:
+    """tara_fno handle: the library's Fourier neural operator (BF16 tensor-core
+    GEMMs with FP32 accumulation, or FP32 for checks).  Data arguments are
+    device pointers (e.g. ``torch_tensor.data_ptr()``) to FP32 NHWC arrays."""
+
+    def __init__(self, cfg: FnoConfig | None = None, **kw):
+        cfg = fno_default_config(**kw) if cfg is None else cfg
+        h = ctypes.c_void_p()
+        _check(lib().tara_fno_create(ctypes.byref(cfg), ctypes.byref(h)))
+        self._h = h
+        self.cfg = cfg
+        self.num_params = int(lib().tara_fno_num_params(h))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().tara_fno_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def get_params(self) -> np.ndarray:
+        out = np.zeros(self.num_params, np.float32)
+        _check(lib().tara_fno_get_params(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
+        return out
+
+    def set_params(self, p: np.ndarray) -> None:
+        p = np.ascontiguousarray(p, np.float32)
+        if p.size != self.num_params:
+            raise ValueError(f"expected {self.num_params} parameters, got {p.size}")
+        _check(lib().tara_fno_set_params(self._h, p.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
+
+    def get_grads(self) -> np.ndarray:
+        out = np.zeros(self.num_params, np.float32)
+        _check(lib().tara_fno_get_grads(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_float))))
+        return out
+
+    def set_mode(self, mode: int) -> None:
+        _check(lib().tara_fno_set_mode(self._h, mode))
+
+    def forward(self, x_ptr: int, y_ptr: int, batch: int) -> None:
+        _check(lib().tara_fno_forward(self._h, ctypes.c_void_p(x_ptr), ctypes.c_void_p(y_ptr), batch))
+
+    def train_step(self, x_ptr: int, t_ptr: int, batch: int, lr: float = 0.0, idx_ptr: int = 0,
+                   n_samples: int | None = None, want_loss: bool = True) -> float | None:
+        """One forward/backward (+ Adam when lr > 0).  With idx_ptr, the batch is
+        gathered from datasets of n_samples samples at x_ptr / t_ptr."""
+        loss = ctypes.c_double()
+        ns = batch if n_samples is None else n_samples
+        _check(lib().tara_fno_train_step(self._h, ctypes.c_void_p(x_ptr), ctypes.c_void_p(t_ptr),
+                                         ctypes.c_void_p(idx_ptr or None), ns, batch, lr,
+                                         ctypes.byref(loss) if want_loss else None))
+        return loss.value if want_loss else None
+
+    @property
+    def adam_steps(self) -> int:
+        return int(lib().tara_fno_adam_steps(self._h))
+
+    @property
+    def stream(self) -> int:
+        return lib().tara_fno_stream(self._h) or 0
+
+
+class Closure:
+    """tara_closure: a coarse Solver2D stepped with the FNO's subgrid flux."""
+
+    def __init__(self, solver: Solver2D, fno: FNO, in_scale: float, out_scale: float):
+        h = ctypes.c_void_p()
+        _check(lib().tara_closure_create(solver._h, fno._h, in_scale, out_scale, ctypes.byref(h)))
+        self._h = h
+        self.solver, self.fno = solver, fno  # keep both alive
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().tara_closure_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def step(self, n: int = 1) -> None:
+        _check(lib().tara_closure_step(self._h, int(n)))

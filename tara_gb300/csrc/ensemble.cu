@@ -5,10 +5,10 @@
 // launches.  One step of the whole ensemble -- every size group, every RK4
 // stage -- is captured once into a CUDA graph with one parallel branch per size
 // group (fork/join events on the groups' streams), and replayed with a single
-// cudaGraphLaunch per step.  Before capture an autotuner times the two tile
-// variants of each of the three kernels on the real batch (tara2d_step_timed
-// reports per-kernel CUDA-event times) and keeps the faster one per kernel and
-// size; the state is saved before and restored after the trial steps.
+// cudaGraphLaunch per step.  Before capture an autotuner (tara2d_autotune) times
+// the three tile variants of each of the three kernels on the real batch
+// (tara2d_step_timed reports per-kernel CUDA-event times) and keeps the fastest
+// per kernel and size; the state is saved before and restored after the trials.
 #include <algorithm>
 #include <cstring>
 #include <map>
@@ -23,7 +23,7 @@ struct tara_ens {
     std::vector<int> runs;  // global run index of each slot
     double2* save_w0 = nullptr;
     double2* save_fold = nullptr;
-    double tuned_ms[2][3] = {{0, 0, 0}, {0, 0, 0}};
+    double tuned_ms[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // [variant][kernel]
   };
   int nruns = 0;
   std::vector<int> group_of, slot_of;
@@ -170,20 +170,10 @@ int tara_ens_create(int nruns, const tara_ens_run* runs, int precision, int sche
 int tara_ens_autotune(tara_ens* e, int trial_steps) {
   if (!e || trial_steps <= 0) return set_error(TARA_ERR_ARGS, "bad arguments");
   TARA_CK(cudaSetDevice(e->dev));
+  TARA_CK(cudaStreamSynchronize(e->main));
   int rc;
-  if ((rc = save_or_restore(e, true))) return rc;
-  for (auto& g : e->groups) {
-    for (int v = 0; v < 2; ++v) {
-      for (int k = 0; k < 3; ++k) g.h->var[k] = v;
-      if ((rc = tara2d_step(g.h, 1))) return rc;  // first use of this variant: smem attributes
-      double ms[3];
-      int cnt[3];
-      if ((rc = tara2d_step_timed(g.h, trial_steps, ms, cnt, nullptr))) return rc;
-      for (int k = 0; k < 3; ++k) g.tuned_ms[v][k] = ms[k] / std::max(1, cnt[k]);
-    }
-    for (int k = 0; k < 3; ++k) g.h->var[k] = g.tuned_ms[1][k] < g.tuned_ms[0][k] ? 1 : 0;
-  }
-  if ((rc = save_or_restore(e, false))) return rc;
+  for (auto& g : e->groups)  // each group saves and restores its own state
+    if ((rc = tara2d_autotune(g.h, trial_steps, nullptr, g.tuned_ms))) return rc;
   drop_graph(e);  // the graph bakes in the launch shapes
   return set_ok();
 }
@@ -240,16 +230,15 @@ int tara_ens_diag(tara_ens* e, int run, double* energy, double* enstrophy) {
 }
 
 int tara_ens_group_info(tara_ens* e, int group, int* n, int* runs, int* variants3,
-                        double* tuned_ms6) {
+                        double* tuned_ms9) {
   if (!e || group < 0 || group >= (int)e->groups.size()) return set_error(TARA_ERR_ARGS, "bad group");
   const auto& g = e->groups[group];
   if (n) *n = g.n;
   if (runs) *runs = (int)g.runs.size();
   if (variants3)
     for (int k = 0; k < 3; ++k) variants3[k] = g.h->var[k];
-  if (tuned_ms6)
-    for (int v = 0; v < 2; ++v)
-      for (int k = 0; k < 3; ++k) tuned_ms6[3 * v + k] = g.tuned_ms[v][k];
+  if (tuned_ms9)
+    for (int i = 0; i < 9; ++i) tuned_ms9[i] = g.tuned_ms[i];
   return set_ok();
 }
 

@@ -75,6 +75,10 @@ struct tara2d {
   void *twx = nullptr, *twy = nullptr;
   double *diag_part = nullptr, *diag_out = nullptr;
   unsigned int* flag = nullptr;
+  const double2* force = nullptr;  // closure forcing spectrum (batch fields), not owned
+  void* scratch = nullptr;         // filter / spectrum / real-state work space
+  size_t scratch_bytes = 0;
+  void *twx64 = nullptr, *twy64 = nullptr;  // FP64 twiddles when the solver runs FP32
   tara::Grid2D grid;
   tara::RhsParams rp;
 };
@@ -86,4 +90,16 @@ int rhs_and_update(tara2d* h, const double2* win, int mode, cudaEvent_t* ev);
 int copy_in_dense(tara2d* h, double2* dst, const double* host);
 int copy_out_dense(tara2d* h, double* host, const double2* src);
 int refresh_tables(tara2d* h);
+// Scratch of at least `bytes` on the handle (kept until destroy).
+int scratch(tara2d* h, size_t bytes, void** out);
+// FP64 twiddles for the handle's grid, whatever the solver's precision.
+int twiddles64(tara2d* h, const void** twx, const void** twy);
+
+// Learned-closure internals (fno.cu).
+int fno_forward_async(tara_fno* f, const float* x_dev, int B, const float** y);
+void fno_bind_stream(tara_fno* f, cudaStream_t s);
+const tara_fno_config& fno_config(const tara_fno* f);
+float* fno_input(tara_fno* f);  // the handle's input buffer (max_batch samples)
+unsigned long long fno_param_version(const tara_fno* f);
+int fno_prepare(tara_fno* f);
 }  // namespace tara

@@ -28,6 +28,15 @@
 
 namespace tara {
 
+// Element loop of a CTA over TOTAL items with THREADS threads (both
+// compile-time): the trip count is a constant, so the loop unrolls and the
+// independent global loads of different iterations issue together.  (With a
+// thread-dependent start the compiler keeps the loop rolled and every element
+// waits out one memory latency, which dominates on small grids.)
+#define TARA_ELEM_LOOP(e, TOTAL, THREADS)                                                   \
+  _Pragma("unroll 4") for (int e##_i = 0; e##_i < ((TOTAL) + (THREADS)-1) / (THREADS); ++e##_i) \
+    if (const int e = tid + e##_i * (THREADS); (TOTAL) % (THREADS) == 0 || e < (TOTAL))
+
 struct Grid2D {
   int nx, ny, nh, pitch;
   const double* __restrict__ kx;   // [nh]
@@ -74,7 +83,9 @@ __host__ __device__ constexpr int pick_rp(int n, int csize) {
   return rp;
 }
 
-// V selects a tile variant for the autotuner: 0 the default tile, 1 half of it.
+// V selects a tile variant for the autotuner: 0 the default tile, 1 half of it,
+// 2 one column (one row pair) per CTA, for grids too small to fill the SMs
+// with the larger tiles.
 template <typename T, int N, int V = 0> struct ColCfg {
   typedef typename cplx_of<T>::type C;
   static constexpr int G = fft_group(N);
@@ -83,8 +94,8 @@ template <typename T, int N, int V = 0> struct ColCfg {
   // pass C: 1 slot/column; a small tile keeps the live (not fully truncated)
   // columns spread evenly over the SMs
   static constexpr int TCC0 = pick_tc(S * (int)sizeof(C), G, 48 * 1024);
-  static constexpr int TCA = (V == 1 && TCA0 > 1) ? TCA0 / 2 : TCA0;
-  static constexpr int TCC = (V == 1 && TCC0 > 1) ? TCC0 / 2 : TCC0;
+  static constexpr int TCA = V == 2 ? 1 : (V == 1 && TCA0 > 1) ? TCA0 / 2 : TCA0;
+  static constexpr int TCC = V == 2 ? 1 : (V == 1 && TCC0 > 1) ? TCC0 / 2 : TCC0;
   static constexpr int THREADS_A = 2 * TCA * G;
   static constexpr int THREADS_C = TCC * G;
   static constexpr int SMEM_A = 2 * TCA * S * (int)sizeof(C);
@@ -95,7 +106,7 @@ template <typename T, int N, int V = 0> struct RowCfg {
   typedef typename cplx_of<T>::type C;
   static constexpr int G = fft_group(N);
   static constexpr int RP0 = pick_rp(N, (int)sizeof(C));
-  static constexpr int RP = (V == 1 && RP0 > 1) ? RP0 / 2 : RP0;
+  static constexpr int RP = V == 2 ? 1 : (V == 1 && RP0 > 1) ? RP0 / 2 : RP0;
   static constexpr int THREADS = 4 * RP * G;
   static constexpr int SL = N;  // smem stride between row slots
   static constexpr int SMEM = RP * 4 * SL * (int)sizeof(C);
@@ -123,7 +134,7 @@ __global__ void __launch_bounds__(ColCfg<T, N, V>::THREADS_A)
   win += blockIdx.z * fsz;
   u += blockIdx.z * 4 * fsz;
   const int slot = tid / G, lane = tid % G;
-  for (int e = tid; e < N * TC; e += CF::THREADS_A) {
+  TARA_ELEM_LOOP(e, N * TC, CF::THREADS_A) {
     const int y = e / TC, c = e % TC, x = x0 + c;
     C fa = mkc<T>(T(0), T(0)), fb = fa;
     if constexpr (sizeof(T) == 4) {
@@ -172,7 +183,7 @@ __global__ void __launch_bounds__(ColCfg<T, N, V>::THREADS_A)
   }
   __syncthreads();
   fft_slot<T, N, true>(sm + slot * S, lane, true, tw);
-  for (int e = tid; e < N * TC; e += CF::THREADS_A) {
+  TARA_ELEM_LOOP(e, N * TC, CF::THREADS_A) {
     const int y = e / TC, c = e % TC, x = x0 + c;
     if (x < g.nh) {
       const size_t q = (size_t)y * g.pitch + x;
@@ -206,7 +217,7 @@ __global__ void __launch_bounds__(RowCfg<T, N, V>::THREADS)
   const size_t fsz = (size_t)g.ny * g.pitch;
   u += blockIdx.y * 4 * fsz;
   nl += blockIdx.y * fsz;
-  for (int e = tid; e < RP * 4 * N; e += RC::THREADS) {
+  TARA_ELEM_LOOP(e, RP * 4 * N, RC::THREADS) {
     const int k = e % N, sl = e / N;
     const int pp = sl >> 2, s = sl & 3;
     const int y = y_base + 2 * pp + (s >> 1);
@@ -227,7 +238,7 @@ __global__ void __launch_bounds__(RowCfg<T, N, V>::THREADS)
   __syncthreads();
   fft_slot<T, N, true>(sm + slot * SL, lane, true, tw);
   // products u_x w_x + u_y w_y for rows a and b, packed as a + i b
-  for (int e = tid; e < RP * N; e += RC::THREADS) {
+  TARA_ELEM_LOOP(e, RP * N, RC::THREADS) {
     const int x = e % N, pp = e / N;
     C* b = sm + (size_t)pp * 4 * SL;
     const C c1a = b[x], c2a = b[SL + x], c1b = b[2 * SL + x], c2b = b[3 * SL + x];
@@ -238,7 +249,7 @@ __global__ void __launch_bounds__(RowCfg<T, N, V>::THREADS)
   __syncthreads();
   fft_slot<T, N, false>(sm + slot * SL, lane, (slot & 3) == 0, tw);
   // split: 2 X_a[k] = Z[k] + conj Z[N-k], 2 X_b[k] = -i (Z[k] - conj Z[N-k])
-  for (int e = tid; e < RP * (H + 1); e += RC::THREADS) {
+  TARA_ELEM_LOOP(e, RP * (H + 1), RC::THREADS) {
     const int k = e % (H + 1), pp = e / (H + 1);
     const int ya = y_base + 2 * pp;
     if (ya < g.ny) {
@@ -261,6 +272,7 @@ struct StepBufs {
   double2* fold;       // AB2 history
   double2* fout;       // MODE_DERIVE output
   unsigned int* flag;  // bit 0: a non-finite value was produced
+  const double2* force;  // optional spectrum added to every right-hand side (nullptr: none)
 };
 
 // blockIdx.y = run of a batch.
@@ -284,23 +296,32 @@ __global__ void __launch_bounds__(ColCfg<T, N, V>::THREADS_C)
     if (sb.acc) sb.acc += off;
     if (sb.fold) sb.fold += off;
     if (sb.fout) sb.fout += off;
+    if (sb.force) sb.force += off;
   }
   // Tiles whose columns all lie at kx >= i0max lose the whole nonlinear term to
   // the 2/3 rule: their transform is skipped (uniform per CTA, so the barriers
   // inside fft_slot stay matched).
   const bool live = x0 < g.i0max;
   if (live) {
-    for (int e = tid; e < N * TC; e += CF::THREADS_C) {
+    TARA_ELEM_LOOP(e, N * TC, CF::THREADS_C) {
       const int y = e / TC, c = e % TC, x = x0 + c;
       sm[c * S + y] = (x < g.nh) ? nl[(size_t)y * g.pitch + x] : mkc<T>(T(0), T(0));
     }
     __syncthreads();
     fft_slot<T, N, false>(sm + (tid / G) * S, tid % G, true, tw);
   }
+  // Pass 1: the right-hand side of every element of this thread (reads only,
+  // so the unrolled loop issues all its loads together).
+  constexpr int PER = (N * TC + CF::THREADS_C - 1) / CF::THREADS_C;
+  double frv[PER], fiv[PER];
   bool bad = false;
-  for (int e = tid; e < N * TC; e += CF::THREADS_C) {
+#pragma unroll
+  for (int i = 0; i < PER; ++i) {
+    const int e = tid + i * CF::THREADS_C;
     const int y = e / TC, c = e % TC, x = x0 + c;
-    if (x >= g.nh) continue;
+    frv[i] = 0.0;
+    fiv[i] = 0.0;
+    if (e >= N * TC || x >= g.nh) continue;
     const size_t q = (size_t)y * g.pitch + x;
     double fr, fi;
     if constexpr (sizeof(T) == 4) {  // FP32 right-hand side, FP64 update below
@@ -344,39 +365,75 @@ __global__ void __launch_bounds__(ColCfg<T, N, V>::THREADS_C)
         fi = -(p.alpha * ni + vk2 * di);
       }
     }
+    if (sb.force) {
+      const double2 fc = sb.force[q];
+      fr += fc.x;
+      fi += fc.y;
+    }
     bad |= !(isfinite(fr) && isfinite(fi));
-    const double dt = p.dt;
-    switch (mode) {
-      case MODE_DERIVE:
-        sb.fout[q] = make_double2(fr, fi);
-        break;
-      case MODE_AB2: {
-        const double2 fo = sb.fold[q];
-        const double2 s = sb.w0[q];
-        sb.w0[q] = make_double2(s.x + (1.5 * fr - 0.5 * fo.x) * dt, s.y + (1.5 * fi - 0.5 * fo.y) * dt);
-        sb.fold[q] = make_double2(fr, fi);
-        break;
+    frv[i] = fr;
+    fiv[i] = fi;
+  }
+  // Pass 2: the stage update, in chunks whose loads all precede their stores
+  // (the state arrays may alias the RHS input, so loads cannot move past stores).
+  constexpr int CH = PER < 8 ? PER : 8;
+  const double dt = p.dt;
+#pragma unroll
+  for (int i0 = 0; i0 < PER; i0 += CH) {
+    double2 a0[CH], a1[CH];
+    size_t qv[CH];
+    bool ok[CH];
+#pragma unroll
+    for (int u = 0; u < CH; ++u) {
+      const int e = tid + (i0 + u) * CF::THREADS_C;
+      const int y = e / TC, x = x0 + e % TC;
+      ok[u] = i0 + u < PER && e < N * TC && x < g.nh;
+      qv[u] = (size_t)y * g.pitch + x;
+      a0[u] = make_double2(0.0, 0.0);
+      a1[u] = a0[u];
+      if (ok[u]) {
+        if (mode == MODE_AB2) {
+          a0[u] = sb.w0[qv[u]];
+          a1[u] = sb.fold[qv[u]];
+        } else if (mode != MODE_DERIVE) {
+          a0[u] = sb.w0[qv[u]];
+          if (mode != MODE_RK1) a1[u] = sb.acc[qv[u]];
+        }
       }
-      case MODE_RK1: {
-        const double2 s = sb.w0[q];
-        sb.acc[q] = make_double2(fr, fi);
-        sb.ws[q] = make_double2(s.x + fr * dt / 2.0, s.y + fi * dt / 2.0);
-        break;
-      }
-      case MODE_RK2:
-      case MODE_RK3: {
-        const double2 s = sb.w0[q];
-        const double2 a = sb.acc[q];
-        const double h = (mode == MODE_RK2) ? dt / 2.0 : dt;
-        sb.acc[q] = make_double2(a.x + 2.0 * fr, a.y + 2.0 * fi);
-        sb.ws[q] = make_double2(s.x + fr * h, s.y + fi * h);
-        break;
-      }
-      default: {  // MODE_RK4
-        const double2 s = sb.w0[q];
-        const double2 a = sb.acc[q];
-        sb.w0[q] = make_double2(s.x + dt / 6.0 * (a.x + fr), s.y + dt / 6.0 * (a.y + fi));
-        break;
+    }
+#pragma unroll
+    for (int u = 0; u < CH; ++u) {
+      if (!ok[u]) continue;
+      const double fr = frv[i0 + u], fi = fiv[i0 + u];
+      const size_t q = qv[u];
+      const double2 s = a0[u];
+      switch (mode) {
+        case MODE_DERIVE:
+          sb.fout[q] = make_double2(fr, fi);
+          break;
+        case MODE_AB2: {
+          const double2 fo = a1[u];
+          sb.w0[q] = make_double2(s.x + (1.5 * fr - 0.5 * fo.x) * dt, s.y + (1.5 * fi - 0.5 * fo.y) * dt);
+          sb.fold[q] = make_double2(fr, fi);
+          break;
+        }
+        case MODE_RK1:
+          sb.acc[q] = make_double2(fr, fi);
+          sb.ws[q] = make_double2(s.x + fr * dt / 2.0, s.y + fi * dt / 2.0);
+          break;
+        case MODE_RK2:
+        case MODE_RK3: {
+          const double2 a = a1[u];
+          const double h = (mode == MODE_RK2) ? dt / 2.0 : dt;
+          sb.acc[q] = make_double2(a.x + 2.0 * fr, a.y + 2.0 * fi);
+          sb.ws[q] = make_double2(s.x + fr * h, s.y + fi * h);
+          break;
+        }
+        default: {  // MODE_RK4
+          const double2 a = a1[u];
+          sb.w0[q] = make_double2(s.x + dt / 6.0 * (a.x + fr), s.y + dt / 6.0 * (a.y + fi));
+          break;
+        }
       }
     }
   }
@@ -387,41 +444,49 @@ __global__ void __launch_bounds__(ColCfg<T, N, V>::THREADS_C)
 // Plain transforms (initial conditions, diagnostics and the transform API)
 // ---------------------------------------------------------------------------
 // Column transform of a half spectrum along y, in place or out of place.
-template <typename T, int N, bool INV>
-__global__ void __launch_bounds__(ColCfg<T, N>::THREADS_C)
+template <typename T, int N, bool INV, int V = 0>
+__global__ void __launch_bounds__(ColCfg<T, N, V>::THREADS_C)
     k_col_fft(const typename cplx_of<T>::type* in, typename cplx_of<T>::type* out, int nh,
               int pitch, const typename cplx_of<T>::type* __restrict__ tw) {
   typedef typename cplx_of<T>::type C;
-  typedef ColCfg<T, N> CF;
+  typedef ColCfg<T, N, V> CF;
   constexpr int TC = CF::TCC, S = CF::S, G = CF::G;
   extern __shared__ __align__(16) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);
   const int x0 = blockIdx.x * TC, tid = threadIdx.x;
-  for (int e = tid; e < N * TC; e += CF::THREADS_C) {
+  TARA_ELEM_LOOP(e, N * TC, CF::THREADS_C) {
     const int y = e / TC, c = e % TC, x = x0 + c;
     sm[c * S + y] = (x < nh) ? in[(size_t)y * pitch + x] : mkc<T>(T(0), T(0));
   }
   __syncthreads();
   fft_slot<T, N, INV>(sm + (tid / G) * S, tid % G, true, tw);
-  for (int e = tid; e < N * TC; e += CF::THREADS_C) {
+  TARA_ELEM_LOOP(e, N * TC, CF::THREADS_C) {
     const int y = e / TC, c = e % TC, x = x0 + c;
     if (x < nh) out[(size_t)y * pitch + x] = sm[c * S + y];
   }
 }
 
+// Row pairs per CTA of the plain row transforms (one slot per pair): four per
+// row pair of the RHS row pass, or a single pair for the small-grid variant.
+template <typename T, int N, int V> struct RowXCfg {
+  static constexpr int NP = V == 2 ? 1 : 4 * RowCfg<T, N, V>::RP;
+  static constexpr int THREADS = NP * fft_group(N);
+  static constexpr int SMEM = NP * N * (int)sizeof(typename cplx_of<T>::type);
+};
+
 // 1D c2r along x for pairs of rows (after the y pass): out rows are real with
 // row pitch rpitch.  Unnormalised.
-template <typename T, int N>
-__global__ void __launch_bounds__(RowCfg<T, N>::THREADS)
+template <typename T, int N, int V = 0>
+__global__ void __launch_bounds__(RowXCfg<T, N, V>::THREADS)
     k_row_c2r(const typename cplx_of<T>::type* __restrict__ in, T* __restrict__ out, int ny,
               int pitch, int rpitch, const typename cplx_of<T>::type* __restrict__ tw) {
   typedef typename cplx_of<T>::type C;
-  typedef RowCfg<T, N> RC;
-  constexpr int G = RC::G, H = N / 2, NP = 4 * RC::RP, SL = RC::SL;  // NP row pairs per CTA
+  typedef RowXCfg<T, N, V> RC;
+  constexpr int G = fft_group(N), H = N / 2, NP = RC::NP, SL = N;  // NP row pairs per CTA
   extern __shared__ __align__(16) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);  // [NP][N]
   const int tid = threadIdx.x, y_base = blockIdx.x * (2 * NP);
-  for (int e = tid; e < NP * N; e += RC::THREADS) {
+  TARA_ELEM_LOOP(e, NP * N, RC::THREADS) {
     const int k = e % N, pp = e / N, ya = y_base + 2 * pp;
     C z = mkc<T>(T(0), T(0));
     if (ya < ny) {
@@ -437,7 +502,7 @@ __global__ void __launch_bounds__(RowCfg<T, N>::THREADS)
   }
   __syncthreads();
   fft_slot<T, N, true>(sm + (tid / G) * SL, tid % G, true, tw);
-  for (int e = tid; e < NP * N; e += RC::THREADS) {
+  TARA_ELEM_LOOP(e, NP * N, RC::THREADS) {
     const int x = e % N, pp = e / N, ya = y_base + 2 * pp;
     if (ya < ny) {
       const C z = sm[pp * SL + x];
@@ -448,24 +513,24 @@ __global__ void __launch_bounds__(RowCfg<T, N>::THREADS)
 }
 
 // 1D r2c along x for pairs of real rows (before the y pass).  Unnormalised.
-template <typename T, int N>
-__global__ void __launch_bounds__(RowCfg<T, N>::THREADS)
+template <typename T, int N, int V = 0>
+__global__ void __launch_bounds__(RowXCfg<T, N, V>::THREADS)
     k_row_r2c(const T* __restrict__ in, typename cplx_of<T>::type* __restrict__ out, int ny,
               int rpitch, int pitch, const typename cplx_of<T>::type* __restrict__ tw) {
   typedef typename cplx_of<T>::type C;
-  typedef RowCfg<T, N> RC;
-  constexpr int G = RC::G, H = N / 2, NP = 4 * RC::RP, SL = RC::SL;
+  typedef RowXCfg<T, N, V> RC;
+  constexpr int G = fft_group(N), H = N / 2, NP = RC::NP, SL = N;
   extern __shared__ __align__(16) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);
   const int tid = threadIdx.x, y_base = blockIdx.x * (2 * NP);
-  for (int e = tid; e < NP * N; e += RC::THREADS) {
+  TARA_ELEM_LOOP(e, NP * N, RC::THREADS) {
     const int x = e % N, pp = e / N, ya = y_base + 2 * pp;
     sm[pp * SL + x] = (ya < ny) ? mkc<T>(in[(size_t)ya * rpitch + x], in[(size_t)(ya + 1) * rpitch + x])
                                : mkc<T>(T(0), T(0));
   }
   __syncthreads();
   fft_slot<T, N, false>(sm + (tid / G) * SL, tid % G, true, tw);
-  for (int e = tid; e < NP * (H + 1); e += RC::THREADS) {
+  TARA_ELEM_LOOP(e, NP * (H + 1), RC::THREADS) {
     const int k = e % (H + 1), pp = e / (H + 1), ya = y_base + 2 * pp;
     if (ya < ny) {
       const C z = sm[pp * SL + k], m = sm[pp * SL + ((N - k) & (N - 1))];

@@ -66,52 +66,68 @@ static int launch_col_forward(int nh, const void* nl, const StepBufs& sb, const 
   return TARA_OK;
 }
 
-template <typename T, int N, bool INV>
+template <typename T, int N, bool INV, int V>
 static int launch_col_fft(int nh, int pitch, const void* in, void* out, const void* tw,
                           cudaStream_t s) {
   typedef typename cplx_of<T>::type C;
-  typedef ColCfg<T, N> CF;
-  static cudaError_t attr = allow_smem(k_col_fft<T, N, INV>, CF::SMEM_C);
+  typedef ColCfg<T, N, V> CF;
+  static cudaError_t attr = allow_smem(k_col_fft<T, N, INV, V>, CF::SMEM_C);
   TARA_CK(attr);
   const int blocks = (nh + CF::TCC - 1) / CF::TCC;
-  k_col_fft<T, N, INV><<<blocks, CF::THREADS_C, CF::SMEM_C, s>>>((const C*)in, (C*)out, nh, pitch,
-                                                                  (const C*)tw);
+  k_col_fft<T, N, INV, V><<<blocks, CF::THREADS_C, CF::SMEM_C, s>>>((const C*)in, (C*)out, nh, pitch,
+                                                                     (const C*)tw);
   TARA_CK(cudaGetLastError());
   return TARA_OK;
 }
 
-template <typename T, int N>
+template <typename T, int N, int V>
 static int launch_row_c2r(int ny, int pitch, int rpitch, const void* in, void* out, const void* tw,
                           cudaStream_t s) {
   typedef typename cplx_of<T>::type C;
-  typedef RowCfg<T, N> RC;
-  static cudaError_t attr = allow_smem(k_row_c2r<T, N>, RC::SMEM);
+  typedef RowXCfg<T, N, V> RC;
+  static cudaError_t attr = allow_smem(k_row_c2r<T, N, V>, RC::SMEM);
   TARA_CK(attr);
-  const int per = 2 * 4 * RC::RP;
-  k_row_c2r<T, N><<<(ny + per - 1) / per, RC::THREADS, RC::SMEM, s>>>((const C*)in, (T*)out, ny,
-                                                                      pitch, rpitch, (const C*)tw);
+  const int per = 2 * RC::NP;
+  k_row_c2r<T, N, V><<<(ny + per - 1) / per, RC::THREADS, RC::SMEM, s>>>((const C*)in, (T*)out, ny,
+                                                                         pitch, rpitch, (const C*)tw);
   TARA_CK(cudaGetLastError());
   return TARA_OK;
 }
 
-template <typename T, int N>
+template <typename T, int N, int V>
 static int launch_row_r2c(int ny, int rpitch, int pitch, const void* in, void* out, const void* tw,
                           cudaStream_t s) {
   typedef typename cplx_of<T>::type C;
-  typedef RowCfg<T, N> RC;
-  static cudaError_t attr = allow_smem(k_row_r2c<T, N>, RC::SMEM);
+  typedef RowXCfg<T, N, V> RC;
+  static cudaError_t attr = allow_smem(k_row_r2c<T, N, V>, RC::SMEM);
   TARA_CK(attr);
-  const int per = 2 * 4 * RC::RP;
-  k_row_r2c<T, N><<<(ny + per - 1) / per, RC::THREADS, RC::SMEM, s>>>((const T*)in, (C*)out, ny,
-                                                                      rpitch, pitch, (const C*)tw);
+  const int per = 2 * RC::NP;
+  k_row_r2c<T, N, V><<<(ny + per - 1) / per, RC::THREADS, RC::SMEM, s>>>((const T*)in, (C*)out, ny,
+                                                                         rpitch, pitch, (const C*)tw);
   TARA_CK(cudaGetLastError());
   return TARA_OK;
+}
+
+// The plain transforms take the one-column / one-row-pair tiles when the
+// default tiles would leave most SMs idle (FP64 work then spreads over more SMs).
+constexpr int kFewCtas = 152;
+
+template <typename T, int N>
+static bool small_col(int nh) {
+  return (nh + ColCfg<T, N>::TCC - 1) / ColCfg<T, N>::TCC < kFewCtas;
+}
+
+template <typename T, int N>
+static bool small_row(int ny) {
+  return (ny + 2 * RowXCfg<T, N, 0>::NP - 1) / (2 * RowXCfg<T, N, 0>::NP) < kFewCtas;
 }
 
 template <typename T>
 int Launch2D<T>::col_inverse(int ny, int nh, const double2* win, void* u, const Grid2D& g,
                              const RhsParams& p, const void* twy, cudaStream_t s, int nb, int v) {
-  if (v) {
+  if (v == 2) {
+    TARA_SWITCH_N(ny, return (launch_col_inverse<T, N, 2>(nh, win, u, g, p, twy, s, nb)));
+  } else if (v == 1) {
     TARA_SWITCH_N(ny, return (launch_col_inverse<T, N, 1>(nh, win, u, g, p, twy, s, nb)));
   } else {
     TARA_SWITCH_N(ny, return (launch_col_inverse<T, N, 0>(nh, win, u, g, p, twy, s, nb)));
@@ -122,7 +138,9 @@ int Launch2D<T>::col_inverse(int ny, int nh, const double2* win, void* u, const 
 template <typename T>
 int Launch2D<T>::row_nl(int nx, int ny, const void* u, void* nl, const Grid2D& g, const void* twx,
                         cudaStream_t s, int nb, int v) {
-  if (v) {
+  if (v == 2) {
+    TARA_SWITCH_N(nx, return (launch_row_nl<T, N, 2>(ny, u, nl, g, twx, s, nb)));
+  } else if (v == 1) {
     TARA_SWITCH_N(nx, return (launch_row_nl<T, N, 1>(ny, u, nl, g, twx, s, nb)));
   } else {
     TARA_SWITCH_N(nx, return (launch_row_nl<T, N, 0>(ny, u, nl, g, twx, s, nb)));
@@ -134,7 +152,9 @@ template <typename T>
 int Launch2D<T>::col_forward(int ny, int nh, const void* nl, const StepBufs& sb, const Grid2D& g,
                              const RhsParams& p, int mode, const void* twy, cudaStream_t s, int nb,
                              int v) {
-  if (v) {
+  if (v == 2) {
+    TARA_SWITCH_N(ny, return (launch_col_forward<T, N, 2>(nh, nl, sb, g, p, mode, twy, s, nb)));
+  } else if (v == 1) {
     TARA_SWITCH_N(ny, return (launch_col_forward<T, N, 1>(nh, nl, sb, g, p, mode, twy, s, nb)));
   } else {
     TARA_SWITCH_N(ny, return (launch_col_forward<T, N, 0>(nh, nl, sb, g, p, mode, twy, s, nb)));
@@ -146,9 +166,13 @@ template <typename T>
 int Launch2D<T>::col_fft(int ny, int nh, int pitch, const void* in, void* out, bool inverse,
                          const void* twy, cudaStream_t s) {
   if (inverse) {
-    TARA_SWITCH_N(ny, return (launch_col_fft<T, N, true>(nh, pitch, in, out, twy, s)));
+    TARA_SWITCH_N(ny, return (small_col<T, N>(nh)
+                                  ? launch_col_fft<T, N, true, 2>(nh, pitch, in, out, twy, s)
+                                  : launch_col_fft<T, N, true, 0>(nh, pitch, in, out, twy, s)));
   } else {
-    TARA_SWITCH_N(ny, return (launch_col_fft<T, N, false>(nh, pitch, in, out, twy, s)));
+    TARA_SWITCH_N(ny, return (small_col<T, N>(nh)
+                                  ? launch_col_fft<T, N, false, 2>(nh, pitch, in, out, twy, s)
+                                  : launch_col_fft<T, N, false, 0>(nh, pitch, in, out, twy, s)));
   }
   return TARA_OK;
 }
@@ -156,14 +180,18 @@ int Launch2D<T>::col_fft(int ny, int nh, int pitch, const void* in, void* out, b
 template <typename T>
 int Launch2D<T>::row_c2r(int nx, int ny, int pitch, int rpitch, const void* in, void* out,
                          const void* twx, cudaStream_t s) {
-  TARA_SWITCH_N(nx, return (launch_row_c2r<T, N>(ny, pitch, rpitch, in, out, twx, s)));
+  TARA_SWITCH_N(nx, return (small_row<T, N>(ny)
+                                ? launch_row_c2r<T, N, 2>(ny, pitch, rpitch, in, out, twx, s)
+                                : launch_row_c2r<T, N, 0>(ny, pitch, rpitch, in, out, twx, s)));
   return TARA_OK;
 }
 
 template <typename T>
 int Launch2D<T>::row_r2c(int nx, int ny, int rpitch, int pitch, const void* in, void* out,
                          const void* twx, cudaStream_t s) {
-  TARA_SWITCH_N(nx, return (launch_row_r2c<T, N>(ny, rpitch, pitch, in, out, twx, s)));
+  TARA_SWITCH_N(nx, return (small_row<T, N>(ny)
+                                ? launch_row_r2c<T, N, 2>(ny, rpitch, pitch, in, out, twx, s)
+                                : launch_row_r2c<T, N, 0>(ny, rpitch, pitch, in, out, twx, s)));
   return TARA_OK;
 }
 

@@ -266,6 +266,7 @@ static int rhs_update_t(tara2d* h, const double2* win, int mode, cudaEvent_t* ev
   sb.fold = h->fold;
   sb.fout = h->fout;
   sb.flag = h->flag;
+  sb.force = h->force;
   int rc;
   const int nb = h->batch;
   if ((rc = Launch2D<T>::col_inverse(h->ny, h->nh, win, h->u, h->grid, h->rp, h->twy, h->stream, nb,
@@ -341,6 +342,33 @@ int refresh_tables(tara2d* h) {
   return TARA_OK;
 }
 
+int scratch(tara2d* h, size_t bytes, void** out) {
+  if (h->scratch_bytes < bytes) {
+    TARA_CK(cudaStreamSynchronize(h->stream));
+    cudaFree(h->scratch);
+    h->scratch = nullptr;
+    h->scratch_bytes = 0;
+    TARA_CK(cudaMalloc(&h->scratch, bytes));
+    h->scratch_bytes = bytes;
+  }
+  *out = h->scratch;
+  return TARA_OK;
+}
+
+int twiddles64(tara2d* h, const void** twx, const void** twy) {
+  if (h->cfg.precision == TARA_PREC_FP64) {
+    *twx = h->twx;
+    *twy = h->twy;
+    return TARA_OK;
+  }
+  int rc;
+  if (!h->twx64 && (rc = make_twiddles(h->nx, false, &h->twx64))) return rc;
+  if (!h->twy64 && (rc = make_twiddles(h->ny, false, &h->twy64))) return rc;
+  *twx = h->twx64;
+  *twy = h->twy64;
+  return TARA_OK;
+}
+
 static int check_flag(tara2d* h) {
   unsigned int f = 0;
   TARA_CK(cudaMemcpyAsync(&f, h->flag, sizeof(f), cudaMemcpyDeviceToHost, h->stream));
@@ -385,7 +413,7 @@ int tara2d_destroy(tara2d* h) {
   cudaSetDevice(h->dev);
   if (h->stream) cudaStreamSynchronize(h->stream);
   void* ptrs[] = {h->w0, h->ws, h->acc, h->fold, h->fout, h->u, h->nl, h->kx, h->ky, h->i0, h->inv, h->tabf,
-                  h->twx, h->twy, h->diag_part, h->diag_out, h->flag};
+                  h->twx, h->twy, h->diag_part, h->diag_out, h->flag, h->scratch, h->twx64, h->twy64};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (h->stream) cudaStreamDestroy(h->stream);
@@ -593,6 +621,55 @@ int tara2d_step_timed(tara2d* h, int nsteps, double* kernel_ms, int* kernel_laun
   for (cudaEvent_t e : ev)
     if (e) cudaEventDestroy(e);
   return rc ? rc : set_ok();
+}
+
+int tara2d_autotune(tara2d* h, int trial_steps, int* variants3, double* ms9) {
+  if (!h || trial_steps <= 0) return set_error(TARA_ERR_ARGS, "bad arguments");
+  TARA_CK(cudaSetDevice(h->dev));
+  const size_t bytes = (size_t)h->batch * h->ny * h->pitch * sizeof(double2);
+  double2 *save_w0 = nullptr, *save_fold = nullptr;
+  int rc = TARA_OK;
+  if (cudaMalloc(&save_w0, bytes) != cudaSuccess || cudaMalloc(&save_fold, bytes) != cudaSuccess)
+    rc = set_error(TARA_ERR_NOMEM, "cudaMalloc in tara2d_autotune");
+  if (!rc && (cudaMemcpyAsync(save_w0, h->w0, bytes, cudaMemcpyDeviceToDevice, h->stream) != cudaSuccess ||
+              cudaMemcpyAsync(save_fold, h->fold, bytes, cudaMemcpyDeviceToDevice, h->stream) != cudaSuccess))
+    rc = set_error(TARA_ERR_CUDA, "state save");
+  double ms[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+  for (int v = 0; v < 3 && !rc; ++v) {
+    for (int k = 0; k < 3; ++k) h->var[k] = v;
+    rc = tara2d_step(h, 1);  // first use of this variant: shared-memory attributes
+    double t[3];
+    int cnt[3];
+    if (!rc) rc = tara2d_step_timed(h, trial_steps, t, cnt, nullptr);
+    if (!rc)
+      for (int k = 0; k < 3; ++k) ms[v][k] = t[k] / (cnt[k] > 0 ? cnt[k] : 1);
+  }
+  if (!rc)
+    for (int k = 0; k < 3; ++k) {
+      int best = 0;
+      for (int v = 1; v < 3; ++v)
+        if (ms[v][k] < ms[best][k]) best = v;
+      h->var[k] = best;
+      if (variants3) variants3[k] = best;
+    }
+  if (!rc && ms9)
+    for (int v = 0; v < 3; ++v)
+      for (int k = 0; k < 3; ++k) ms9[3 * v + k] = ms[v][k];
+  if (!rc && (cudaMemcpyAsync(h->w0, save_w0, bytes, cudaMemcpyDeviceToDevice, h->stream) != cudaSuccess ||
+              cudaMemcpyAsync(h->fold, save_fold, bytes, cudaMemcpyDeviceToDevice, h->stream) != cudaSuccess ||
+              cudaStreamSynchronize(h->stream) != cudaSuccess))
+    rc = set_error(TARA_ERR_CUDA, "state restore");
+  cudaFree(save_w0);
+  cudaFree(save_fold);
+  return rc ? rc : set_ok();
+}
+
+int tara2d_set_variants(tara2d* h, const int* variants3) {
+  if (!h || !variants3) return set_error(TARA_ERR_ARGS, "null argument");
+  for (int k = 0; k < 3; ++k)
+    if (variants3[k] < 0 || variants3[k] > 2) return set_error(TARA_ERR_ARGS, "variants are 0, 1 or 2");
+  for (int k = 0; k < 3; ++k) h->var[k] = variants3[k];
+  return set_ok();
 }
 
 int tara2d_rhs(tara2d* h, double* dt_omegak) {

@@ -53,8 +53,8 @@ def test_autotune_keeps_state_and_picks_variants():
         groups = e.groups()
         assert sorted(g["n"] for g in groups) == [32, 64, 128]
         for g in groups:
-            assert all(v in (0, 1) for v in g["variants"])
-            assert all(t > 0 for t in g["tuned_ms"])
+            assert all(v in (0, 1, 2) for v in g["variants"])
+            assert len(g["tuned_ms"]) == 9 and all(t > 0 for t in g["tuned_ms"])
         e.step(3)  # graph captured with the chosen variants
         e.synchronize()
         assert e.launches_per_step == 3 * 12
@@ -69,3 +69,31 @@ def test_ensemble_run_matches_oracle(oracle):
     assert rel_l2(w0, oracle.ic_random(64, 64, 6.0, 0.5, 20240512)) < 1e-13
     ref, _ = oracle.run(w0, rhs=0, scheme=1, nu=1e-4, dt=5e-5, steps=10)
     assert rel_l2(w, ref) < 1e-12
+
+
+@pytest.mark.parametrize("n", [64, 256])
+@pytest.mark.parametrize("prec", [tg.PREC_FP64, tg.PREC_FP32])
+def test_tile_variants_are_bitwise_equal(n, prec):
+    """Every tile variant runs the same per-column / per-row arithmetic."""
+    out = []
+    for v in ((0, 0, 0), (1, 1, 1), (2, 2, 2), (2, 0, 1)):
+        with tg.Solver2D(n, scheme=tg.SCHEME_RK4, precision=prec, nu=1e-3, dt=1e-4) as s:
+            s.init_random(6.0, 0.5, 4100)
+            s.set_variants(v)
+            s.step(3)
+            s.synchronize()
+            out.append(s.get_state())
+    for o in out[1:]:
+        assert np.array_equal(o, out[0])
+
+
+def test_solver_autotune_restores_state():
+    with tg.Solver2D(128, scheme=tg.SCHEME_AB2, nu=1e-3, dt=1e-4) as s:
+        s.init_random(6.0, 0.5, 4101)
+        s.step(2)
+        w, fo = s.get_state(with_history=True)
+        r = s.autotune(2)
+        w2, fo2 = s.get_state(with_history=True)
+        assert np.array_equal(w, w2) and np.array_equal(fo, fo2)
+        assert all(v in (0, 1, 2) for v in r["variants"])
+        assert all(t > 0 for row in r["ms"] for t in row)
