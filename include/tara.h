@@ -390,14 +390,31 @@ int tara2d_set_state_real_device(tara2d* h, int run, const double* omega_dev);
  * so that sum_k E[k] is the energy when kmax covers the grid. */
 int tara2d_spectrum(tara2d* h, int run, int kmax, double* E);
 
+/* Input features of the closure network from run `run`'s state, in real space
+ * on the handle's grid: the first nf (1..6) of w, dw/dx, dw/dy, du/dx, du/dy,
+ * dv/dx (u = d psi/dy, v = -d psi/dx, spectral derivatives, FP64), each times
+ * scales[c] (NULL: 1), written as FP32 (Ny, Nx, nf) at out_dev. */
+int tara2d_features(tara2d* h, int run, int nf, const double* scales, float* out_dev);
+
+/* Training-set augmentation by the eight symmetries of the square periodic
+ * grid (g = bit 0: x -> -x, bit 1: y -> -y, bit 2: transpose, in that order):
+ * sample g*n_samples + i of the outputs is symmetry g of sample i.  x: features
+ * (n_samples, n, n, nf) as tara2d_features writes them; t: subgrid fluxes
+ * (n_samples, n, n, 2) as tara2d_filter writes them.  Reflections negate w and
+ * the derivatives across them; the transpose swaps the x and y components.
+ * Either input may be NULL.  Synchronous (legacy default stream). */
+int tara_closure_augment(const float* x_dev, const float* t_dev, int n_samples, int n, int nf,
+                         float* x_out, float* t_out);
+
 /* A coarse plain-solver handle advanced with the FNO's subgrid flux: every
- * step evaluates y = FNO(in_scale * omega) on the runs' real vorticity, takes
+ * step evaluates y = FNO(features) with the network's ci feature channels
+ * (tara2d_features, scaled by in_scales[0..ci-1]) on every run, takes
  * flux = out_scale * y and adds -div(flux) (2/3-truncated) to the right-hand
  * side of every stage of the step.  The handle and the network stay owned by
  * the caller and must outlive the closure; the network's batch must hold the
  * handle's runs and its grid must be the handle's. */
 typedef struct tara_closure tara_closure;
-int tara_closure_create(tara2d* coarse, tara_fno* fno, double in_scale, double out_scale,
+int tara_closure_create(tara2d* coarse, tara_fno* fno, const double* in_scales, double out_scale,
                         tara_closure** out);
 int tara_closure_destroy(tara_closure* c);
 /* Advance nsteps closure steps (enqueued on the handle's stream). */

@@ -134,8 +134,8 @@ def adam(params, grad, m, v, step: int, lr: float, b1=0.9, b2=0.999, eps=1e-8):
 # ---------------------------------------------------------------------------
 def velocity(omega: np.ndarray):
     """u = d psi/dy, v = -d psi/dx with -lap psi = omega on the 2pi-periodic grid (y rows, x columns),
-    integer wavenumbers; the mean mode of psi is zero.  (The solver's plain RHS convention:
-    u_x = i ky psi_hat, u_y = -i kx psi_hat.)"""
+    integer wavenumbers; the mean mode of psi is zero and the Nyquist modes (kx = nx/2 or
+    ky = -ny/2) contribute nothing.  (u_x = i ky psi_hat, u_y = -i kx psi_hat.)"""
     ny, nx = omega.shape
     w = np.fft.rfft2(omega)
     ky = np.fft.fftfreq(ny, 1.0 / ny)[:, None]
@@ -144,6 +144,8 @@ def velocity(omega: np.ndarray):
     k2[0, 0] = 1.0
     psi = w / k2
     psi[0, 0] = 0.0
+    psi[ny // 2, :] = 0.0  # no odd derivative of the Nyquist modes
+    psi[:, nx // 2] = 0.0
     return np.fft.irfft2(1j * ky * psi, s=omega.shape), np.fft.irfft2(-1j * kx * psi, s=omega.shape)
 
 

@@ -190,7 +190,9 @@ def _declare(L: ctypes.CDLL) -> None:
     L.tara2d_set_variants.argtypes = [vp, ip]
     L.tara2d_set_state_real_device.argtypes = [vp, c_int, vp]
     L.tara2d_spectrum.argtypes = [vp, c_int, c_int, dp]
-    L.tara_closure_create.argtypes = [vp, vp, c_double, c_double, ctypes.POINTER(vp)]
+    L.tara_closure_create.argtypes = [vp, vp, dp, c_double, ctypes.POINTER(vp)]
+    L.tara2d_features.argtypes = [vp, c_int, c_int, dp, vp]
+    L.tara_closure_augment.argtypes = [vp, vp, c_int, c_int, c_int, vp, vp]
     L.tara_closure_destroy.argtypes = [vp]
     L.tara_closure_step.argtypes = [vp, c_int]
 
@@ -445,6 +447,12 @@ class Solver2D:
         (FP32 omega_bar, FP32 (.., 2) flux, FP64 omega_bar64), 0 to skip."""
         _check(lib().tara2d_filter(self._h, run, factor, ctypes.c_void_p(omega_bar or None),
                                    ctypes.c_void_p(flux or None), ctypes.c_void_p(omega_bar64 or None)))
+
+    def features(self, run: int, nf: int, out_ptr: int, scales=None) -> None:
+        """Closure input features (FP32 (Ny, Nx, nf)) of run `run` at a device pointer."""
+        sc = None if scales is None else np.ascontiguousarray(np.asarray(scales, np.float64))
+        _check(lib().tara2d_features(self._h, run, nf, None if sc is None else _dp(sc),
+                                     ctypes.c_void_p(out_ptr)))
 
     def set_state_real_device(self, run: int, ptr: int) -> None:
         _check(lib().tara2d_set_state_real_device(self._h, run, ctypes.c_void_p(ptr)))
@@ -733,12 +741,24 @@ class FNO:
         return lib().tara_fno_stream(self._h) or 0
 
 
+def closure_augment(x_ptr: int, t_ptr: int, n_samples: int, n: int, nf: int, x_out: int, t_out: int) -> None:
+    """Eight-fold symmetry augmentation of closure samples (device pointers; 0 skips)."""
+    _check(lib().tara_closure_augment(ctypes.c_void_p(x_ptr or None), ctypes.c_void_p(t_ptr or None),
+                                      n_samples, n, nf, ctypes.c_void_p(x_out or None),
+                                      ctypes.c_void_p(t_out or None)))
+
+
 class Closure:
     """tara_closure: a coarse Solver2D stepped with the FNO's subgrid flux."""
 
-    def __init__(self, solver: Solver2D, fno: FNO, in_scale: float, out_scale: float):
+    def __init__(self, solver: Solver2D, fno: FNO, in_scale, out_scale: float):
+        """in_scale: one value per input feature channel (a scalar for one channel)."""
+        sc = np.atleast_1d(np.asarray(in_scale, np.float64))
+        if sc.size != int(fno.cfg.ci):
+            raise ValueError(f"expected {int(fno.cfg.ci)} input scales, got {sc.size}")
         h = ctypes.c_void_p()
-        _check(lib().tara_closure_create(solver._h, fno._h, in_scale, out_scale, ctypes.byref(h)))
+        _check(lib().tara_closure_create(solver._h, fno._h, _dp(np.ascontiguousarray(sc)), out_scale,
+                                         ctypes.byref(h)))
         self._h = h
         self.solver, self.fno = solver, fno  # keep both alive
 

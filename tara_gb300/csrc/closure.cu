@@ -5,6 +5,7 @@
 // None of this has a counterpart in the reference; it reuses the solver's
 // FP64 transform kernels (Stockham column and row passes) and adds the
 // pointwise kernels below.
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -13,10 +14,12 @@
 struct tara_closure {
   tara2d* h = nullptr;
   tara_fno* f = nullptr;
-  double in_scale = 1.0, out_scale = 1.0;
+  int nf = 1;                  // input feature channels
+  double* in_scale = nullptr;  // device, nf values (the input scale / (NxNy))
+  double out_scale = 1.0;
   int rpitch = 0;
-  double2* spec = nullptr;   // batch fields: c2r input copies / 2*batch r2c outputs
-  double* real = nullptr;    // 2*batch real fields
+  double2* spec = nullptr;   // max(nf, 2) * batch spectra
+  double* real = nullptr;    // max(nf, 2) * batch real fields
   double2* force = nullptr;  // batch forcing spectra
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -39,9 +42,13 @@ __global__ void k_vel_spectra(const double2* __restrict__ w, Grid2D g, double2* 
     const double inv = g.inv[(size_t)y * g.nh + x];
     const double pr = v.x * inv, pim = v.y * inv;
     const double kx = g.kx[x], ky = g.ky[y];
+    // the odd derivatives of the Nyquist modes (kx = Nx/2 or ky = -Ny/2) are
+    // dropped: a real field's derivative has no such component, and keeping
+    // the one-sided value would break the reflection symmetry of the data
+    const bool nyq = 2 * x == g.nx || 2 * y == g.ny;
     out[q] = v;
-    out[fsz + q] = make_double2(-ky * pim, ky * pr);
-    out[2 * fsz + q] = make_double2(kx * pim, -(kx * pr));
+    out[fsz + q] = nyq ? make_double2(0.0, 0.0) : make_double2(-ky * pim, ky * pr);
+    out[2 * fsz + q] = nyq ? make_double2(0.0, 0.0) : make_double2(kx * pim, -(kx * pr));
   }
 }
 
@@ -108,14 +115,44 @@ __global__ void k_shell_spectrum(const double2* __restrict__ w, Grid2D g, int km
     if (sh[k] != 0.0) atomicAdd(&E[k], sh[k]);
 }
 
-// FNO input: x[b][y][x] = s * r[b][y][x] (pitched FP64 -> dense FP32)
+// Feature spectra of the closure network for one run, `nf` of the fields
+// 0 w, 1 dw/dx, 2 dw/dy, 3 du/dx, 4 du/dy, 5 dv/dx  with u = i ky psi, v = -i kx psi,
+// psi = w inv (inv = 1/k^2, 0 at k = 0), into nf pitched fields.
+constexpr int kMaxFeat = 6;
+__global__ void k_feature_spectra(const double2* __restrict__ w, Grid2D g, int nf, double2* __restrict__ out) {
+  const size_t total = (size_t)g.ny * g.nh, fsz = (size_t)g.ny * g.pitch;
+  w += blockIdx.y * fsz;  // run blockIdx.y: state fsz apart, features nf * fsz apart
+  out += blockIdx.y * nf * fsz;
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += (size_t)gridDim.x * blockDim.x) {
+    const int y = (int)(t / g.nh), x = (int)(t % g.nh);
+    const size_t q = (size_t)y * g.pitch + x;
+    const double2 v = w[q];
+    const double inv = g.inv[(size_t)y * g.nh + x];
+    const double pr = v.x * inv, pim = v.y * inv;
+    const double kx = g.kx[x], ky = g.ky[y];
+    double2 f[kMaxFeat];
+    const bool nyq = 2 * x == g.nx || 2 * y == g.ny;  // odd derivatives dropped there
+    f[0] = v;
+    f[1] = make_double2(-kx * v.y, kx * v.x);                 // i kx w
+    f[2] = make_double2(-ky * v.y, ky * v.x);                 // i ky w
+    f[3] = make_double2(-(kx * ky) * pr, -(kx * ky) * pim);   // i kx u = -kx ky psi
+    f[4] = make_double2(-(ky * ky) * pr, -(ky * ky) * pim);   // i ky u = -ky^2 psi
+    f[5] = make_double2((kx * kx) * pr, (kx * kx) * pim);     // i kx v = kx^2 psi
+    for (int c = 0; c < nf; ++c) out[c * fsz + q] = (c > 0 && nyq) ? make_double2(0.0, 0.0) : f[c];
+  }
+}
+
+// FNO input: x[b][y][x][c] = s[c] * r[b*nf + c][y][x] (pitched FP64 fields -> NHWC FP32)
 __global__ void k_real_to_input(const double* __restrict__ r, int nx, int ny, int rp, size_t rf, int B,
-                                double s, float* __restrict__ x) {
-  const size_t n = (size_t)B * nx * ny;
+                                int nf, const double* __restrict__ s, float* __restrict__ x) {
+  const size_t n = (size_t)B * nx * ny * nf;
   for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
-    const size_t b = t / ((size_t)nx * ny), e = t % ((size_t)nx * ny);
+    const int c = (int)(t % nf);
+    const size_t p = t / nf;
+    const size_t b = p / ((size_t)nx * ny), e = p % ((size_t)nx * ny);
     const size_t y = e / nx, xx = e % nx;
-    x[t] = (float)(r[b * rf + y * rp + xx] * s);
+    x[t] = (float)(r[(b * nf + c) * rf + y * rp + xx] * s[c]);
   }
 }
 
@@ -152,6 +189,49 @@ __global__ void k_div_forcing(const double2* __restrict__ fl, Grid2D g, int B, d
   }
 }
 
+// The eight symmetries of the square periodic grid (bit 0: x -> -x, bit 1:
+// y -> -y, bit 2: transpose x <-> y, applied in that order) acting on closure
+// samples.  Under x -> -x, w and its y derivatives change sign
+// (w' = -w(-x, y), u' = (-u_x, u_y)(-x, y)); under transpose w' = -w(y, x) and
+// the velocity components swap.  Sign and channel tables per channel of the
+// features (w, dw/dx, dw/dy, du/dx, du/dy, dv/dx) and of the flux (x, y).
+__constant__ float kSgnFx[6] = {-1.f, 1.f, -1.f, 1.f, -1.f, -1.f};
+__constant__ float kSgnFy[6] = {-1.f, -1.f, 1.f, 1.f, -1.f, -1.f};
+__constant__ float kSgnFt[6] = {-1.f, -1.f, -1.f, -1.f, 1.f, 1.f};
+__constant__ int kPermFt[6] = {0, 2, 1, 3, 5, 4};
+__constant__ float kSgnPx[2] = {1.f, -1.f};
+__constant__ float kSgnPy[2] = {-1.f, 1.f};
+__constant__ float kSgnPt[2] = {-1.f, -1.f};
+__constant__ int kPermPt[2] = {1, 0};
+
+// out[g*N + i] = symmetry g of sample i, for (N, n, n, nc) arrays; flux != 0
+// selects the flux tables, else the feature tables.
+__global__ void k_augment(const float* __restrict__ in, int N, int n, int nc, int flux, float* __restrict__ out) {
+  const size_t per = (size_t)n * n * nc, total = (size_t)8 * N * per;
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
+    const size_t smp = t / per, e = t % per;
+    const int g = (int)(smp / N), i = (int)(smp % N);
+    const int c = (int)(e % nc), x = (int)((e / nc) % n), y = (int)(e / ((size_t)nc * n));
+    int xs = x, ys = y, cs = c;
+    float sg = 1.f;
+    if (g & 4) {  // undo the transpose first (it was applied last)
+      xs = y;
+      ys = x;
+      sg *= flux ? kSgnPt[c] : kSgnFt[c];
+      cs = flux ? kPermPt[c] : kPermFt[c];
+    }
+    if (g & 2) {
+      ys = n - 1 - ys;
+      sg *= flux ? kSgnPy[cs] : kSgnFy[cs];
+    }
+    if (g & 1) {
+      xs = n - 1 - xs;
+      sg *= flux ? kSgnPx[cs] : kSgnFx[cs];
+    }
+    out[t] = sg * in[(size_t)i * per + ((size_t)ys * n + xs) * nc + cs];
+  }
+}
+
 constexpr int kBlocks = 152 * 4, kThreads = 256;
 
 // c2r of `nf` pitched spectra (fields fsz apart; `in` is left untouched when
@@ -161,15 +241,9 @@ int c2r_fields(tara2d* h, const double2* in, double2* spec, double* real, int nf
   int rc;
   if ((rc = twiddles64(h, &tx, &ty))) return rc;
   const size_t fsz = (size_t)h->ny * h->pitch, rfs = (size_t)h->ny * rpitch;
-  for (int f = 0; f < nf; ++f) {
-    if ((rc = Launch2D<double>::col_fft(h->ny, h->nh, h->pitch, in + f * fsz, spec + f * fsz, true, ty,
-                                        h->stream)))
-      return rc;
-    if ((rc = Launch2D<double>::row_c2r(h->nx, h->ny, h->pitch, rpitch, spec + f * fsz, real + f * rfs, tx,
-                                        h->stream)))
-      return rc;
-  }
-  return TARA_OK;
+  if ((rc = Launch2D<double>::col_fft(h->ny, h->nh, h->pitch, in, spec, true, ty, h->stream, nf, fsz)))
+    return rc;
+  return Launch2D<double>::row_c2r(h->nx, h->ny, h->pitch, rpitch, spec, real, tx, h->stream, nf, fsz, rfs);
 }
 
 int r2c_fields(tara2d* h, const double* real, double2* spec, int nf, int rpitch) {
@@ -177,14 +251,24 @@ int r2c_fields(tara2d* h, const double* real, double2* spec, int nf, int rpitch)
   int rc;
   if ((rc = twiddles64(h, &tx, &ty))) return rc;
   const size_t fsz = (size_t)h->ny * h->pitch, rfs = (size_t)h->ny * rpitch;
-  for (int f = 0; f < nf; ++f) {
-    if ((rc = Launch2D<double>::row_r2c(h->nx, h->ny, rpitch, h->pitch, real + f * rfs, spec + f * fsz, tx,
-                                        h->stream)))
-      return rc;
-    if ((rc = Launch2D<double>::col_fft(h->ny, h->nh, h->pitch, spec + f * fsz, spec + f * fsz, false, ty,
-                                        h->stream)))
-      return rc;
-  }
+  if ((rc = Launch2D<double>::row_r2c(h->nx, h->ny, rpitch, h->pitch, real, spec, tx, h->stream, nf, rfs, fsz)))
+    return rc;
+  return Launch2D<double>::col_fft(h->ny, h->nh, h->pitch, spec, spec, false, ty, h->stream, nf, fsz);
+}
+
+// Feature fields of runs [r0, r0+nr) as NHWC FP32 (nf channels) at dst, each
+// channel multiplied by s[c] (device, already divided by NxNy).  spec/real hold
+// nf*nr fields.
+int features(tara2d* h, int r0, int nr, int nf, double2* spec, double* real, int rpitch,
+             const double* s, float* dst) {
+  const size_t fsz = (size_t)h->ny * h->pitch, rfs = (size_t)h->ny * rpitch;
+  int rc;
+  k_feature_spectra<<<dim3(kBlocks / 4, nr), kThreads, 0, h->stream>>>(h->w0 + (size_t)r0 * fsz, h->grid, nf,
+                                                                        spec);
+  TARA_CK(cudaGetLastError());
+  if ((rc = c2r_fields(h, spec, spec, real, nf * nr, rpitch))) return rc;
+  k_real_to_input<<<kBlocks, kThreads, 0, h->stream>>>(real, h->nx, h->ny, rpitch, rfs, nr, nf, s, dst);
+  TARA_CK(cudaGetLastError());
   return TARA_OK;
 }
 
@@ -193,12 +277,8 @@ int closure_step_once(tara_closure* c) {
   tara2d* h = c->h;
   const int B = h->batch;
   const size_t rfs = (size_t)h->ny * c->rpitch;
-  const double nn = (double)h->nx * (double)h->ny;
   int rc;
-  if ((rc = c2r_fields(h, h->w0, c->spec, c->real, B, c->rpitch))) return rc;
-  k_real_to_input<<<kBlocks, kThreads, 0, h->stream>>>(c->real, h->nx, h->ny, c->rpitch, rfs, B,
-                                                        c->in_scale / nn, fno_input(c->f));
-  TARA_CK(cudaGetLastError());
+  if ((rc = features(h, 0, B, c->nf, c->spec, c->real, c->rpitch, c->in_scale, fno_input(c->f)))) return rc;
   const float* y = nullptr;
   fno_bind_stream(c->f, h->stream);
   rc = fno_forward_async(c->f, nullptr, B, &y);
@@ -292,32 +372,44 @@ int tara_closure_destroy(tara_closure* c) {
   if (c->graph) cudaGraphDestroy(c->graph);
   cudaFree(c->spec);
   cudaFree(c->real);
+  cudaFree(c->in_scale);
   cudaFree(c->force);
   delete c;
   return set_ok();
 }
 
-int tara_closure_create(tara2d* h, tara_fno* f, double in_scale, double out_scale, tara_closure** out) {
-  if (!h || !f || !out) return set_error(TARA_ERR_ARGS, "null argument");
+int tara_closure_create(tara2d* h, tara_fno* f, const double* in_scales, double out_scale,
+                        tara_closure** out) {
+  if (!h || !f || !out || !in_scales) return set_error(TARA_ERR_ARGS, "null argument");
   *out = nullptr;
   const tara_fno_config& fc = fno_config(f);
-  if (fc.h != h->ny || fc.w != h->nx || fc.ci != 1 || fc.co != 2 || fc.max_batch < h->batch)
+  if (fc.h != h->ny || fc.w != h->nx || fc.ci < 1 || fc.ci > kMaxFeat || fc.co != 2 ||
+      fc.max_batch < h->batch)
     return set_error(TARA_ERR_ARGS, "network grid, channels or batch do not fit the handle");
   if (h->cfg.rhs != TARA_RHS_PLAIN) return set_error(TARA_ERR_ARGS, "the closure drives the plain RHS");
   TARA_CK(cudaSetDevice(h->dev));
   tara_closure* c = new tara_closure();
   c->h = h;
   c->f = f;
-  c->in_scale = in_scale;
+  c->nf = fc.ci;
   c->out_scale = out_scale;
   c->rpitch = round_up(h->nx, 8);
   const int B = h->batch;
+  const int nfield = std::max(c->nf, 2) * B;
   const size_t fsz = (size_t)h->ny * h->pitch, rfs = (size_t)h->ny * c->rpitch;
-  if (cudaMalloc(&c->spec, 2 * B * fsz * sizeof(double2)) != cudaSuccess ||
-      cudaMalloc(&c->real, 2 * B * rfs * sizeof(double)) != cudaSuccess ||
+  if (cudaMalloc(&c->spec, nfield * fsz * sizeof(double2)) != cudaSuccess ||
+      cudaMalloc(&c->real, nfield * rfs * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&c->in_scale, kMaxFeat * sizeof(double)) != cudaSuccess ||
       cudaMalloc(&c->force, B * fsz * sizeof(double2)) != cudaSuccess) {
     tara_closure_destroy(c);
     return set_error(TARA_ERR_NOMEM, "cudaMalloc in tara_closure_create");
+  }
+  double sc[kMaxFeat];
+  const double nn = (double)h->nx * (double)h->ny;
+  for (int i = 0; i < c->nf; ++i) sc[i] = in_scales[i] / nn;
+  if (cudaMemcpy(c->in_scale, sc, c->nf * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) {
+    tara_closure_destroy(c);
+    return set_error(TARA_ERR_CUDA, "scale upload");
   }
   const void *tx, *ty;
   int rc;
@@ -326,6 +418,45 @@ int tara_closure_create(tara2d* h, tara_fno* f, double in_scale, double out_scal
     return rc;
   }
   *out = c;
+  return set_ok();
+}
+
+int tara_closure_augment(const float* x_dev, const float* t_dev, int n_samples, int n, int nf, float* x_out,
+                         float* t_out) {
+  if (n_samples < 1 || n < 2 || nf < 1 || nf > kMaxFeat || (!x_dev && !t_dev) || (x_dev && !x_out) ||
+      (t_dev && !t_out))
+    return set_error(TARA_ERR_ARGS, "bad augmentation arguments");
+  if (x_dev) {
+    k_augment<<<kBlocks * 4, kThreads>>>(x_dev, n_samples, n, nf, 0, x_out);
+    TARA_CK(cudaGetLastError());
+  }
+  if (t_dev) {
+    k_augment<<<kBlocks * 4, kThreads>>>(t_dev, n_samples, n, 2, 1, t_out);
+    TARA_CK(cudaGetLastError());
+  }
+  TARA_CK(cudaDeviceSynchronize());
+  return set_ok();
+}
+
+int tara2d_features(tara2d* h, int run, int nf, const double* scales, float* out_dev) {
+  if (!h || !out_dev || run < 0 || run >= h->batch || nf < 1 || nf > kMaxFeat)
+    return set_error(TARA_ERR_ARGS, "bad feature arguments");
+  TARA_CK(cudaSetDevice(h->dev));
+  const int rpitch = round_up(h->nx, 8);
+  const size_t fsz = (size_t)h->ny * h->pitch, rfs = (size_t)h->ny * rpitch;
+  void* ws = nullptr;
+  int rc;
+  if ((rc = scratch(h, nf * (fsz * sizeof(double2) + rfs * sizeof(double)) + kMaxFeat * sizeof(double), &ws)))
+    return rc;
+  double2* spec = (double2*)ws;
+  double* real = (double*)(spec + nf * fsz);
+  double* ds = real + nf * rfs;
+  double sc[kMaxFeat];
+  const double nn = (double)h->nx * (double)h->ny;
+  for (int i = 0; i < nf; ++i) sc[i] = (scales ? scales[i] : 1.0) / nn;
+  TARA_CK(cudaMemcpyAsync(ds, sc, nf * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  if ((rc = features(h, run, 1, nf, spec, real, rpitch, ds, out_dev))) return rc;
+  TARA_CK(cudaStreamSynchronize(h->stream));
   return set_ok();
 }
 

@@ -46,12 +46,13 @@ struct Launch2D {
   static int col_forward(int ny, int nh, const void* nl, const StepBufs& sb, const Grid2D& g,
                          const RhsParams& p, int mode, const void* twy, cudaStream_t s,
                          int nb = 1, int v = 0);
+  // plain transforms of nf fields (fs / fs_in / fs_out elements apart)
   static int col_fft(int ny, int nh, int pitch, const void* in, void* out, bool inverse,
-                     const void* twy, cudaStream_t s);
+                     const void* twy, cudaStream_t s, int nf = 1, size_t fs = 0);
   static int row_c2r(int nx, int ny, int pitch, int rpitch, const void* in, void* out,
-                     const void* twx, cudaStream_t s);
+                     const void* twx, cudaStream_t s, int nf = 1, size_t fs_in = 0, size_t fs_out = 0);
   static int row_r2c(int nx, int ny, int rpitch, int pitch, const void* in, void* out,
-                     const void* twx, cudaStream_t s);
+                     const void* twx, cudaStream_t s, int nf = 1, size_t fs_in = 0, size_t fs_out = 0);
 };
 
 // Twiddle table exp(-2 pi i m/n), m < n, in precision T, uploaded to device.

@@ -447,13 +447,15 @@ __global__ void __launch_bounds__(ColCfg<T, N, V>::THREADS_C)
 template <typename T, int N, bool INV, int V = 0>
 __global__ void __launch_bounds__(ColCfg<T, N, V>::THREADS_C)
     k_col_fft(const typename cplx_of<T>::type* in, typename cplx_of<T>::type* out, int nh,
-              int pitch, const typename cplx_of<T>::type* __restrict__ tw) {
+              int pitch, size_t fs, const typename cplx_of<T>::type* __restrict__ tw) {
   typedef typename cplx_of<T>::type C;
   typedef ColCfg<T, N, V> CF;
   constexpr int TC = CF::TCC, S = CF::S, G = CF::G;
   extern __shared__ __align__(16) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);
   const int x0 = blockIdx.x * TC, tid = threadIdx.x;
+  in += blockIdx.y * fs;  // field of a batch (blockIdx.y), fs elements apart
+  out += blockIdx.y * fs;
   TARA_ELEM_LOOP(e, N * TC, CF::THREADS_C) {
     const int y = e / TC, c = e % TC, x = x0 + c;
     sm[c * S + y] = (x < nh) ? in[(size_t)y * pitch + x] : mkc<T>(T(0), T(0));
@@ -479,13 +481,16 @@ template <typename T, int N, int V> struct RowXCfg {
 template <typename T, int N, int V = 0>
 __global__ void __launch_bounds__(RowXCfg<T, N, V>::THREADS)
     k_row_c2r(const typename cplx_of<T>::type* __restrict__ in, T* __restrict__ out, int ny,
-              int pitch, int rpitch, const typename cplx_of<T>::type* __restrict__ tw) {
+              int pitch, int rpitch, size_t fs_in, size_t fs_out,
+              const typename cplx_of<T>::type* __restrict__ tw) {
   typedef typename cplx_of<T>::type C;
   typedef RowXCfg<T, N, V> RC;
   constexpr int G = fft_group(N), H = N / 2, NP = RC::NP, SL = N;  // NP row pairs per CTA
   extern __shared__ __align__(16) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);  // [NP][N]
   const int tid = threadIdx.x, y_base = blockIdx.x * (2 * NP);
+  in += blockIdx.y * fs_in;  // field of a batch (blockIdx.y)
+  out += blockIdx.y * fs_out;
   TARA_ELEM_LOOP(e, NP * N, RC::THREADS) {
     const int k = e % N, pp = e / N, ya = y_base + 2 * pp;
     C z = mkc<T>(T(0), T(0));
@@ -516,13 +521,16 @@ __global__ void __launch_bounds__(RowXCfg<T, N, V>::THREADS)
 template <typename T, int N, int V = 0>
 __global__ void __launch_bounds__(RowXCfg<T, N, V>::THREADS)
     k_row_r2c(const T* __restrict__ in, typename cplx_of<T>::type* __restrict__ out, int ny,
-              int rpitch, int pitch, const typename cplx_of<T>::type* __restrict__ tw) {
+              int rpitch, int pitch, size_t fs_in, size_t fs_out,
+              const typename cplx_of<T>::type* __restrict__ tw) {
   typedef typename cplx_of<T>::type C;
   typedef RowXCfg<T, N, V> RC;
   constexpr int G = fft_group(N), H = N / 2, NP = RC::NP, SL = N;
   extern __shared__ __align__(16) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);
   const int tid = threadIdx.x, y_base = blockIdx.x * (2 * NP);
+  in += blockIdx.y * fs_in;  // field of a batch (blockIdx.y)
+  out += blockIdx.y * fs_out;
   TARA_ELEM_LOOP(e, NP * N, RC::THREADS) {
     const int x = e % N, pp = e / N, ya = y_base + 2 * pp;
     sm[pp * SL + x] = (ya < ny) ? mkc<T>(in[(size_t)ya * rpitch + x], in[(size_t)(ya + 1) * rpitch + x])

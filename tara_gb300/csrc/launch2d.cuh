@@ -68,13 +68,13 @@ static int launch_col_forward(int nh, const void* nl, const StepBufs& sb, const 
 
 template <typename T, int N, bool INV, int V>
 static int launch_col_fft(int nh, int pitch, const void* in, void* out, const void* tw,
-                          cudaStream_t s) {
+                          cudaStream_t s, int nf, size_t fs) {
   typedef typename cplx_of<T>::type C;
   typedef ColCfg<T, N, V> CF;
   static cudaError_t attr = allow_smem(k_col_fft<T, N, INV, V>, CF::SMEM_C);
   TARA_CK(attr);
-  const int blocks = (nh + CF::TCC - 1) / CF::TCC;
-  k_col_fft<T, N, INV, V><<<blocks, CF::THREADS_C, CF::SMEM_C, s>>>((const C*)in, (C*)out, nh, pitch,
+  const dim3 blocks((nh + CF::TCC - 1) / CF::TCC, nf);
+  k_col_fft<T, N, INV, V><<<blocks, CF::THREADS_C, CF::SMEM_C, s>>>((const C*)in, (C*)out, nh, pitch, fs,
                                                                      (const C*)tw);
   TARA_CK(cudaGetLastError());
   return TARA_OK;
@@ -82,28 +82,30 @@ static int launch_col_fft(int nh, int pitch, const void* in, void* out, const vo
 
 template <typename T, int N, int V>
 static int launch_row_c2r(int ny, int pitch, int rpitch, const void* in, void* out, const void* tw,
-                          cudaStream_t s) {
+                          cudaStream_t s, int nf, size_t fs_in, size_t fs_out) {
   typedef typename cplx_of<T>::type C;
   typedef RowXCfg<T, N, V> RC;
   static cudaError_t attr = allow_smem(k_row_c2r<T, N, V>, RC::SMEM);
   TARA_CK(attr);
   const int per = 2 * RC::NP;
-  k_row_c2r<T, N, V><<<(ny + per - 1) / per, RC::THREADS, RC::SMEM, s>>>((const C*)in, (T*)out, ny,
-                                                                         pitch, rpitch, (const C*)tw);
+  const dim3 blocks((ny + per - 1) / per, nf);
+  k_row_c2r<T, N, V><<<blocks, RC::THREADS, RC::SMEM, s>>>((const C*)in, (T*)out, ny, pitch, rpitch, fs_in,
+                                                           fs_out, (const C*)tw);
   TARA_CK(cudaGetLastError());
   return TARA_OK;
 }
 
 template <typename T, int N, int V>
 static int launch_row_r2c(int ny, int rpitch, int pitch, const void* in, void* out, const void* tw,
-                          cudaStream_t s) {
+                          cudaStream_t s, int nf, size_t fs_in, size_t fs_out) {
   typedef typename cplx_of<T>::type C;
   typedef RowXCfg<T, N, V> RC;
   static cudaError_t attr = allow_smem(k_row_r2c<T, N, V>, RC::SMEM);
   TARA_CK(attr);
   const int per = 2 * RC::NP;
-  k_row_r2c<T, N, V><<<(ny + per - 1) / per, RC::THREADS, RC::SMEM, s>>>((const T*)in, (C*)out, ny,
-                                                                         rpitch, pitch, (const C*)tw);
+  const dim3 blocks((ny + per - 1) / per, nf);
+  k_row_r2c<T, N, V><<<blocks, RC::THREADS, RC::SMEM, s>>>((const T*)in, (C*)out, ny, rpitch, pitch, fs_in,
+                                                           fs_out, (const C*)tw);
   TARA_CK(cudaGetLastError());
   return TARA_OK;
 }
@@ -113,13 +115,13 @@ static int launch_row_r2c(int ny, int rpitch, int pitch, const void* in, void* o
 constexpr int kFewCtas = 152;
 
 template <typename T, int N>
-static bool small_col(int nh) {
-  return (nh + ColCfg<T, N>::TCC - 1) / ColCfg<T, N>::TCC < kFewCtas;
+static bool small_col(int nh, int nf) {
+  return nf * ((nh + ColCfg<T, N>::TCC - 1) / ColCfg<T, N>::TCC) < kFewCtas;
 }
 
 template <typename T, int N>
-static bool small_row(int ny) {
-  return (ny + 2 * RowXCfg<T, N, 0>::NP - 1) / (2 * RowXCfg<T, N, 0>::NP) < kFewCtas;
+static bool small_row(int ny, int nf) {
+  return nf * ((ny + 2 * RowXCfg<T, N, 0>::NP - 1) / (2 * RowXCfg<T, N, 0>::NP)) < kFewCtas;
 }
 
 template <typename T>
@@ -164,34 +166,34 @@ int Launch2D<T>::col_forward(int ny, int nh, const void* nl, const StepBufs& sb,
 
 template <typename T>
 int Launch2D<T>::col_fft(int ny, int nh, int pitch, const void* in, void* out, bool inverse,
-                         const void* twy, cudaStream_t s) {
+                         const void* twy, cudaStream_t s, int nf, size_t fs) {
   if (inverse) {
-    TARA_SWITCH_N(ny, return (small_col<T, N>(nh)
-                                  ? launch_col_fft<T, N, true, 2>(nh, pitch, in, out, twy, s)
-                                  : launch_col_fft<T, N, true, 0>(nh, pitch, in, out, twy, s)));
+    TARA_SWITCH_N(ny, return (small_col<T, N>(nh, nf)
+                                  ? launch_col_fft<T, N, true, 2>(nh, pitch, in, out, twy, s, nf, fs)
+                                  : launch_col_fft<T, N, true, 0>(nh, pitch, in, out, twy, s, nf, fs)));
   } else {
-    TARA_SWITCH_N(ny, return (small_col<T, N>(nh)
-                                  ? launch_col_fft<T, N, false, 2>(nh, pitch, in, out, twy, s)
-                                  : launch_col_fft<T, N, false, 0>(nh, pitch, in, out, twy, s)));
+    TARA_SWITCH_N(ny, return (small_col<T, N>(nh, nf)
+                                  ? launch_col_fft<T, N, false, 2>(nh, pitch, in, out, twy, s, nf, fs)
+                                  : launch_col_fft<T, N, false, 0>(nh, pitch, in, out, twy, s, nf, fs)));
   }
   return TARA_OK;
 }
 
 template <typename T>
 int Launch2D<T>::row_c2r(int nx, int ny, int pitch, int rpitch, const void* in, void* out,
-                         const void* twx, cudaStream_t s) {
-  TARA_SWITCH_N(nx, return (small_row<T, N>(ny)
-                                ? launch_row_c2r<T, N, 2>(ny, pitch, rpitch, in, out, twx, s)
-                                : launch_row_c2r<T, N, 0>(ny, pitch, rpitch, in, out, twx, s)));
+                         const void* twx, cudaStream_t s, int nf, size_t fs_in, size_t fs_out) {
+  TARA_SWITCH_N(nx, return (small_row<T, N>(ny, nf)
+                                ? launch_row_c2r<T, N, 2>(ny, pitch, rpitch, in, out, twx, s, nf, fs_in, fs_out)
+                                : launch_row_c2r<T, N, 0>(ny, pitch, rpitch, in, out, twx, s, nf, fs_in, fs_out)));
   return TARA_OK;
 }
 
 template <typename T>
 int Launch2D<T>::row_r2c(int nx, int ny, int rpitch, int pitch, const void* in, void* out,
-                         const void* twx, cudaStream_t s) {
-  TARA_SWITCH_N(nx, return (small_row<T, N>(ny)
-                                ? launch_row_r2c<T, N, 2>(ny, rpitch, pitch, in, out, twx, s)
-                                : launch_row_r2c<T, N, 0>(ny, rpitch, pitch, in, out, twx, s)));
+                         const void* twx, cudaStream_t s, int nf, size_t fs_in, size_t fs_out) {
+  TARA_SWITCH_N(nx, return (small_row<T, N>(ny, nf)
+                                ? launch_row_r2c<T, N, 2>(ny, rpitch, pitch, in, out, twx, s, nf, fs_in, fs_out)
+                                : launch_row_r2c<T, N, 0>(ny, rpitch, pitch, in, out, twx, s, nf, fs_in, fs_out)));
   return TARA_OK;
 }
 

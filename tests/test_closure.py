@@ -123,3 +123,69 @@ def test_closure_steps_match_oracle(oracle):
         assert rel_l2(got[k] - w, w1 - w) < 1e-5, k
         assert np.linalg.norm(F) > 0.02 * np.linalg.norm(k1)  # the closure term is not negligible
         w = got[k]
+
+
+def test_features_match_numpy():
+    n = 64
+    with tg.Solver2D(n, scheme=tg.SCHEME_RK4, nu=1e-3, dt=1e-3) as s:
+        s.init_random(6.0, 0.5, 83)
+        w = s.get_state()
+        out = torch.empty((n, n, 6), dtype=torch.float32, device="cuda")
+        sc = np.array([1.0, 0.5, 0.25, 2.0, 3.0, 4.0])
+        torch.cuda.synchronize()
+        s.features(0, 6, out.data_ptr(), sc)
+        got = out.cpu().numpy()
+    ky = np.fft.fftfreq(n, 1.0 / n)[:, None]
+    kx = np.arange(n // 2 + 1)[None, :]
+    k2 = (kx * kx + ky * ky).astype(float)
+    inv = np.where(k2 > 0, 1.0 / np.where(k2 > 0, k2, 1.0), 0.0)
+    psi = w * inv
+    nyq = np.zeros(w.shape, bool)
+    nyq[n // 2, :] = True
+    nyq[:, n // 2] = True
+    specs = [w, 1j * kx * w, 1j * ky * w, -kx * ky * psi, -ky * ky * psi, kx * kx * psi]
+    specs = [specs[0]] + [np.where(nyq, 0.0, sp) for sp in specs[1:]]  # odd derivatives: no Nyquist
+    for c, sp in enumerate(specs):
+        ref = sc[c] * _real(sp, n)
+        assert rel_l2(got[..., c], ref) < 1e-6, c
+
+
+def _d4(a, g):
+    """Symmetry g (bit 0 x-flip, bit 1 y-flip, bit 2 transpose) of a real vorticity
+    field on a (y, x) grid: w' = -w at the reflected point for each reflection."""
+    if g & 1:
+        a = -a[:, ::-1]
+    if g & 2:
+        a = -a[::-1, :]
+    if g & 4:
+        a = -a.T
+    return np.ascontiguousarray(a)
+
+
+def test_augment_equals_filtered_transformed_field():
+    """Symmetry g of (features, flux) of a filtered field equals the features
+    and flux of the filtered transformed fine field."""
+    n, f = 64, 4
+    nc = n // f
+    with tg.Solver2D(n, scheme=tg.SCHEME_RK4, nu=1e-3, dt=1e-3) as fine, \
+            tg.Solver2D(nc, scheme=tg.SCHEME_RK4, nu=1e-3, dt=1e-3) as coarse:
+        fine.init_random(5.0, 0.5, 84)
+        wf = _real(fine.get_state(), n)
+        X = torch.empty((8, nc, nc, 6), dtype=torch.float32, device="cuda")
+        T = torch.empty((8, nc, nc, 2), dtype=torch.float32, device="cuda")
+        wb = torch.empty((nc, nc), dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        for g in range(8):
+            src = torch.from_numpy(_d4(wf, g)).cuda()
+            torch.cuda.synchronize()
+            fine.set_state_real_device(0, src.data_ptr())
+            fine.filter(0, f, 0, T[g].data_ptr(), wb.data_ptr())
+            coarse.set_state_real_device(0, wb.data_ptr())
+            coarse.features(0, 6, X[g].data_ptr())
+        Xa = torch.empty((8, nc, nc, 6), dtype=torch.float32, device="cuda")
+        Ta = torch.empty((8, nc, nc, 2), dtype=torch.float32, device="cuda")
+        torch.cuda.synchronize()
+        tg.closure_augment(X[0:1].data_ptr(), T[0:1].data_ptr(), 1, nc, 6, Xa.data_ptr(), Ta.data_ptr())
+        for g in range(8):
+            assert rel_l2(Xa[g].cpu().numpy(), X[g].cpu().numpy()) < 1e-5, g
+            assert rel_l2(Ta[g].cpu().numpy(), T[g].cpu().numpy()) < 1e-5, g
