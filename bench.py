@@ -307,7 +307,7 @@ def timed_on_stream(stream_ptr: int, fn):
 
 
 def run_ensemble(args) -> None:
-    """Config 4: 384 independent 2D runs (128 each at 128^2, 256^2, 512^2), RK4,
+    """Ensemble of 384 independent 2D runs (128 each at 128^2, 256^2, 512^2), RK4,
     nu = 1e-3, dt = 1e-4, FP32 transforms and products with FP64 state,
     k0 ~ U[4,10] (numpy default_rng(4000)), seed 4000 + r.  One CUDA-graph launch
     per ensemble step; tile variants picked by the autotuner first."""
@@ -331,7 +331,7 @@ def run_ensemble(args) -> None:
             "value": pts * args.steps / (ms * 1e-3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
             "dtype": "f32 transforms / f64 state", "data": "synthetic (seeded random-phase spectra)",
-            "config": {"workload": "config 4 ensemble", "graph": "one cudaGraphLaunch per step",
+            "config": {"workload": "ensemble of uneven runs", "graph": "one cudaGraphLaunch per step",
                        "l2": "working set > L2 (no flush)"},
             "gpu_launches": e.launches_per_step * args.steps, "autotune": e.groups()}
     if args.ens_error_steps:
@@ -354,7 +354,7 @@ def run_ensemble(args) -> None:
 
 
 def mhd3d_initial_state(n: int, seed: int = 3):
-    """Config 3 initial condition as real fields (rho, rho u, E, B): u = (-sin y,
+    """3D MHD initial condition as real fields (rho, rho u, E, B): u = (-sin y,
     sin x, 0), B = (-sin y, sin 2x, 0), rho = 1, plus a seeded 1 % random-phase
     solenoidal perturbation of u and B at |k| <= 4; E = 1 + |u|^2/2 + |B|^2/2."""
     import numpy as np
@@ -384,7 +384,7 @@ def mhd3d_initial_state(n: int, seed: int = 3):
 
 
 def run_mhd3d(args) -> None:
-    """Config 3: 128^3 compressible MHD, FP64, AB2, nu = eta = 0.01, dt = 1e-3."""
+    """128^3 compressible MHD, FP64, AB2, nu = eta = 0.01, dt = 1e-3."""
     import torch
 
     import tara_gb300 as tg
@@ -401,12 +401,47 @@ def run_mhd3d(args) -> None:
     line = {"metric": "grid-pt*steps/s at 128^3 FP64 (3D compressible MHD, AB2)",
             "value": n**3 * args.steps / (ms * 1e-3), "unit": UNIT, "n_gpus": 1,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
-            "higher_is_better": True, "dtype": "f64", "data": "synthetic (config 3 profile)",
-            "config": {"workload": "config 3: 128^3, nu=eta=0.01, dt=1e-3, AB2, 20 transforms/step"},
+            "higher_is_better": True, "dtype": "f64", "data": "synthetic (Orszag-Tang-type profile + 1% solenoidal noise)",
+            "config": {"workload": "3D MHD 128^3, nu=eta=0.01, dt=1e-3, AB2, 20 transforms/step"},
             "gpu_launches": None, "diag": {"pressure": d[0], "kinetic": d[1], "total_E": d[2],
                                            "magnetic": d[3]}}
     print(json.dumps(line), flush=True)
     s.close()
+
+
+def run_closure(args) -> None:
+    """Learned closure: training data from 1024^2 FP64 decaying-turbulence runs
+    (nu = 5e-5, k0 = 8), box-filtered (8 x 8 block means) to 128^2 with the exact
+    subgrid vorticity flux as target; 4-layer FNO, 32 channels, 16 modes per
+    axis, GELU, BF16 tensor-core GEMMs with FP32 accumulation, Adam lr 1e-3,
+    batch 32; flux amplitude calibrated on validation seeds; evaluated on
+    held-out seeds over 5 eddy-turnover times against the filtered 1024^2 plain
+    run.  The value is the closure's simulated time per wall-second over that of
+    the plain 1024^2 FP64 solver on the same GPU (one run each, CUDA events)."""
+    import torch
+
+    from tara_gb300 import closure as cl
+
+    torch.cuda.set_device(0)
+    s = cl.ClosureSetup(epochs=args.closure_epochs)
+    out = cl.run_all(s, log=lambda m: print(m, file=sys.stderr, flush=True))
+    ev, tp = out["eval"], out["throughput"]
+    line = {"metric": "closure speedup: simulated time per wall-second, 128^2 + FNO closure vs plain 1024^2 FP64",
+            "value": tp["closure_speedup"], "unit": "x", "n_gpus": 1, "steps": None, "warmup": None,
+            "ms_per_step": tp["closure_ms_per_step"], "higher_is_better": True, "vs_baseline": None,
+            "dtype": "bf16 GEMMs / f32 network / f64 state", "data": "synthetic (seeded decaying turbulence)",
+            "config": {"workload": "learned closure 1024^2 -> 128^2, 5 eddy times", "fine_dt": s.dt_fine,
+                       "coarse_dt": s.dt_coarse, "coarse_precision": "fp32 transforms" if s.coarse_precision else "fp64",
+                       "eval_runs": s.eval_runs, "samples": s.samples},
+            "spectrum_error": {"avg_spectrum_closure": ev["err_avg_closure"], "avg_spectrum_plain_coarse": ev["err_avg_plain"],
+                               "mean_per_sample_closure": ev["mean_err_closure"],
+                               "mean_per_sample_plain_coarse": ev["mean_err_plain"], "shells": ev["kmax"],
+                               "fallback": ev["fallback"]},
+            "a_priori": out["train"]["val"], "alpha": out["alpha"],
+            "calibration": {k: out["calibration"][k] for k in ("err_avg", "best", "seed")} if "calibration" in out else None,
+            "throughput": tp, "train": {k: out["train"][k] for k in ("train_steps", "wall_s", "best_epoch")},
+            "data_gen_s": out["data"]["train"]["wall_s"]}
+    print(json.dumps(line, default=str), flush=True)
 
 
 def main() -> None:
@@ -418,12 +453,13 @@ def main() -> None:
     ap.add_argument("--n", type=int, default=2048)
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="rk4-2048", choices=["rk4-2048", "ensemble", "mhd3d"],
-                    help="rk4-2048 is the headline; the others measure configs 4 and 3")
+    ap.add_argument("--workload", default="rk4-2048", choices=["rk4-2048", "ensemble", "mhd3d", "closure"],
+                    help="rk4-2048 is the headline; the others measure the ensemble, 3D MHD and the learned closure")
     ap.add_argument("--ens-runs-per-size", type=int, default=128,
-                    help="ensemble: runs of each size (config 4 uses 128)")
+                    help="ensemble: runs of each size (the 384-run ensemble uses 128)")
     ap.add_argument("--ens-error-steps", type=int, default=0,
                     help="ensemble: also report the per-run error vs FP64 after this many steps")
+    ap.add_argument("--closure-epochs", type=int, default=10, help="closure: training epochs")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -433,6 +469,8 @@ def main() -> None:
         run_ensemble(args)
     elif args.workload == "mhd3d":
         run_mhd3d(args)
+    elif args.workload == "closure":
+        run_closure(args)
     else:
         run_ours(args)
 

@@ -62,7 +62,7 @@ int make_twiddles(int n, bool fp32, void** dev);
 
 struct tara2d {
   tara2d_config cfg;
-  int batch = 1;          // runs advanced together (config 4 ensembles)
+  int batch = 1;          // runs advanced together (ensembles)
   int var[3] = {0, 0, 0};  // tile variants of the three kernels (autotuner)
   int dev = 0;
   int nx = 0, ny = 0, nh = 0, pitch = 0;
