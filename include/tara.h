@@ -309,6 +309,28 @@ int tara_fortran_read_int(const char* s, long long* out);
 /* One list-directed output record of n REAL(8) values, gfortran style. */
 int tara_fortran_list_record(const double* v, int n, char* buf, int buflen);
 
+/* ---- Lagrangian passive particles ------------------------------------------ */
+/* The plain serial driver's particles (src/main2csh.f95:93-96, 187-273): after a
+ * step, u_x = i ky psi, u_y = -i kx psi with psi = omega/(kx^2+ky^2) and the
+ * driver's wavenumbers kx = 2*kpi*i/lx (true pi, ini box) are transformed to the
+ * grid (c2r / (Nx*Ny)), interpolated bilinearly at each particle and the particle
+ * moves one Euler step, wrapped into (0, L] as the reference does.  Where the
+ * reference's last-column / last-row branches read outside ux(Nx,Ny), the
+ * neighbour wraps periodically (defined behaviour).  Positions live on the
+ * device; run 0 of the handle drives them. */
+typedef struct tara_particles tara_particles;
+int tara_particles_create(tara2d* h, double kpi, double lx, double ly, int np, const double* xp,
+                          const double* yp, tara_particles** out);
+int tara_particles_destroy(tara_particles* p);
+/* One Euler step of length dt with the current state's velocity (asynchronous,
+ * on the solver's stream; call it after tara2d_step as the reference driver does). */
+int tara_particles_advance(tara_particles* p, double dt);
+int tara_particles_get(tara_particles* p, double* xp, double* yp);
+/* The minimal-standard LCG (Park & Miller 1988, a = 16807, m = 2^31-1) that GNU
+ * Fortran documents for its RAND intrinsic, as a REAL(4) in [0,1); the driver
+ * draws the initial positions xp = rand()*Lx, yp = rand()*Ly with it (state 1). */
+float tara_park_miller_rand(uint64_t* state);
+
 /* ---- standalone transforms ------------------------------------------------ */
 /* Unnormalised 2D transforms with FFTW's rank-2 r2c/c2r semantics, i.e. what
  * dfftw_plan_dft_{r2c,c2r}_2d(plan, Nx, Ny, ...) computes in the reference

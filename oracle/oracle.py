@@ -82,6 +82,9 @@ class Oracle:
         L.oracle_ab3com.argtypes = [c_int, c_int, c_int, c_double, vp, vp, vp, vp]
         L.oracle_run3d.argtypes = [c_int, c_int, c_int, vp, c_double, c_int, vp, vp]
         L.oracle_ic3d_abc.argtypes = [c_int, c_int, c_int, c_double, c_double, c_double, vp]
+        L.oracle_driver_velocity.argtypes = [c_int, c_int, c_double, c_double, vp, vp, vp]
+        L.oracle_particles_step.argtypes = [c_int, c_int, c_double, c_double, vp, vp, c_int, vp, vp,
+                                            c_double]
         self.is_fftw = bool(L.oracle_backend_is_fftw())
 
     def set_threads(self, n: int) -> None:
@@ -175,6 +178,23 @@ class Oracle:
         out = np.zeros(6)
         self.L.oracle_diag_css(2 * (nh - 1), ny, lx, ly, lam, w.ctypes.data, out.ctypes.data)
         return out
+
+    # Lagrangian particles of the plain driver
+    def driver_velocity(self, w, lx, ly):
+        w = np.ascontiguousarray(w, np.complex128)
+        ny, nh = w.shape
+        nx = 2 * (nh - 1)
+        ux, uy = np.zeros((ny, nx)), np.zeros((ny, nx))
+        self.L.oracle_driver_velocity(nx, ny, lx, ly, w.ctypes.data, ux.ctypes.data, uy.ctypes.data)
+        return ux, uy
+
+    def particles_step(self, ux, uy, xp, yp, lx, ly, dt):
+        ux, uy = np.ascontiguousarray(ux, np.float64), np.ascontiguousarray(uy, np.float64)
+        xp, yp = np.array(xp, np.float64), np.array(yp, np.float64)
+        ny, nx = ux.shape
+        self.L.oracle_particles_step(nx, ny, lx, ly, ux.ctypes.data, uy.ctypes.data, xp.size,
+                                     xp.ctypes.data, yp.ctypes.data, dt)
+        return xp, yp
 
     # 3D MHD: arrays are (Nz, Ny, Nh) complex / (Nz, Ny, Nx) real; a state is (8, Nz, Ny, Nh)
     def r2c3(self, x):

@@ -848,6 +848,68 @@ static double k3_of(int i0, int n, double pi, double l, int signed_) {
   return 2.0 * pi * (double)(i0 - n) / l;
 }
 
+/* src/main2csh.f95:128-172 */
+void oracle_driver_velocity(int nx, int ny, double lx, double ly, const double* omegak, double* ux,
+                            double* uy) {
+  const double pi = 3.14159265358979323846;
+  const int nh = nx / 2 + 1;
+  double* a = (double*)calloc((size_t)2 * nh * ny, sizeof(double));
+  double* b = (double*)calloc((size_t)2 * nh * ny, sizeof(double));
+  for (int i = 0; i < nh; ++i) {
+    const double kx = 2.0 * pi * (double)i / lx;
+    for (int j = 0; j < ny; ++j) {
+      const double ky = j < ny / 2 ? 2.0 * pi * (double)j / ly : 2.0 * pi * ((double)j - ny) / ly;
+      const size_t q = (size_t)j * nh + i;
+      if (i == 0 && j == 0) continue;
+      const double k2 = kx * kx + ky * ky;
+      const double pr = omegak[2 * q] / k2, pim = omegak[2 * q + 1] / k2;
+      a[2 * q] = -ky * pim;  /* (0,1)*ky*psik */
+      a[2 * q + 1] = ky * pr;
+      b[2 * q] = kx * pim;   /* -(0,1)*kx*psik */
+      b[2 * q + 1] = -(kx * pr);
+    }
+  }
+  oracle_c2r_2d(nx, ny, a, ux);
+  oracle_c2r_2d(nx, ny, b, uy);
+  const double nn = (double)(nx * ny);
+  for (size_t t = 0; t < (size_t)nx * ny; ++t) {
+    ux[t] = ux[t] / nn;
+    uy[t] = uy[t] / nn;
+  }
+  free(a);
+  free(b);
+}
+
+/* src/main2csh.f95:187-271 (defined periodic neighbours at the last column/row) */
+void oracle_particles_step(int nx, int ny, double lx, double ly, const double* ux, const double* uy,
+                           int np, double* xp, double* yp, double dt) {
+  const double dx = lx / (double)nx, dy = ly / (double)ny;
+  const double h = 1.0 / (dx * dy);
+  for (int i = 0; i < np; ++i) {
+    const double x = xp[i], y = yp[i];
+    int m = (int)(x / dx), n = (int)(y / dy); /* aint, 0-based */
+    if (m > nx - 1) m = nx - 1;
+    if (n > ny - 1) n = ny - 1;
+    const int m1 = m + 1 < nx ? m + 1 : 0, n1 = n + 1 < ny ? n + 1 : 0;
+    const double xm = (double)m * dx, xm1 = m + 1 < nx ? (double)(m + 1) * dx : lx;
+    const double yn = (double)n * dy, yn1 = n + 1 < ny ? (double)(n + 1) * dy : ly;
+    const double* f[2] = {ux, uy};
+    double v[2];
+    for (int c = 0; c < 2; ++c) {
+      const double* u = f[c];
+      v[c] = u[(size_t)n * nx + m] * (xm1 - x) * (yn1 - y) * h + u[(size_t)n * nx + m1] * (x - xm) * (yn1 - y) * h +
+             u[(size_t)n1 * nx + m] * (xm1 - x) * (y - yn) * h + u[(size_t)n1 * nx + m1] * (x - xm) * (y - yn) * h;
+    }
+    double a = x + v[0] * dt, b = y + v[1] * dt;
+    a = a - (double)(int)(a / lx) * lx;
+    if (a <= 0.0) a = a + lx;
+    b = b - (double)(int)(b / ly) * ly;
+    if (b <= 0.0) b = b + ly;
+    xp[i] = a;
+    yp[i] = b;
+  }
+}
+
 void oracle_derive3com(int nx, int ny, int nz, const oracle_mhd_params* p, const double* state,
                        double* dstate) {
   const int nh = nx / 2 + 1;

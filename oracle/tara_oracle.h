@@ -92,6 +92,19 @@ void oracle_energy_enstrophy(int nx, int ny, double lx, double ly, const double*
 void oracle_diag_css(int nx, int ny, double lx, double ly, double lambda, const double* omegak,
                      double* out);
 
+/* Velocity of the plain driver on the grid (src/main2csh.f95:128-172): psi =
+ * omegak/(kx^2+ky^2) (0 at the origin), ux = c2r(i ky psi)/(Nx*Ny), uy =
+ * c2r(-i kx psi)/(Nx*Ny), kx = 2*pi*i/lx with the true pi (lx, ly true lengths).
+ * ux, uy are (Ny, Nx) real arrays, x fastest. */
+void oracle_driver_velocity(int nx, int ny, double lx, double ly, const double* omegak, double* ux,
+                            double* uy);
+
+/* One Euler step of np particles with bilinear interpolation of ux, uy
+ * (src/main2csh.f95:187-271); the last column / row take the periodic neighbour
+ * (the reference reads outside its arrays there). */
+void oracle_particles_step(int nx, int ny, double lx, double ly, const double* ux, const double* uy,
+                           int np, double* xp, double* yp, double dt);
+
 /* ---- 3D compressible MHD (src/derive3com.f95, src/ab3com.f95) ---------- */
 /* Half spectra are (Nh,Ny,Nz) complex(8), x fastest; real fields (Nx,Ny,Nz).
  * The state is 8 consecutive half spectra in the order of the reference's

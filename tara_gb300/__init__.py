@@ -8,6 +8,7 @@ calling it without a GPU, raises.
 from __future__ import annotations
 
 import ctypes
+import math
 import os
 from pathlib import Path
 
@@ -186,6 +187,12 @@ def _declare(L: ctypes.CDLL) -> None:
     L.tara_fno_stream.argtypes = [vp]
     L.tara_fno_stream.restype = vp
     L.tara2d_filter.argtypes = [vp, c_int, c_int, vp, vp, vp]
+    L.tara_particles_create.argtypes = [vp, c_double, c_double, c_double, c_int, dp, dp, ctypes.POINTER(vp)]
+    L.tara_particles_destroy.argtypes = [vp]
+    L.tara_particles_advance.argtypes = [vp, c_double]
+    L.tara_particles_get.argtypes = [vp, dp, dp]
+    L.tara_park_miller_rand.argtypes = [ctypes.POINTER(ctypes.c_uint64)]
+    L.tara_park_miller_rand.restype = ctypes.c_float
     L.tara2d_autotune.argtypes = [vp, c_int, ip, dp]
     L.tara2d_set_variants.argtypes = [vp, ip]
     L.tara2d_set_state_real_device.argtypes = [vp, c_int, vp]
@@ -781,3 +788,54 @@ class Closure:
 
     def step(self, n: int = 1) -> None:
         _check(lib().tara_closure_step(self._h, int(n)))
+
+
+# ---------------------------------------------------------------------------
+# Lagrangian passive particles (plain driver)
+# ---------------------------------------------------------------------------
+class Particles:
+    """tara_particles: passive particles moved by a Solver2D's velocity (run 0)
+    with the plain driver's interpolation, Euler step and wrap."""
+
+    def __init__(self, solver: Solver2D, xp, yp, lx: float, ly: float, kpi: float = math.pi):
+        xp = np.ascontiguousarray(xp, np.float64)
+        yp = np.ascontiguousarray(yp, np.float64)
+        if xp.shape != yp.shape or xp.ndim != 1:
+            raise ValueError("xp and yp must be 1-D arrays of equal length")
+        h = ctypes.c_void_p()
+        _check(lib().tara_particles_create(solver._h, kpi, lx, ly, xp.size, _dp(xp), _dp(yp), ctypes.byref(h)))
+        self._h = h
+        self.np = xp.size
+        self.solver = solver
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().tara_particles_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def advance(self, dt: float) -> None:
+        _check(lib().tara_particles_advance(self._h, dt))
+
+    def positions(self):
+        x, y = np.zeros(self.np), np.zeros(self.np)
+        _check(lib().tara_particles_get(self._h, _dp(x), _dp(y)))
+        return x, y
+
+
+def park_miller(n: int, state: int = 1):
+    """n draws of the driver's RAND generator (minimal-standard LCG) and the final state."""
+    st = ctypes.c_uint64(state)
+    out = np.array([lib().tara_park_miller_rand(ctypes.byref(st)) for _ in range(n)], np.float32)
+    return out, st.value

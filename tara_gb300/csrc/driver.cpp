@@ -104,7 +104,6 @@ int run_2d(Reader& R, const std::string& out, int max_steps, bool screened) {
   R.d("initialProfile", "m0", m0);
   R.d("initialProfile", "d", d);
   if (!R.ok) return set_error(TARA_ERR_INI, R.err);
-  (void)np;  // Lagrangian particles (src/main2csh.f95:187-273) are not part of this build
   lx = lx * kPi;
   ly = ly * kPi;
   const double dx = lx / (double)nx, dy = ly / (double)ny;
@@ -163,6 +162,24 @@ int run_2d(Reader& R, const std::string& out, int max_steps, bool screened) {
         f10.rec({xs[i], ys[j], om[r], psi[r], ux[r], uy[r]});
       }
   }
+  // Lagrangian particles of the plain driver (src/main2csh.f95:93-96, 187-273);
+  // the screened driver reads Np but moves none
+  tara_particles* parts = nullptr;
+  struct PGuard {
+    tara_particles** p;
+    ~PGuard() { tara_particles_destroy(*p); }
+  } pguard{&parts};
+  std::vector<double> xp, yp;
+  if (!screened && np > 0) {
+    xp.resize(np);
+    yp.resize(np);
+    uint64_t state = 1;
+    for (int i = 0; i < np; ++i) {
+      xp[i] = (double)tara_park_miller_rand(&state) * lx;  // xp(i) = rand()*Lx
+      yp[i] = (double)tara_park_miller_rand(&state) * ly;
+    }
+    if (tara_particles_create(h, kPi, lx, ly, np, xp.data(), yp.data(), &parts)) return fail_rc();
+  }
   Out energy(out + "/Energy.dat");  // written every step by the screened driver only
   const tara2d_diag_params dp = {kPi, lx, ly, screened ? lambda : 0.0, screened ? 1 : 0};
   const long n = trip_count(tmin, tmax, dt);
@@ -186,14 +203,24 @@ int run_2d(Reader& R, const std::string& out, int max_steps, bool screened) {
           }
       }
       energy.rec({time, usq, y_energy});
-    } else if (t % every == 0) {
-      if (tara2d_real_fields(h, &dp, nullptr, om.data(), ux.data(), uy.data())) return fail_rc();
-      Out snap(fort_name(out, t + 100));
-      for (int i = 0; i < nx; ++i)
-        for (int j = 0; j < ny; ++j) {
-          const size_t r = (size_t)j * nx + i;
-          snap.rec({xs[i], ys[j], om[r], ux[r], uy[r]});
+    } else {
+      if (t % every == 0) {
+        if (tara2d_real_fields(h, &dp, nullptr, om.data(), ux.data(), uy.data())) return fail_rc();
+        Out snap(fort_name(out, t + 100));
+        for (int i = 0; i < nx; ++i)
+          for (int j = 0; j < ny; ++j) {
+            const size_t r = (size_t)j * nx + i;
+            snap.rec({xs[i], ys[j], om[r], ux[r], uy[r]});
+          }
+      }
+      if (parts) {
+        if (tara_particles_advance(parts, dt)) return fail_rc();
+        if (t % every == 0) {  // fort.(t+105): one "xp yp" record per particle
+          if (tara_particles_get(parts, xp.data(), yp.data())) return fail_rc();
+          Out pf(fort_name(out, t + 105));
+          for (int i = 0; i < np; ++i) pf.rec({xp[i], yp[i]});
         }
+      }
     }
     time = time + dt;
   }

@@ -117,6 +117,14 @@ def test_plain_driver_matches_oracle(tmp_path, oracle):
     assert np.abs(snap[:, 2:] - ref).max() < 1e-10 * np.abs(ref).max()
     x = np.arange(64) * (2 * PI / 64)
     assert np.allclose(snap[::64, 0], x, atol=1e-14)
+    # Lagrangian particles (Np = 10): positions after the first step in fort.(0+105)
+    r, _ = tg.park_miller(20)
+    xp, yp = r[0::2].astype(np.float64) * (2 * PI), r[1::2].astype(np.float64) * (2 * PI)
+    vx, vy = oracle.driver_velocity(w, 2 * PI, 2 * PI)
+    xp, yp = oracle.particles_step(vx, vy, xp, yp, 2 * PI, 2 * PI, 1e-4)
+    parts = rows(out / "fort.00000105")
+    assert parts.shape == (10, 2)
+    assert np.abs(parts - np.stack([xp, yp], axis=1)).max() < 1e-12
 
 
 INI3D = """[dimension]
