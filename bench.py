@@ -199,6 +199,7 @@ def run_ours(args) -> None:
     n = args.n
     s = tg.Solver2D(n, scheme=tg.SCHEME_RK4, nu=NU, dt=DT)
     s.init_random(K0, ENERGY, SEED.get(n, 1))
+    tuned = s.autotune(2)  # tile variant per kernel (the state is restored)
     s.step(args.warmup)
     s.synchronize()
 
@@ -285,6 +286,7 @@ def run_ours(args) -> None:
                      "fp64_pipe_busy_pct_ncu": from_profiles("fp64_pipe_busy_pct", dom, n),
                      "per_kernel_ms": {k: v["ms"] / max(1, v["launches"]) for k, v in ks.items()}},
         "clocks": clocks,
+        "tile_variants": tuned["variants"],
         "diag": {"energy": e, "enstrophy": z},
         "cpu_baseline": cpu,
     }
@@ -444,6 +446,74 @@ def run_closure(args) -> None:
     print(json.dumps(line, default=str), flush=True)
 
 
+def run_fno_train(args) -> None:
+    """Training step of the closure network: 128^2, 6 input channels, 4 Fourier
+    layers, 32 channels, 16 modes per axis, projection 128, batch 32, BF16
+    tensor-core GEMMs with FP32 accumulation, Adam (lr 1e-4) on seeded random
+    data; CUDA events on the network's stream."""
+    import torch
+
+    import tara_gb300 as tg
+
+    torch.cuda.set_device(0)
+    B = 32
+    net = tg.FNO(tg.fno_default_config(ci=6, max_batch=B))
+    g = torch.Generator(device="cuda").manual_seed(7)
+    x = torch.randn(B, 128, 128, 6, device="cuda", generator=g)
+    t = torch.randn(B, 128, 128, 2, device="cuda", generator=g)
+    torch.cuda.synchronize()
+    for _ in range(args.warmup):
+        net.train_step(x.data_ptr(), t.data_ptr(), B, lr=1e-4, want_loss=False)
+
+    def steps():
+        for _ in range(args.steps):
+            net.train_step(x.data_ptr(), t.data_ptr(), B, lr=1e-4, want_loss=False)
+
+    ms = timed_on_stream(net.stream, steps)
+    line = {"metric": "closure-network training samples/s (128^2, 6->32 ch, 4 layers, 16 modes, batch 32)",
+            "value": B * args.steps / (ms * 1e-3), "unit": "samples/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "vs_baseline": None, "dtype": "bf16 GEMM operands / f32 accumulation and activations",
+            "data": "synthetic (seeded normal inputs and targets)",
+            "config": {"workload": "FNO train step", "batch": B, "params": net.num_params}}
+    print(json.dumps(line), flush=True)
+    net.close()
+
+
+def run_closure_step(args) -> None:
+    """One coarse closure step at 128^2: the 6 feature channels of the state,
+    the FNO forward (batch 1), the flux divergence and an RK4 step of the
+    FP32-form solver (dt 4e-3, nu 5e-5), replayed as one CUDA graph; CUDA
+    events on the solver's stream.  Random-initialised network (the cost does
+    not depend on the weights)."""
+    import numpy as np
+    import torch
+
+    import tara_gb300 as tg
+
+    torch.cuda.set_device(0)
+    s = tg.Solver2D(128, scheme=tg.SCHEME_RK4, precision=tg.PREC_FP32, nu=5e-5, dt=4e-3,
+                    kpi=np.pi, lx=2 * np.pi, ly=2 * np.pi)
+    s.init_random(8.0, 0.5, 9000)
+    s.autotune(2)
+    net = tg.FNO(tg.fno_default_config(ci=6, max_batch=1))
+    c = tg.Closure(s, net, np.full(6, 0.05), 0.01)
+    c.step(args.warmup)
+    s.synchronize()
+    ms = timed_on_stream(s.stream, lambda: c.step(args.steps))
+    s.synchronize()
+    line = {"metric": "closure steps/s (128^2 FP32-form RK4 + FNO subgrid flux, one run)",
+            "value": args.steps / (ms * 1e-3), "unit": "steps/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+            "vs_baseline": None, "dtype": "bf16 GEMMs / f32 network / f64 state",
+            "data": "synthetic (seeded random-phase state, random network)",
+            "config": {"workload": "closure step", "graph": "one cudaGraphLaunch per step"}}
+    print(json.dumps(line), flush=True)
+    c.close()
+    net.close()
+    s.close()
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -453,7 +523,8 @@ def main() -> None:
     ap.add_argument("--n", type=int, default=2048)
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", default="rk4-2048", choices=["rk4-2048", "ensemble", "mhd3d", "closure"],
+    ap.add_argument("--workload", default="rk4-2048",
+                    choices=["rk4-2048", "ensemble", "mhd3d", "closure", "fno-train", "closure-step"],
                     help="rk4-2048 is the headline; the others measure the ensemble, 3D MHD and the learned closure")
     ap.add_argument("--ens-runs-per-size", type=int, default=128,
                     help="ensemble: runs of each size (the 384-run ensemble uses 128)")
@@ -471,6 +542,10 @@ def main() -> None:
         run_mhd3d(args)
     elif args.workload == "closure":
         run_closure(args)
+    elif args.workload == "fno-train":
+        run_fno_train(args)
+    elif args.workload == "closure-step":
+        run_closure_step(args)
     else:
         run_ours(args)
 

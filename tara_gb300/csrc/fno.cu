@@ -181,6 +181,218 @@ __global__ void __launch_bounds__(256) k_gemm_fp32(GemmArgs g) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// Tall-skinny tensor-core GEMMs of the channel mixing (BF16 mode): the rows are
+// the B*H*W grid points and stream through; the small weight matrix (K, N in
+// {32, 128}) stays in shared memory as BF16.  Operand tiles are loaded with
+// float4 reads, rounded to BF16 in shared memory (rows padded by 8 BF16 so the
+// fragment loads are conflict-free), multiplied with mma.sync.m16n8k16 into
+// FP32 accumulators.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void mma_bf16_16816(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 "
+      "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+__device__ __forceinline__ uint32_t lds32(const __nv_bfloat16* p) { return *reinterpret_cast<const uint32_t*>(p); }
+
+constexpr int kTsRows = 128;  // rows per tile: 8 warps x 16
+
+// C[r, n] (+)= sum_k A[r, k] B(k, n) (+ bias[n]) for r < M; B(k, n) = Bw[k*N + n],
+// or Bw[n*K + k] with transB.  act: a second output at C's offsets
+// (act_mode 1: GELU, 2: copy).  Persistent CTAs loop over 128-row tiles.
+template <int K, int N>
+__global__ void __launch_bounds__(256) k_ts_gemm(const float* __restrict__ A, long long M,
+                                                 const float* __restrict__ Bw, int transB,
+                                                 const float* __restrict__ bias, float* C, int accumulate,
+                                                 float* act, int act_mode) {
+  constexpr int KP = K + 8, NT = N / 8;
+  __shared__ __align__(16) __nv_bfloat16 Bs[N * KP];
+  __shared__ __align__(16) __nv_bfloat16 As[kTsRows * KP];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, gid = lane >> 2, tig = lane & 3;
+  for (int e = tid; e < K * N; e += 256) {
+    const int k = transB ? e % K : e / N, n = transB ? e / K : e % N;
+    Bs[n * KP + k] = __float2bfloat16_rn(Bw[e]);
+  }
+  const long long tiles = (M + kTsRows - 1) / kTsRows;
+  const int ra = warp * 16 + gid;
+  for (long long tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    const long long r0 = tile * kTsRows;
+    __syncthreads();  // Bs written / previous tile's As consumed
+    for (int e = tid; e < kTsRows * K / 4; e += 256) {
+      const int r = e / (K / 4), k4 = (e % (K / 4)) * 4;
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (r0 + r < M) v = *reinterpret_cast<const float4*>(A + (r0 + r) * K + k4);
+      *reinterpret_cast<__nv_bfloat162*>(&As[r * KP + k4]) = __floats2bfloat162_rn(v.x, v.y);
+      *reinterpret_cast<__nv_bfloat162*>(&As[r * KP + k4 + 2]) = __floats2bfloat162_rn(v.z, v.w);
+    }
+    __syncthreads();
+    float acc[NT][4];
+#pragma unroll
+    for (int nt = 0; nt < NT; ++nt)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) acc[nt][q] = 0.f;
+#pragma unroll
+    for (int ks = 0; ks < K; ks += 16) {
+      uint32_t a[4];
+      a[0] = lds32(&As[ra * KP + ks + 2 * tig]);
+      a[1] = lds32(&As[(ra + 8) * KP + ks + 2 * tig]);
+      a[2] = lds32(&As[ra * KP + ks + 2 * tig + 8]);
+      a[3] = lds32(&As[(ra + 8) * KP + ks + 2 * tig + 8]);
+#pragma unroll
+      for (int nt = 0; nt < NT; ++nt) {
+        const __nv_bfloat16* b = &Bs[(nt * 8 + gid) * KP + ks + 2 * tig];
+        mma_bf16_16816(acc[nt], a, lds32(b), lds32(b + 8));
+      }
+    }
+#pragma unroll
+    for (int nt = 0; nt < NT; ++nt)
+#pragma unroll
+      for (int hh = 0; hh < 2; ++hh) {
+        const long long r = r0 + ra + 8 * hh;
+        if (r >= M) continue;
+        const int n = nt * 8 + 2 * tig;
+        float2 v = make_float2(acc[nt][2 * hh], acc[nt][2 * hh + 1]);
+        if (bias) {
+          v.x += bias[n];
+          v.y += bias[n + 1];
+        }
+        float2* pc = reinterpret_cast<float2*>(C + r * N + n);
+        if (accumulate) {
+          const float2 o = *pc;
+          v.x += o.x;
+          v.y += o.y;
+        }
+        *pc = v;
+        if (act)
+          *reinterpret_cast<float2*>(act + r * N + n) =
+              act_mode == 1 ? make_float2(gelu(v.x), gelu(v.y)) : v;
+      }
+  }
+}
+
+// Weight gradient dW(k, n) = sum_r A[r, k] B[r, n] over the rows of this CTA's
+// chunk, as a partial sum into part[blockIdx.x] (K x N), and with bias_part the
+// FP32 column sums of B (the bias gradient) into bias_part[blockIdx.x] (N).
+// Sub-tiles of 64 rows are staged transposed (rows contiguous) so that the row
+// index is the MMA reduction dimension.
+template <int K, int N>
+__global__ void __launch_bounds__(256) k_ts_wgrad(const float* __restrict__ A, const float* __restrict__ B,
+                                                  long long M, long long rows_per_cta, float* __restrict__ part,
+                                                  float* __restrict__ bias_part) {
+  constexpr int RT = 64, RP = RT + 8;
+  constexpr int TM = K / 16, TN = N / 8, TPW = TM * TN / 8;  // output tiles per warp
+  static_assert(TM * TN % 8 == 0 && 256 % (N / 4) == 0, "tile split");
+  __shared__ __align__(16) __nv_bfloat16 At[K * RP];
+  __shared__ __align__(16) __nv_bfloat16 Bt[N * RP];
+  __shared__ float bsum[N];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31, gid = lane >> 2, tig = lane & 3;
+  const long long rb = (long long)blockIdx.x * rows_per_cta;
+  const long long re = rb + rows_per_cta < M ? rb + rows_per_cta : M;
+  float acc[TPW][4];
+#pragma unroll
+  for (int t = 0; t < TPW; ++t)
+#pragma unroll
+    for (int q = 0; q < 4; ++q) acc[t][q] = 0.f;
+  float bs[4] = {0.f, 0.f, 0.f, 0.f};  // this thread's column sums (fixed columns)
+  for (int e = tid; e < N; e += 256) bsum[e] = 0.f;
+  for (long long r0 = rb; r0 < re; r0 += RT) {
+    __syncthreads();
+    for (int e = tid; e < RT * K / 4; e += 256) {
+      const int r = e / (K / 4), k4 = (e % (K / 4)) * 4;
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (r0 + r < re) v = *reinterpret_cast<const float4*>(A + (r0 + r) * K + k4);
+      At[(k4 + 0) * RP + r] = __float2bfloat16_rn(v.x);
+      At[(k4 + 1) * RP + r] = __float2bfloat16_rn(v.y);
+      At[(k4 + 2) * RP + r] = __float2bfloat16_rn(v.z);
+      At[(k4 + 3) * RP + r] = __float2bfloat16_rn(v.w);
+    }
+    for (int e = tid; e < RT * N / 4; e += 256) {
+      const int r = e / (N / 4), n4 = (e % (N / 4)) * 4;
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (r0 + r < re) v = *reinterpret_cast<const float4*>(B + (r0 + r) * N + n4);
+      bs[0] += v.x;
+      bs[1] += v.y;
+      bs[2] += v.z;
+      bs[3] += v.w;
+      Bt[(n4 + 0) * RP + r] = __float2bfloat16_rn(v.x);
+      Bt[(n4 + 1) * RP + r] = __float2bfloat16_rn(v.y);
+      Bt[(n4 + 2) * RP + r] = __float2bfloat16_rn(v.z);
+      Bt[(n4 + 3) * RP + r] = __float2bfloat16_rn(v.w);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < RT; kk += 16) {
+#pragma unroll
+      for (int t = 0; t < TPW; ++t) {
+        const int tile = warp * TPW + t, tm = tile / TN, tn = tile % TN;
+        uint32_t a[4];
+        const int ma = tm * 16 + gid;
+        a[0] = lds32(&At[ma * RP + kk + 2 * tig]);
+        a[1] = lds32(&At[(ma + 8) * RP + kk + 2 * tig]);
+        a[2] = lds32(&At[ma * RP + kk + 2 * tig + 8]);
+        a[3] = lds32(&At[(ma + 8) * RP + kk + 2 * tig + 8]);
+        const __nv_bfloat16* b = &Bt[(tn * 8 + gid) * RP + kk + 2 * tig];
+        mma_bf16_16816(acc[t], a, lds32(b), lds32(b + 8));
+      }
+    }
+  }
+  float* out = part + (size_t)blockIdx.x * K * N;
+#pragma unroll
+  for (int t = 0; t < TPW; ++t) {
+    const int tile = warp * TPW + t, tm = tile / TN, tn = tile % TN;
+    const int m = tm * 16 + gid, n = tn * 8 + 2 * tig;
+    out[m * N + n] = acc[t][0];
+    out[m * N + n + 1] = acc[t][1];
+    out[(m + 8) * N + n] = acc[t][2];
+    out[(m + 8) * N + n + 1] = acc[t][3];
+  }
+  if (bias_part) {
+    __syncthreads();
+    const int n4 = (tid % (N / 4)) * 4;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) atomicAdd(&bsum[n4 + q], bs[q]);
+    __syncthreads();
+    for (int e = tid; e < N; e += 256) bias_part[(size_t)blockIdx.x * N + e] = bsum[e];
+  }
+}
+
+// Weight gradient for a small side (K*N <= 1024 outputs, e.g. the 128 x 2 output
+// projection or the ci x 32 lifting), CUDA cores: thread t owns outputs
+// t, t + 256, ... of the K x N matrix; per-CTA partial sums into part.
+__global__ void __launch_bounds__(256) k_wgrad_small(const float* __restrict__ A, int K, const float* __restrict__ B,
+                                                     int N, long long M, long long rows_per_cta,
+                                                     float* __restrict__ part) {
+  const long long rb = (long long)blockIdx.x * rows_per_cta;
+  const long long re = rb + rows_per_cta < M ? rb + rows_per_cta : M;
+  for (int o = threadIdx.x; o < K * N; o += blockDim.x) {
+    const int k = o / N, n = o % N;
+    float s = 0.f;
+#pragma unroll 8
+    for (long long r = rb; r < re; ++r) s = fmaf(A[r * K + k], B[r * N + n], s);
+    part[(size_t)blockIdx.x * K * N + o] = s;
+  }
+}
+
+// dh = GELU'(zh) * (dy Q2^T), the output projection's and the head GELU's
+// backward.  Launch with blockDim.x = P (<= 256): thread p keeps its row of Q2
+// (co <= 4) in registers; rows are strided over the grid.
+__global__ void k_head_back(const float* __restrict__ dy, const float* __restrict__ Q2,
+                            const float* __restrict__ zh, float* __restrict__ dh, long long rows, int P, int CO) {
+  const int p = threadIdx.x;
+  float q[4];
+  for (int o = 0; o < 4; ++o) q[o] = o < CO ? Q2[p * CO + o] : 0.f;
+  for (long long r = blockIdx.x; r < rows; r += gridDim.x) {
+    float s = 0.f;
+    for (int o = 0; o < CO; ++o) s = fmaf(dy[r * CO + o], q[o], s);
+    const long long t = r * P + p;
+    dh[t] = s * gelu_grad(zh[t]);
+  }
+}
+
 // Per-mode mixing for small batches (a GEMV per mode: tensor-core tiles would be
 // all padding): Y[b, m, :] = X[b, m, :] Rb[m] for b < B <= kMixB, one CTA per
 // mode, thread o owns output column o.  With bf16 != 0 both operands are
@@ -213,12 +425,24 @@ __global__ void __launch_bounds__(128) k_mode_mix(const float* __restrict__ X, c
 }
 
 // sum over `parts` partial results of length n (split-K reduction)
-__global__ void k_sum_parts(const float* __restrict__ part, int parts, int n, float* __restrict__ out,
-                            int accumulate) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+// Launch with blockDim (32, 8): threadIdx.y splits the parts, a fixed-order tree
+// in shared memory combines them (deterministic).
+__global__ void __launch_bounds__(256) k_sum_parts(const float* __restrict__ part, int parts, int n,
+                                                   float* __restrict__ out, int accumulate) {
+  __shared__ float sh[8][33];
+  for (int i0 = blockIdx.x * 32; i0 < n; i0 += gridDim.x * 32) {
+    const int i = i0 + threadIdx.x;
     float s = 0.f;
-    for (int p = 0; p < parts; ++p) s += part[(size_t)p * n + i];
-    out[i] = accumulate ? out[i] + s : s;
+    if (i < n)
+      for (int p = threadIdx.y; p < parts; p += 8) s += part[(size_t)p * n + i];
+    sh[threadIdx.y][threadIdx.x] = s;
+    __syncthreads();
+    if (threadIdx.y == 0 && i < n) {
+      float t = 0.f;
+      for (int y = 0; y < 8; ++y) t += sh[y][threadIdx.x];
+      out[i] = accumulate ? out[i] + t : t;
+    }
+    __syncthreads();
   }
 }
 
@@ -230,43 +454,54 @@ __global__ void k_sum_parts(const float* __restrict__ part, int parts, int n, fl
 // ---------------------------------------------------------------------------
 constexpr int kCpb = 8;
 
-// x_to_modes: A[b,y,kx,r,c] = s_kx * sum_x v[b,y,x,c] * (cos, -sin)(2 pi kx x / W)
+// x_to_modes: A[b,y,kx,r,c] = s_kx * sum_x v[b,y,x,c] * (cos, -sin)(2 pi kx x / W).
+// One CTA per row (b, y); a thread owns one kx and four channels, so each
+// step of the x sum is one 16-byte activation load, one twiddle load and
+// eight FMAs.  C is a multiple of 4 (8 in practice).
 __global__ void __launch_bounds__(256) k_x_to_modes(const float* __restrict__ v, float* __restrict__ a,
                                                     int W, int C, int MX, const float* __restrict__ cs,
                                                     const float* __restrict__ scale) {
-  extern __shared__ float sm[];
-  float* sv = sm;           // [W][C]
-  float* tw = sm + W * C;   // [W][2]
+  extern __shared__ __align__(16) float sm[];
+  float* sv = sm;          // [W][C]
+  float* tw = sm + W * C;  // [W][2]
   const int row = blockIdx.x;  // b*H + y
-  const float* src = v + (size_t)row * W * C;
-  for (int e = threadIdx.x; e < W * C; e += blockDim.x) sv[e] = src[e];
+  const float4* src = reinterpret_cast<const float4*>(v + (size_t)row * W * C);
+  for (int e = threadIdx.x; e < W * C / 4; e += blockDim.x) reinterpret_cast<float4*>(sv)[e] = src[e];
   for (int e = threadIdx.x; e < 2 * W; e += blockDim.x) tw[e] = cs[e];
   __syncthreads();
   float* dst = a + (size_t)row * MX * 2 * C;
-  const int mask = W - 1;
-  for (int e = threadIdx.x; e < MX * C; e += blockDim.x) {
-    const int kx = e / C, c = e % C;
-    float re = 0.f, im = 0.f;
+  const int mask = W - 1, C4 = C / 4;
+  for (int e = threadIdx.x; e < MX * C4; e += blockDim.x) {
+    const int kx = e / C4, c = (e % C4) * 4;
+    float4 re = make_float4(0.f, 0.f, 0.f, 0.f), im = re;
     int t = 0;
     for (int x = 0; x < W; ++x) {
-      const float val = sv[x * C + c];
-      re = fmaf(val, tw[2 * t], re);
-      im = fmaf(-val, tw[2 * t + 1], im);
+      const float4 val = *reinterpret_cast<const float4*>(&sv[x * C + c]);
+      const float2 w = *reinterpret_cast<const float2*>(&tw[2 * t]);
+      re.x = fmaf(val.x, w.x, re.x);
+      re.y = fmaf(val.y, w.x, re.y);
+      re.z = fmaf(val.z, w.x, re.z);
+      re.w = fmaf(val.w, w.x, re.w);
+      im.x = fmaf(-val.x, w.y, im.x);
+      im.y = fmaf(-val.y, w.y, im.y);
+      im.z = fmaf(-val.z, w.y, im.z);
+      im.w = fmaf(-val.w, w.y, im.w);
       t = (t + kx) & mask;
     }
     const float s = scale ? scale[kx] : 1.f;
-    dst[(kx * 2 + 0) * C + c] = s * re;
-    dst[(kx * 2 + 1) * C + c] = s * im;
+    *reinterpret_cast<float4*>(&dst[(kx * 2 + 0) * C + c]) = make_float4(s * re.x, s * re.y, s * re.z, s * re.w);
+    *reinterpret_cast<float4*>(&dst[(kx * 2 + 1) * C + c]) = make_float4(s * im.x, s * im.y, s * im.z, s * im.w);
   }
 }
 
-// modes_to_x: out[b,y,x,c] (+)= sum_kx s_kx * (Ar cos - Ai sin)(2 pi kx x / W)
+// modes_to_x: out[b,y,x,c] (+)= sum_kx s_kx * (Ar cos - Ai sin)(2 pi kx x / W);
+// a thread owns one x and four channels.
 __global__ void __launch_bounds__(256) k_modes_to_x(const float* __restrict__ a, float* __restrict__ out,
                                                     int W, int C, int MX, const float* __restrict__ cs,
                                                     const float* __restrict__ scale, int accumulate) {
-  extern __shared__ float sm[];
-  float* sa = sm;                 // [MX][2][C], pre-scaled by s_kx
-  float* tw = sm + MX * 2 * C;    // [W][2]
+  extern __shared__ __align__(16) float sm[];
+  float* sa = sm;               // [MX][2][C], pre-scaled by s_kx
+  float* tw = sm + MX * 2 * C;  // [W][2]
   const int row = blockIdx.x;
   const float* src = a + (size_t)row * MX * 2 * C;
   for (int e = threadIdx.x; e < MX * 2 * C; e += blockDim.x)
@@ -274,16 +509,30 @@ __global__ void __launch_bounds__(256) k_modes_to_x(const float* __restrict__ a,
   for (int e = threadIdx.x; e < 2 * W; e += blockDim.x) tw[e] = cs[e];
   __syncthreads();
   float* dst = out + (size_t)row * W * C;
-  const int mask = W - 1;
-  for (int e = threadIdx.x; e < W * C; e += blockDim.x) {
-    const int x = e / C, c = e % C;
-    float s = 0.f;
+  const int mask = W - 1, C4 = C / 4;
+  for (int e = threadIdx.x; e < W * C4; e += blockDim.x) {
+    const int x = e / C4, c = (e % C4) * 4;
+    float4 s4 = make_float4(0.f, 0.f, 0.f, 0.f);
     int t = 0;
     for (int kx = 0; kx < MX; ++kx) {
-      s = fmaf(sa[(kx * 2) * C + c], tw[2 * t], fmaf(-sa[(kx * 2 + 1) * C + c], tw[2 * t + 1], s));
+      const float4 ar = *reinterpret_cast<const float4*>(&sa[(kx * 2) * C + c]);
+      const float4 ai = *reinterpret_cast<const float4*>(&sa[(kx * 2 + 1) * C + c]);
+      const float2 w = *reinterpret_cast<const float2*>(&tw[2 * t]);
+      s4.x = fmaf(ar.x, w.x, fmaf(-ai.x, w.y, s4.x));
+      s4.y = fmaf(ar.y, w.x, fmaf(-ai.y, w.y, s4.y));
+      s4.z = fmaf(ar.z, w.x, fmaf(-ai.z, w.y, s4.z));
+      s4.w = fmaf(ar.w, w.x, fmaf(-ai.w, w.y, s4.w));
       t = (t + x) & mask;
     }
-    dst[e] = accumulate ? dst[e] + s : s;
+    float4* pd = reinterpret_cast<float4*>(&dst[x * C + c]);
+    if (accumulate) {
+      const float4 o = *pd;
+      s4.x += o.x;
+      s4.y += o.y;
+      s4.z += o.z;
+      s4.w += o.w;
+    }
+    *pd = s4;
   }
 }
 
@@ -416,15 +665,19 @@ __global__ void __launch_bounds__(256) k_colsum_part(const float* __restrict__ x
 }
 
 // lifting with CI input channels
+// v = x Pw + Pb; thread (row slot, channel): blockDim.x = C (<= 64), rows
+// strided over blockDim.y and the grid.
 __global__ void k_lift(const float* __restrict__ x, const float* __restrict__ Pw,
                        const float* __restrict__ Pb, float* __restrict__ v, long long rows, int CI, int C) {
-  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < rows * C;
-       t += (long long)gridDim.x * blockDim.x) {
-    const long long r = t / C;
-    const int c = (int)(t % C);
-    float s = Pb[c];
-    for (int i = 0; i < CI; ++i) s = fmaf(x[r * CI + i], Pw[i * C + c], s);
-    v[t] = s;
+  const int c = threadIdx.x;
+  float w[8];
+  for (int i = 0; i < CI && i < 8; ++i) w[i] = Pw[i * C + c];
+  const float b = Pb[c];
+  for (long long r = (long long)blockIdx.x * blockDim.y + threadIdx.y; r < rows;
+       r += (long long)gridDim.x * blockDim.y) {
+    float s = b;
+    for (int i = 0; i < CI; ++i) s = fmaf(x[r * CI + i], i < 8 ? w[i] : Pw[i * C + c], s);
+    v[r * C + c] = s;
   }
 }
 
@@ -581,6 +834,59 @@ int gemm(tara_fno* f, const GemmArgs& a) {
   return TARA_OK;
 }
 
+constexpr int kTsCtas = 152 * 2;
+
+// C (M x N) (+)= A (M x K) B(K x N) (+bias) with the tall-skinny tensor-core kernel
+// in BF16 mode for the shapes it is instantiated for; false when not handled.
+bool ts_gemm(tara_fno* f, const float* A, long long M, int K, int N, const float* Bw, int transB,
+             const float* bias, float* C, int accumulate, float* act, int act_mode) {
+  if (f->cfg.mode != TARA_FNO_BF16) return false;
+  const long long tiles = (M + kTsRows - 1) / kTsRows;
+  const int grid = (int)std::min<long long>(tiles, kTsCtas * 2);
+#define TS_CASE(KK, NN)                                                                          \
+  if (K == KK && N == NN) {                                                                      \
+    k_ts_gemm<KK, NN><<<grid, 256, 0, f->stream>>>(A, M, Bw, transB, bias, C, accumulate, act, act_mode); \
+    return true;                                                                                 \
+  }
+  TS_CASE(32, 32)
+  TS_CASE(32, 128)
+  TS_CASE(128, 32)
+#undef TS_CASE
+  return false;
+}
+
+// dW (K x N) = A^T B over M rows (+ bias gradient = column sums of B) with the
+// tensor-core reduction kernel in BF16 mode; false when not handled.
+bool ts_wgrad(tara_fno* f, const float* A, int K, const float* B, int N, long long M, float* dW, float* dbias) {
+  if (f->cfg.mode != TARA_FNO_BF16) return false;
+  const int ctas = (int)std::min<long long>(kTsCtas, (M + 63) / 64);
+  const long long per = ((M + ctas - 1) / ctas + 63) / 64 * 64;
+  float* bias_part = f->part + (size_t)ctas * K * N;
+  if ((size_t)ctas * (K * N + N) > f->part_n) return false;
+#define TW_CASE(KK, NN)                                                                            \
+  if (K == KK && N == NN) {                                                                        \
+    k_ts_wgrad<KK, NN><<<ctas, 256, 0, f->stream>>>(A, B, M, per, f->part, dbias ? bias_part : nullptr); \
+    k_sum_parts<<<64, dim3(32, 8), 0, f->stream>>>(f->part, ctas, K * N, dW, 0);                           \
+    if (dbias) k_sum_parts<<<1, dim3(32, 8), 0, f->stream>>>(bias_part, ctas, N, dbias, 0);                \
+    return true;                                                                                   \
+  }
+  TW_CASE(32, 32)
+  TW_CASE(32, 128)
+#undef TW_CASE
+  return false;
+}
+
+// dW (K x N) = A^T B for a small K*N (<= 1024), CUDA cores
+int wgrad_small(tara_fno* f, const float* A, int K, const float* B, int N, long long M, float* dW) {
+  const int ctas = (int)std::min<long long>(std::max<size_t>(1, f->part_n / ((size_t)K * N)),
+                                            std::min<long long>(4096, (M + 127) / 128));
+  const long long per = (M + ctas - 1) / ctas;
+  k_wgrad_small<<<ctas, 256, 0, f->stream>>>(A, K, B, N, M, per, f->part);
+  k_sum_parts<<<64, dim3(32, 8), 0, f->stream>>>(f->part, ctas, K * N, dW, 0);
+  TARA_CK(cudaGetLastError());
+  return TARA_OK;
+}
+
 // C[M x N] (+)= A^T B over a long shared dimension K (rows): split-K into the
 // `part` buffer, then one reduction.  A is (K x M) row-major with leading dim lda,
 // B is (K x N) row-major with leading dim ldb.
@@ -625,7 +931,7 @@ int gemm_tn_long(tara_fno* f, const float* A, long long lda, const float* B, lon
     int rc = gemm(f, a);
     if (rc) return rc;
   }
-  k_sum_parts<<<64, 256, 0, f->stream>>>(f->part, parts, M * N, C, accumulate);
+  k_sum_parts<<<64, dim3(32, 8), 0, f->stream>>>(f->part, parts, M * N, C, accumulate);
   TARA_CK(cudaGetLastError());
   return TARA_OK;
 }
@@ -634,7 +940,7 @@ int colsum(tara_fno* f, const float* x, long long M, int N, float* out) {
   const int parts = 128;
   k_colsum_part<<<parts, 256, 0, f->stream>>>(x, M, N, f->part);
   TARA_CK(cudaGetLastError());
-  k_sum_parts<<<64, 256, 0, f->stream>>>(f->part, parts, N, out, 0);
+  k_sum_parts<<<64, dim3(32, 8), 0, f->stream>>>(f->part, parts, N, out, 0);
   TARA_CK(cudaGetLastError());
   return TARA_OK;
 }
@@ -733,8 +1039,8 @@ int forward(tara_fno* f, int B) {
   const long long rows = (long long)B * c.h * c.w;
   int rc;
   if ((rc = refresh_rb(f))) return rc;
-  k_lift<<<kPw, kTh, 0, f->stream>>>(f->x, f->p + f->off_Pw, f->p + f->off_Pb, act_v(f, 0), rows,
-                                     c.ci, C);
+  k_lift<<<(int)std::min<long long>((rows + 7) / 8, 152 * 32), dim3(C, 256 / C), 0, f->stream>>>(
+      f->x, f->p + f->off_Pw, f->p + f->off_Pb, act_v(f, 0), rows, c.ci, C);
   TARA_CK(cudaGetLastError());
   for (int l = 1; l <= c.layers; ++l) {
     float* z = act_z(f, l);
@@ -758,7 +1064,7 @@ int forward(tara_fno* f, int B) {
     a.bias = f->p + f->off_b[l - 1];
     a.act = act_v(f, l);
     a.act_mode = l < c.layers ? 1 : 2;
-    if ((rc = gemm(f, a))) return rc;
+    if (!ts_gemm(f, a.A, rows, C, C, a.B, 0, a.bias, z, 1, a.act, a.act_mode) && (rc = gemm(f, a))) return rc;
   }
   GemmArgs a{};  // zh = v_L Q1 + q1 ; h = GELU(zh)
   a.M = (int)rows;
@@ -778,7 +1084,7 @@ int forward(tara_fno* f, int B) {
   a.bias = f->p + f->off_q1;
   a.act = f->h;
   a.act_mode = 1;
-  if ((rc = gemm(f, a))) return rc;
+  if (!ts_gemm(f, a.A, rows, C, c.p, a.B, 0, a.bias, f->zh, 0, f->h, 1) && (rc = gemm(f, a))) return rc;
   if (c.co <= 4)
     k_proj_out_warp<<<(int)std::min<long long>((rows + 7) / 8, 152 * 16), 256, 0, f->stream>>>(
         f->h, f->p + f->off_Q2, f->p + f->off_q2, f->y, rows, c.p, c.co);
@@ -796,14 +1102,25 @@ int backward(tara_fno* f, int B) {
   TARA_CK(cudaMemsetAsync(f->g, 0, f->np * sizeof(float), f->stream));
   // projection
   if ((rc = colsum(f, f->dy, rows, c.co, f->g + f->off_q2))) return rc;
-  if ((rc = gemm_tn_long(f, f->h, c.p, f->dy, c.co, f->g + f->off_Q2, c.p, c.co, rows, 0))) return rc;
-  k_proj_out_back<<<kPw, kTh, 0, f->stream>>>(f->dy, f->p + f->off_Q2, f->dh, rows, c.p, c.co);
-  k_gelu_back<<<kPw, kTh, 0, f->stream>>>(f->zh, f->dh, f->dh, (size_t)rows * c.p);
-  TARA_CK(cudaGetLastError());
-  if ((rc = colsum(f, f->dh, rows, c.p, f->g + f->off_q1))) return rc;
-  if ((rc = gemm_tn_long(f, act_v(f, c.layers), C, f->dh, c.p, f->g + f->off_Q1, C, c.p, rows, 0)))
+  if (c.p * c.co <= 1024) {
+    if ((rc = wgrad_small(f, f->h, c.p, f->dy, c.co, rows, f->g + f->off_Q2))) return rc;
+  } else if ((rc = gemm_tn_long(f, f->h, c.p, f->dy, c.co, f->g + f->off_Q2, c.p, c.co, rows, 0))) {
     return rc;
-  {
+  }
+  if (c.co <= 4) {
+    k_head_back<<<(int)std::min<long long>(rows, 152 * 64), c.p, 0, f->stream>>>(f->dy, f->p + f->off_Q2, f->zh,
+                                                                               f->dh, rows, c.p, c.co);
+  } else {
+    k_proj_out_back<<<kPw, kTh, 0, f->stream>>>(f->dy, f->p + f->off_Q2, f->dh, rows, c.p, c.co);
+    k_gelu_back<<<kPw, kTh, 0, f->stream>>>(f->zh, f->dh, f->dh, (size_t)rows * c.p);
+  }
+  TARA_CK(cudaGetLastError());
+  if (!ts_wgrad(f, act_v(f, c.layers), C, f->dh, c.p, rows, f->g + f->off_Q1, f->g + f->off_q1)) {
+    if ((rc = colsum(f, f->dh, rows, c.p, f->g + f->off_q1))) return rc;
+    if ((rc = gemm_tn_long(f, act_v(f, c.layers), C, f->dh, c.p, f->g + f->off_Q1, C, c.p, rows, 0)))
+      return rc;
+  }
+  if (!ts_gemm(f, f->dh, rows, c.p, C, f->p + f->off_Q1, 1, nullptr, f->dv, 0, nullptr, 0)) {
     GemmArgs a{};  // dv = dh Q1^T
     a.M = (int)rows;
     a.N = C;
@@ -830,9 +1147,11 @@ int backward(tara_fno* f, int B) {
       TARA_CK(cudaMemcpyAsync(dz, f->dv, (size_t)rows * C * sizeof(float), cudaMemcpyDeviceToDevice, f->stream));
     }
     const float* vprev = act_v(f, l - 1);
-    if ((rc = colsum(f, dz, rows, C, f->g + f->off_b[l - 1]))) return rc;
-    if ((rc = gemm_tn_long(f, vprev, C, dz, C, f->g + f->off_W[l - 1], C, C, rows, 0))) return rc;
-    {
+    if (!ts_wgrad(f, vprev, C, dz, C, rows, f->g + f->off_W[l - 1], f->g + f->off_b[l - 1])) {
+      if ((rc = colsum(f, dz, rows, C, f->g + f->off_b[l - 1]))) return rc;
+      if ((rc = gemm_tn_long(f, vprev, C, dz, C, f->g + f->off_W[l - 1], C, C, rows, 0))) return rc;
+    }
+    if (!ts_gemm(f, dz, rows, C, C, f->p + f->off_W[l - 1], 1, nullptr, f->dv, 0, nullptr, 0)) {
       GemmArgs a{};  // dv = dz W^T
       a.M = (int)rows;
       a.N = C;
@@ -906,7 +1225,11 @@ int backward(tara_fno* f, int B) {
   }
   // lifting
   if ((rc = colsum(f, f->dv, rows, C, f->g + f->off_Pb))) return rc;
-  if ((rc = gemm_tn_long(f, f->x, c.ci, f->dv, C, f->g + f->off_Pw, c.ci, C, rows, 0))) return rc;
+  if (c.ci * C <= 1024) {
+    if ((rc = wgrad_small(f, f->x, c.ci, f->dv, C, rows, f->g + f->off_Pw))) return rc;
+  } else if ((rc = gemm_tn_long(f, f->x, c.ci, f->dv, C, f->g + f->off_Pw, c.ci, C, rows, 0))) {
+    return rc;
+  }
   return TARA_OK;
 }
 
@@ -1030,6 +1353,8 @@ int tara_fno_create(const tara_fno_config* cfg, tara_fno** out) {
   FA(f->Rb, (size_t)c.layers * c.my * c.mx * 4 * c.c * c.c); FA(f->dRb, (size_t)c.my * c.mx * 4 * c.c * c.c);
   FA(f->dv, rows * c.c); FA(f->dz, rows * c.c);
   f->part_n = std::max<size_t>((size_t)256 * c.p * std::max(c.c, c.co), (size_t)128 * std::max(c.p, c.c) * 4);
+  f->part_n = std::max<size_t>(f->part_n, (size_t)kTsCtas * 2 *
+                                             ((size_t)std::max(c.c * c.p, std::max(c.c * c.c, 1024)) + c.p + c.c));
   FA(f->part, f->part_n);
   FA(f->lpart, kPw);
   FA(f->bad, 1);

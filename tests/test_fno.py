@@ -146,3 +146,31 @@ def test_training_reduces_loss():
             net.train_step(xd.data_ptr(), td.data_ptr(), 4, lr=3e-3, want_loss=False)
         last = net.train_step(xd.data_ptr(), td.data_ptr(), 4, lr=0.0)
         assert last < 0.1 * first
+
+
+CLOSURE_CH = dict(h=32, w=32, ci=6, c=32, co=2, mx=8, my=16, layers=2, p=128, max_batch=8)
+
+
+@pytest.mark.parametrize("batch", [2, 6])
+def test_tensor_core_kernels_match_oracle(batch):
+    """BF16 mode at the closure's channel counts (6 -> 32 -> 128 -> 2), where the
+    tall-skinny tensor-core GEMMs (pointwise mixing, head, input gradients) and
+    the weight-gradient reductions (with the fused bias gradients) run."""
+    cfg = tg.fno_default_config(**CLOSURE_CH)
+    with tg.FNO(cfg) as net:
+        s = fo.FnoShape.of(cfg)
+        x, t = _data(net, batch, 20 + batch)
+        p = net.get_params()
+        y = _forward_gpu(net, x, batch)
+        ref = fo.forward(torch.tensor(p, dtype=torch.float64), torch.tensor(x, dtype=torch.float64), s)
+        assert rel_l2(y, ref.numpy()) < 2e-2
+        xd, td = _dev(x), _dev(t)
+        loss = net.train_step(xd.data_ptr(), td.data_ptr(), batch, lr=0.0)
+        g = net.get_grads()
+        ref_loss, ref_g = fo.loss_and_grad(p, x, t, s)
+        assert abs(loss - ref_loss) < 2e-2 * ref_loss
+        gb, rb = _blocks(s, g), _blocks(s, ref_g)
+        for name in gb:
+            assert rel_l2(gb[name], rb[name]) < 4e-2, name
+        cos = float(np.dot(g, ref_g) / (np.linalg.norm(g) * np.linalg.norm(ref_g)))
+        assert cos > 0.996
