@@ -530,7 +530,7 @@ def main() -> None:
                     help="ensemble: runs of each size (the 384-run ensemble uses 128)")
     ap.add_argument("--ens-error-steps", type=int, default=0,
                     help="ensemble: also report the per-run error vs FP64 after this many steps")
-    ap.add_argument("--closure-epochs", type=int, default=10, help="closure: training epochs")
+    ap.add_argument("--closure-epochs", type=int, default=20, help="closure: training epochs")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -47,15 +47,15 @@ class ClosureSetup:
     eval_seed: int = 9000
     batch: int = 32
     lr: float = 1e-3
-    epochs: int = 10
+    epochs: int = 20
     coarse_precision: int = PREC_FP32
     kmax: int | None = None    # spectrum shells 1..kmax (default: the coarse 2/3 cutoff)
     samples: int = 40          # spectrum samples over the evaluation interval
-    eval_runs: int = 4         # held-out evaluation runs (seeds eval_seed..)
+    eval_runs: int = 8         # held-out evaluation runs (seeds eval_seed..)
     features: int = 6          # input channels: w, dw/dx, dw/dy, du/dx, du/dy, dv/dx (first n)
     augment: bool = True       # train on the 8 grid symmetries of every pair
     calibrate: bool = True     # pick the flux amplitude on validation seeds (a-posteriori)
-    alphas: tuple = (1.0, 2.0, 3.0, 4.0, 5.0)
+    alphas: tuple = (1.0, 2.0, 3.0, 3.5, 4.0, 4.5, 5.0)
     fno: dict = field(default_factory=dict)  # overrides of the FNO config
 
     @property
