@@ -55,7 +55,7 @@ class ClosureSetup:
     features: int = 6          # input channels: w, dw/dx, dw/dy, du/dx, du/dy, dv/dx (first n)
     augment: bool = True       # train on the 8 grid symmetries of every pair
     calibrate: bool = True     # pick the flux amplitude on validation seeds (a-posteriori)
-    alphas: tuple = (1.0, 2.0, 3.0, 3.5, 4.0, 4.5, 5.0)
+    alphas: tuple = (1.0, 2.0, 3.0, 4.0, 4.5, 5.0, 5.5, 6.0, 7.0)
     fno: dict = field(default_factory=dict)  # overrides of the FNO config
 
     @property
