@@ -446,6 +446,58 @@ def run_closure(args) -> None:
     print(json.dumps(line, default=str), flush=True)
 
 
+def run_cufft(args) -> None:
+    """Comparison only: cuFFT (through torch.fft) doing just the transforms of
+    one right-hand side -- 4 inverse 2D c2r of (N, N/2+1) spectra and 1 forward
+    2D r2c -- against one complete fused right-hand side of ours (Poisson
+    inversion, derivatives, the same transforms, the dealiased product and the
+    stage update), at N^2 in FP64 and in the FP32 form.  CUDA events; ours from
+    tara2d_step_timed (an RK4 step is four right-hand sides)."""
+    import torch
+
+    import tara_gb300 as tg
+
+    torch.cuda.set_device(0)
+    n = args.n
+    reps = max(3, args.steps)
+    out = {}
+    for name, cdt, rdt, prec in (("fp64", torch.complex128, torch.float64, tg.PREC_FP64),
+                                 ("fp32", torch.complex64, torch.float32, tg.PREC_FP32)):
+        g = torch.Generator(device="cuda").manual_seed(11)
+        spec = torch.randn(4, n, n // 2 + 1, dtype=cdt, device="cuda", generator=g)
+        real = torch.randn(n, n, dtype=rdt, device="cuda", generator=g)
+        for _ in range(args.warmup):
+            torch.fft.irfft2(spec, s=(n, n))
+            torch.fft.rfft2(real)
+        st = torch.cuda.current_stream()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record(st)
+        for _ in range(reps):
+            torch.fft.irfft2(spec, s=(n, n))
+            torch.fft.rfft2(real)
+        b.record(st)
+        torch.cuda.synchronize()
+        cufft_ms = a.elapsed_time(b) / reps
+        s = tg.Solver2D(n, scheme=tg.SCHEME_RK4, precision=prec, nu=NU, dt=DT)
+        s.init_random(K0, ENERGY, SEED.get(n, 1))
+        s.autotune(2)
+        s.step(args.warmup)
+        ours_ms = s.step_timed(reps)["total_ms"] / (4 * reps)
+        s.close()
+        out[name] = {"cufft_transforms_ms": cufft_ms, "ours_full_rhs_ms": ours_ms,
+                     "ratio_cufft_over_ours": cufft_ms / ours_ms}
+        del spec, real
+    line = {"metric": f"one RHS at {n}^2: cuFFT transforms only vs our fused RHS (comparison)",
+            "value": out["fp64"]["ratio_cufft_over_ours"], "unit": "x (cuFFT time / ours)", "n_gpus": 1,
+            "steps": reps, "warmup": args.warmup, "higher_is_better": True, "vs_baseline": None,
+            "dtype": "f64 and f32", "data": "synthetic (random spectra / seeded state)",
+            "config": {"workload": "cuFFT comparison", "cufft": "torch.fft.irfft2 of 4 fields + rfft2 of 1",
+                       "ours": "tara2d RK4 step / 4 (3 fused kernels per RHS)"},
+            "results": out}
+    print(json.dumps(line), flush=True)
+
+
 def run_fno_train(args) -> None:
     """Training step of the closure network: 128^2, 6 input channels, 4 Fourier
     layers, 32 channels, 16 modes per axis, projection 128, batch 32, BF16
@@ -524,7 +576,7 @@ def main() -> None:
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="rk4-2048",
-                    choices=["rk4-2048", "ensemble", "mhd3d", "closure", "fno-train", "closure-step"],
+                    choices=["rk4-2048", "ensemble", "mhd3d", "closure", "fno-train", "closure-step", "cufft"],
                     help="rk4-2048 is the headline; the others measure the ensemble, 3D MHD and the learned closure")
     ap.add_argument("--ens-runs-per-size", type=int, default=128,
                     help="ensemble: runs of each size (the 384-run ensemble uses 128)")
@@ -544,6 +596,8 @@ def main() -> None:
         run_closure(args)
     elif args.workload == "fno-train":
         run_fno_train(args)
+    elif args.workload == "cufft":
+        run_cufft(args)
     elif args.workload == "closure-step":
         run_closure_step(args)
     else:
