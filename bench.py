@@ -197,7 +197,8 @@ def run_ours(args) -> None:
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     n = args.n
-    s = tg.Solver2D(n, scheme=tg.SCHEME_RK4, nu=NU, dt=DT)
+    prec = tg.PREC_FP32 if args.precision == "fp32" else tg.PREC_FP64
+    s = tg.Solver2D(n, scheme=tg.SCHEME_RK4, nu=NU, dt=DT, precision=prec)
     s.init_random(K0, ENERGY, SEED.get(n, 1))
     tuned = s.autotune(2)  # tile variant per kernel (the state is restored)
     s.step(args.warmup)
@@ -270,7 +271,7 @@ def run_ours(args) -> None:
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": el_ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if prec == tg.PREC_FP64 else "f32 transforms / f64 state",
         "data": "synthetic (seeded random-phase spectrum, Philox4x32-10)",
         "config": {"workload": f"2D vorticity plain RHS (derive2csh), classic RK4, {n}x{n}, "
                                f"2pi box, nu={NU}, dt={DT}, k0={K0}, E=0.5, seed {SEED.get(n, 1)}",
@@ -583,6 +584,8 @@ def main() -> None:
     ap.add_argument("--ens-error-steps", type=int, default=0,
                     help="ensemble: also report the per-run error vs FP64 after this many steps")
     ap.add_argument("--closure-epochs", type=int, default=20, help="closure: training epochs")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"],
+                    help="rk4-2048: fp32 runs the FP32 form (FP32 transforms, FP64 state); the headline is fp64")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
