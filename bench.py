@@ -269,7 +269,8 @@ def run_ours(args) -> None:
     value = n * n * args.steps * ws / (el_ms * 1e-3)
     cpu = cpu_baseline(n, budget_s=args.cpu_budget) if not args.no_cpu_baseline else None
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "metric": METRIC if prec == tg.PREC_FP64 else METRIC.replace("FP64", "FP32 form"),
+        "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": el_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64" if prec == tg.PREC_FP64 else "f32 transforms / f64 state",
         "data": "synthetic (seeded random-phase spectrum, Philox4x32-10)",
