@@ -24,6 +24,8 @@
 // feeds it non-Hermitian spectra (e.g. i ky w on the ky = -Ny/2 row), so the
 // order and the discard rule are kept exactly.
 #pragma once
+#include <type_traits>
+
 #include "fft.cuh"
 
 namespace tara {
@@ -312,15 +314,19 @@ __global__ void __launch_bounds__(ColCfg<T, N, V>::THREADS_C)
   }
   // Pass 1: the right-hand side of every element of this thread (reads only,
   // so the unrolled loop issues all its loads together).
+  // The FP32 form keeps its right-hand side in FP32 registers until the update
+  // (its value is an FP32 number either way); the optional forcing is added in
+  // pass 2 in FP64.
+  typedef typename std::conditional<sizeof(T) == 4, float, double>::type RT;
   constexpr int PER = (N * TC + CF::THREADS_C - 1) / CF::THREADS_C;
-  double frv[PER], fiv[PER];
+  RT frv[PER], fiv[PER];
   bool bad = false;
 #pragma unroll
   for (int i = 0; i < PER; ++i) {
     const int e = tid + i * CF::THREADS_C;
     const int y = e / TC, c = e % TC, x = x0 + c;
-    frv[i] = 0.0;
-    fiv[i] = 0.0;
+    frv[i] = RT(0);
+    fiv[i] = RT(0);
     if (e >= N * TC || x >= g.nh) continue;
     const size_t q = (size_t)y * g.pitch + x;
     double fr, fi;
@@ -365,18 +371,21 @@ __global__ void __launch_bounds__(ColCfg<T, N, V>::THREADS_C)
         fi = -(p.alpha * ni + vk2 * di);
       }
     }
-    if (sb.force) {
-      const double2 fc = sb.force[q];
-      fr += fc.x;
-      fi += fc.y;
+    if constexpr (sizeof(T) == 8) {
+      if (sb.force) {
+        const double2 fc = sb.force[q];
+        fr += fc.x;
+        fi += fc.y;
+      }
+      bad |= !(isfinite(fr) && isfinite(fi));
     }
-    bad |= !(isfinite(fr) && isfinite(fi));
-    frv[i] = fr;
-    fiv[i] = fi;
+    frv[i] = (RT)fr;  // exact: an FP32 value in the FP32 form, unchanged in FP64
+    fiv[i] = (RT)fi;
   }
   // Pass 2: the stage update, in chunks whose loads all precede their stores
   // (the state arrays may alias the RHS input, so loads cannot move past stores).
-  constexpr int CH = PER < 8 ? PER : 8;
+  constexpr int CHM = sizeof(T) == 8 ? 8 : 8;
+  constexpr int CH = PER < CHM ? PER : CHM;
   const double dt = p.dt;
 #pragma unroll
   for (int i0 = 0; i0 < PER; i0 += CH) {
@@ -404,8 +413,16 @@ __global__ void __launch_bounds__(ColCfg<T, N, V>::THREADS_C)
 #pragma unroll
     for (int u = 0; u < CH; ++u) {
       if (!ok[u]) continue;
-      const double fr = frv[i0 + u], fi = fiv[i0 + u];
+      double fr = (double)frv[i0 + u], fi = (double)fiv[i0 + u];
       const size_t q = qv[u];
+      if constexpr (sizeof(T) == 4) {  // the FP32 form adds the forcing here, in FP64
+        if (sb.force) {
+          const double2 fc = sb.force[q];
+          fr += fc.x;
+          fi += fc.y;
+        }
+        bad |= !(isfinite(fr) && isfinite(fi));
+      }
       const double2 s = a0[u];
       switch (mode) {
         case MODE_DERIVE:
