@@ -204,7 +204,7 @@ __global__ void __launch_bounds__(ColCfg<T, N, V>::THREADS_A)
 // imaginary parts of the k = 0 and k = N/2 bins dropped first.
 // blockIdx.y = run of a batch.
 template <typename T, int N, int V>
-__global__ void __launch_bounds__(RowCfg<T, N, V>::THREADS)
+__global__ void __launch_bounds__(RowCfg<T, N, V>::THREADS, (sizeof(T) == 4 && RowCfg<T, N, V>::THREADS >= 512) ? 2 : 1)
     k_row_nl(const typename cplx_of<T>::type* __restrict__ u,
              typename cplx_of<T>::type* __restrict__ nl, Grid2D g,
              const typename cplx_of<T>::type* __restrict__ tw) {
