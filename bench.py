@@ -197,7 +197,7 @@ def run_ours(args) -> None:
     local = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(local)
     n = args.n
-    prec = tg.PREC_FP32 if args.precision == "fp32" else tg.PREC_FP64
+    prec = {"fp32": tg.PREC_FP32, "df64": tg.PREC_DF64}.get(args.precision, tg.PREC_FP64)
     s = tg.Solver2D(n, scheme=tg.SCHEME_RK4, nu=NU, dt=DT, precision=prec)
     s.init_random(K0, ENERGY, SEED.get(n, 1))
     tuned = s.autotune(2)  # tile variant per kernel (the state is restored)
@@ -265,14 +265,16 @@ def run_ours(args) -> None:
     avg_ms = ks[dom]["ms"] / max(1, ks[dom]["launches"])
     peak, peak_kind = peaks()
     achieved = alg_bytes[dom] / (avg_ms * 1e-3) / 1e9
-    traffic = from_profiles("traffic_bytes_per_launch", dom, n)
+    traffic = from_profiles("traffic_bytes_per_launch", dom, n) if prec == tg.PREC_FP64 else None
     value = n * n * args.steps * ws / (el_ms * 1e-3)
     cpu = cpu_baseline(n, budget_s=args.cpu_budget) if not args.no_cpu_baseline else None
     line = {
-        "metric": METRIC if prec == tg.PREC_FP64 else METRIC.replace("FP64", "FP32 form"),
+        "metric": {tg.PREC_FP64: METRIC, tg.PREC_FP32: METRIC.replace("FP64", "FP32 form"),
+                   tg.PREC_DF64: METRIC.replace("FP64", "double-float form")}[prec],
         "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": el_ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64" if prec == tg.PREC_FP64 else "f32 transforms / f64 state",
+        "scaling": "weak", "vs_baseline": None, "dtype": {tg.PREC_FP64: "f64", tg.PREC_FP32: "f32 transforms / f64 state",
+                                                  tg.PREC_DF64: "df64 (f32 pair) transforms / f64 state"}[prec],
         "data": "synthetic (seeded random-phase spectrum, Philox4x32-10)",
         "config": {"workload": f"2D vorticity plain RHS (derive2csh), classic RK4, {n}x{n}, "
                                f"2pi box, nu={NU}, dt={DT}, k0={K0}, E=0.5, seed {SEED.get(n, 1)}",
@@ -284,8 +286,10 @@ def run_ours(args) -> None:
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "avg_launch_ms": avg_ms,
-                     "limiter": "FP64 pipe (GB300: 2 FP64 thread-instructions per SM per cycle)",
-                     "fp64_pipe_busy_pct_ncu": from_profiles("fp64_pipe_busy_pct", dom, n),
+                     "limiter": ("FP64 pipe (GB300: 2 FP64 thread-instructions per SM per cycle)"
+                                 if prec == tg.PREC_FP64 else "FP32 issue (profiled for the FP64 form only)"),
+                     "fp64_pipe_busy_pct_ncu": (from_profiles("fp64_pipe_busy_pct", dom, n)
+                                                if prec == tg.PREC_FP64 else None),
                      "per_kernel_ms": {k: v["ms"] / max(1, v["launches"]) for k, v in ks.items()}},
         "clocks": clocks,
         "tile_variants": tuned["variants"],
@@ -585,8 +589,9 @@ def main() -> None:
     ap.add_argument("--ens-error-steps", type=int, default=0,
                     help="ensemble: also report the per-run error vs FP64 after this many steps")
     ap.add_argument("--closure-epochs", type=int, default=20, help="closure: training epochs")
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"],
-                    help="rk4-2048: fp32 runs the FP32 form (FP32 transforms, FP64 state); the headline is fp64")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32", "df64"],
+                    help="rk4-2048: fp32 runs the FP32 form (FP32 transforms, FP64 state), df64 the "
+                         "double-float form (transforms in FP32 pairs, FP64 state); the headline is fp64")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

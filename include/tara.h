@@ -96,6 +96,7 @@ void tara_set_css_params(double lx, double ly, double lambda);
 #define TARA_SCHEME_RK4 1
 #define TARA_PREC_FP64 0   /* FFTs, products and state in FP64 */
 #define TARA_PREC_FP32 1   /* FP32 FFTs and products; FP64 state and reductions */
+#define TARA_PREC_DF64 2   /* double-float (FP32 pair) FFTs and products; FP64 state */
 
 typedef struct tara2d_config {
   int nx, ny;      /* powers of two, 16..2048 */

@@ -27,7 +27,7 @@ TARA_ERR_INI = 6
 
 RHS_PLAIN, RHS_SCREEN = 0, 1
 SCHEME_AB2, SCHEME_RK4 = 0, 1
-PREC_FP64, PREC_FP32 = 0, 1
+PREC_FP64, PREC_FP32, PREC_DF64 = 0, 1, 2
 
 PI_R4 = float(np.float32(3.1428))  # real(8), parameter :: pi = 3.1428 (default-real literal)
 

@@ -21,7 +21,7 @@ LIB = PKG / "libtara.so"
 ORACLE = ROOT / "oracle"
 REFERENCE = Path(os.environ.get("TARA_REFERENCE", "/root/reference"))
 
-SOURCES = ["launch_fp64.cu", "launch_fp32.cu", "solver2d.cu", "capi.cu", "noalloc.cu", "mhd3d.cu",
+SOURCES = ["launch_fp64.cu", "launch_fp32.cu", "launch_df64.cu", "solver2d.cu", "capi.cu", "noalloc.cu", "mhd3d.cu",
            "ensemble.cu", "fno.cu", "closure.cu", "particles.cu", "ini.cpp",
            "driver.cpp"]
 EXE = PKG / "tara"

@@ -27,6 +27,12 @@ namespace tara {
 template <typename T> struct cplx_of;
 template <> struct cplx_of<double> { typedef double2 type; };
 template <> struct cplx_of<float> { typedef float2 type; };
+}  // namespace tara
+
+#include "df64.cuh"
+
+namespace tara {
+template <> struct cplx_of<df64> { typedef df64c type; };
 
 template <typename T>
 __device__ __forceinline__ typename cplx_of<T>::type mkc(T x, T y) {
@@ -92,6 +98,15 @@ template <bool INV, typename C>
 __device__ __forceinline__ C load_tw(const C* __restrict__ tw, int m) {
   C w = __ldg(tw + m);
   if (INV) w.y = -w.y;
+  return w;
+}
+
+template <bool INV>
+__device__ __forceinline__ df64c load_tw(const df64c* __restrict__ tw, int m) {
+  const float4 v = __ldg(reinterpret_cast<const float4*>(tw) + m);
+  df64c w;
+  w.x = df64(v.x, v.y);
+  w.y = INV ? df64(-v.z, -v.w) : df64(v.z, v.w);
   return w;
 }
 

@@ -57,6 +57,8 @@ struct Launch2D {
 
 // Twiddle table exp(-2 pi i m/n), m < n, in precision T, uploaded to device.
 int make_twiddles(int n, bool fp32, void** dev);
+// The same table as double-float (hi, lo) pairs: float4 {re.hi, re.lo, im.hi, im.lo}.
+int make_twiddles_df64(int n, void** dev);
 
 }  // namespace tara
 

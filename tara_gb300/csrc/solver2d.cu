@@ -91,6 +91,22 @@ int make_twiddles(int n, bool fp32, void** dev) {
   return TARA_OK;
 }
 
+// The same table as double-float pairs (hi, lo) per component, for the
+// double-float transforms: hi = fl32(w), lo = fl32(w - hi).
+int make_twiddles_df64(int n, void** dev) {
+  const long double tp = 6.283185307179586476925286766559005768L;
+  std::vector<float4> w(n);
+  for (int m = 0; m < n; ++m) {
+    const long double a = tp * (long double)m / (long double)n;
+    const double c = (double)std::cos(a), s = (double)-std::sin(a);
+    const float ch = (float)c, sh = (float)s;
+    w[m] = make_float4(ch, (float)(c - (double)ch), sh, (float)(s - (double)sh));
+  }
+  TARA_CK(cudaMalloc(dev, n * sizeof(float4)));
+  TARA_CK(cudaMemcpy(*dev, w.data(), n * sizeof(float4), cudaMemcpyHostToDevice));
+  return TARA_OK;
+}
+
 // ---------------------------------------------------------------------------
 // diagnostics
 // ---------------------------------------------------------------------------
@@ -287,8 +303,11 @@ static int rhs_update_t(tara2d* h, const double2* win, int mode, cudaEvent_t* ev
 // One RHS evaluation of `win` followed by the update of `mode`; when ev is not
 // null, ev[0..2] are recorded after the three launches.
 int rhs_and_update(tara2d* h, const double2* win, int mode, cudaEvent_t* ev) {
-  return h->cfg.precision == TARA_PREC_FP32 ? rhs_update_t<float>(h, win, mode, ev)
-                                            : rhs_update_t<double>(h, win, mode, ev);
+  switch (h->cfg.precision) {
+    case TARA_PREC_FP32: return rhs_update_t<float>(h, win, mode, ev);
+    case TARA_PREC_DF64: return rhs_update_t<df64>(h, win, mode, ev);
+    default: return rhs_update_t<double>(h, win, mode, ev);
+  }
 }
 
 int copy_in_dense(tara2d* h, double2* dst, const double* host) {
@@ -430,7 +449,8 @@ int tara2d_create(const tara2d_config* cfg, tara2d** out) {
     return set_error(TARA_ERR_ARGS, "unknown rhs kind");
   if (cfg->scheme != TARA_SCHEME_AB2 && cfg->scheme != TARA_SCHEME_RK4)
     return set_error(TARA_ERR_ARGS, "unknown scheme");
-  if (cfg->precision != TARA_PREC_FP64 && cfg->precision != TARA_PREC_FP32)
+  if (cfg->precision != TARA_PREC_FP64 && cfg->precision != TARA_PREC_FP32 &&
+      cfg->precision != TARA_PREC_DF64)
     return set_error(TARA_ERR_ARGS, "unknown precision");
   if (!(cfg->lx > 0.0) || !(cfg->ly > 0.0) || !(cfg->kpi > 0.0))
     return set_error(TARA_ERR_ARGS, "box lengths and kpi must be positive");
@@ -455,7 +475,9 @@ int tara2d_create(const tara2d_config* cfg, tara2d** out) {
   CKC(cudaGetDevice(&h->dev));
   CKC(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
   const size_t fbytes = (size_t)h->batch * h->ny * h->pitch * sizeof(double2);
-  const size_t csize = cfg->precision == TARA_PREC_FP32 ? sizeof(float2) : sizeof(double2);
+  const size_t csize = cfg->precision == TARA_PREC_FP32 ? sizeof(float2)
+                       : cfg->precision == TARA_PREC_DF64 ? sizeof(df64c)
+                                                          : sizeof(double2);
   const size_t wbytes = (size_t)h->batch * h->ny * h->pitch * csize;
   CKC(cudaMalloc(&h->w0, fbytes));
   CKC(cudaMalloc(&h->fold, fbytes));
@@ -483,9 +505,14 @@ int tara2d_create(const tara2d_config* cfg, tara2d** out) {
   CKC(cudaMemsetAsync(h->nl, 0, wbytes, h->stream));
   CKC(cudaMemsetAsync(h->flag, 0, sizeof(unsigned int), h->stream));
 #undef CKC
-  const bool f32 = cfg->precision == TARA_PREC_FP32;
-  if ((rc = make_twiddles(h->nx, f32, &h->twx))) return fail(rc);
-  if ((rc = make_twiddles(h->ny, f32, &h->twy))) return fail(rc);
+  if (cfg->precision == TARA_PREC_DF64) {
+    if ((rc = make_twiddles_df64(h->nx, &h->twx))) return fail(rc);
+    if ((rc = make_twiddles_df64(h->ny, &h->twy))) return fail(rc);
+  } else {
+    const bool f32 = cfg->precision == TARA_PREC_FP32;
+    if ((rc = make_twiddles(h->nx, f32, &h->twx))) return fail(rc);
+    if ((rc = make_twiddles(h->ny, f32, &h->twy))) return fail(rc);
+  }
   h->grid.nx = h->nx;
   h->grid.ny = h->ny;
   h->grid.nh = h->nh;
