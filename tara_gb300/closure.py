@@ -56,6 +56,10 @@ class ClosureSetup:
     augment: bool = True       # train on the 8 grid symmetries of every pair
     calibrate: bool = True     # pick the flux amplitude on validation seeds (a-posteriori)
     alphas: tuple = (1.0, 2.0, 3.0, 4.0, 4.5, 5.0, 5.5, 6.0, 7.0)
+    # extra coarse-grid viscosities calibrated jointly with alpha: a constant
+    # eddy viscosity beside the learned flux drains what the flux injects at the
+    # large scales (0 = the learned flux alone)
+    eddy_nus: tuple = (0.0,)
     fno: dict = field(default_factory=dict)  # overrides of the FNO config
 
     @property
@@ -88,9 +92,9 @@ def _torch():
     return torch
 
 
-def _solver(n, s: ClosureSetup, dt, precision=PREC_FP64, batch=1) -> Solver2D:
+def _solver(n, s: ClosureSetup, dt, precision=PREC_FP64, batch=1, nu_extra: float = 0.0) -> Solver2D:
     # true pi and a 2 pi box: integer wavenumbers
-    return Solver2D(n, scheme=SCHEME_RK4, precision=precision, nu=s.nu, dt=dt, batch=batch,
+    return Solver2D(n, scheme=SCHEME_RK4, precision=precision, nu=s.nu + nu_extra, dt=dt, batch=batch,
                     kpi=math.pi, lx=2 * math.pi, ly=2 * math.pi)
 
 
@@ -245,13 +249,15 @@ def spectrum_error(E, Eref, kmax: int) -> float:
     return float(np.linalg.norm(a - b) / np.linalg.norm(b))
 
 
-def evaluate(s: ClosureSetup, net: FNO | None = None, in_scale=1.0, out_scale: float = 1.0, *,
-             closures: dict | None = None, seed: int | None = None) -> dict:
+def evaluate(s: ClosureSetup, net: FNO | None = None, in_scale=1.0, out_scale: float = 1.0,
+             nu_extra: float = 0.0, *, closures: dict | None = None, seed: int | None = None) -> dict:
     """Held-out runs (seeds seed..seed+eval_runs, default eval_seed) of the fine
     plain solver (the judge) and of the coarse solver without a closure and with
     each closure, from the box-filtered fine initial state.  `closures` maps a
-    name to (net, in_scale, out_scale), each net a separate handle whose batch
-    holds eval_runs; `net` alone stands for {"closure": (net, in_scale, out_scale)}.
+    name to (net, in_scale, out_scale[, nu_extra]), each net a separate handle
+    whose batch holds eval_runs, nu_extra an eddy viscosity added to the coarse
+    solver of that closure; `net` alone stands for {"closure": (net, in_scale,
+    out_scale, nu_extra)}.
     Spectra (shells 1..kmax) are sampled `samples` times over the interval.
     Reported errors, each a relative L2 over the shells against the filtered
     fine run:
@@ -264,7 +270,7 @@ def evaluate(s: ClosureSetup, net: FNO | None = None, in_scale=1.0, out_scale: f
     non-finite falls back to the plain fine-grid run from then on (recorded)."""
     torch = _torch()
     if closures is None:
-        closures = {"closure": (net, in_scale, out_scale)} if net is not None else {}
+        closures = {"closure": (net, in_scale, out_scale, nu_extra)} if net is not None else {}
     seed = s.eval_seed if seed is None else seed
     nc, kmax, R = s.n_coarse, s.shells, s.eval_runs
     ratio = s.coarse_dt_ratio
@@ -287,8 +293,10 @@ def evaluate(s: ClosureSetup, net: FNO | None = None, in_scale=1.0, out_scale: f
     try:
         fine = handles["fine"] = _solver(s.n_fine, s, s.dt_fine, batch=R)
         judge = handles["judge"] = _solver(nc, s, s.dt_coarse, precision=s.coarse_precision, batch=R)
-        coarse = {k: _solver(nc, s, s.dt_coarse, precision=s.coarse_precision, batch=R)
-                  for k in ["plain"] + names}
+        coarse = {"plain": _solver(nc, s, s.dt_coarse, precision=s.coarse_precision, batch=R)}
+        for k in names:
+            nu_e = closures[k][3] if len(closures[k]) > 3 else 0.0
+            coarse[k] = _solver(nc, s, s.dt_coarse, precision=s.coarse_precision, batch=R, nu_extra=nu_e)
         handles.update({"c_" + k: v for k, v in coarse.items()})
         for r in range(R):
             fine.init_random(s.k0, s.energy, seed + r, run=r)
@@ -301,7 +309,7 @@ def evaluate(s: ClosureSetup, net: FNO | None = None, in_scale=1.0, out_scale: f
                 c.set_state_real_device(r, wbar.data_ptr())
         e_init = [judge.diag_run(r)[0] for r in range(R)]
         for k in names:
-            nk, ik, ok = closures[k]
+            nk, ik, ok = closures[k][:3]
             objs[k] = Closure(coarse[k], nk, ik, ok)
         for j in range(ns):
             fine.step(stride_f)
@@ -351,33 +359,37 @@ def evaluate(s: ClosureSetup, net: FNO | None = None, in_scale=1.0, out_scale: f
 
 
 def calibrate(s: ClosureSetup, params, in_scale, out_scale: float, alphas=(1.0, 1.5, 2.0, 3.0),
-              seed: int | None = None) -> dict:
-    """A-posteriori calibration of the flux amplitude on held-out validation
-    seeds (never the evaluation seeds): the closure with out_scale * alpha for
-    each alpha runs beside one fine run; returns the errors and, among the
-    alphas whose runs needed no fallback, the one whose time-averaged spectrum
-    error is lowest."""
+              seed: int | None = None, eddy_nus=(0.0,)) -> dict:
+    """A-posteriori calibration of the flux amplitude alpha and the extra
+    coarse viscosity nu_e on held-out validation seeds (never the evaluation
+    seeds): the closure with out_scale * alpha on a coarse solver of viscosity
+    nu + nu_e, for every pair, runs beside one fine run; returns the errors and,
+    among the pairs whose runs needed no fallback, the one whose time-averaged
+    spectrum error is lowest ("best": alpha, "best_nu": nu_e)."""
     seed = s.seed0 + 200 if seed is None else seed
+    grid = [(a, v) for v in eddy_nus for a in alphas]
+    name = {(a, v): f"a{a:g}" if v == 0.0 else f"a{a:g}_nu{v:g}" for a, v in grid}
     nets = {}
     try:
-        for a in alphas:
+        for a, v in grid:
             n = FNO(fno_config(s, max(1, s.eval_runs)))
             n.set_params(params)
-            nets[f"a{a:g}"] = (n, in_scale, out_scale * a)
+            nets[name[a, v]] = (n, in_scale, out_scale * a, v)
         ev = evaluate(s, closures=nets, seed=seed)
     finally:
-        for n, _, _ in nets.values():
-            n.close()
-    errs = {a: ev[f"err_avg_a{a:g}"] for a in alphas}
-    fell = {a: ev["fallback"][f"a{a:g}"] for a in alphas}
-    ok = [a for a in alphas if fell[a] is None] or [min(alphas)]
-    best = min(ok, key=lambda a: errs[a])
-    return {"alphas": list(alphas), "err_avg": errs, "fallback": fell, "err_avg_plain": ev["err_avg_plain"],
-            "best": best, "energy": ev["energy"], "seed": seed}
+        for n in nets.values():
+            n[0].close()
+    errs = {name[g]: ev[f"err_avg_{name[g]}"] for g in grid}
+    fell = {name[g]: ev["fallback"][name[g]] for g in grid}
+    ok = [g for g in grid if fell[name[g]] is None] or [min(grid)]
+    best = min(ok, key=lambda g: errs[name[g]])
+    return {"alphas": list(alphas), "eddy_nus": list(eddy_nus), "err_avg": errs, "fallback": fell,
+            "err_avg_plain": ev["err_avg_plain"], "best": best[0], "best_nu": best[1],
+            "energy": ev["energy"], "seed": seed}
 
 
 def throughput(s: ClosureSetup, net: FNO | None, in_scale=1.0, out_scale: float = 1.0,
-               steps: int = 200) -> dict:
+               steps: int = 200, nu_extra: float = 0.0) -> dict:
     """Simulated time per wall-second of one fine plain run and of one coarse run
     with the closure (and without), on the same GPU: CUDA events around `steps`
     steps on each solver's stream, after autotuning and warm-up."""
@@ -386,7 +398,7 @@ def throughput(s: ClosureSetup, net: FNO | None, in_scale=1.0, out_scale: float 
     out = {}
     with _solver(s.n_fine, s, s.dt_fine) as fine, \
             _solver(nc, s, s.dt_coarse, precision=s.coarse_precision) as plain_c, \
-            _solver(nc, s, s.dt_coarse, precision=s.coarse_precision) as clos_c:
+            _solver(nc, s, s.dt_coarse, precision=s.coarse_precision, nu_extra=nu_extra) as clos_c:
         fine.init_random(s.k0, s.energy, s.eval_seed)
         wbar = torch.empty((nc, nc), dtype=torch.float64, device="cuda")
         torch.cuda.synchronize()
@@ -429,17 +441,18 @@ def run_all(s: ClosureSetup, log=print) -> dict:
                              log=log)
         log(f"validation {out['train']['val']}")
         params = net.get_params()
-    alpha = 1.0
+    alpha, nu_e = 1.0, 0.0
     if s.calibrate:
-        out["calibration"] = calibrate(s, params, ins, outs, s.alphas)
-        alpha = out["calibration"]["best"]
-        log(f"calibration {out['calibration']['err_avg']} -> alpha {alpha}")
+        out["calibration"] = calibrate(s, params, ins, outs, s.alphas, eddy_nus=s.eddy_nus)
+        alpha, nu_e = out["calibration"]["best"], out["calibration"]["best_nu"]
+        log(f"calibration {out['calibration']['err_avg']} -> alpha {alpha}, nu_e {nu_e}")
     out["alpha"] = alpha
+    out["nu_e"] = nu_e
     with FNO(fno_config(s, max(1, s.eval_runs))) as neval:
         neval.set_params(params)
-        out["eval"] = evaluate(s, neval, ins, outs * alpha)
+        out["eval"] = evaluate(s, neval, ins, outs * alpha, nu_e)
     with FNO(fno_config(s, 1)) as net1:
         net1.set_params(params)
-        out["throughput"] = throughput(s, net1, ins, outs * alpha)
+        out["throughput"] = throughput(s, net1, ins, outs * alpha, nu_extra=nu_e)
     out["params"] = params
     return out
