@@ -422,9 +422,9 @@ def run_closure(args) -> None:
     (nu = 5e-5, k0 = 8), box-filtered (8 x 8 block means) to 128^2 with the exact
     subgrid vorticity flux as target; 4-layer FNO, 32 channels, 16 modes per
     axis, GELU, BF16 tensor-core GEMMs with FP32 accumulation, Adam lr 1e-3,
-    batch 32; flux amplitude calibrated on validation seeds; evaluated on
-    held-out seeds over 5 eddy-turnover times against the filtered 1024^2 plain
-    run.  The value is the closure's simulated time per wall-second over that of
+    batch 32; flux amplitude and an extra coarse eddy viscosity calibrated on 16
+    validation seeds; evaluated on 32 held-out seeds over 5 eddy-turnover times
+    against the filtered 1024^2 plain run.  The value is the closure's simulated time per wall-second over that of
     the plain 1024^2 FP64 solver on the same GPU (one run each, CUDA events)."""
     import torch
 
@@ -440,13 +440,15 @@ def run_closure(args) -> None:
             "dtype": "bf16 GEMMs / f32 network / f64 state", "data": "synthetic (seeded decaying turbulence)",
             "config": {"workload": "learned closure 1024^2 -> 128^2, 5 eddy times", "fine_dt": s.dt_fine,
                        "coarse_dt": s.dt_coarse, "coarse_precision": "fp32 transforms" if s.coarse_precision else "fp64",
-                       "eval_runs": s.eval_runs, "samples": s.samples},
+                       "eval_runs": s.eval_runs, "cal_runs": s.cal_runs, "samples": s.samples},
             "spectrum_error": {"avg_spectrum_closure": ev["err_avg_closure"], "avg_spectrum_plain_coarse": ev["err_avg_plain"],
                                "mean_per_sample_closure": ev["mean_err_closure"],
                                "mean_per_sample_plain_coarse": ev["mean_err_plain"], "shells": ev["kmax"],
                                "fallback": ev["fallback"]},
-            "a_priori": out["train"]["val"], "alpha": out["alpha"],
-            "calibration": {k: out["calibration"][k] for k in ("err_avg", "best", "seed")} if "calibration" in out else None,
+            "a_priori": out["train"]["val"], "alpha": out["alpha"], "nu_e": out["nu_e"],
+            "calibration": ({k: out["calibration"][k] for k in ("err_avg", "best", "best_nu", "seed", "runs")}
+                            if "calibration" in out else None),
+            "energy_first_last": {k: [v[0], v[-1]] for k, v in ev["energy"].items()},
             "throughput": tp, "train": {k: out["train"][k] for k in ("train_steps", "wall_s", "best_epoch")},
             "data_gen_s": out["data"]["train"]["wall_s"]}
     print(json.dumps(line, default=str), flush=True)

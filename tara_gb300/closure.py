@@ -51,15 +51,16 @@ class ClosureSetup:
     coarse_precision: int = PREC_FP32
     kmax: int | None = None    # spectrum shells 1..kmax (default: the coarse 2/3 cutoff)
     samples: int = 40          # spectrum samples over the evaluation interval
-    eval_runs: int = 8         # held-out evaluation runs (seeds eval_seed..)
+    eval_runs: int = 32        # held-out evaluation runs (seeds eval_seed..)
+    cal_runs: int = 16         # validation runs of the a-posteriori calibration (seeds seed0 + 200..)
     features: int = 6          # input channels: w, dw/dx, dw/dy, du/dx, du/dy, dv/dx (first n)
     augment: bool = True       # train on the 8 grid symmetries of every pair
     calibrate: bool = True     # pick the flux amplitude on validation seeds (a-posteriori)
-    alphas: tuple = (1.0, 2.0, 3.0, 4.0, 4.5, 5.0, 5.5, 6.0, 7.0)
+    alphas: tuple = (3.0, 4.0, 5.0, 6.0, 7.0)
     # extra coarse-grid viscosities calibrated jointly with alpha: a constant
     # eddy viscosity beside the learned flux drains what the flux injects at the
     # large scales (0 = the learned flux alone)
-    eddy_nus: tuple = (0.0,)
+    eddy_nus: tuple = (0.0, 5e-5, 1e-4, 2e-4)
     fno: dict = field(default_factory=dict)  # overrides of the FNO config
 
     @property
@@ -250,7 +251,8 @@ def spectrum_error(E, Eref, kmax: int) -> float:
 
 
 def evaluate(s: ClosureSetup, net: FNO | None = None, in_scale=1.0, out_scale: float = 1.0,
-             nu_extra: float = 0.0, *, closures: dict | None = None, seed: int | None = None) -> dict:
+             nu_extra: float = 0.0, *, closures: dict | None = None, seed: int | None = None,
+             runs: int | None = None) -> dict:
     """Held-out runs (seeds seed..seed+eval_runs, default eval_seed) of the fine
     plain solver (the judge) and of the coarse solver without a closure and with
     each closure, from the box-filtered fine initial state.  `closures` maps a
@@ -258,7 +260,8 @@ def evaluate(s: ClosureSetup, net: FNO | None = None, in_scale=1.0, out_scale: f
     whose batch holds eval_runs, nu_extra an eddy viscosity added to the coarse
     solver of that closure; `net` alone stands for {"closure": (net, in_scale,
     out_scale, nu_extra)}.
-    Spectra (shells 1..kmax) are sampled `samples` times over the interval.
+    `runs` overrides eval_runs.  Spectra (shells 1..kmax) are sampled `samples`
+    times over the interval.
     Reported errors, each a relative L2 over the shells against the filtered
     fine run:
       * err_avg_*: of the spectra averaged over the samples and runs (the
@@ -272,7 +275,7 @@ def evaluate(s: ClosureSetup, net: FNO | None = None, in_scale=1.0, out_scale: f
     if closures is None:
         closures = {"closure": (net, in_scale, out_scale, nu_extra)} if net is not None else {}
     seed = s.eval_seed if seed is None else seed
-    nc, kmax, R = s.n_coarse, s.shells, s.eval_runs
+    nc, kmax, R = s.n_coarse, s.shells, (s.eval_runs if runs is None else runs)
     ratio = s.coarse_dt_ratio
     steps_f = s.fine_steps
     ns = max(1, min(s.samples, steps_f // ratio))
@@ -367,15 +370,16 @@ def calibrate(s: ClosureSetup, params, in_scale, out_scale: float, alphas=(1.0, 
     among the pairs whose runs needed no fallback, the one whose time-averaged
     spectrum error is lowest ("best": alpha, "best_nu": nu_e)."""
     seed = s.seed0 + 200 if seed is None else seed
+    R = max(1, s.cal_runs)
     grid = [(a, v) for v in eddy_nus for a in alphas]
     name = {(a, v): f"a{a:g}" if v == 0.0 else f"a{a:g}_nu{v:g}" for a, v in grid}
     nets = {}
     try:
         for a, v in grid:
-            n = FNO(fno_config(s, max(1, s.eval_runs)))
+            n = FNO(fno_config(s, R))
             n.set_params(params)
             nets[name[a, v]] = (n, in_scale, out_scale * a, v)
-        ev = evaluate(s, closures=nets, seed=seed)
+        ev = evaluate(s, closures=nets, seed=seed, runs=R)
     finally:
         for n in nets.values():
             n[0].close()
@@ -385,7 +389,7 @@ def calibrate(s: ClosureSetup, params, in_scale, out_scale: float, alphas=(1.0, 
     best = min(ok, key=lambda g: errs[name[g]])
     return {"alphas": list(alphas), "eddy_nus": list(eddy_nus), "err_avg": errs, "fallback": fell,
             "err_avg_plain": ev["err_avg_plain"], "best": best[0], "best_nu": best[1],
-            "energy": ev["energy"], "seed": seed}
+            "energy": ev["energy"], "seed": seed, "runs": R}
 
 
 def throughput(s: ClosureSetup, net: FNO | None, in_scale=1.0, out_scale: float = 1.0,

@@ -112,11 +112,11 @@ __device__ __forceinline__ df64c load_tw(const df64c* __restrict__ tw, int m) {
 
 // In-place length-N transform of buf (unnormalised).  tw[m] = exp(-2 pi i m/N).
 // Forward: X[k] = sum x[n] e^{-2 pi i nk/N}; inverse uses e^{+...}.
-template <typename T, int N, bool INV>
+// G threads share the transform (default N/16; up to N/4, one butterfly each).
+template <typename T, int N, bool INV, int G = fft_group(N)>
 __device__ __forceinline__ void fft_slot(typename cplx_of<T>::type* buf, int lane, bool active,
                                          const typename cplx_of<T>::type* __restrict__ tw) {
   typedef typename cplx_of<T>::type C;
-  constexpr int G = fft_group(N);
   constexpr int Q = N / 4;
   constexpr int LG = ilog2c(N);
   constexpr int NR4 = LG / 2;

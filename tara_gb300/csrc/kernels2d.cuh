@@ -249,7 +249,9 @@ __global__ void __launch_bounds__(RowCfg<T, N, V>::THREADS, (sizeof(T) == 4 && R
     b[x] = mkc<T>(na, nb);
   }
   __syncthreads();
-  fft_slot<T, N, false>(sm + slot * SL, lane, (slot & 3) == 0, tw);
+  // forward transform of each pair's packed products (its first slot), shared
+  // by all 4 G threads of the pair so that no thread idles through it
+  fft_slot<T, N, false, 4 * G>(sm + (tid / (4 * G)) * 4 * SL, tid % (4 * G), true, tw);
   // split: 2 X_a[k] = Z[k] + conj Z[N-k], 2 X_b[k] = -i (Z[k] - conj Z[N-k])
   TARA_ELEM_LOOP(e, RP * (H + 1), RC::THREADS) {
     const int k = e % (H + 1), pp = e / (H + 1);
