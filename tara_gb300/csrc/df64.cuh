@@ -81,4 +81,51 @@ struct __align__(16) df64c {
   df64 x, y;
 };
 
+// Conversions between double and df64 by integer operations on the bit
+// patterns: on GB300 every FP64-pipe instruction (including F2F conversions)
+// issues at 2 per SM per cycle, so the kernels that read the FP64 state split
+// it without touching that pipe.
+//
+// double -> df64: hi = the double truncated to 24 significant bits (exact),
+// lo = the remaining 29 bits rounded to 24, so hi + lo = d within 2^-48 |d|.
+// Magnitudes below 2^-126 become 0 (absolute error < 2^-126); lo is dropped
+// below 2^-74 (absolute error < 2^-98); infinities and NaNs map to FP32 ones.
+__device__ __forceinline__ df64 split_double(double d) {
+  const unsigned int hw = (unsigned int)__double2hiint(d), lw = (unsigned int)__double2loint(d);
+  const unsigned int sgn = hw & 0x80000000u;
+  const int e = (int)((hw >> 20) & 0x7ffu);  // biased double exponent
+  const unsigned int top = ((hw & 0xfffffu) << 3) | (lw >> 29);  // 23 mantissa bits after the leading 1
+  if (e > 1150) {  // beyond the FP32 range: infinity, or NaN (mantissa kept non-zero)
+    const unsigned int nan = (e == 2047 && ((hw & 0xfffffu) | lw)) ? 0x400000u : 0u;
+    return df64(__uint_as_float(sgn | 0x7f800000u | nan), 0.f);
+  }
+  if (e < 897) return df64(__uint_as_float(sgn), 0.f);
+  const float hi = __uint_as_float(sgn | ((unsigned int)(e - 896) << 23) | top);
+  float lo = 0.f;
+  if (e >= 949) {
+    const unsigned int m = lw & 0x1fffffffu;  // 29 bits below hi's last bit
+    // exact FP32 values of the two parts of m (each below 2^23) by the 2^23 bias trick
+    const float mh = __fsub_rn(__uint_as_float(0x4b000000u | (m >> 23)), 8388608.f);
+    const float ml = __fsub_rn(__uint_as_float(0x4b000000u | (m & 0x7fffffu)), 8388608.f);
+    const float fm = __fmaf_rn(mh, 8388608.f, ml);                        // m, rounded to 24 bits
+    const float scale = __uint_as_float((unsigned int)(e - 948) << 23);  // 2^(e - 1075)
+    lo = __uint_as_float(__float_as_uint(__fmul_rn(fm, scale)) | sgn);
+  }
+  return df64(hi, lo);
+}
+
+// FP32 value -> the bits of the equal double (exact), by integer operations.
+__device__ __forceinline__ double float_bits_to_double(float f) {
+  const unsigned int b = __float_as_uint(f);
+  const unsigned int sgn = b & 0x80000000u, ef = (b >> 23) & 0xffu, mf = b & 0x7fffffu;
+  if (ef == 0u) return __hiloint2double((int)sgn, 0);  // zero (subnormals flush to 0)
+  const unsigned int ed = ef == 0xffu ? 0x7ffu : ef + 896u;
+  return __hiloint2double((int)(sgn | (ed << 20) | (mf >> 3)), (int)(mf << 29));
+}
+
+// df64 -> double: both parts widened exactly, one FP64 add.
+__device__ __forceinline__ double to_double(df64 a) {
+  return float_bits_to_double(a.hi) + float_bits_to_double(a.lo);
+}
+
 }  // namespace tara

@@ -74,6 +74,7 @@ struct tara2d {
   void* nl = nullptr;  // x-r2c output of the products
   double *kx = nullptr, *ky = nullptr, *inv = nullptr;
   float* tabf = nullptr;  // kx, ky, inv in FP32 (nh + ny + nh*ny floats)
+  tara::df64* tabd = nullptr;  // kx, ky, inv in double-float (double-float mode only)
   int* i0 = nullptr;
   void *twx = nullptr, *twy = nullptr;
   double *diag_part = nullptr, *diag_out = nullptr;

@@ -39,6 +39,12 @@ namespace tara {
   _Pragma("unroll 4") for (int e##_i = 0; e##_i < ((TOTAL) + (THREADS)-1) / (THREADS); ++e##_i) \
     if (const int e = tid + e##_i * (THREADS); (TOTAL) % (THREADS) == 0 || e < (TOTAL))
 
+// A double is finite when its exponent field is not all ones (an integer test on
+// the high word, kept off the FP64 pipe).
+__device__ __forceinline__ bool finite_bits(double v) {
+  return ((unsigned int)__double2hiint(v) & 0x7ff00000u) != 0x7ff00000u;
+}
+
 struct Grid2D {
   int nx, ny, nh, pitch;
   const double* __restrict__ kx;   // [nh]
@@ -51,6 +57,11 @@ struct Grid2D {
   const float* __restrict__ kxf;
   const float* __restrict__ kyf;
   const float* __restrict__ invf;
+  // double-float copies of kx, ky, inv for the double-float mode, whose
+  // spectral products run on the FP32 pipes
+  const df64* __restrict__ kxd;
+  const df64* __restrict__ kyd;
+  const df64* __restrict__ invd;
 };
 
 enum StepMode {
@@ -68,7 +79,11 @@ struct RhsParams {
   double nl_scale;  // 1/2 (pair split) * 1/(Nx Ny)^2 (two unnormalised c2r)
   double dt;
   float nu_f, alpha_f, nl_scale_f;  // the same in FP32 for the FP32-transform mode
+  df64 nu_d, alpha_d, nl_scale_d;   // and in double-float for the double-float mode
 };
+
+template <typename T>
+constexpr bool is_df64() { return std::is_same<T, df64>::value; }
 
 // Largest power-of-two column tile with tile smem <= budget and <= 512 threads.
 __host__ __device__ constexpr int pick_tc(int bytes_per_col, int threads_per_col,
@@ -157,6 +172,26 @@ __global__ void __launch_bounds__(ColCfg<T, N, V>::THREADS_A)
           }
           fa = mkc<T>(-kx * di, kx * dr);
           fb = mkc<T>(-ky * di, ky * dr);
+        }
+      }
+    } else if constexpr (is_df64<T>()) {
+      if (x < g.nh) {  // double-float products from the FP64 state (FP32 pipes only)
+        const double2 wd = win[(size_t)y * g.pitch + x];
+        const df64 wx = split_double(wd.x), wy = split_double(wd.y);
+        const df64 kx = g.kxd[x], ky = g.kyd[y], inv = g.invd[(size_t)y * g.nh + x];
+        if (pair == 0) {
+          const df64 pr = wx * inv, pim = wy * inv;
+          fa = mkc<T>(-(ky * pim), ky * pr);
+          fb = mkc<T>(kx * pim, -(kx * pr));
+        } else {
+          df64 dr = wx, di = wy;
+          if (p.rhs) {
+            const df64 k2 = kx * kx + ky * ky;
+            dr = k2 * (wx * inv);
+            di = k2 * (wy * inv);
+          }
+          fa = mkc<T>(-(kx * di), kx * dr);
+          fb = mkc<T>(-(ky * di), ky * dr);
         }
       }
     } else if (x < g.nh) {
@@ -352,6 +387,30 @@ __global__ void __launch_bounds__(ColCfg<T, N, V>::THREADS_C)
         fr = (double)(-(p.alpha_f * nr + vk2 * (k2 * (wx * inv))));
         fi = (double)(-(p.alpha_f * ni + vk2 * (k2 * (wy * inv))));
       }
+    } else if constexpr (is_df64<T>()) {  // double-float right-hand side, one FP64 add to widen
+      df64 nr(0.f, 0.f), ni(0.f, 0.f);
+      if (x < g.i0[y]) {
+        const C v = sm[c * S + y];
+        nr = v.x * p.nl_scale_d;
+        ni = v.y * p.nl_scale_d;
+      }
+      const df64 kx = g.kxd[x], ky = g.kyd[y];
+      const df64 k2 = kx * kx + ky * ky;
+      const df64 vk2 = p.nu_d * k2;
+      const double2 wd = sb.win[q];
+      const df64 wx = split_double(wd.x), wy = split_double(wd.y);
+      df64 rr, ri;
+      if (p.rhs == 0) {
+        rr = -(nr + vk2 * wx);
+        ri = -(ni + vk2 * wy);
+      } else {
+        const df64 inv = g.invd[(size_t)y * g.nh + x];
+        rr = -(p.alpha_d * nr + vk2 * (k2 * (wx * inv)));
+        ri = -(p.alpha_d * ni + vk2 * (k2 * (wy * inv)));
+      }
+      bad |= !(isfinite(rr.hi) && isfinite(ri.hi));
+      fr = to_double(rr);
+      fi = to_double(ri);
     } else {
       double nr = 0.0, ni = 0.0;
       if (x < g.i0[y]) {  // 2/3 truncation of the nonlinear term only
@@ -373,13 +432,20 @@ __global__ void __launch_bounds__(ColCfg<T, N, V>::THREADS_C)
         fi = -(p.alpha * ni + vk2 * di);
       }
     }
-    if constexpr (sizeof(T) == 8) {
+    if constexpr (std::is_same<T, double>::value) {
       if (sb.force) {
         const double2 fc = sb.force[q];
         fr += fc.x;
         fi += fc.y;
       }
-      bad |= !(isfinite(fr) && isfinite(fi));
+      bad |= !(finite_bits(fr) && finite_bits(fi));
+    } else if constexpr (is_df64<T>()) {
+      if (sb.force) {
+        const double2 fc = sb.force[q];
+        fr += fc.x;
+        fi += fc.y;
+        bad |= !(finite_bits(fr) && finite_bits(fi));
+      }
     }
     frv[i] = (RT)fr;  // exact: an FP32 value in the FP32 form, unchanged in FP64
     fiv[i] = (RT)fi;
@@ -423,7 +489,7 @@ __global__ void __launch_bounds__(ColCfg<T, N, V>::THREADS_C)
           fr += fc.x;
           fi += fc.y;
         }
-        bad |= !(isfinite(fr) && isfinite(fi));
+        bad |= !(finite_bits(fr) && finite_bits(fi));
       }
       const double2 s = a0[u];
       switch (mode) {

@@ -182,6 +182,7 @@ extern "C" int tara_derive2csh_noalloc(int nx, int ny, double nu, const void* om
   p.alpha_f = 1.0f;
   p.nl_scale_f = (float)p.nl_scale;
   g.kxf = g.kyf = g.invf = nullptr;  // FP64 kernels only
+  g.kxd = g.kyd = g.invd = nullptr;
   StepBufs sb = {};
   sb.win = (const double2*)omegak_dev;
   sb.fout = (double2*)dt_omegak_dev;

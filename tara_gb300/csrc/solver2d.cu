@@ -339,6 +339,14 @@ int refresh_tables(tara2d* h) {
   for (size_t q = 0; q < inv.size(); ++q) tf[h->nh + h->ny + q] = (float)inv[q];
   TARA_CK(cudaMemcpyAsync(h->tabf, tf.data(), tf.size() * sizeof(float), cudaMemcpyHostToDevice,
                           h->stream));
+  std::vector<df64> td;
+  if (h->tabd) {  // round-to-nearest splits hi = fl32(v), lo = fl32(v - hi)
+    td.resize(tf.size());
+    for (int i = 0; i < h->nh; ++i) td[i] = df64(kx[i]);
+    for (int j = 0; j < h->ny; ++j) td[h->nh + j] = df64(ky[j]);
+    for (size_t q = 0; q < inv.size(); ++q) td[h->nh + h->ny + q] = df64(inv[q]);
+    TARA_CK(cudaMemcpyAsync(h->tabd, td.data(), td.size() * sizeof(df64), cudaMemcpyHostToDevice, h->stream));
+  }
   TARA_CK(cudaMemcpyAsync(h->kx, kx.data(), h->nh * sizeof(double), cudaMemcpyHostToDevice,
                           h->stream));
   TARA_CK(cudaMemcpyAsync(h->ky, ky.data(), h->ny * sizeof(double), cudaMemcpyHostToDevice,
@@ -348,6 +356,9 @@ int refresh_tables(tara2d* h) {
   h->grid.kxf = h->tabf;
   h->grid.kyf = h->tabf + h->nh;
   h->grid.invf = h->tabf + h->nh + h->ny;
+  h->grid.kxd = h->tabd;
+  h->grid.kyd = h->tabd ? h->tabd + h->nh : nullptr;
+  h->grid.invd = h->tabd ? h->tabd + h->nh + h->ny : nullptr;
   h->rp.rhs = h->cfg.rhs;
   h->rp.nu = h->cfg.nu;
   h->rp.alpha = h->cfg.alpha;
@@ -358,6 +369,9 @@ int refresh_tables(tara2d* h) {
   h->rp.nu_f = (float)h->rp.nu;
   h->rp.alpha_f = (float)h->rp.alpha;
   h->rp.nl_scale_f = (float)h->rp.nl_scale;
+  h->rp.nu_d = df64(h->rp.nu);
+  h->rp.alpha_d = df64(h->rp.alpha);
+  h->rp.nl_scale_d = df64(h->rp.nl_scale);
   return TARA_OK;
 }
 
@@ -432,7 +446,7 @@ int tara2d_destroy(tara2d* h) {
   cudaSetDevice(h->dev);
   if (h->stream) cudaStreamSynchronize(h->stream);
   void* ptrs[] = {h->w0, h->ws, h->acc, h->fold, h->fout, h->u, h->nl, h->kx, h->ky, h->i0, h->inv, h->tabf,
-                  h->twx, h->twy, h->diag_part, h->diag_out, h->flag, h->scratch, h->twx64, h->twy64};
+                  h->tabd, h->twx, h->twy, h->diag_part, h->diag_out, h->flag, h->scratch, h->twx64, h->twy64};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (h->stream) cudaStreamDestroy(h->stream);
@@ -493,6 +507,8 @@ int tara2d_create(const tara2d_config* cfg, tara2d** out) {
   CKC(cudaMalloc(&h->i0, h->ny * sizeof(int)));
   CKC(cudaMalloc(&h->inv, (size_t)h->ny * h->nh * sizeof(double)));
   CKC(cudaMalloc(&h->tabf, ((size_t)h->ny * h->nh + h->nh + h->ny) * sizeof(float)));
+  if (cfg->precision == TARA_PREC_DF64)
+    CKC(cudaMalloc(&h->tabd, ((size_t)h->ny * h->nh + h->nh + h->ny) * sizeof(df64)));
   CKC(cudaMalloc(&h->diag_part, 2 * kDiagBlocks * sizeof(double)));
   CKC(cudaMalloc(&h->diag_out, 4 * sizeof(double)));
   CKC(cudaMalloc(&h->flag, sizeof(unsigned int)));

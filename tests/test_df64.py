@@ -99,3 +99,29 @@ def test_df64_ensemble_equals_single_runs():
             s.step(7)
             ref = s.get_state()
         assert np.array_equal(got[r], ref), r
+
+
+@pytest.mark.parametrize("value", [np.nan, np.inf])
+def test_df64_nonfinite_state_is_reported(golden, value):
+    w = golden["ic_spec"].copy()
+    w[3, 4] = value
+    with tg.Solver2D(64, precision=DF) as s:
+        s.set_state(w)
+        s.step(1)
+        with pytest.raises(tg.TaraError) as e:
+            s.synchronize()
+        assert e.value.code == tg.TARA_ERR_NONFINITE
+
+
+def test_df64_tiny_and_huge_spectra(oracle):
+    """States scaled by 1e-10 and 1e+10 keep the FP64 bars.  (The double-float
+    form has FP32's exponent range: the unnormalised products, about
+    N^4 |u| |grad w|, must stay below 3e38, and parts below 2^-126 flush.)"""
+    w0 = oracle.ic_random(64, 64, 6.0, 0.5, 4200)
+    for scale in (1e-10, 1e10):
+        ref, _ = oracle.run(w0 * scale, rhs=0, scheme=1, nu=1e-3, dt=1e-4 / max(1.0, scale), steps=3)
+        with tg.Solver2D(64, scheme=tg.SCHEME_RK4, nu=1e-3, dt=1e-4 / max(1.0, scale), precision=DF) as s:
+            s.set_state(w0 * scale)
+            s.step(3)
+            w = s.get_state()
+        assert rel_l2(w, ref) < 1e-12, scale
