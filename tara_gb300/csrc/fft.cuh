@@ -94,6 +94,71 @@ __device__ __forceinline__ void dft4_tw(C& v0, C& v1, C& v2, C& v3, const C w1, 
   }
 }
 
+// Radix-2 butterfly x = a + w c, y = a - w c (two-sided FMA form).
+template <typename C>
+__device__ __forceinline__ void bfly2_tw(const C a, const C c, const C w, C& x, C& y) {
+  typedef decltype(a.x) T;
+  x.x = fma(c.x, w.x, fma(-c.y, w.y, a.x));
+  x.y = fma(c.x, w.y, fma(c.y, w.x, a.y));
+  y.x = fma(T(2), a.x, -x.x);
+  y.y = fma(T(2), a.y, -x.y);
+}
+
+// Double-float butterflies: the same dataflow with unnormalised intermediate
+// sums and products (add_u, mul_u) and one renormalisation per output.
+template <bool INV>
+__device__ __forceinline__ void dft4(df64c& v0, df64c& v1, df64c& v2, df64c& v3) {
+  const df64 a0r = add_u(v0.x, v2.x), a0i = add_u(v0.y, v2.y);
+  const df64 a1r = sub_u(v0.x, v2.x), a1i = sub_u(v0.y, v2.y);
+  const df64 a2r = add_u(v1.x, v3.x), a2i = add_u(v1.y, v3.y);
+  const df64 a3r = sub_u(v1.x, v3.x), a3i = sub_u(v1.y, v3.y);
+  v0.x = renorm(add_u(a0r, a2r)); v0.y = renorm(add_u(a0i, a2i));
+  v2.x = renorm(sub_u(a0r, a2r)); v2.y = renorm(sub_u(a0i, a2i));
+  if (!INV) {
+    v1.x = renorm(add_u(a1r, a3i)); v1.y = renorm(sub_u(a1i, a3r));
+    v3.x = renorm(sub_u(a1r, a3i)); v3.y = renorm(add_u(a1i, a3r));
+  } else {
+    v1.x = renorm(sub_u(a1r, a3i)); v1.y = renorm(add_u(a1i, a3r));
+    v3.x = renorm(add_u(a1r, a3i)); v3.y = renorm(sub_u(a1i, a3r));
+  }
+}
+
+__device__ __forceinline__ void cmul_u(const df64c v, const df64c w, df64& r, df64& i) {
+  r = sub_u(mul_u(v.x, w.x), mul_u(v.y, w.y));
+  i = add_u(mul_u(v.x, w.y), mul_u(v.y, w.x));
+}
+
+template <bool INV>
+__device__ __forceinline__ void dft4_tw(df64c& v0, df64c& v1, df64c& v2, df64c& v3, const df64c w1,
+                                        const df64c w2, const df64c w3) {
+  df64 cr, ci, t1r, t1i, t3r, t3i;
+  cmul_u(v2, w2, cr, ci);
+  cmul_u(v1, w1, t1r, t1i);
+  cmul_u(v3, w3, t3r, t3i);
+  const df64 a0r = add_u(v0.x, cr), a0i = add_u(v0.y, ci);
+  const df64 a1r = sub_u(v0.x, cr), a1i = sub_u(v0.y, ci);
+  const df64 a2r = add_u(t1r, t3r), a2i = add_u(t1i, t3i);
+  const df64 a3r = sub_u(t1r, t3r), a3i = sub_u(t1i, t3i);
+  v0.x = renorm(add_u(a0r, a2r)); v0.y = renorm(add_u(a0i, a2i));
+  v2.x = renorm(sub_u(a0r, a2r)); v2.y = renorm(sub_u(a0i, a2i));
+  if (!INV) {
+    v1.x = renorm(add_u(a1r, a3i)); v1.y = renorm(sub_u(a1i, a3r));
+    v3.x = renorm(sub_u(a1r, a3i)); v3.y = renorm(add_u(a1i, a3r));
+  } else {
+    v1.x = renorm(sub_u(a1r, a3i)); v1.y = renorm(add_u(a1i, a3r));
+    v3.x = renorm(add_u(a1r, a3i)); v3.y = renorm(sub_u(a1i, a3r));
+  }
+}
+
+__device__ __forceinline__ void bfly2_tw(const df64c a, const df64c c, const df64c w, df64c& x, df64c& y) {
+  df64 tr, ti;
+  cmul_u(c, w, tr, ti);
+  x.x = renorm(add_u(a.x, tr));
+  x.y = renorm(add_u(a.y, ti));
+  y.x = renorm(sub_u(a.x, tr));
+  y.y = renorm(sub_u(a.y, ti));
+}
+
 template <bool INV, typename C>
 __device__ __forceinline__ C load_tw(const C* __restrict__ tw, int m) {
   C w = __ldg(tw + m);
@@ -167,10 +232,10 @@ __device__ __forceinline__ void fft_slot(typename cplx_of<T>::type* buf, int lan
         const int j = lane + b * G;
         const C a = buf[j], c = buf[j + H];
         const C w = load_tw<INV>(tw, j);
-        const T xr = fma(c.x, w.x, fma(-c.y, w.y, a.x));
-        const T xi = fma(c.x, w.y, fma(c.y, w.x, a.y));
-        buf[j] = mkc<T>(xr, xi);
-        buf[j + H] = mkc<T>(fma(T(2), a.x, -xr), fma(T(2), a.y, -xi));
+        C x, y;
+        bfly2_tw(a, c, w, x, y);
+        buf[j] = x;
+        buf[j + H] = y;
       }
     }
     __syncthreads();
