@@ -446,7 +446,7 @@ def run_closure(args) -> None:
                                "mean_per_sample_plain_coarse": ev["mean_err_plain"], "shells": ev["kmax"],
                                "fallback": ev["fallback"]},
             "a_priori": out["train"]["val"], "alpha": out["alpha"], "nu_e": out["nu_e"],
-            "calibration": ({k: out["calibration"][k] for k in ("err_avg", "best", "best_nu", "seed", "runs")}
+            "calibration": ({k: out["calibration"][k] for k in ("err_avg", "fallback", "best", "best_nu", "seed", "runs")}
                             if "calibration" in out else None),
             "energy_first_last": {k: [v[0], v[-1]] for k, v in ev["energy"].items()},
             "throughput": tp, "train": {k: out["train"][k] for k in ("train_steps", "wall_s", "best_epoch")},
