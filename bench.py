@@ -287,7 +287,9 @@ def run_ours(args) -> None:
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "avg_launch_ms": avg_ms,
                      "limiter": ("FP64 pipe (GB300: 2 FP64 thread-instructions per SM per cycle)"
-                                 if prec == tg.PREC_FP64 else "FP32 issue (profiled for the FP64 form only)"),
+                                 if prec == tg.PREC_FP64 else
+                                 "FP32 pipes and global-load latency (double-float: profiles/rhs2d_df64_2048_ncu_full.md)"
+                                 if prec == tg.PREC_DF64 else "FP32 pipes and shared-memory bank conflicts"),
                      "fp64_pipe_busy_pct_ncu": (from_profiles("fp64_pipe_busy_pct", dom, n)
                                                 if prec == tg.PREC_FP64 else None),
                      "per_kernel_ms": {k: v["ms"] / max(1, v["launches"]) for k, v in ks.items()}},
