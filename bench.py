@@ -187,6 +187,39 @@ def run_reference(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def fft_fp64_inst(n: int) -> int:
+    """FP64 instructions of one length-n transform of fft.cuh, counted from its
+    butterflies: an untwiddled radix-4 first stage (16 adds per butterfly),
+    twiddled radix-4 stages (24 per butterfly) and, for odd log2 n, a twiddled
+    radix-2 stage (6 per butterfly)."""
+    lg = n.bit_length() - 1
+    q = n // 4
+    return q * 16 + q * 24 * (lg // 2 - 1) + ((n // 2) * 6 if lg % 2 else 0)
+
+
+def fp64_pipe(n: int, per_kernel_ms: dict, sm_mhz, probe_tinst) -> dict:
+    """FP64-pipe roofline of the three kernels at n x n: the transforms' FP64
+    instructions per launch (element work excluded, so the fractions are lower
+    bounds) over the measured launch time, against the nominal rate (2 FP64
+    thread-instructions per SM per cycle at the sampled SM clock) and the DFMA
+    rate measured by tara_measure_dfma_rate."""
+    import math
+
+    import torch
+    nh = n // 2 + 1
+    live = math.ceil((n + n) / 2.0 / 3.0)  # columns below the 2/3 cut (integer wavenumbers)
+    f = fft_fp64_inst(n)
+    inst = {"k_col_inverse": 4 * nh * f, "k_row_nl": (n // 2) * 5 * f, "k_col_forward": live * f}
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    nominal = 2.0 * sms * (sm_mhz or 2070.0) * 1e6
+    ach = {k: inst[k] / (per_kernel_ms[k] * 1e-3) for k in inst if k in per_kernel_ms}
+    return {"inst_per_launch": inst, "achieved_inst_per_s": ach, "nominal_inst_per_s": nominal,
+            "measured_dfma_inst_per_s": probe_tinst,
+            "frac_of_nominal": {k: v / nominal for k, v in ach.items()},
+            "frac_of_measured_dfma": {k: v / probe_tinst for k, v in ach.items()} if probe_tinst else None,
+            "count": "transform butterflies only; element work excluded (fractions are lower bounds)"}
+
+
 def run_ours(args) -> None:
     import numpy as np
     import torch
@@ -201,6 +234,7 @@ def run_ours(args) -> None:
     s = tg.Solver2D(n, scheme=tg.SCHEME_RK4, nu=NU, dt=DT, precision=prec)
     s.init_random(K0, ENERGY, SEED.get(n, 1))
     tuned = s.autotune(2)  # tile variant per kernel (the state is restored)
+    dfma_rate = tg.measure_dfma_rate(5) if prec == tg.PREC_FP64 and rank == 0 else None
     s.step(args.warmup)
     s.synchronize()
 
@@ -294,6 +328,8 @@ def run_ours(args) -> None:
                                                 if prec == tg.PREC_FP64 else None),
                      "per_kernel_ms": {k: v["ms"] / max(1, v["launches"]) for k, v in ks.items()}},
         "clocks": clocks,
+        "fp64_pipe": (fp64_pipe(n, {k: v["ms"] / max(1, v["launches"]) for k, v in ks.items()},
+                                (clocks or {}).get("sm_mhz"), dfma_rate) if prec == tg.PREC_FP64 else None),
         "tile_variants": tuned["variants"],
         "diag": {"energy": e, "enstrophy": z},
         "cpu_baseline": cpu,

@@ -461,6 +461,12 @@ int tara_closure_step(tara_closure* c, int nsteps);
 int tara_derive2csh_noalloc(int nx, int ny, double nu, const void* omegak_dev,
                             void* dt_omegak_dev, void* stream);
 
+/* Measured FP64 FMA throughput of the current device in thread-instructions
+ * per second: one kernel of independent DFMA chains filling every SM, timed with
+ * CUDA events over `reps` launches after a warm-up launch (about 20 ms each).
+ * The measured denominator of the FP64-pipe roofline. */
+int tara_measure_dfma_rate(int reps, double* inst_per_s);
+
 /* Library version string. */
 const char* tara_version(void);
 

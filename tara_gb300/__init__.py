@@ -298,6 +298,13 @@ def set_css_params(lx: float, ly: float, lam: float) -> None:
     lib().tara_set_css_params(lx, ly, lam)
 
 
+def measure_dfma_rate(reps: int = 5) -> float:
+    """FP64 FMA thread-instructions per second measured on the current device."""
+    v = ctypes.c_double()
+    _check(lib().tara_measure_dfma_rate(int(reps), ctypes.byref(v)))
+    return v.value
+
+
 def fft2d_r2c(x: np.ndarray, precision: int = PREC_FP64) -> np.ndarray:
     """Unnormalised r2c of a real (Ny, Nx) field -> (Ny, Nh) complex (FFTW semantics)."""
     x = np.ascontiguousarray(x, dtype=np.float64)

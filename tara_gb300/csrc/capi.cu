@@ -210,6 +210,54 @@ void rk42css_(const int* Nx, const int* Ny, const int* Nh, const double* alpha, 
 
 // ---- standalone transforms (FFTW rank-2 semantics, unnormalised) ----------
 // in: real (Nx,Ny) x-fastest; out: complex (Nh,Ny) interleaved.
+// Eight independent FMA chains per thread; the store happens only for a value
+// the chains never reach, but depends on all of them, so none is removed.
+__global__ void __launch_bounds__(256) k_dfma_probe(double* out, int iters, double b, double c) {
+  double a[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) a[k] = 1.0 + 1e-3 * k + 1e-9 * threadIdx.x;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) a[k] = fma(a[k], b, c);
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) s += a[k];
+  if (s == -1.0) out[0] = s;
+}
+
+int tara_measure_dfma_rate(int reps, double* inst_per_s) {
+  if (!inst_per_s || reps < 1) return set_error(TARA_ERR_ARGS, "bad argument");
+  int dev, sms;
+  TARA_CK(cudaGetDevice(&dev));
+  TARA_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int blocks = sms * 8, threads = 256, iters = 4096;
+  double* out = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaStream_t s = nullptr;
+  auto done = [&](int rc) {
+    if (s) cudaStreamSynchronize(s);
+    cudaFree(out);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (s) cudaStreamDestroy(s);
+    return rc;
+  };
+  if (cudaMalloc(&out, sizeof(double)) != cudaSuccess || cudaEventCreate(&e0) != cudaSuccess ||
+      cudaEventCreate(&e1) != cudaSuccess || cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess)
+    return done(set_error(TARA_ERR_CUDA, "probe setup"));
+  k_dfma_probe<<<blocks, threads, 0, s>>>(out, iters, 0.9999999, 1e-7);
+  cudaEventRecord(e0, s);
+  for (int r = 0; r < reps; ++r) k_dfma_probe<<<blocks, threads, 0, s>>>(out, iters, 0.9999999, 1e-7);
+  cudaEventRecord(e1, s);
+  cudaError_t e = cudaEventSynchronize(e1);
+  if (e != cudaSuccess) return done(cuda_fail(e, "dfma probe"));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  *inst_per_s = (double)blocks * threads * iters * 8.0 * reps / (ms * 1e-3);
+  return done(set_ok());
+}
+
 int tara_fft2d_r2c(int nx, int ny, int precision, const double* in, double* out) {
   if (!is_pow2_in_range(nx) || !is_pow2_in_range(ny) || !in || !out)
     return set_error(TARA_ERR_ARGS, "bad transform arguments");
