@@ -135,8 +135,11 @@ template <typename T, int N, int V = 0> struct RowCfg {
 // blockIdx.y = 0: (u_x, u_y); blockIdx.y = 1: (i kx w, i ky w).  Splitting the
 // two field pairs over the grid halves the tail of the last wave.
 // blockIdx.z = run of a batch (runs are ny*pitch apart in every field).
+// The double-float form asks for three 256-thread CTAs per SM (80 registers,
+// a little spill): its prologue waits on strided loads, which a third CTA hides
+// (measured 255 -> 240 us at 2048^2); the FP64 form gains nothing from it.
 template <typename T, int N, int V>
-__global__ void __launch_bounds__(ColCfg<T, N, V>::THREADS_A)
+__global__ void __launch_bounds__(ColCfg<T, N, V>::THREADS_A, (is_df64<T>() && ColCfg<T, N, V>::THREADS_A == 256) ? 3 : 1)
     k_col_inverse(const double2* __restrict__ win, typename cplx_of<T>::type* __restrict__ u,
                   Grid2D g, RhsParams p, const typename cplx_of<T>::type* __restrict__ tw) {
   typedef typename cplx_of<T>::type C;
