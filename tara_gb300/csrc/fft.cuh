@@ -159,19 +159,20 @@ __device__ __forceinline__ void bfly2_tw(const df64c a, const df64c c, const df6
   y.y = renorm(sub_u(a.y, ti));
 }
 
-template <bool INV, typename C>
+// Twiddle W^m of a length-N table, conjugated for the inverse transform.  The
+// tables hold tw[N - m] = conj(tw[m]) exactly, so the conjugate is a load at
+// the mirrored index and costs no arithmetic.
+template <bool INV, int N, typename C>
 __device__ __forceinline__ C load_tw(const C* __restrict__ tw, int m) {
-  C w = __ldg(tw + m);
-  if (INV) w.y = -w.y;
-  return w;
+  return __ldg(tw + (INV ? ((N - m) & (N - 1)) : m));
 }
 
-template <bool INV>
+template <bool INV, int N>
 __device__ __forceinline__ df64c load_tw(const df64c* __restrict__ tw, int m) {
-  const float4 v = __ldg(reinterpret_cast<const float4*>(tw) + m);
+  const float4 v = __ldg(reinterpret_cast<const float4*>(tw) + (INV ? ((N - m) & (N - 1)) : m));
   df64c w;
   w.x = df64(v.x, v.y);
-  w.y = INV ? df64(-v.z, -v.w) : df64(v.z, v.w);
+  w.y = df64(v.z, v.w);
   return w;
 }
 
@@ -210,9 +211,9 @@ __device__ __forceinline__ void fft_slot(typename cplx_of<T>::type* buf, int lan
           dft4<INV>(v[b][0], v[b][1], v[b][2], v[b][3]);
         } else {
           const int step = k * (N / (4 * Ns));
-          const C w1 = load_tw<INV>(tw, step);
-          const C w2 = load_tw<INV>(tw, 2 * step);
-          const C w3 = load_tw<INV>(tw, 3 * step);
+          const C w1 = load_tw<INV, N>(tw, step);
+          const C w2 = load_tw<INV, N>(tw, 2 * step);
+          const C w3 = load_tw<INV, N>(tw, 3 * step);
           dft4_tw<INV>(v[b][0], v[b][1], v[b][2], v[b][3], w1, w2, w3);
         }
         const int base = ((j - k) << 2) + k;
@@ -231,7 +232,7 @@ __device__ __forceinline__ void fft_slot(typename cplx_of<T>::type* buf, int lan
       for (int b = 0; b < B2; ++b) {
         const int j = lane + b * G;
         const C a = buf[j], c = buf[j + H];
-        const C w = load_tw<INV>(tw, j);
+        const C w = load_tw<INV, N>(tw, j);
         C x, y;
         bfly2_tw(a, c, w, x, y);
         buf[j] = x;

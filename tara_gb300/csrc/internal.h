@@ -55,6 +55,8 @@ struct Launch2D {
                      const void* twx, cudaStream_t s, int nf = 1, size_t fs_in = 0, size_t fs_out = 0);
 };
 
+// Twiddle exp(-2 pi i m/n) in FP64 with tw[n - m] = conj(tw[m]) exactly.
+void twiddle(int n, int m, double* re, double* im);
 // Twiddle table exp(-2 pi i m/n), m < n, in precision T, uploaded to device.
 int make_twiddles(int n, bool fp32, void** dev);
 // The same table as double-float (hi, lo) pairs: float4 {re.hi, re.lo, im.hi, im.lo}.

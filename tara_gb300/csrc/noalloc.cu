@@ -113,11 +113,11 @@ static int noalloc_setup(unsigned char** out) {
     cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
     double2 tw[kTwElems];
-    const long double tp = 6.283185307179586476925286766559005768L;
     for (int n = 16; n <= kNoAllocMaxN; n *= 2)
       for (int m = 0; m < n; ++m) {
-        const long double a = tp * (long double)m / (long double)n;
-        tw[tw_offset(n) + m] = make_double2((double)std::cos(a), (double)-std::sin(a));
+        double c, sn;
+        twiddle(n, m, &c, &sn);
+        tw[tw_offset(n) + m] = make_double2(c, sn);
       }
     e = cudaMemcpy((unsigned char*)p + kOffTw, tw, sizeof(tw), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(twiddles)");

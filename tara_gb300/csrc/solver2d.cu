@@ -69,21 +69,44 @@ void make_inverse_table(int nx, int ny, const double* kx, const double* ky, bool
     }
 }
 
-int make_twiddles(int n, bool fp32, void** dev) {
+void twiddle(int n, int m, double* re, double* im) {
+  // exp(-2 pi i m/n) from long-double cos/sin on [0, n/2]; the quarter points
+  // exact, and tw[n - m] = conj(tw[m]) exactly, so that an inverse transform
+  // reads its conjugate twiddle by index instead of negating it
   const long double tp = 6.283185307179586476925286766559005768L;
+  const int r = m <= n / 2 ? m : n - m;
+  double c, s;
+  if (4 * r == n) {
+    c = 0.0;
+    s = -1.0;
+  } else if (r == 0 || 2 * r == n) {
+    c = r == 0 ? 1.0 : -1.0;
+    s = 0.0;
+  } else {
+    const long double a = tp * (long double)r / (long double)n;
+    c = (double)std::cos(a);
+    s = (double)-std::sin(a);
+  }
+  *re = c;
+  *im = m <= n / 2 ? s : -s;
+}
+
+int make_twiddles(int n, bool fp32, void** dev) {
   if (fp32) {
     std::vector<float2> w(n);
     for (int m = 0; m < n; ++m) {
-      const long double a = tp * (long double)m / (long double)n;
-      w[m] = make_float2((float)std::cos(a), (float)-std::sin(a));
+      double c, s;
+      twiddle(n, m, &c, &s);
+      w[m] = make_float2((float)c, (float)s);
     }
     TARA_CK(cudaMalloc(dev, n * sizeof(float2)));
     TARA_CK(cudaMemcpy(*dev, w.data(), n * sizeof(float2), cudaMemcpyHostToDevice));
   } else {
     std::vector<double2> w(n);
     for (int m = 0; m < n; ++m) {
-      const long double a = tp * (long double)m / (long double)n;
-      w[m] = make_double2((double)std::cos(a), (double)-std::sin(a));
+      double c, s;
+      twiddle(n, m, &c, &s);
+      w[m] = make_double2(c, s);
     }
     TARA_CK(cudaMalloc(dev, n * sizeof(double2)));
     TARA_CK(cudaMemcpy(*dev, w.data(), n * sizeof(double2), cudaMemcpyHostToDevice));
@@ -94,11 +117,10 @@ int make_twiddles(int n, bool fp32, void** dev) {
 // The same table as double-float pairs (hi, lo) per component, for the
 // double-float transforms: hi = fl32(w), lo = fl32(w - hi).
 int make_twiddles_df64(int n, void** dev) {
-  const long double tp = 6.283185307179586476925286766559005768L;
   std::vector<float4> w(n);
   for (int m = 0; m < n; ++m) {
-    const long double a = tp * (long double)m / (long double)n;
-    const double c = (double)std::cos(a), s = (double)-std::sin(a);
+    double c, s;
+    twiddle(n, m, &c, &s);
     const float ch = (float)c, sh = (float)s;
     w[m] = make_float4(ch, (float)(c - (double)ch), sh, (float)(s - (double)sh));
   }
