@@ -160,11 +160,19 @@ __device__ __forceinline__ void bfly2_tw(const df64c a, const df64c c, const df6
 }
 
 // Twiddle W^m of a length-N table, conjugated for the inverse transform.  The
-// tables hold tw[N - m] = conj(tw[m]) exactly, so the conjugate is a load at
-// the mirrored index and costs no arithmetic.
+// tables hold tw[N - m] = conj(tw[m]) exactly, so for FP64 the conjugate is a
+// load at the mirrored index (a negation would be one more FP64-pipe
+// instruction); an FP32 negation is free and the FP32 form measured faster
+// reading the plain index.
 template <bool INV, int N, typename C>
 __device__ __forceinline__ C load_tw(const C* __restrict__ tw, int m) {
-  return __ldg(tw + (INV ? ((N - m) & (N - 1)) : m));
+  if constexpr (sizeof(C) == 8) {
+    C w = __ldg(tw + m);
+    if (INV) w.y = -w.y;
+    return w;
+  } else {
+    return __ldg(tw + (INV ? ((N - m) & (N - 1)) : m));
+  }
 }
 
 template <bool INV, int N>

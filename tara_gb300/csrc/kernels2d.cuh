@@ -137,9 +137,14 @@ template <typename T, int N, int V = 0> struct RowCfg {
 // blockIdx.z = run of a batch (runs are ny*pitch apart in every field).
 // The double-float form asks for three 256-thread CTAs per SM (80 registers,
 // a little spill): its prologue waits on strided loads, which a third CTA hides
-// (measured 255 -> 240 us at 2048^2); the FP64 form gains nothing from it.
+// (measured 255 -> 240 us at 2048^2); the FP64 form gains nothing from it.  The
+// FP32 form keeps two 512-thread CTAs per SM (64 registers; at 80 registers one
+// CTA per SM took 113 instead of 95 us at 2048^2).
 template <typename T, int N, int V>
-__global__ void __launch_bounds__(ColCfg<T, N, V>::THREADS_A, (is_df64<T>() && ColCfg<T, N, V>::THREADS_A == 256) ? 3 : 1)
+__global__ void __launch_bounds__(ColCfg<T, N, V>::THREADS_A,
+                                  (is_df64<T>() && ColCfg<T, N, V>::THREADS_A == 256)       ? 3
+                                  : (sizeof(T) == 4 && ColCfg<T, N, V>::THREADS_A == 512) ? 2
+                                                                                          : 1)
     k_col_inverse(const double2* __restrict__ win, typename cplx_of<T>::type* __restrict__ u,
                   Grid2D g, RhsParams p, const typename cplx_of<T>::type* __restrict__ tw) {
   typedef typename cplx_of<T>::type C;
