@@ -47,6 +47,17 @@ __host__ __device__ constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c
 // threads per transform of length N
 __host__ __device__ constexpr int fft_group(int n) { return n >= 16 ? n / 16 : 1; }
 
+// Twiddle table of a length-n transform (LG = log2 n, LG/2 radix-4 stages):
+//   [0, n)           W^m = exp(-2 pi i m/n), with tw[n - m] = conj(tw[m]) exactly
+//   [n, n + S)       forward stage tables
+//   [n + S, n + 2S)  inverse stage tables (the same, conjugated), S = 4^(LG/2) - 4
+// The twiddled radix-4 stage s (Ns = 4^s, 1 <= s < LG/2) owns entries
+// [Ns - 4, 4 Ns - 4) of each direction's stage tables: W^(r k n/(4 Ns)) at
+// [(r - 1) Ns + k] for r = 1, 2, 3 and k < Ns, so the lanes of a warp (consecutive
+// k) read consecutive entries.
+__host__ __device__ constexpr int tw_stage_span(int n) { return (1 << (2 * (ilog2c(n) / 2))) - 4; }
+__host__ __device__ constexpr int tw_count(int n) { return n + 2 * tw_stage_span(n); }
+
 // Untwiddled radix-4 DFT (first stage).  Forward: y1 = a1 - i a3, y3 = a1 + i a3.
 template <bool INV, typename C>
 __device__ __forceinline__ void dft4(C& v0, C& v1, C& v2, C& v3) {
@@ -164,6 +175,19 @@ __device__ __forceinline__ void bfly2_tw(const df64c a, const df64c c, const df6
 // load at the mirrored index (a negation would be one more FP64-pipe
 // instruction); an FP32 negation is free and the FP32 form measured faster
 // reading the plain index.
+template <typename C>
+__device__ __forceinline__ C load_tw_raw(const C* __restrict__ tw, int i) {
+  return __ldg(tw + i);
+}
+
+__device__ __forceinline__ df64c load_tw_raw(const df64c* __restrict__ tw, int i) {
+  const float4 v = __ldg(reinterpret_cast<const float4*>(tw) + i);
+  df64c w;
+  w.x = df64(v.x, v.y);
+  w.y = df64(v.z, v.w);
+  return w;
+}
+
 template <bool INV, int N, typename C>
 __device__ __forceinline__ C load_tw(const C* __restrict__ tw, int m) {
   if constexpr (sizeof(C) == 8) {
@@ -184,7 +208,8 @@ __device__ __forceinline__ df64c load_tw(const df64c* __restrict__ tw, int m) {
   return w;
 }
 
-// In-place length-N transform of buf (unnormalised).  tw[m] = exp(-2 pi i m/N).
+// In-place length-N transform of buf (unnormalised); tw is the length-N twiddle
+// table described above (tw_count(N) entries).
 // Forward: X[k] = sum x[n] e^{-2 pi i nk/N}; inverse uses e^{+...}.
 // G threads share the transform (default N/16; up to N/4, one butterfly each).
 template <typename T, int N, bool INV, int G = fft_group(N)>
@@ -218,10 +243,11 @@ __device__ __forceinline__ void fft_slot(typename cplx_of<T>::type* buf, int lan
         if (s == 0) {
           dft4<INV>(v[b][0], v[b][1], v[b][2], v[b][3]);
         } else {
-          const int step = k * (N / (4 * Ns));
-          const C w1 = load_tw<INV, N>(tw, step);
-          const C w2 = load_tw<INV, N>(tw, 2 * step);
-          const C w3 = load_tw<INV, N>(tw, 3 * step);
+          // this stage's table, already conjugated for the inverse
+          const C* ts = tw + N + (INV ? tw_stage_span(N) : 0) + (Ns - 4);
+          const C w1 = load_tw_raw(ts, k);
+          const C w2 = load_tw_raw(ts, Ns + k);
+          const C w3 = load_tw_raw(ts, 2 * Ns + k);
           dft4_tw<INV>(v[b][0], v[b][1], v[b][2], v[b][3], w1, w2, w3);
         }
         const int base = ((j - k) << 2) + k;

@@ -57,6 +57,8 @@ struct Launch2D {
 
 // Twiddle exp(-2 pi i m/n) in FP64 with tw[n - m] = conj(tw[m]) exactly.
 void twiddle(int n, int m, double* re, double* im);
+// Entry idx < tw_count(n) of the length-n twiddle table (layout in fft.cuh).
+void twiddle_entry(int n, int idx, double* re, double* im);
 // Twiddle table exp(-2 pi i m/n), m < n, in precision T, uploaded to device.
 int make_twiddles(int n, bool fp32, void** dev);
 // The same table as double-float (hi, lo) pairs: float4 {re.hi, re.lo, im.hi, im.lo}.

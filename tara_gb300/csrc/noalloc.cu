@@ -41,7 +41,8 @@ namespace {
 constexpr int kNoAllocMaxN = 256;
 constexpr int kNhMax = kNoAllocMaxN / 2 + 1;
 constexpr size_t kFieldElems = (size_t)kNoAllocMaxN * kNhMax;  // dense [Ny][Nh] at the maximum
-constexpr int kTwElems = 16 + 32 + 64 + 128 + 256;            // twiddles for N = 16..256
+using tara::tw_count;
+constexpr int kTwElems = tw_count(16) + tw_count(32) + tw_count(64) + tw_count(128) + tw_count(256);
 
 constexpr size_t align256(size_t b) { return (b + 255) / 256 * 256; }
 constexpr size_t kOffU = 0;
@@ -54,8 +55,9 @@ constexpr size_t kOffInv = kOffI0 + align256(kNoAllocMaxN * sizeof(int));
 constexpr size_t kOffFlag = kOffInv + align256(kFieldElems * sizeof(double));
 constexpr size_t kScratchBytes = kOffFlag + 256;
 
-// offset of the length-n twiddle table inside the twiddle region
-constexpr int tw_offset(int n) { return n - 16; }
+// offset of the length-n twiddle table inside the twiddle region (tables for
+// 16, 32, ... n/2 precede it)
+constexpr int tw_offset(int n) { return n <= 16 ? 0 : tw_offset(n / 2) + tw_count(n / 2); }
 
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_mu;
@@ -114,9 +116,9 @@ static int noalloc_setup(unsigned char** out) {
     if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
     double2 tw[kTwElems];
     for (int n = 16; n <= kNoAllocMaxN; n *= 2)
-      for (int m = 0; m < n; ++m) {
+      for (int m = 0; m < tw_count(n); ++m) {
         double c, sn;
-        twiddle(n, m, &c, &sn);
+        twiddle_entry(n, m, &c, &sn);
         tw[tw_offset(n) + m] = make_double2(c, sn);
       }
     e = cudaMemcpy((unsigned char*)p + kOffTw, tw, sizeof(tw), cudaMemcpyHostToDevice);

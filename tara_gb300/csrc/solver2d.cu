@@ -91,25 +91,43 @@ void twiddle(int n, int m, double* re, double* im) {
   *im = m <= n / 2 ? s : -s;
 }
 
+void twiddle_entry(int n, int idx, double* re, double* im) {
+  if (idx < n) {
+    twiddle(n, idx, re, im);
+    return;
+  }
+  int t = idx - n;
+  const int span = tw_stage_span(n);
+  const bool inv = t >= span;
+  if (inv) t -= span;
+  int ns = 4;  // stage s owns [Ns - 4, 4 Ns - 4)
+  while (4 * ns - 4 <= t) ns *= 4;
+  const int off = t - (ns - 4);
+  const int r = off / ns + 1, k = off % ns;
+  twiddle(n, r * k * (n / (4 * ns)), re, im);
+  if (inv) *im = -*im;
+}
+
 int make_twiddles(int n, bool fp32, void** dev) {
+  const int cnt = tw_count(n);
   if (fp32) {
-    std::vector<float2> w(n);
-    for (int m = 0; m < n; ++m) {
+    std::vector<float2> w(cnt);
+    for (int m = 0; m < cnt; ++m) {
       double c, s;
-      twiddle(n, m, &c, &s);
+      twiddle_entry(n, m, &c, &s);
       w[m] = make_float2((float)c, (float)s);
     }
-    TARA_CK(cudaMalloc(dev, n * sizeof(float2)));
-    TARA_CK(cudaMemcpy(*dev, w.data(), n * sizeof(float2), cudaMemcpyHostToDevice));
+    TARA_CK(cudaMalloc(dev, cnt * sizeof(float2)));
+    TARA_CK(cudaMemcpy(*dev, w.data(), cnt * sizeof(float2), cudaMemcpyHostToDevice));
   } else {
-    std::vector<double2> w(n);
-    for (int m = 0; m < n; ++m) {
+    std::vector<double2> w(cnt);
+    for (int m = 0; m < cnt; ++m) {
       double c, s;
-      twiddle(n, m, &c, &s);
+      twiddle_entry(n, m, &c, &s);
       w[m] = make_double2(c, s);
     }
-    TARA_CK(cudaMalloc(dev, n * sizeof(double2)));
-    TARA_CK(cudaMemcpy(*dev, w.data(), n * sizeof(double2), cudaMemcpyHostToDevice));
+    TARA_CK(cudaMalloc(dev, cnt * sizeof(double2)));
+    TARA_CK(cudaMemcpy(*dev, w.data(), cnt * sizeof(double2), cudaMemcpyHostToDevice));
   }
   return TARA_OK;
 }
@@ -117,15 +135,16 @@ int make_twiddles(int n, bool fp32, void** dev) {
 // The same table as double-float pairs (hi, lo) per component, for the
 // double-float transforms: hi = fl32(w), lo = fl32(w - hi).
 int make_twiddles_df64(int n, void** dev) {
-  std::vector<float4> w(n);
-  for (int m = 0; m < n; ++m) {
+  const int cnt = tw_count(n);
+  std::vector<float4> w(cnt);
+  for (int m = 0; m < cnt; ++m) {
     double c, s;
-    twiddle(n, m, &c, &s);
+    twiddle_entry(n, m, &c, &s);
     const float ch = (float)c, sh = (float)s;
     w[m] = make_float4(ch, (float)(c - (double)ch), sh, (float)(s - (double)sh));
   }
-  TARA_CK(cudaMalloc(dev, n * sizeof(float4)));
-  TARA_CK(cudaMemcpy(*dev, w.data(), n * sizeof(float4), cudaMemcpyHostToDevice));
+  TARA_CK(cudaMalloc(dev, cnt * sizeof(float4)));
+  TARA_CK(cudaMemcpy(*dev, w.data(), cnt * sizeof(float4), cudaMemcpyHostToDevice));
   return TARA_OK;
 }
 
