@@ -252,6 +252,58 @@ void ab3com_(const int* Nx, const int* Ny, const int* Nz, const int* Nh, const d
              const double* d_Bx_k_dt_old, const double* d_Bx_k_dt_new, const double* d_By_k_dt_old,
              const double* d_By_k_dt_new, const double* d_Bz_k_dt_old, const double* d_Bz_k_dt_new);
 
+/* ---- 2D compressible isothermal hydro (derive2coh / ab2coh) ------------- */
+
+/* Replaces subroutine derive2coh (src/derive2coh.f95:6): writes dn_dt_new,
+ * dux_dt_new, duy_dt_new from the density and velocity spectra nk, ukx, uky
+ * (complex(8) (Nh,Ny)); the *_old arrays and time are unused.  Lx, Ly, mux, muy,
+ * CS come from the caller's common block /comm/ (comm_, the layout
+ * Lx,Ly,mux,muy,ms,CS,dt of src/derive2coh.f95:30); wavenumbers use the pi
+ * argument.  Sizes: powers of two in [16, 2048]. */
+void derive2coh_(const int* Nx, const int* Ny, const int* Nh, const double* pi, const double* time,
+                 const double* nk, const double* ukx, const double* uky, double* dn_dt_old,
+                 double* dux_dt_old, double* duy_dt_old, double* dn_dt_new, double* dux_dt_new,
+                 double* duy_dt_new);
+
+/* Replaces subroutine ab2coh (src/ab2coh.f95:5): AB2 of the three fields with dt
+ * from /comm/. */
+void ab2coh_(const int* Nx, const int* Ny, const int* Nh, const double* pi, const double* time,
+             const double* nk, const double* ukx, const double* uky, double* nk_new, double* ukx_new,
+             double* uky_new, const double* dn_dt_old, const double* dux_dt_old,
+             const double* duy_dt_old, const double* dn_dt_new, const double* dux_dt_new,
+             const double* duy_dt_new);
+
+typedef struct tara_coh2d_config {
+  int nx, ny;        /* powers of two, 16..2048 */
+  double kpi;        /* the pi of kx = 2*pi*(i-1)/Lx */
+  double lx, ly;     /* box lengths */
+  double mux, muy;   /* viscosities (the reference driver: 0.0002) */
+  double cs;         /* sound speed CS (the reference driver: U0/M = 3.77) */
+  double dt;         /* AB2 time step */
+} tara_coh2d_config;
+
+typedef struct tara_coh2d tara_coh2d;
+
+/* The reference driver's values (src/main2coh.f95): 2 pi box, true pi. */
+void tara_coh2d_default_config(tara_coh2d_config* cfg, int nx, int ny);
+int tara_coh2d_create(const tara_coh2d_config* cfg, tara_coh2d** out);
+int tara_coh2d_destroy(tara_coh2d* h);
+/* state3 = nk, ukx, uky as three dense complex (Nh,Ny) arrays back to back;
+ * hist3 the AB2 history (dn_dt_old, dux_dt_old, duy_dt_old) or NULL for zero. */
+int tara_coh2d_set_state(tara_coh2d* h, const double* state3, const double* hist3);
+int tara_coh2d_get_state(tara_coh2d* h, double* state3, double* hist3);
+/* derive2coh of the current state into d3 (three dense spectra) */
+int tara_coh2d_rhs(tara_coh2d* h, double* d3);
+/* nsteps of derive2coh + ab2coh + the history rotation (enqueued on the stream) */
+int tara_coh2d_step(tara_coh2d* h, int nsteps);
+int tara_coh2d_synchronize(tara_coh2d* h);
+void* tara_coh2d_stream(tara_coh2d* h);
+int tara_coh2d_launches_per_step(tara_coh2d* h);
+/* The driver's initial state (src/main2coh.f95:140-210): n = 1, a vorticity disk
+ * and five point vortices, velocity from the streamfunction; Lx = lx_ini*pi.
+ * Zero history. */
+int tara_coh2d_init_vortices(tara_coh2d* h, double lx_ini, double ly_ini);
+
 typedef struct tara3d_config {
   int nx, ny, nz;      /* powers of two, 16..256 */
   int defined;         /* 0: k^2 f / 450 as the reference; 1: nu_u k^2 u and eta_b k^2 B */

@@ -56,6 +56,18 @@ class MhdParams(ctypes.Structure):
                 ("defined", ctypes.c_int), ("nu_u", ctypes.c_double), ("eta_b", ctypes.c_double)]
 
 
+class CohParams(ctypes.Structure):
+    """oracle_coh_params (oracle/tara_oracle.h)."""
+    _fields_ = [("pi", ctypes.c_double), ("lx", ctypes.c_double), ("ly", ctypes.c_double),
+                ("mux", ctypes.c_double), ("muy", ctypes.c_double), ("cs", ctypes.c_double)]
+
+
+def coh_params(pi=PI_R8, lx=2 * PI_R8, ly=2 * PI_R8, mux=2e-4, muy=2e-4, cs=3.77) -> CohParams:
+    """Defaults: the values src/main2coh.f95 sets (Lx = Ly = 2 pi, mux = muy =
+    0.0002, CS = U0/M = 1.885/0.5)."""
+    return CohParams(pi, lx, ly, mux, muy, cs)
+
+
 def mhd_params(lx=2 * PI_R8, ly=2 * PI_R8, lz=2 * PI_R8, mu=0.01, eta=0.005, cs=10.0,
                defined=0, nu_u=0.0, eta_b=0.0) -> MhdParams:
     return MhdParams(lx, ly, lz, mu, eta, cs, defined, nu_u, eta_b)
@@ -85,6 +97,10 @@ class Oracle:
         L.oracle_driver_velocity.argtypes = [c_int, c_int, c_double, c_double, vp, vp, vp]
         L.oracle_particles_step.argtypes = [c_int, c_int, c_double, c_double, vp, vp, c_int, vp, vp,
                                             c_double]
+        L.oracle_derive2coh.argtypes = [c_int, c_int, vp, vp, vp]
+        L.oracle_ab2coh.argtypes = [c_int, c_int, c_double, vp, vp, vp, vp]
+        L.oracle_run_coh.argtypes = [c_int, c_int, vp, c_double, c_int, vp, vp]
+        L.oracle_ic_coh.argtypes = [c_int, c_int, c_double, c_double, vp]
         self.is_fftw = bool(L.oracle_backend_is_fftw())
 
     def set_threads(self, n: int) -> None:
@@ -210,6 +226,36 @@ class Oracle:
         nx = 2 * (nh - 1)
         out = np.zeros((nz, ny, nx), np.float64)
         self.L.oracle_c2r_3d(nx, ny, nz, c.ctypes.data, out.ctypes.data)
+        return out
+
+    # 2D compressible isothermal hydro: state (3, Ny, Nh) = (nk, ukx, uky)
+    def derive2coh(self, state, params):
+        state = np.ascontiguousarray(state, np.complex128)
+        _, ny, nh = state.shape
+        out = np.zeros_like(state)
+        self.L.oracle_derive2coh(2 * (nh - 1), ny, ctypes.addressof(params), state.ctypes.data,
+                                 out.ctypes.data)
+        return out
+
+    def ab2coh(self, state, d_old, d_new, dt):
+        state, d_old, d_new = (np.ascontiguousarray(a, np.complex128) for a in (state, d_old, d_new))
+        _, ny, nh = state.shape
+        out = np.zeros_like(state)
+        self.L.oracle_ab2coh(2 * (nh - 1), ny, dt, state.ctypes.data, out.ctypes.data,
+                             d_old.ctypes.data, d_new.ctypes.data)
+        return out
+
+    def run_coh(self, state, params, dt, steps, hist=None):
+        st = np.ascontiguousarray(state, np.complex128).copy()
+        h = np.zeros_like(st) if hist is None else np.ascontiguousarray(hist, np.complex128).copy()
+        _, ny, nh = st.shape
+        self.L.oracle_run_coh(2 * (nh - 1), ny, ctypes.addressof(params), dt, int(steps),
+                              st.ctypes.data, h.ctypes.data)
+        return st, h
+
+    def ic_coh(self, nx, ny, l_ini=2.0):
+        out = np.zeros((3, ny, nx // 2 + 1), np.complex128)
+        self.L.oracle_ic_coh(nx, ny, l_ini, l_ini, out.ctypes.data)
         return out
 
     def derive3com(self, state, params):

@@ -1133,3 +1133,171 @@ void oracle_ic3d_abc(int nx, int ny, int nz, double lx_ini, double ly_ini, doubl
     }
   }
 }
+
+/* ------------------------------------------------------------------------- */
+/* derive2coh -- src/derive2coh.f95:6-265                                     */
+/* ------------------------------------------------------------------------- */
+void oracle_derive2coh(int nx, int ny, const oracle_coh_params* p, const double* state,
+                       double* dstate) {
+  const int nh = nx / 2 + 1;
+  const size_t ns = (size_t)nh * ny, nr = (size_t)nx * ny;
+  const double* nk = state;
+  const double* ukx = state + 2 * ns;
+  const double* uky = state + 4 * ns;
+  /* 13 spectra in the order of the c2r calls (:95-132): nk, ukx, uky, i kx nk,
+   * i ky nk, i kx ukx, i ky ukx, i kx uky, i ky uky, kx^2 ukx, ky^2 ukx,
+   * kx^2 uky, ky^2 uky */
+  double* sp = (double*)xcalloc(13 * 2 * ns, sizeof(double));
+  double* re = (double*)xcalloc(13 * nr, sizeof(double));
+  double* pr = (double*)xcalloc(9 * nr, sizeof(double));  /* Px Py Vxx Vxy Vyx Vyy NLn NLx NLy */
+  double* pk = (double*)xcalloc(9 * 2 * ns, sizeof(double));
+  for (int i = 0; i < nh; ++i) {
+    const double kx = kx_of(i, p->pi, p->lx);
+    for (int j = 0; j < ny; ++j) {
+      const double ky = ky_of(j, ny, p->pi, p->ly);
+      const size_t q = 2 * ((size_t)j * nh + i);
+      const double a[3][2] = {{nk[q], nk[q + 1]}, {ukx[q], ukx[q + 1]}, {uky[q], uky[q + 1]}};
+      double* o = sp + q;
+#define SET(f, r_, i_) (o[2 * ns * (f)] = (r_), o[2 * ns * (f) + 1] = (i_))
+      SET(0, a[0][0], a[0][1]);
+      SET(1, a[1][0], a[1][1]);
+      SET(2, a[2][0], a[2][1]);
+      /* (0,1)*k*f = (-k Im f, k Re f) (:57-82) */
+      SET(3, -kx * a[0][1], kx * a[0][0]);
+      SET(4, -ky * a[0][1], ky * a[0][0]);
+      SET(5, -kx * a[1][1], kx * a[1][0]);
+      SET(6, -ky * a[1][1], ky * a[1][0]);
+      SET(7, -kx * a[2][1], kx * a[2][0]);
+      SET(8, -ky * a[2][1], ky * a[2][0]);
+      /* kx*kx*f (:66-69) */
+      SET(9, kx * kx * a[1][0], kx * kx * a[1][1]);
+      SET(10, ky * ky * a[1][0], ky * ky * a[1][1]);
+      SET(11, kx * kx * a[2][0], kx * kx * a[2][1]);
+      SET(12, ky * ky * a[2][0], ky * ky * a[2][1]);
+#undef SET
+    }
+  }
+  for (int f = 0; f < 13; ++f) oracle_c2r_2d(nx, ny, sp + 2 * ns * f, re + nr * f); /* :95-132 */
+  const double nn = (double)nx * (double)ny;
+  for (size_t r = 0; r < nr; ++r) { /* :140-169 */
+    double v[13];
+    for (int f = 0; f < 13; ++f) v[f] = re[nr * f + r] / nn;
+    const double n = v[0], ux = v[1], uy = v[2], dn_dx = v[3], dn_dy = v[4], dux_dx = v[5],
+                 dux_dy = v[6], duy_dx = v[7], duy_dy = v[8];
+    pr[0 * nr + r] = dn_dx / n;  /* Px */
+    pr[1 * nr + r] = dn_dy / n;  /* Py */
+    pr[2 * nr + r] = v[9] / n;   /* Viscxx */
+    pr[3 * nr + r] = v[10] / n;  /* Viscxy */
+    pr[4 * nr + r] = v[11] / n;  /* Viscyx */
+    pr[5 * nr + r] = v[12] / n;  /* Viscyy */
+    pr[6 * nr + r] = ux * dn_dx + uy * dn_dy + n * (dux_dx + duy_dy); /* NLn */
+    pr[7 * nr + r] = ux * dux_dx + uy * dux_dy;                        /* NLx */
+    pr[8 * nr + r] = ux * duy_dx + uy * duy_dy;                        /* NLy */
+  }
+  for (int f = 0; f < 9; ++f) oracle_r2c_2d(nx, ny, pr + nr * f, pk + 2 * ns * f); /* :173-198 */
+  const double cut = ((double)(nx + ny) / 2.0) / 3.0;
+  const double cs2 = p->cs * p->cs;
+  double* dn = dstate;
+  double* dux = dstate + 2 * ns;
+  double* duy = dstate + 4 * ns;
+  for (int i = 0; i < nh; ++i) {
+    const double kx = kx_of(i, p->pi, p->lx);
+    for (int j = 0; j < ny; ++j) {
+      const double ky = ky_of(j, ny, p->pi, p->ly);
+      const size_t q = 2 * ((size_t)j * nh + i);
+      if (sqrt(kx * kx + ky * ky) >= cut) { /* :205-242: all nine spectra */
+        for (int f = 0; f < 9; ++f) pk[2 * ns * f + q] = pk[2 * ns * f + q + 1] = 0.0;
+      }
+      for (int c = 0; c < 2; ++c) { /* :249-256 */
+        const double Pkx = pk[0 * 2 * ns + q + c], Pky = pk[1 * 2 * ns + q + c];
+        const double Vxx = pk[2 * 2 * ns + q + c], Vxy = pk[3 * 2 * ns + q + c];
+        const double Vyx = pk[4 * 2 * ns + q + c], Vyy = pk[5 * 2 * ns + q + c];
+        const double NLkn = pk[6 * 2 * ns + q + c];
+        const double NLkx = pk[7 * 2 * ns + q + c] + (p->mux * Vxx + p->muy * Vxy) + cs2 * Pkx;
+        const double NLky = pk[8 * 2 * ns + q + c] + (p->mux * Vyx + p->muy * Vyy) + cs2 * Pky;
+        dn[q + c] = -NLkn;
+        dux[q + c] = -NLkx;
+        duy[q + c] = -NLky;
+      }
+    }
+  }
+  free(sp); free(re); free(pr); free(pk);
+}
+
+/* ab2coh -- src/ab2coh.f95:19-27 */
+void oracle_ab2coh(int nx, int ny, double dt, const double* state, double* state_new,
+                   const double* d_old, const double* d_new) {
+  const int nh = nx / 2 + 1;
+  const size_t n2 = 2 * (size_t)nh * ny;
+  for (int f = 0; f < 3; ++f)
+    ab2_update(nh, ny, dt, state + f * n2, state_new + f * n2, d_old + f * n2, d_new + f * n2);
+}
+
+void oracle_run_coh(int nx, int ny, const oracle_coh_params* p, double dt, int nsteps,
+                    double* state, double* hist) {
+  const int nh = nx / 2 + 1;
+  const size_t n6 = 6 * (size_t)nh * ny;
+  double* sn = (double*)xcalloc(n6, sizeof(double));
+  double* dn = (double*)xcalloc(n6, sizeof(double));
+  for (int s = 0; s < nsteps; ++s) {
+    oracle_derive2coh(nx, ny, p, state, dn);
+    oracle_ab2coh(nx, ny, dt, state, sn, hist, dn);
+    memcpy(hist, dn, n6 * sizeof(double));
+    memcpy(state, sn, n6 * sizeof(double));
+  }
+  free(sn); free(dn);
+}
+
+/* src/main2coh.f95:140-210 */
+void oracle_ic_coh(int nx, int ny, double lx_ini, double ly_ini, double* state) {
+  const double pi = PI_R8;
+  const double lx = lx_ini * pi, ly = ly_ini * pi;
+  const double dx = lx / (double)nx, dy = ly / (double)ny;
+  const double n0 = 1.0, d = 0.40 * 2.0 * pi, rb = 0.30 * 2.0 * pi;
+  const int pvn = 5;
+  const double theta = 2.0 * pi / (double)pvn;
+  const int nh = nx / 2 + 1;
+  const size_t ns = (size_t)nh * ny, nr = (size_t)nx * ny;
+  double* n = (double*)xcalloc(nr, sizeof(double));
+  double* w = (double*)xcalloc(nr, sizeof(double));
+  double* wk = (double*)xcalloc(2 * ns, sizeof(double));
+  for (int i = 0; i < nx; ++i) {
+    const double x = (double)(float)(i) * dx; /* 0.0d0+real(i-1)*dx */
+    for (int j = 0; j < ny; ++j) {
+      const double y = (double)(float)(j) * dy;
+      const size_t r = (size_t)j * nx + i;
+      n[r] = n0;
+      const double ax = x - lx / 2.0, ay = y - ly / 2.0;
+      w[r] = (ax * ax + ay * ay <= rb * rb) ? 1.0 : 0.0;
+      for (int pv = 1; pv <= pvn; ++pv) {
+        const int npv = -pv;
+        const double bx = x - (lx / 2.0 + d * cos(npv * theta));
+        const double by = y - (ly / 2.0 + d * sin(npv * theta));
+        if (bx * bx + by * by <= 0.20 * 0.20) w[r] = 10.0;
+      }
+    }
+  }
+  double* nk = state;
+  double* ukx = state + 2 * ns;
+  double* uky = state + 4 * ns;
+  oracle_r2c_2d(nx, ny, n, nk);
+  oracle_r2c_2d(nx, ny, w, wk);
+  for (int i = 0; i < nh; ++i) {
+    const double kx = kx_of(i, pi, lx);
+    for (int j = 0; j < ny; ++j) {
+      const double ky = ky_of(j, ny, pi, ly);
+      const size_t q = 2 * ((size_t)j * nh + i);
+      if (i == 0 && j == 0) {
+        ukx[q] = ukx[q + 1] = uky[q] = uky[q + 1] = 0.0;
+      } else {
+        const double k2 = kx * kx + ky * ky;
+        const double pr = wk[q] / k2, pim = wk[q + 1] / k2;
+        ukx[q] = -ky * pim; /* + (0,1) ky psi */
+        ukx[q + 1] = ky * pr;
+        uky[q] = kx * pim;  /* - (0,1) kx psi */
+        uky[q + 1] = -(kx * pr);
+      }
+    }
+  }
+  free(n); free(w); free(wk);
+}

@@ -136,6 +136,32 @@ void oracle_run3d(int nx, int ny, int nz, const oracle_mhd_params* p, double dt,
 void oracle_ic3d_abc(int nx, int ny, int nz, double lx_ini, double ly_ini, double lz_ini,
                      double* real8);
 
+/* ---- 2D compressible isothermal hydro (src/derive2coh.f95, src/ab2coh.f95) ---- */
+typedef struct {
+  double pi;       /* the pi argument of kx = 2 pi (i-1)/Lx */
+  double lx, ly;   /* /comm/ Lx, Ly */
+  double mux, muy; /* /comm/ viscosities */
+  double cs;       /* /comm/ sound speed CS */
+} oracle_coh_params;
+
+/* src/derive2coh.f95:6-265: state = (nk, ukx, uky), three complex (Nh,Ny) spectra
+ * back to back; writes (dn_dt_new, dux_dt_new, duy_dt_new) likewise. */
+void oracle_derive2coh(int nx, int ny, const oracle_coh_params* p, const double* state,
+                       double* dstate);
+/* src/ab2coh.f95:5-34: AB2 of the three fields */
+void oracle_ab2coh(int nx, int ny, double dt, const double* state, double* state_new,
+                   const double* d_old, const double* d_new);
+/* derive2coh + ab2coh + the rotation of src/main2coh.f95:277-298, nsteps times */
+void oracle_run_coh(int nx, int ny, const oracle_coh_params* p, double dt, int nsteps,
+                    double* state, double* hist);
+/* Initial state of src/main2coh.f95:140-210: uniform density n0 = 1, vorticity 1
+ * in a disk of radius 0.6 pi about the centre and 10 in five disks of radius 0.2
+ * at distance 0.8 pi, velocity from psi = omega_hat/k^2 (true pi, Lx = lx_ini pi).
+ * The reference's vortex angles come from an uninitialised counter whose
+ * residues mod 5 give the same five positions at every grid point; they are
+ * taken here as 2 pi r/5 with r = -1..-5. */
+void oracle_ic_coh(int nx, int ny, double lx_ini, double ly_ini, double* state);
+
 #ifdef __cplusplus
 }
 #endif

@@ -58,6 +58,16 @@ class Config3D(ctypes.Structure):
     ]
 
 
+class CohConfig(ctypes.Structure):
+    _fields_ = [("nx", ctypes.c_int), ("ny", ctypes.c_int)] + [
+        (n, ctypes.c_double) for n in ("kpi", "lx", "ly", "mux", "muy", "cs", "dt")]
+
+
+class CohCommon(ctypes.Structure):
+    """The 2D compressible code's view of /comm/ (src/derive2coh.f95:30)."""
+    _fields_ = [(n, ctypes.c_double) for n in ("Lx", "Ly", "mux", "muy", "ms", "CS", "dt")]
+
+
 class MhdCommon(ctypes.Structure):
     """The reference's common block /comm/ (src/derive3com.f95:62) as libtara sees it."""
     _fields_ = [("iret", ctypes.c_int32), ("thread_num", ctypes.c_int32)] + [
@@ -146,6 +156,9 @@ def _declare(L: ctypes.CDLL) -> None:
     L.tara3d_diag.argtypes = [vp, dp]
     L.tara3d_stream.argtypes = [vp]
     L.tara3d_stream.restype = vp
+    L.tara_coh2d_stream.argtypes = [vp]
+    L.tara_coh2d_stream.restype = vp
+    L.tara_coh2d_init_vortices.argtypes = [vp, c_double, c_double]
     L.tara2d_set_state_run.argtypes = [vp, c_int, dp, dp]
     L.tara2d_get_state_run.argtypes = [vp, c_int, dp, dp]
     L.tara2d_diag_run.argtypes = [vp, c_int, dp, dp]
@@ -590,6 +603,113 @@ class Solver3D:
         out = (ctypes.c_double * 4)()
         _check(lib().tara3d_diag(self._h, out))
         return list(out)
+
+
+# ---------------------------------------------------------------------------
+# 2D compressible isothermal hydro
+# ---------------------------------------------------------------------------
+def coh_common() -> CohCommon:
+    """libtara's /comm/ seen with the 2D compressible layout (read by derive2coh_/ab2coh_)."""
+    return CohCommon.from_address(ctypes.addressof(MhdCommon.in_dll(lib(), "comm_")))
+
+
+def _state3(a) -> np.ndarray:
+    a = np.ascontiguousarray(a, dtype=np.complex128)
+    if a.ndim != 3 or a.shape[0] != 3:
+        raise ValueError("expected a (3, Ny, Nh) state (nk, ukx, uky)")
+    return a
+
+
+def derive2coh(state, pi: float = 3.14159265358979323846, time: float = 0.0) -> np.ndarray:
+    """subroutine derive2coh (src/derive2coh.f95:6): (dn_dt_new, dux_dt_new, duy_dt_new)."""
+    st = _state3(state)
+    _, ny, nh = st.shape
+    out = np.zeros_like(st)
+    old = np.zeros_like(st[0])
+    lib().derive2coh_(*_ints(2 * (nh - 1), ny, nh), *_dbls(pi, time),
+                      *[st[f].ctypes.data for f in range(3)], *[old.ctypes.data] * 3,
+                      *[out[f].ctypes.data for f in range(3)])
+    _check(lib().tara_last_error())
+    return out
+
+
+def ab2coh(state, d_old, d_new, pi: float = 3.14159265358979323846, time: float = 0.0) -> np.ndarray:
+    """subroutine ab2coh (src/ab2coh.f95:5): (nk_new, ukx_new, uky_new), dt from /comm/."""
+    st, do, dn = _state3(state), _state3(d_old), _state3(d_new)
+    _, ny, nh = st.shape
+    out = np.zeros_like(st)
+    lib().ab2coh_(*_ints(2 * (nh - 1), ny, nh), *_dbls(pi, time),
+                  *[st[f].ctypes.data for f in range(3)], *[out[f].ctypes.data for f in range(3)],
+                  *[do[f].ctypes.data for f in range(3)], *[dn[f].ctypes.data for f in range(3)])
+    _check(lib().tara_last_error())
+    return out
+
+
+class Coh2D:
+    """Device-resident 2D compressible isothermal hydro state (tara_coh2d handle)."""
+
+    def __init__(self, nx: int, ny: int | None = None, **kw):
+        ny = nx if ny is None else ny
+        cfg = CohConfig()
+        lib().tara_coh2d_default_config(ctypes.byref(cfg), nx, ny)
+        for k, v in kw.items():
+            setattr(cfg, k, v)
+        h = ctypes.c_void_p()
+        _check(lib().tara_coh2d_create(ctypes.byref(cfg), ctypes.byref(h)))
+        self._h = h
+        self.shape = (ny, nx // 2 + 1)
+        self.nx, self.ny = nx, ny
+        self.cfg = cfg
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().tara_coh2d_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def set_state(self, state, hist=None):
+        st = _state3(state)
+        h = None if hist is None else _state3(hist)
+        _check(lib().tara_coh2d_set_state(self._h, st.ctypes.data, None if h is None else h.ctypes.data))
+
+    def get_state(self, with_history: bool = False):
+        st = np.zeros((3,) + self.shape, np.complex128)
+        h = np.zeros_like(st) if with_history else None
+        _check(lib().tara_coh2d_get_state(self._h, st.ctypes.data, None if h is None else h.ctypes.data))
+        return (st, h) if with_history else st
+
+    def init_vortices(self, lx_ini: float = 2.0, ly_ini: float = 2.0):
+        _check(lib().tara_coh2d_init_vortices(self._h, lx_ini, ly_ini))
+
+    def rhs(self):
+        out = np.zeros((3,) + self.shape, np.complex128)
+        _check(lib().tara_coh2d_rhs(self._h, out.ctypes.data))
+        return out
+
+    def step(self, n: int = 1):
+        _check(lib().tara_coh2d_step(self._h, int(n)))
+
+    def synchronize(self):
+        _check(lib().tara_coh2d_synchronize(self._h))
+
+    @property
+    def stream(self) -> int:
+        return lib().tara_coh2d_stream(self._h) or 0
+
+    @property
+    def launches_per_step(self) -> int:
+        return lib().tara_coh2d_launches_per_step(self._h)
 
 
 # ---------------------------------------------------------------------------

@@ -13,11 +13,6 @@
 
 #include "internal.h"
 
-namespace tara {
-__global__ void k_ab2_dense(const double2* w, double2* out, const double2* __restrict__ fo,
-                            const double2* __restrict__ fn, size_t n, double dt);
-}
-
 using namespace tara;
 
 namespace {

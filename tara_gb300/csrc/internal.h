@@ -91,6 +91,16 @@ struct tara2d {
   tara::RhsParams rp;
 };
 
+// Fortran common block /comm/: one symbol shared by the reference programs, each
+// reading its own layout over it (the 3D code's below; the 2D compressible
+// code's Lx, Ly, mux, muy, ms, CS, dt in coh2d.cu).  A Fortran caller that links
+// libtara supplies it; mhd3d.cu holds a weak definition so the library loads alone.
+struct TaraMhdCommon {
+  int32_t iret, thread_num;
+  double time_max, Lx, Ly, Lz, dx, dy, dz, spheat, mu, ms, CS, mu_0, eta, dt, kf;
+};
+extern "C" TaraMhdCommon comm_;
+
 namespace tara {
 // One RHS evaluation of `win` followed by the update of `mode`; when ev is not
 // null, ev[0..2] are recorded on the handle's stream after the three launches.

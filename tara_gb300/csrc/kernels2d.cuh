@@ -649,5 +649,8 @@ __global__ void k_diag_partial(const double2* __restrict__ w, Grid2D g, double* 
 __global__ void k_diag_final(const double* __restrict__ part, int nparts, double inv,
                              double* __restrict__ out, unsigned int* flag);
 __global__ void k_mul(double2* __restrict__ w, size_t n, double s);
+// out = w + (3/2 fn - 1/2 fo) dt over n elements (src/ab2csh.f95:10-14)
+__global__ void k_ab2_dense(const double2* w, double2* out, const double2* __restrict__ fo,
+                            const double2* __restrict__ fn, size_t n, double dt);
 
 }  // namespace tara

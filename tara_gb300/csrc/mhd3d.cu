@@ -322,10 +322,6 @@ using namespace tara;
 // src/derive3com.f95:62, src/ab3com.f95:29).  A Fortran caller that links
 // libtara supplies it; this weak definition (the reference's main3com values for
 // a 2*pi box) lets the library load on its own.
-struct TaraMhdCommon {
-  int32_t iret, thread_num;
-  double time_max, Lx, Ly, Lz, dx, dy, dz, spheat, mu, ms, CS, mu_0, eta, dt, kf;
-};
 extern "C" __attribute__((weak)) TaraMhdCommon comm_ = {
     0, 1, 1.0, 2.0 * 3.14159265358979323846, 2.0 * 3.14159265358979323846,
     2.0 * 3.14159265358979323846, 0.0, 0.0, 0.0, 1.0, 0.01, 1.0, 10.0, 1.0, 0.005, 1e-3, 1.0};

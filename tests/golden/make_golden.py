@@ -85,6 +85,35 @@ def main3d() -> None:
     print(f"wrote {out} ({out.stat().st_size} bytes)")
 
 
+def main_coh() -> None:
+    """tests/golden/golden_coh.npz: the 2D compressible isothermal path at 64^2
+    from the FFTW oracle: the driver's initial state (src/main2coh.f95:140-210),
+    one derive2coh of it and of a seeded smooth state, and AB2 runs with the
+    driver's parameters (mux = muy = 2e-4, CS = 3.77, 2 pi box, dt = 1e-3)."""
+    O = orc.load(fftw=True)
+    out = Path(__file__).resolve().parent / "golden_coh.npz"
+    p = orc.coh_params()
+    st = O.ic_coh(64, 64)
+    g = {"ic": st, "rhs_ic": O.derive2coh(st, p)}
+    rng = np.random.default_rng(20240601)
+    n = 64
+    ky = np.fft.fftfreq(n, 1.0 / n)[:, None]
+    kx = np.arange(n // 2 + 1)[None, :]
+    env = np.exp(-(kx**2 + ky**2) / 18.0)
+    sm = np.stack([env * (rng.standard_normal((n, n // 2 + 1)) + 1j * rng.standard_normal((n, n // 2 + 1)))
+                   for _ in range(3)]) * 40.0
+    sm[0, 0, 0] = n * n  # mean density 1
+    g["smooth"] = sm
+    g["rhs_smooth"] = O.derive2coh(sm, orc.coh_params(mux=1e-3, muy=5e-4, cs=2.0))
+    for steps in (1, 10, 2000):
+        s2, h2 = O.run_coh(st, p, 1e-3, steps)
+        g[f"ab2_{steps}"] = s2
+        g[f"ab2_{steps}_hist"] = h2
+    np.savez_compressed(out, **g)
+    print(f"wrote {out} ({out.stat().st_size} bytes)")
+
+
 if __name__ == "__main__":
     main()
     main3d()
+    main_coh()
