@@ -156,9 +156,24 @@ def _declare(L: ctypes.CDLL) -> None:
     L.tara3d_diag.argtypes = [vp, dp]
     L.tara3d_stream.argtypes = [vp]
     L.tara3d_stream.restype = vp
+    L.tara_measure_dfma_rate.argtypes = [c_int, dp]
+    L.tara_coh2d_default_config.argtypes = [vp, c_int, c_int]
+    L.tara_coh2d_default_config.restype = None
+    L.tara_coh2d_create.argtypes = [vp, vp]
+    L.tara_coh2d_destroy.argtypes = [vp]
+    L.tara_coh2d_set_state.argtypes = [vp, vp, vp]
+    L.tara_coh2d_get_state.argtypes = [vp, vp, vp]
+    L.tara_coh2d_rhs.argtypes = [vp, vp]
+    L.tara_coh2d_step.argtypes = [vp, c_int]
+    L.tara_coh2d_synchronize.argtypes = [vp]
+    L.tara_coh2d_launches_per_step.argtypes = [vp]
     L.tara_coh2d_stream.argtypes = [vp]
     L.tara_coh2d_stream.restype = vp
     L.tara_coh2d_init_vortices.argtypes = [vp, c_double, c_double]
+    L.derive2coh_.argtypes = [ip, ip, ip, dp, dp] + [vp] * 9
+    L.derive2coh_.restype = None
+    L.ab2coh_.argtypes = [ip, ip, ip, dp, dp] + [vp] * 12
+    L.ab2coh_.restype = None
     L.tara2d_set_state_run.argtypes = [vp, c_int, dp, dp]
     L.tara2d_get_state_run.argtypes = [vp, c_int, dp, dp]
     L.tara2d_diag_run.argtypes = [vp, c_int, dp, dp]
