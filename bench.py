@@ -429,6 +429,104 @@ def mhd3d_initial_state(n: int, seed: int = 3):
     return np.stack([rho, u[0], u[1], u[2], e, b[0], b[1], b[2]])
 
 
+def run_coh2d(args) -> None:
+    """2D compressible isothermal hydro (derive2coh + ab2coh, FP64) from the
+    reference driver's initial state (src/main2coh.f95: disk + five point
+    vortices, n = 1, mux = muy = 2e-4, CS = 3.77, 2 pi box), AB2 steps at n^2.
+    CUDA events on the solver's stream; e2e through tara_coh2d_set_state (pinned
+    host) + tara_coh2d_step(1) + tara_coh2d_get_state; the FP64-pipe roofline of
+    the whole step from the transforms' FP64 instructions (11 inverse and 3
+    forward real 2D transforms per step)."""
+    import numpy as np
+    import torch
+
+    import tara_gb300 as tg
+
+    torch.cuda.set_device(0)
+    n = args.n
+    dt = 2.5e-4 * (1024.0 / n)  # CFL-scaled from the reference's 1e-3 at 64^2-256^2
+    s = tg.Coh2D(n, dt=dt)
+    s.init_vortices(2.0, 2.0)
+    s.step(args.warmup)
+    s.synchronize()
+    st = torch.cuda.ExternalStream(s.stream)
+    sampler = ClockSampler(0).start()
+    time.sleep(0.5)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    sampler.mark("start")
+    a.record(st)
+    s.step(args.steps)
+    b.record(st)
+    torch.cuda.synchronize()
+    sampler.mark("end")
+    clocks = sampler.stop()
+    el_ms = a.elapsed_time(b)
+    s.synchronize()  # raises on non-finite values
+    nh = n // 2 + 1
+    F = 16.0 * nh * n
+    host_in = torch.empty((3, n, nh), dtype=torch.complex128, pin_memory=True).numpy()
+    host_out = torch.empty((3, n, nh), dtype=torch.complex128, pin_memory=True).numpy()
+    host_in[:] = s.get_state()
+    e2e_steps = max(1, min(args.steps, 10))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        s.set_state(host_in)  # history reset: the e2e loop times the transfer path only
+        s.step(1)
+        s.get_state_into(host_out)
+        host_in, host_out = host_out, host_in
+    torch.cuda.synchronize()
+    e2e_el = time.perf_counter() - t0
+    f = fft_fp64_inst(n)
+    inst = (11 + 3) * nh * f + (11 + 3) * (n // 2) * f
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    nominal = 2.0 * sms * ((clocks or {}).get("sm_mhz") or 2070.0) * 1e6
+    ms_step = el_ms / args.steps
+    peak, peak_kind = peaks()
+    # dominant launch: the 11-field inverse column transform, reads and writes 11 spectra
+    cpu = None
+    if not args.no_cpu_baseline:
+        from oracle import oracle as orc
+
+        O = orc.load()
+        O.set_threads(os.cpu_count() or 1)
+        m = 512
+        st0 = O.ic_coh(m, m)
+        steps_c, t_c = 0, 0.0
+        while t_c < args.cpu_budget and steps_c < 200:
+            t1 = time.perf_counter()
+            st0, _ = O.run_coh(st0, orc.coh_params(), 2.5e-4 * 1024.0 / m, 1)
+            t_c += time.perf_counter() - t1
+            steps_c += 1
+        cpu = {"value": m * m * steps_c / t_c, "unit": UNIT, "cores": O.threads(), "kind": "port",
+               "sample": f"{steps_c} AB2 step(s) at {m}^2 in {t_c:.2f} s (oracle C restatement of "
+                         f"derive2coh/ab2coh, own radix-2 FFT, {O.threads()} OpenMP threads)"}
+    line = {"metric": f"grid-pt*steps/s at {n}^2, 2D compressible isothermal hydro (derive2coh + ab2coh), FP64",
+            "value": n * n * args.steps / (el_ms * 1e-3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (the reference driver's vortex initial state)",
+            "config": {"workload": f"derive2coh + ab2coh, {n}x{n}, 2pi box, mux=muy=2e-4, CS=3.77, dt={dt:g}",
+                       "l2": "working set > L2 (no flush)"},
+            "e2e": {"value": n * n * e2e_steps / e2e_el, "unit": UNIT, "h2d_bytes_per_step": int(3 * F),
+                    "d2h_bytes_per_step": int(3 * F),
+                    "path": "tara_coh2d_set_state(pinned host) + tara_coh2d_step(1) + tara_coh2d_get_state"},
+            "gpu_launches": s.launches_per_step * args.steps,
+            "roofline": {"bound": "hbm", "kernel": "whole AB2 step (7 launches)",
+                         "achieved": 85 * F / (ms_step * 1e-3) / 1e9, "peak": peak, "peak_kind": peak_kind,
+                         "unit": "GB/s", "frac": 85 * F / (ms_step * 1e-3) / 1e9 / peak, "traffic": None,
+                         "bytes_per_step": "85 F (F = one FP64 half spectrum): 11 spectra formed, transformed "
+                                           "and read back as real fields, 3 products transformed forward, the "
+                                           "update of 3 fields and their history",
+                         "limiter": "FP64 pipe"},
+            "fp64_pipe": {"inst_per_step": inst, "achieved_inst_per_s": inst / (ms_step * 1e-3),
+                          "nominal_inst_per_s": nominal, "frac_of_nominal": inst / (ms_step * 1e-3) / nominal,
+                          "count": "transform butterflies only (11 c2r + 3 r2c); element work excluded"},
+            "clocks": clocks, "cpu_baseline": cpu}
+    s.close()
+    print(json.dumps(line), flush=True)
+
+
 def run_mhd3d(args) -> None:
     """128^3 compressible MHD, FP64, AB2, nu = eta = 0.01, dt = 1e-3."""
     import torch
@@ -622,7 +720,8 @@ def main() -> None:
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="rk4-2048",
-                    choices=["rk4-2048", "ensemble", "mhd3d", "closure", "fno-train", "closure-step", "cufft"],
+                    choices=["rk4-2048", "ensemble", "mhd3d", "closure", "fno-train", "closure-step", "cufft",
+                             "coh2d"],
                     help="rk4-2048 is the headline; the others measure the ensemble, 3D MHD and the learned closure")
     ap.add_argument("--ens-runs-per-size", type=int, default=128,
                     help="ensemble: runs of each size (the 384-run ensemble uses 128)")
@@ -641,6 +740,8 @@ def main() -> None:
         run_ensemble(args)
     elif args.workload == "mhd3d":
         run_mhd3d(args)
+    elif args.workload == "coh2d":
+        run_coh2d(args)
     elif args.workload == "closure":
         run_closure(args)
     elif args.workload == "fno-train":

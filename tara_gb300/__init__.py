@@ -704,6 +704,12 @@ class Coh2D:
         _check(lib().tara_coh2d_get_state(self._h, st.ctypes.data, None if h is None else h.ctypes.data))
         return (st, h) if with_history else st
 
+    def get_state_into(self, out: np.ndarray) -> None:
+        """Copy the state into a caller-owned (3, Ny, Nh) complex128 array (e.g. pinned)."""
+        if out.shape != (3,) + self.shape or out.dtype != np.complex128 or not out.flags.c_contiguous:
+            raise ValueError("out must be a C-contiguous (3, Ny, Nh) complex128 array")
+        _check(lib().tara_coh2d_get_state(self._h, out.ctypes.data, None))
+
     def init_vortices(self, lx_ini: float = 2.0, ly_ini: float = 2.0):
         _check(lib().tara_coh2d_init_vortices(self._h, lx_ini, ly_ini))
 
