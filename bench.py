@@ -430,13 +430,17 @@ def mhd3d_initial_state(n: int, seed: int = 3):
 
 
 def run_coh2d(args) -> None:
-    """2D compressible isothermal hydro (derive2coh + ab2coh, FP64) from the
-    reference driver's initial state (src/main2coh.f95: disk + five point
-    vortices, n = 1, mux = muy = 2e-4, CS = 3.77, 2 pi box), AB2 steps at n^2.
-    CUDA events on the solver's stream; e2e through tara_coh2d_set_state (pinned
-    host) + tara_coh2d_step(1) + tara_coh2d_get_state; the FP64-pipe roofline of
-    the whole step from the transforms' FP64 instructions (11 inverse and 3
-    forward real 2D transforms per step)."""
+    """The 2D compressible solvers, AB2 steps at n^2 from the reference drivers'
+    initial states, FP64:
+      coh2d  isothermal hydro (derive2coh + ab2coh; src/main2coh.f95: disk + five
+             point vortices, n = 1, mux = muy = 2e-4, CS = 3.77, 2 pi box);
+             11 inverse and 3 forward real 2D transforms per step
+      com2d  MHD (derive2com + ab2com; src/main2com.f95: rho = 1, ux = -sin y,
+             uy = sin x, B = (1, 1), CS = 100, mu = 1e-3, eta = 1e-4, forcing
+             kf = A = 1); 8 inverse and 11 forward real 2D transforms per step
+    CUDA events on the solver's stream; e2e through set_state (pinned host) +
+    step(1) + get_state; the FP64-pipe roofline of the whole step from the
+    transforms' FP64 instructions."""
     import numpy as np
     import torch
 
@@ -444,9 +448,17 @@ def run_coh2d(args) -> None:
 
     torch.cuda.set_device(0)
     n = args.n
-    dt = 2.5e-4 * (1024.0 / n)  # CFL-scaled from the reference's 1e-3 at 64^2-256^2
-    s = tg.Coh2D(n, dt=dt)
-    s.init_vortices(2.0, 2.0)
+    mhd = args.workload == "com2d"
+    if mhd:
+        dt = 1e-5 * (2048.0 / n)  # sound-speed CFL at CS = 100
+        s = tg.Com2D(n, dt=dt)
+        s.init_reference(2.0, 2.0, 1.0)
+        nfield, ninv, nfwd = 6, 8, 11
+    else:
+        dt = 2.5e-4 * (1024.0 / n)  # CFL-scaled from the reference's 1e-3 at 64^2-256^2
+        s = tg.Coh2D(n, dt=dt)
+        s.init_vortices(2.0, 2.0)
+        nfield, ninv, nfwd = 3, 11, 3
     s.step(args.warmup)
     s.synchronize()
     st = torch.cuda.ExternalStream(s.stream)
@@ -465,8 +477,8 @@ def run_coh2d(args) -> None:
     s.synchronize()  # raises on non-finite values
     nh = n // 2 + 1
     F = 16.0 * nh * n
-    host_in = torch.empty((3, n, nh), dtype=torch.complex128, pin_memory=True).numpy()
-    host_out = torch.empty((3, n, nh), dtype=torch.complex128, pin_memory=True).numpy()
+    host_in = torch.empty((nfield, n, nh), dtype=torch.complex128, pin_memory=True).numpy()
+    host_out = torch.empty((nfield, n, nh), dtype=torch.complex128, pin_memory=True).numpy()
     host_in[:] = s.get_state()
     e2e_steps = max(1, min(args.steps, 10))
     torch.cuda.synchronize()
@@ -479,11 +491,14 @@ def run_coh2d(args) -> None:
     torch.cuda.synchronize()
     e2e_el = time.perf_counter() - t0
     f = fft_fp64_inst(n)
-    inst = (11 + 3) * nh * f + (11 + 3) * (n // 2) * f
+    inst = (ninv + nfwd) * nh * f + (ninv + nfwd) * (n // 2) * f
     sms = torch.cuda.get_device_properties(0).multi_processor_count
     nominal = 2.0 * sms * ((clocks or {}).get("sm_mhz") or 2070.0) * 1e6
     ms_step = el_ms / args.steps
     peak, peak_kind = peaks()
+    # spectra F, real fields F/2: coh 3+11 | 22 | 11+5.5 | 5.5+1.5 | 1.5+3 | 6 | 15 ;
+    # com 12 | 16 | 8+4 | 4+2 | 2+4 | 8 | 4 | 2+1 | 4+3.5+1+3.5 | 3.5+7 | 14 | 7+4+6+18+18
+    traffic_f = 130 if mhd else 85
     # dominant launch: the 11-field inverse column transform, reads and writes 11 spectra
     cpu = None
     if not args.no_cpu_baseline:
@@ -492,36 +507,42 @@ def run_coh2d(args) -> None:
         O = orc.load()
         O.set_threads(os.cpu_count() or 1)
         m = 512
-        st0 = O.ic_coh(m, m)
+        st0 = O.ic_com(m, m) if mhd else O.ic_coh(m, m)
         steps_c, t_c = 0, 0.0
         while t_c < args.cpu_budget and steps_c < 200:
             t1 = time.perf_counter()
-            st0, _ = O.run_coh(st0, orc.coh_params(), 2.5e-4 * 1024.0 / m, 1)
+            if mhd:
+                st0, _ = O.run_com(st0, orc.com_params(), 1e-5 * 2048.0 / m, 1)
+            else:
+                st0, _ = O.run_coh(st0, orc.coh_params(), 2.5e-4 * 1024.0 / m, 1)
             t_c += time.perf_counter() - t1
             steps_c += 1
+        name = "derive2com/ab2com" if mhd else "derive2coh/ab2coh"
         cpu = {"value": m * m * steps_c / t_c, "unit": UNIT, "cores": O.threads(), "kind": "port",
                "sample": f"{steps_c} AB2 step(s) at {m}^2 in {t_c:.2f} s (oracle C restatement of "
-                         f"derive2coh/ab2coh, own radix-2 FFT, {O.threads()} OpenMP threads)"}
-    line = {"metric": f"grid-pt*steps/s at {n}^2, 2D compressible isothermal hydro (derive2coh + ab2coh), FP64",
+                         f"{name}, own radix-2 FFT, {O.threads()} OpenMP threads)"}
+    what = ("2D compressible MHD (derive2com + ab2com)" if mhd
+            else "2D compressible isothermal hydro (derive2coh + ab2coh)")
+    workload = (f"derive2com + ab2com, {n}x{n}, 2pi box, mu=1e-3, eta=1e-4, CS=100, kf=A=1, dt={dt:g}" if mhd
+                else f"derive2coh + ab2coh, {n}x{n}, 2pi box, mux=muy=2e-4, CS=3.77, dt={dt:g}")
+    line = {"metric": f"grid-pt*steps/s at {n}^2, {what}, FP64",
             "value": n * n * args.steps / (el_ms * 1e-3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic (the reference driver's vortex initial state)",
-            "config": {"workload": f"derive2coh + ab2coh, {n}x{n}, 2pi box, mux=muy=2e-4, CS=3.77, dt={dt:g}",
-                       "l2": "working set > L2 (no flush)"},
-            "e2e": {"value": n * n * e2e_steps / e2e_el, "unit": UNIT, "h2d_bytes_per_step": int(3 * F),
-                    "d2h_bytes_per_step": int(3 * F),
-                    "path": "tara_coh2d_set_state(pinned host) + tara_coh2d_step(1) + tara_coh2d_get_state"},
+            "config": {"workload": workload, "l2": "working set > L2 (no flush)"},
+            "e2e": {"value": n * n * e2e_steps / e2e_el, "unit": UNIT, "h2d_bytes_per_step": int(nfield * F),
+                    "d2h_bytes_per_step": int(nfield * F),
+                    "path": ("tara_com2d" if mhd else "tara_coh2d") + "_set_state(pinned host) + _step(1) + _get_state"},
             "gpu_launches": s.launches_per_step * args.steps,
-            "roofline": {"bound": "hbm", "kernel": "whole AB2 step (7 launches)",
-                         "achieved": 85 * F / (ms_step * 1e-3) / 1e9, "peak": peak, "peak_kind": peak_kind,
-                         "unit": "GB/s", "frac": 85 * F / (ms_step * 1e-3) / 1e9 / peak, "traffic": None,
-                         "bytes_per_step": "85 F (F = one FP64 half spectrum): 11 spectra formed, transformed "
-                                           "and read back as real fields, 3 products transformed forward, the "
-                                           "update of 3 fields and their history",
+            "roofline": {"bound": "hbm", "kernel": f"whole AB2 step ({s.launches_per_step} launches)",
+                         "achieved": traffic_f * F / (ms_step * 1e-3) / 1e9, "peak": peak, "peak_kind": peak_kind,
+                         "unit": "GB/s", "frac": traffic_f * F / (ms_step * 1e-3) / 1e9 / peak, "traffic": None,
+                         "bytes_per_step": f"{traffic_f} F (F = one FP64 half spectrum): the unfused passes' reads "
+                                           "and writes of spectra (F each) and real fields (F/2 each)",
                          "limiter": "FP64 pipe"},
             "fp64_pipe": {"inst_per_step": inst, "achieved_inst_per_s": inst / (ms_step * 1e-3),
                           "nominal_inst_per_s": nominal, "frac_of_nominal": inst / (ms_step * 1e-3) / nominal,
-                          "count": "transform butterflies only (11 c2r + 3 r2c); element work excluded"},
+                          "count": f"transform butterflies only ({ninv} c2r + {nfwd} r2c); element work excluded"},
             "clocks": clocks, "cpu_baseline": cpu}
     s.close()
     print(json.dumps(line), flush=True)
@@ -721,7 +742,7 @@ def main() -> None:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="rk4-2048",
                     choices=["rk4-2048", "ensemble", "mhd3d", "closure", "fno-train", "closure-step", "cufft",
-                             "coh2d"],
+                             "coh2d", "com2d"],
                     help="rk4-2048 is the headline; the others measure the ensemble, 3D MHD and the learned closure")
     ap.add_argument("--ens-runs-per-size", type=int, default=128,
                     help="ensemble: runs of each size (the 384-run ensemble uses 128)")
@@ -740,7 +761,7 @@ def main() -> None:
         run_ensemble(args)
     elif args.workload == "mhd3d":
         run_mhd3d(args)
-    elif args.workload == "coh2d":
+    elif args.workload in ("coh2d", "com2d"):
         run_coh2d(args)
     elif args.workload == "closure":
         run_closure(args)

@@ -304,6 +304,64 @@ int tara_coh2d_launches_per_step(tara_coh2d* h);
  * Zero history. */
 int tara_coh2d_init_vortices(tara_coh2d* h, double lx_ini, double ly_ini);
 
+/* ---- 2D compressible MHD (derive2com / ab2com) --------------------------- */
+
+/* Replaces subroutine derive2com (src/derive2com.f95:5): writes the six
+ * d_*_k_dt_new arrays (rho, rho ux, rho uy, E, Bx, By) from the six state spectra;
+ * the *_old arrays and time are unused.  Lx, Ly, mu, CS, eta, kf, A come from the
+ * caller's /comm/ (comm_, the layout Lx,Ly,spheat,mu,ms,CS,mu_0,eta,dt,kf,A of
+ * src/derive2com.f95:43).  Faithful to the reference's curl B (built from
+ * d_ux_dx and d_uy_dy, :186-187); the forcing uses the grid coordinates the
+ * reference leaves unset.  Sizes: powers of two in [16, 2048]. */
+void derive2com_(const int* Nx, const int* Ny, const int* Nh, const double* pi, const double* time,
+                 const double* rho_k, const double* rho_ux_k, const double* rho_uy_k,
+                 const double* E_k, const double* Bx_k, const double* By_k, double* d_rho_k_dt_old,
+                 double* d_rho_k_dt_new, double* d_rho_ux_k_dt_old, double* d_rho_ux_k_dt_new,
+                 double* d_rho_uy_k_dt_old, double* d_rho_uy_k_dt_new, double* d_E_k_dt_old,
+                 double* d_E_k_dt_new, double* d_Bx_k_dt_old, double* d_Bx_k_dt_new,
+                 double* d_By_k_dt_old, double* d_By_k_dt_new);
+
+/* Replaces subroutine ab2com (src/ab2com.f95): AB2 of the six fields with dt from
+ * /comm/. */
+void ab2com_(const int* Nx, const int* Ny, const int* Nh, const double* pi, const double* time,
+             const double* rho_k, const double* rho_ux_k, const double* rho_uy_k, const double* E_k,
+             const double* Bx_k, const double* By_k, double* rho_k_new, double* rho_ux_k_new,
+             double* rho_uy_k_new, double* E_k_new, double* Bx_k_new, double* By_k_new,
+             const double* d_rho_k_dt_old, const double* d_rho_k_dt_new,
+             const double* d_rho_ux_k_dt_old, const double* d_rho_ux_k_dt_new,
+             const double* d_rho_uy_k_dt_old, const double* d_rho_uy_k_dt_new,
+             const double* d_E_k_dt_old, const double* d_E_k_dt_new, const double* d_Bx_k_dt_old,
+             const double* d_Bx_k_dt_new, const double* d_By_k_dt_old, const double* d_By_k_dt_new);
+
+typedef struct tara_com2d_config {
+  int nx, ny;      /* powers of two, 16..2048 */
+  int defined;     /* 0: curl B as the reference (from d_ux_dx, d_uy_dy); 1: from dB/dx, dB/dy */
+  double kpi;      /* the pi of kx = 2*pi*(i-1)/Lx */
+  double lx, ly;   /* box lengths */
+  double mu, eta;  /* viscosity (ini nu), resistivity (the reference driver: 1e-4) */
+  double cs;       /* sound speed, P = CS^2 rho (the reference driver: 1/M = 100) */
+  double kf, a;    /* forcing wavenumber and amplitude (the reference driver: 1, 1) */
+  double dt;       /* AB2 time step */
+} tara_com2d_config;
+
+typedef struct tara_com2d tara_com2d;
+
+void tara_com2d_default_config(tara_com2d_config* cfg, int nx, int ny);
+int tara_com2d_create(const tara_com2d_config* cfg, tara_com2d** out);
+int tara_com2d_destroy(tara_com2d* h);
+/* state6 = rho, rho ux, rho uy, E, Bx, By as six dense complex (Nh,Ny) arrays;
+ * hist6 the AB2 history or NULL for zero. */
+int tara_com2d_set_state(tara_com2d* h, const double* state6, const double* hist6);
+int tara_com2d_get_state(tara_com2d* h, double* state6, double* hist6);
+int tara_com2d_rhs(tara_com2d* h, double* d6);
+int tara_com2d_step(tara_com2d* h, int nsteps);
+int tara_com2d_synchronize(tara_com2d* h);
+void* tara_com2d_stream(tara_com2d* h);
+int tara_com2d_launches_per_step(tara_com2d* h);
+/* The driver's initial state (src/main2com.f95:229-291) with the handle's CS
+ * and kf: rho = 1, ux = -sin(kf y), uy = sin(kf x), Bx = By = b0, Lx = lx_ini*pi. */
+int tara_com2d_init_reference(tara_com2d* h, double lx_ini, double ly_ini, double b0);
+
 typedef struct tara3d_config {
   int nx, ny, nz;      /* powers of two, 16..256 */
   int defined;         /* 0: k^2 f / 450 as the reference; 1: nu_u k^2 u and eta_b k^2 B */

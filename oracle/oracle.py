@@ -68,6 +68,19 @@ def coh_params(pi=PI_R8, lx=2 * PI_R8, ly=2 * PI_R8, mux=2e-4, muy=2e-4, cs=3.77
     return CohParams(pi, lx, ly, mux, muy, cs)
 
 
+class ComParams(ctypes.Structure):
+    """oracle_com_params (oracle/tara_oracle.h)."""
+    _fields_ = [(n, ctypes.c_double) for n in ("pi", "lx", "ly", "mu", "eta", "cs", "kf", "a")] + [
+        ("defined", ctypes.c_int)]
+
+
+def com_params(pi=PI_R8, lx=2 * PI_R8, ly=2 * PI_R8, mu=1e-3, eta=1e-4, cs=100.0, kf=1.0, a=1.0,
+               defined=0) -> ComParams:
+    """Defaults: src/main2com.f95 (eta = 1e-4, CS = 1/M = 100, kf = A = 1; mu is the
+    ini's nu, 1e-3 here)."""
+    return ComParams(pi, lx, ly, mu, eta, cs, kf, a, defined)
+
+
 def mhd_params(lx=2 * PI_R8, ly=2 * PI_R8, lz=2 * PI_R8, mu=0.01, eta=0.005, cs=10.0,
                defined=0, nu_u=0.0, eta_b=0.0) -> MhdParams:
     return MhdParams(lx, ly, lz, mu, eta, cs, defined, nu_u, eta_b)
@@ -101,6 +114,10 @@ class Oracle:
         L.oracle_ab2coh.argtypes = [c_int, c_int, c_double, vp, vp, vp, vp]
         L.oracle_run_coh.argtypes = [c_int, c_int, vp, c_double, c_int, vp, vp]
         L.oracle_ic_coh.argtypes = [c_int, c_int, c_double, c_double, vp]
+        L.oracle_derive2com.argtypes = [c_int, c_int, vp, vp, vp]
+        L.oracle_ab2com.argtypes = [c_int, c_int, c_double, vp, vp, vp, vp]
+        L.oracle_run_com.argtypes = [c_int, c_int, vp, c_double, c_int, vp, vp]
+        L.oracle_ic_com.argtypes = [c_int, c_int, c_double, c_double, c_double, c_double, c_double, vp]
         self.is_fftw = bool(L.oracle_backend_is_fftw())
 
     def set_threads(self, n: int) -> None:
@@ -256,6 +273,36 @@ class Oracle:
     def ic_coh(self, nx, ny, l_ini=2.0):
         out = np.zeros((3, ny, nx // 2 + 1), np.complex128)
         self.L.oracle_ic_coh(nx, ny, l_ini, l_ini, out.ctypes.data)
+        return out
+
+    # 2D compressible MHD: state (6, Ny, Nh) = (rho, rho ux, rho uy, E, Bx, By)
+    def derive2com(self, state, params):
+        state = np.ascontiguousarray(state, np.complex128)
+        _, ny, nh = state.shape
+        out = np.zeros_like(state)
+        self.L.oracle_derive2com(2 * (nh - 1), ny, ctypes.addressof(params), state.ctypes.data,
+                                 out.ctypes.data)
+        return out
+
+    def ab2com(self, state, d_old, d_new, dt):
+        state, d_old, d_new = (np.ascontiguousarray(a, np.complex128) for a in (state, d_old, d_new))
+        _, ny, nh = state.shape
+        out = np.zeros_like(state)
+        self.L.oracle_ab2com(2 * (nh - 1), ny, dt, state.ctypes.data, out.ctypes.data,
+                             d_old.ctypes.data, d_new.ctypes.data)
+        return out
+
+    def run_com(self, state, params, dt, steps, hist=None):
+        st = np.ascontiguousarray(state, np.complex128).copy()
+        h = np.zeros_like(st) if hist is None else np.ascontiguousarray(hist, np.complex128).copy()
+        _, ny, nh = st.shape
+        self.L.oracle_run_com(2 * (nh - 1), ny, ctypes.addressof(params), dt, int(steps),
+                              st.ctypes.data, h.ctypes.data)
+        return st, h
+
+    def ic_com(self, nx, ny, l_ini=2.0, cs=100.0, kf=1.0, b0=1.0):
+        out = np.zeros((6, ny, nx // 2 + 1), np.complex128)
+        self.L.oracle_ic_com(nx, ny, l_ini, l_ini, cs, kf, b0, out.ctypes.data)
         return out
 
     def derive3com(self, state, params):

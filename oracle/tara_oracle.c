@@ -1301,3 +1301,178 @@ void oracle_ic_coh(int nx, int ny, double lx_ini, double ly_ini, double* state) 
   }
   free(n); free(w); free(wk);
 }
+
+/* ------------------------------------------------------------------------- */
+/* derive2com -- src/derive2com.f95:5-426                                     */
+/* ------------------------------------------------------------------------- */
+void oracle_derive2com(int nx, int ny, const oracle_com_params* p, const double* state,
+                       double* dstate) {
+  const int nh = nx / 2 + 1;
+  const size_t ns = (size_t)nh * ny, nr = (size_t)nx * ny, s2 = 2 * ns;
+  const double* rho_ux_k = state + s2;
+  const double* rho_uy_k = state + 2 * s2;
+  const double* Bx_k = state + 4 * s2;
+  const double* By_k = state + 5 * s2;
+  double* re = (double*)xcalloc(6 * nr, sizeof(double));  /* rho rho_ux rho_uy E Bx By */
+  double* vel = (double*)xcalloc(4 * nr, sizeof(double)); /* ux uy Fx Fy */
+  double* vk = (double*)xcalloc(4 * s2, sizeof(double));  /* ux_k uy_k Fx_k Fy_k */
+  double* dk = (double*)xcalloc(4 * s2, sizeof(double));  /* i kx ux, i ky uy, i ky Bx, i kx By */
+  double* dr = (double*)xcalloc(4 * nr, sizeof(double));
+  double* tr = (double*)xcalloc(9 * nr, sizeof(double));  /* the nine flux fields */
+  double* tk = (double*)xcalloc(9 * s2, sizeof(double));
+  for (int f = 0; f < 6; ++f) oracle_c2r_2d(nx, ny, state + f * s2, re + f * nr); /* :68-84 */
+  const double nn = (double)nx * (double)ny;
+  const double dx = p->lx / (double)nx, dy = p->ly / (double)ny;
+  for (int j = 0; j < ny; ++j) {
+    const double y = (double)(float)j * dy;
+    for (int i = 0; i < nx; ++i) {
+      const double x = (double)(float)i * dx;
+      const size_t r = (size_t)j * nx + i;
+      for (int f = 0; f < 6; ++f) re[f * nr + r] = re[f * nr + r] / nn; /* :90-101 */
+      const double rho = re[r];
+      vel[r] = re[nr + r] / rho;          /* ux (:104) */
+      vel[nr + r] = re[2 * nr + r] / rho; /* uy (:105) */
+      vel[2 * nr + r] = -(rho * p->a * sin(p->kf * y)); /* Fx (:108) */
+      vel[3 * nr + r] = +rho * p->a * sin(p->kf * x);   /* Fy (:109) */
+    }
+  }
+  for (int f = 0; f < 4; ++f) oracle_r2c_2d(nx, ny, vel + f * nr, vk + f * s2); /* :122-132 */
+  for (int i = 0; i < nh; ++i) { /* :136-160 */
+    const double kx = kx_of(i, p->pi, p->lx);
+    for (int j = 0; j < ny; ++j) {
+      const double ky = ky_of(j, ny, p->pi, p->ly);
+      const size_t q = 2 * ((size_t)j * nh + i);
+      dk[q] = -kx * vk[q + 1];            dk[q + 1] = kx * vk[q];
+      dk[s2 + q] = -ky * vk[s2 + q + 1];  dk[s2 + q + 1] = ky * vk[s2 + q];
+      dk[2 * s2 + q] = -ky * Bx_k[q + 1]; dk[2 * s2 + q + 1] = ky * Bx_k[q];
+      dk[3 * s2 + q] = -kx * By_k[q + 1]; dk[3 * s2 + q + 1] = kx * By_k[q];
+    }
+  }
+  for (int f = 0; f < 4; ++f) oracle_c2r_2d(nx, ny, dk + f * s2, dr + f * nr); /* :165-175 */
+  for (size_t r = 0; r < nr; ++r) { /* :181-213 */
+    const double d_ux_dx = dr[r] / nn, d_uy_dy = dr[nr + r] / nn;
+    double d_Bx_dy, d_By_dx;
+    if (p->defined) {
+      d_Bx_dy = dr[2 * nr + r] / nn;
+      d_By_dx = dr[3 * nr + r] / nn;
+    } else { /* :186-187 */
+      d_Bx_dy = d_ux_dx / nn;
+      d_By_dx = d_uy_dy / nn;
+    }
+    const double curl_B = d_By_dx - d_Bx_dy;
+    const double rho = re[r], rho_ux = re[nr + r], rho_uy = re[2 * nr + r], E = re[3 * nr + r];
+    const double Bx = re[4 * nr + r], By = re[5 * nr + r];
+    const double ux = vel[r], uy = vel[nr + r];
+    const double B2 = Bx * Bx + By * By;
+    const double P = p->cs * p->cs * rho;
+    tr[0 * nr + r] = rho_ux * ux + P + B2 / 2.0 - Bx * Bx; /* Mom_x_1 */
+    tr[1 * nr + r] = rho_ux * uy - Bx * By;                /* Mom_x_2 */
+    tr[2 * nr + r] = rho_ux * uy - Bx * By;                /* Mom_y_1 */
+    tr[3 * nr + r] = rho_uy * uy + P + B2 / 2.0 - By * By; /* Mom_y_2 */
+    double ex = (E + P + B2 / 2.0) * ux - ux * Bx * Bx - uy * Bx * By;
+    ex = ex - p->eta * By * curl_B;
+    double ey = (E + P + B2 / 2.0) * uy - ux * Bx * By - uy * By * By;
+    ey = ey + p->eta * Bx * curl_B;
+    tr[4 * nr + r] = ex;                                   /* Energy_x */
+    tr[5 * nr + r] = ey;                                   /* Energy_y */
+    const double dv = d_ux_dx + d_uy_dy;
+    tr[6 * nr + r] = dv * dv;                              /* E_Visc */
+    tr[7 * nr + r] = uy * Bx - By * ux;                    /* Mag_x */
+    tr[8 * nr + r] = ux * By - Bx * uy;                    /* Mag_y */
+  }
+  for (int f = 0; f < 9; ++f) oracle_r2c_2d(nx, ny, tr + f * nr, tk + f * s2); /* :217-241 */
+  const double cut = ((double)(nx + ny) / 2.0) / 3.0;
+  for (int i = 0; i < nh; ++i) { /* :248-414 */
+    const double kx = kx_of(i, p->pi, p->lx);
+    for (int j = 0; j < ny; ++j) {
+      const double ky = ky_of(j, ny, p->pi, p->ly);
+      const size_t q = 2 * ((size_t)j * nh + i);
+      const int cut_here = sqrt(kx * kx + ky * ky) >= cut;
+      for (int c = 0; c < 2; ++c) {
+        /* (0,1) k f: real part -k Im f, imaginary part k Re f */
+#define IK(k_, f_) ((c) == 0 ? -(k_) * (f_)[q + 1] : (k_) * (f_)[q])
+        double ikx_rux = IK(kx, rho_ux_k), iky_ruy = IK(ky, rho_uy_k);
+        double ikx_m11 = IK(kx, tk), iky_m12 = IK(ky, tk + s2);
+        double ikx_m21 = IK(kx, tk + 2 * s2), iky_m22 = IK(ky, tk + 3 * s2);
+        double kx2ux = kx * kx * vk[q + c], ky2ux = ky * ky * vk[q + c];
+        double kx2uy = kx * kx * vk[s2 + q + c], ky2uy = ky * ky * vk[s2 + q + c];
+        double ikx_ex = IK(kx, tk + 4 * s2), iky_ey = IK(ky, tk + 5 * s2);
+        double ev = tk[6 * s2 + q + c];
+        double iky_mgx = IK(ky, tk + 7 * s2), ikx_mgy = IK(kx, tk + 8 * s2);
+        double kx2bx = kx * kx * Bx_k[q + c], ky2bx = ky * ky * Bx_k[q + c];
+        double kx2by = kx * kx * By_k[q + c], ky2by = ky * ky * By_k[q + c];
+#undef IK
+        if (cut_here) {
+          ikx_rux = iky_ruy = ikx_m11 = iky_m12 = ikx_m21 = iky_m22 = 0.0;
+          kx2ux = ky2ux = kx2uy = ky2uy = ikx_ex = iky_ey = ev = iky_mgx = ikx_mgy = 0.0;
+          kx2bx = ky2bx = kx2by = ky2by = 0.0;
+        }
+        const double fx = vk[2 * s2 + q + c], fy = vk[3 * s2 + q + c];
+        double d;
+        dstate[q + c] = -(ikx_rux + iky_ruy);
+        d = -(ikx_m11 + iky_m12);
+        dstate[s2 + q + c] = d - p->mu * (kx2ux + ky2ux) + fx;
+        d = -(ikx_m21 + iky_m22);
+        dstate[2 * s2 + q + c] = d - p->mu * (kx2uy + ky2uy) + fy;
+        d = -(ikx_ex + iky_ey);
+        dstate[3 * s2 + q + c] = d + p->mu * ev;
+        dstate[4 * s2 + q + c] = -iky_mgx - p->eta * (kx2bx + ky2bx);
+        dstate[5 * s2 + q + c] = -ikx_mgy - p->eta * (kx2by + ky2by);
+      }
+    }
+  }
+  free(re); free(vel); free(vk); free(dk); free(dr); free(tr); free(tk);
+}
+
+void oracle_ab2com(int nx, int ny, double dt, const double* state, double* state_new,
+                   const double* d_old, const double* d_new) {
+  const int nh = nx / 2 + 1;
+  const size_t n2 = 2 * (size_t)nh * ny;
+  for (int f = 0; f < 6; ++f)
+    ab2_update(nh, ny, dt, state + f * n2, state_new + f * n2, d_old + f * n2, d_new + f * n2);
+}
+
+void oracle_run_com(int nx, int ny, const oracle_com_params* p, double dt, int nsteps,
+                    double* state, double* hist) {
+  const int nh = nx / 2 + 1;
+  const size_t n12 = 12 * (size_t)nh * ny;
+  double* sn = (double*)xcalloc(n12, sizeof(double));
+  double* dn = (double*)xcalloc(n12, sizeof(double));
+  for (int s = 0; s < nsteps; ++s) {
+    oracle_derive2com(nx, ny, p, state, dn);
+    oracle_ab2com(nx, ny, dt, state, sn, hist, dn);
+    memcpy(hist, dn, n12 * sizeof(double));
+    memcpy(state, sn, n12 * sizeof(double));
+  }
+  free(sn); free(dn);
+}
+
+void oracle_ic_com(int nx, int ny, double lx_ini, double ly_ini, double cs, double kf, double b0,
+                   double* state) {
+  const double pi = PI_R8;
+  const double lx = lx_ini * pi, ly = ly_ini * pi;
+  const double dx = lx / (double)nx, dy = ly / (double)ny;
+  const double spheat = 5.0 / 3.0, rho0 = 1.0;
+  const int nh = nx / 2 + 1;
+  const size_t ns = (size_t)nh * ny, nr = (size_t)nx * ny;
+  double* re = (double*)xcalloc(6 * nr, sizeof(double));
+  for (int i = 0; i < nx; ++i) {
+    const double x = (double)(float)i * dx;
+    for (int j = 0; j < ny; ++j) {
+      const double y = (double)(float)j * dy;
+      const size_t r = (size_t)j * nx + i;
+      const double rho = rho0, ux = -sin(kf * y), uy = sin(kf * x);
+      const double P = cs * cs * rho, Bx = b0, By = b0;
+      const double E = P / (spheat - 1.0) + 0.50 * rho * (ux * ux + uy * uy) + 0.50 * (Bx * Bx + By * By);
+      re[r] = rho;
+      re[nr + r] = rho * ux;
+      re[2 * nr + r] = rho * uy;
+      re[3 * nr + r] = E;
+      re[4 * nr + r] = Bx;
+      re[5 * nr + r] = By;
+    }
+  }
+  for (int f = 0; f < 6; ++f) oracle_r2c_2d(nx, ny, re + f * nr, state + f * 2 * ns);
+  free(re);
+}
+

@@ -162,6 +162,35 @@ void oracle_run_coh(int nx, int ny, const oracle_coh_params* p, double dt, int n
  * taken here as 2 pi r/5 with r = -1..-5. */
 void oracle_ic_coh(int nx, int ny, double lx_ini, double ly_ini, double* state);
 
+/* ---- 2D compressible MHD (src/derive2com.f95, src/ab2com.f95) ---------- */
+typedef struct {
+  double pi;       /* the pi argument of kx = 2 pi (i-1)/Lx */
+  double lx, ly;   /* /comm/ Lx, Ly */
+  double mu, eta;  /* /comm/ viscosity, resistivity */
+  double cs;       /* /comm/ sound speed, P = CS^2 rho */
+  double kf, a;    /* /comm/ forcing wavenumber and amplitude */
+  int defined;     /* 0: curl B from d_ux_dx, d_uy_dy / (Nx Ny) as the reference
+                      (src/derive2com.f95:186-187); 1: from dBx/dy, dBy/dx */
+} oracle_com_params;
+
+/* src/derive2com.f95:5-426: state = (rho, rho ux, rho uy, E, Bx, By), six
+ * complex (Nh,Ny) spectra back to back; writes the six d/dt spectra.  The
+ * forcing's coordinates x(i), y(j) are local arrays the reference never sets
+ * (:16,109-110); here they are the driver's grid, (i-1) Lx/Nx and (j-1) Ly/Ny. */
+void oracle_derive2com(int nx, int ny, const oracle_com_params* p, const double* state,
+                       double* dstate);
+/* src/ab2com.f95: AB2 of the six fields */
+void oracle_ab2com(int nx, int ny, double dt, const double* state, double* state_new,
+                   const double* d_old, const double* d_new);
+/* derive2com + ab2com + the rotation of src/main2com.f95:375-414, nsteps times */
+void oracle_run_com(int nx, int ny, const oracle_com_params* p, double dt, int nsteps,
+                    double* state, double* hist);
+/* Initial state of src/main2com.f95:229-291: rho = 1, ux = -sin(kf y),
+ * uy = sin(kf x), P = CS^2 rho, Bx = By = B0, E = P/(5/3 - 1) + rho |u|^2/2 +
+ * |B|^2/2 (x = 0.0d0+real(i-1)*dx, Lx = lx_ini pi). */
+void oracle_ic_com(int nx, int ny, double lx_ini, double ly_ini, double cs, double kf, double b0,
+                   double* state);
+
 #ifdef __cplusplus
 }
 #endif

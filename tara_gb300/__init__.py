@@ -63,6 +63,17 @@ class CohConfig(ctypes.Structure):
         (n, ctypes.c_double) for n in ("kpi", "lx", "ly", "mux", "muy", "cs", "dt")]
 
 
+class ComConfig(ctypes.Structure):
+    _fields_ = [("nx", ctypes.c_int), ("ny", ctypes.c_int), ("defined", ctypes.c_int)] + [
+        (n, ctypes.c_double) for n in ("kpi", "lx", "ly", "mu", "eta", "cs", "kf", "a", "dt")]
+
+
+class ComCommon(ctypes.Structure):
+    """The 2D compressible MHD code's view of /comm/ (src/derive2com.f95:43)."""
+    _fields_ = [(n, ctypes.c_double) for n in ("Lx", "Ly", "spheat", "mu", "ms", "CS", "mu_0", "eta",
+                                                 "dt", "kf", "A")]
+
+
 class CohCommon(ctypes.Structure):
     """The 2D compressible code's view of /comm/ (src/derive2coh.f95:30)."""
     _fields_ = [(n, ctypes.c_double) for n in ("Lx", "Ly", "mux", "muy", "ms", "CS", "dt")]
@@ -170,6 +181,23 @@ def _declare(L: ctypes.CDLL) -> None:
     L.tara_coh2d_stream.argtypes = [vp]
     L.tara_coh2d_stream.restype = vp
     L.tara_coh2d_init_vortices.argtypes = [vp, c_double, c_double]
+    L.tara_com2d_default_config.argtypes = [vp, c_int, c_int]
+    L.tara_com2d_default_config.restype = None
+    L.tara_com2d_create.argtypes = [vp, vp]
+    L.tara_com2d_destroy.argtypes = [vp]
+    L.tara_com2d_set_state.argtypes = [vp, vp, vp]
+    L.tara_com2d_get_state.argtypes = [vp, vp, vp]
+    L.tara_com2d_rhs.argtypes = [vp, vp]
+    L.tara_com2d_step.argtypes = [vp, c_int]
+    L.tara_com2d_synchronize.argtypes = [vp]
+    L.tara_com2d_launches_per_step.argtypes = [vp]
+    L.tara_com2d_stream.argtypes = [vp]
+    L.tara_com2d_stream.restype = vp
+    L.tara_com2d_init_reference.argtypes = [vp, c_double, c_double, c_double]
+    L.derive2com_.argtypes = [ip, ip, ip, dp, dp] + [vp] * 18
+    L.derive2com_.restype = None
+    L.ab2com_.argtypes = [ip, ip, ip, dp, dp] + [vp] * 24
+    L.ab2com_.restype = None
     L.derive2coh_.argtypes = [ip, ip, ip, dp, dp] + [vp] * 9
     L.derive2coh_.restype = None
     L.ab2coh_.argtypes = [ip, ip, ip, dp, dp] + [vp] * 12
@@ -731,6 +759,123 @@ class Coh2D:
     @property
     def launches_per_step(self) -> int:
         return lib().tara_coh2d_launches_per_step(self._h)
+
+
+# ---------------------------------------------------------------------------
+# 2D compressible MHD
+# ---------------------------------------------------------------------------
+def com_common() -> ComCommon:
+    """libtara's /comm/ seen with the 2D compressible MHD layout (read by derive2com_/ab2com_)."""
+    return ComCommon.from_address(ctypes.addressof(MhdCommon.in_dll(lib(), "comm_")))
+
+
+def _state6(a) -> np.ndarray:
+    a = np.ascontiguousarray(a, dtype=np.complex128)
+    if a.ndim != 3 or a.shape[0] != 6:
+        raise ValueError("expected a (6, Ny, Nh) state (rho, rho ux, rho uy, E, Bx, By)")
+    return a
+
+
+def derive2com(state, pi: float = 3.14159265358979323846, time: float = 0.0) -> np.ndarray:
+    """subroutine derive2com (src/derive2com.f95:5): the six d_*_k_dt_new arrays."""
+    st = _state6(state)
+    _, ny, nh = st.shape
+    out = np.zeros_like(st)
+    old = np.zeros_like(st[0])
+    args = []
+    for f in range(6):
+        args += [old.ctypes.data, out[f].ctypes.data]
+    lib().derive2com_(*_ints(2 * (nh - 1), ny, nh), *_dbls(pi, time), *[st[f].ctypes.data for f in range(6)],
+                      *args)
+    _check(lib().tara_last_error())
+    return out
+
+
+def ab2com(state, d_old, d_new, pi: float = 3.14159265358979323846, time: float = 0.0) -> np.ndarray:
+    """subroutine ab2com (src/ab2com.f95): the six *_k_new arrays, dt from /comm/."""
+    st, do, dn = _state6(state), _state6(d_old), _state6(d_new)
+    _, ny, nh = st.shape
+    out = np.zeros_like(st)
+    pairs = []
+    for f in range(6):
+        pairs += [do[f].ctypes.data, dn[f].ctypes.data]
+    lib().ab2com_(*_ints(2 * (nh - 1), ny, nh), *_dbls(pi, time), *[st[f].ctypes.data for f in range(6)],
+                  *[out[f].ctypes.data for f in range(6)], *pairs)
+    _check(lib().tara_last_error())
+    return out
+
+
+class Com2D:
+    """Device-resident 2D compressible MHD state (tara_com2d handle)."""
+
+    def __init__(self, nx: int, ny: int | None = None, **kw):
+        ny = nx if ny is None else ny
+        cfg = ComConfig()
+        lib().tara_com2d_default_config(ctypes.byref(cfg), nx, ny)
+        for k, v in kw.items():
+            setattr(cfg, k, v)
+        h = ctypes.c_void_p()
+        _check(lib().tara_com2d_create(ctypes.byref(cfg), ctypes.byref(h)))
+        self._h = h
+        self.shape = (ny, nx // 2 + 1)
+        self.nx, self.ny = nx, ny
+        self.cfg = cfg
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().tara_com2d_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def set_state(self, state, hist=None):
+        st = _state6(state)
+        h = None if hist is None else _state6(hist)
+        _check(lib().tara_com2d_set_state(self._h, st.ctypes.data, None if h is None else h.ctypes.data))
+
+    def get_state(self, with_history: bool = False):
+        st = np.zeros((6,) + self.shape, np.complex128)
+        h = np.zeros_like(st) if with_history else None
+        _check(lib().tara_com2d_get_state(self._h, st.ctypes.data, None if h is None else h.ctypes.data))
+        return (st, h) if with_history else st
+
+    def get_state_into(self, out: np.ndarray) -> None:
+        """Copy the state into a caller-owned (6, Ny, Nh) complex128 array (e.g. pinned)."""
+        if out.shape != (6,) + self.shape or out.dtype != np.complex128 or not out.flags.c_contiguous:
+            raise ValueError("out must be a C-contiguous (6, Ny, Nh) complex128 array")
+        _check(lib().tara_com2d_get_state(self._h, out.ctypes.data, None))
+
+    def init_reference(self, lx_ini: float = 2.0, ly_ini: float = 2.0, b0: float = 1.0):
+        _check(lib().tara_com2d_init_reference(self._h, lx_ini, ly_ini, b0))
+
+    def rhs(self):
+        out = np.zeros((6,) + self.shape, np.complex128)
+        _check(lib().tara_com2d_rhs(self._h, out.ctypes.data))
+        return out
+
+    def step(self, n: int = 1):
+        _check(lib().tara_com2d_step(self._h, int(n)))
+
+    def synchronize(self):
+        _check(lib().tara_com2d_synchronize(self._h))
+
+    @property
+    def stream(self) -> int:
+        return lib().tara_com2d_stream(self._h) or 0
+
+    @property
+    def launches_per_step(self) -> int:
+        return lib().tara_com2d_launches_per_step(self._h)
 
 
 # ---------------------------------------------------------------------------

@@ -6,7 +6,7 @@ transform through FFTW 3.3.9 compiled from the reference's own vendored sources
 transform as src/derive2csh.f95:73-106 does.  The fixtures pin the portable
 own-FFT oracle (tests/test_oracle.py) and the GPU path (tests/test_gpu_*.py).
 
-Run from the repository root:  python tests/golden/make_golden.py
+Run from the repository root:  python tests/golden/make_golden.py [2d] [3d] [coh] [com]
 """
 from __future__ import annotations
 
@@ -113,7 +113,60 @@ def main_coh() -> None:
     print(f"wrote {out} ({out.stat().st_size} bytes)")
 
 
+def smooth_com_state(O, n: int, seed: int) -> np.ndarray:
+    """A smooth six-field MHD state: rho = 1 + 0.05 r, u and B fluctuations of
+    order 0.3 about B0 = 1, E = P/(2/3) + kinetic + magnetic with CS = 100."""
+    rng = np.random.default_rng(seed)
+    x = np.arange(n) * (2 * np.pi / n)
+    X, Y = np.meshgrid(x, x)  # [y][x]
+
+    def field():
+        f = np.zeros((n, n))
+        for _ in range(6):
+            kx, ky = rng.integers(-3, 4, size=2)
+            f += rng.standard_normal() * np.cos(kx * X + ky * Y + rng.uniform(0, 2 * np.pi))
+        return f / 6.0
+
+    rho = 1.0 + 0.05 * field()
+    ux, uy = 0.3 * field(), 0.3 * field()
+    bx, by = 1.0 + 0.3 * field(), 1.0 + 0.3 * field()
+    E = 100.0**2 * rho / (5.0 / 3.0 - 1.0) + 0.5 * rho * (ux * ux + uy * uy) + 0.5 * (bx * bx + by * by)
+    return np.stack([O.r2c(f) for f in (rho, rho * ux, rho * uy, E, bx, by)])
+
+
+def main_com() -> None:
+    """tests/golden/golden_com.npz: the 2D compressible MHD path at 64^2 from the
+    FFTW oracle: the driver's initial state (src/main2com.f95:229-291), one
+    derive2com of it and of a smooth state in the faithful and the defined mode,
+    and AB2 runs from the initial state (mu = 1e-3, eta = 1e-4, CS = 100,
+    kf = A = 1, dt = 2e-4)."""
+    O = orc.load(fftw=True)
+    out = Path(__file__).resolve().parent / "golden_com.npz"
+    st = O.ic_com(64, 64)
+    g = {"ic": st, "rhs_ic": O.derive2com(st, orc.com_params())}
+    sm = smooth_com_state(O, 64, 20240602)
+    g["smooth"] = sm
+    g["rhs_smooth"] = O.derive2com(sm, orc.com_params())
+    g["rhs_smooth_defined"] = O.derive2com(sm, orc.com_params(defined=1))
+    for steps in (1, 10, 500):
+        s2, h2 = O.run_com(st, orc.com_params(), 2e-4, steps)
+        g[f"ab2_{steps}"] = s2
+        g[f"ab2_{steps}_hist"] = h2
+    s2, _ = O.run_com(sm, orc.com_params(defined=1), 2e-4, 50)
+    g["ab2_smooth_defined_50"] = s2
+    np.savez_compressed(out, **g)
+    print(f"wrote {out} ({out.stat().st_size} bytes)")
+
+
 if __name__ == "__main__":
-    main()
-    main3d()
-    main_coh()
+    import sys as _sys
+
+    which = _sys.argv[1:] or ["2d", "3d", "coh", "com"]
+    if "2d" in which:
+        main()
+    if "3d" in which:
+        main3d()
+    if "coh" in which:
+        main_coh()
+    if "com" in which:
+        main_com()
