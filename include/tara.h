@@ -303,6 +303,12 @@ int tara_coh2d_launches_per_step(tara_coh2d* h);
  * and five point vortices, velocity from the streamfunction; Lx = lx_ini*pi.
  * Zero history. */
 int tara_coh2d_init_vortices(tara_coh2d* h, double lx_ini, double ly_ini);
+/* The driver's per-step record (src/main2coh.f95:388-429) of the current state:
+ * out6 = Energy/(2NxNy), y_Energy/(2NxNy), C0..C3/(NxNy) with Energy = sum of
+ * ux^2+uy^2, y_Energy = sum of uy^2, Cp = sum of omega^p over the grid. */
+int tara_coh2d_diag(tara_coh2d* h, double* out6);
+/* n, ux, uy, omega on the grid, each [Ny][Nx] (NULL skips a field). */
+int tara_coh2d_real_fields(tara_coh2d* h, double* n, double* ux, double* uy, double* omega);
 
 /* ---- 2D compressible MHD (derive2com / ab2com) --------------------------- */
 
@@ -361,6 +367,14 @@ int tara_com2d_launches_per_step(tara_com2d* h);
 /* The driver's initial state (src/main2com.f95:229-291) with the handle's CS
  * and kf: rho = 1, ux = -sin(kf y), uy = sin(kf x), Bx = By = b0, Lx = lx_ini*pi. */
 int tara_com2d_init_reference(tara_com2d* h, double lx_ini, double ly_ini, double b0);
+/* The driver's record (src/main2com.f95:556-580) of the current state:
+ * out5 = Energy, B_Field, C2, C3, div_B_Tot, the sums over the grid of
+ * (ux^2+uy^2)/N^2, (Bx^2+By^2)/N^2, omega^2/N^2, j^2/N^2, divB/N^2 (N^2 = NxNy,
+ * omega and j the curls of u and B). */
+int tara_com2d_diag(tara_com2d* h, double* out5);
+/* rho, ux, uy, P = CS^2 rho, E, Bx, By on the grid, each [Ny][Nx] (NULL skips). */
+int tara_com2d_real_fields(tara_com2d* h, double* rho, double* ux, double* uy, double* P, double* E,
+                           double* Bx, double* By);
 
 typedef struct tara3d_config {
   int nx, ny, nz;      /* powers of two, 16..256 */

@@ -38,6 +38,7 @@ struct tara_coh2d {
   double2 *st = nullptr, *hist = nullptr, *dnew = nullptr, *spec = nullptr;
   double *real = nullptr, *prod = nullptr;
   double *kx = nullptr, *ky = nullptr;
+  double* diag = nullptr;  // per-block partial sums of the driver diagnostics
   int* i0 = nullptr;
   void *twx = nullptr, *twy = nullptr;
   unsigned int* flag = nullptr;
@@ -149,6 +150,59 @@ __global__ void k_coh_velocity(const double2* __restrict__ wk, const double* __r
     }
     ukx[q] = a;
     uky[q] = b;
+  }
+}
+
+// Driver diagnostics (src/main2coh.f95:301-429): n, ux, uy and the vorticity
+// omega_k = (0,1) kx uky - (0,1) ky ukx on the grid.
+__global__ void k_coh_diag_spec(const double2* __restrict__ st, size_t fs, const double* __restrict__ kx,
+                                const double* __restrict__ ky, int nh, int ny, int pitch,
+                                double2* __restrict__ sp) {
+  const size_t total = (size_t)ny * nh;
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += (size_t)gridDim.x * blockDim.x) {
+    const int y = (int)(t / nh), x = (int)(t % nh);
+    const size_t q = (size_t)y * pitch + x;
+    const double2 ux = st[fs + q], uy = st[2 * fs + q];
+    const double a = kx[x], b = ky[y];
+    sp[q] = st[q];
+    sp[fs + q] = ux;
+    sp[2 * fs + q] = uy;
+    sp[3 * fs + q] = make_double2((-a * uy.y) - (-b * ux.y), (a * uy.x) - (b * ux.x));
+  }
+}
+
+constexpr int kDiagBlocksC = 304;
+
+// Per-block sums of ux^2 + uy^2, uy^2, omega^0..3 (:396-405); the real fields
+// are the unnormalised c2r outputs, divided by Nx Ny here as the reference does.
+__global__ void __launch_bounds__(256) k_coh_diag_sum(const double* __restrict__ re, size_t rfs, int nx, int ny,
+                                                      int rpitch, double nn, double* __restrict__ part) {
+  double acc[6] = {0, 0, 0, 0, 0, 0};
+  const size_t total = (size_t)ny * nx;
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += (size_t)gridDim.x * blockDim.x) {
+    const size_t r = (t / nx) * rpitch + (t % nx);
+    const double ux = re[rfs + r] / nn, uy = re[2 * rfs + r] / nn, w = re[3 * rfs + r] / nn;
+    acc[0] += ux * ux + uy * uy;
+    acc[1] += uy * uy;
+    acc[2] += pow(w, 0.0);
+    acc[3] += pow(w, 1.0);
+    acc[4] += pow(w, 2.0);
+    acc[5] += pow(w, 3.0);
+  }
+  __shared__ double sh[6][8];
+#pragma unroll
+  for (int k = 0; k < 6; ++k) {
+    double v = acc[k];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) sh[k][threadIdx.x >> 5] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 6) {
+    double v = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v += sh[threadIdx.x][w];
+    part[blockIdx.x * 6 + threadIdx.x] = v;
   }
 }
 
@@ -295,7 +349,8 @@ int tara_coh2d_destroy(tara_coh2d* h) {
   if (!h) return set_ok();
   cudaSetDevice(h->dev);
   if (h->stream) cudaStreamSynchronize(h->stream);
-  void* ptrs[] = {h->st, h->hist, h->dnew, h->spec, h->real, h->prod, h->kx, h->ky, h->i0, h->twx, h->twy, h->flag};
+  void* ptrs[] = {h->st, h->hist, h->dnew, h->spec, h->real, h->prod, h->kx, h->ky, h->diag, h->i0, h->twx, h->twy,
+                  h->flag};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (h->stream) cudaStreamDestroy(h->stream);
@@ -341,6 +396,7 @@ int tara_coh2d_create(const tara_coh2d_config* cfg, tara_coh2d** out) {
   CKC(cudaMalloc(&h->ky, h->ny * sizeof(double)));
   CKC(cudaMalloc(&h->i0, h->ny * sizeof(int)));
   CKC(cudaMalloc(&h->flag, sizeof(unsigned int)));
+  CKC(cudaMalloc(&h->diag, 6 * kDiagBlocksC * sizeof(double)));
   CKC(cudaMemsetAsync(h->st, 0, 3 * sb, h->stream));
   CKC(cudaMemsetAsync(h->hist, 0, 3 * sb, h->stream));
   CKC(cudaMemsetAsync(h->dnew, 0, 3 * sb, h->stream));
@@ -420,6 +476,59 @@ int tara_coh2d_synchronize(tara_coh2d* h) {
 }
 
 void* tara_coh2d_stream(tara_coh2d* h) { return h ? (void*)h->stream : nullptr; }
+
+// n, ux, uy, omega of the current state on the grid (real spectra of the c2r
+// divided by Nx Ny) into h->real[0..3].
+static int coh_grid_fields(tara_coh2d* h) {
+  int rc;
+  k_coh_diag_spec<<<kElemBlocks, kElemThreads, 0, h->stream>>>(h->st, h->fs, h->kx, h->ky, h->nh, h->ny,
+                                                                h->pitch, h->spec);
+  TARA_CK(cudaGetLastError());
+  if ((rc = Launch2D<double>::col_fft(h->ny, h->nh, h->pitch, h->spec, h->spec, true, h->twy, h->stream, 4, h->fs)))
+    return rc;
+  return Launch2D<double>::row_c2r(h->nx, h->ny, h->pitch, h->rpitch, h->spec, h->real, h->twx, h->stream, 4,
+                                   h->fs, h->rfs);
+}
+
+int tara_coh2d_diag(tara_coh2d* h, double* out6) {
+  if (!h || !out6) return set_error(TARA_ERR_ARGS, "null argument");
+  TARA_CK(cudaSetDevice(h->dev));
+  int rc;
+  if ((rc = coh_grid_fields(h))) return rc;
+  const double nn = (double)h->nx * (double)h->ny;
+  double* part = h->diag;  // 6 x kDiagBlocksC doubles
+  k_coh_diag_sum<<<kDiagBlocksC, 256, 0, h->stream>>>(h->real, h->rfs, h->nx, h->ny, h->rpitch, nn, part);
+  TARA_CK(cudaGetLastError());
+  std::vector<double> hp(6 * kDiagBlocksC);
+  TARA_CK(cudaMemcpyAsync(hp.data(), part, hp.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  if ((rc = coh_check(h))) return rc;
+  double s[6] = {0, 0, 0, 0, 0, 0};
+  for (int b = 0; b < kDiagBlocksC; ++b)
+    for (int k = 0; k < 6; ++k) s[k] += hp[b * 6 + k];
+  out6[0] = s[0] / (2.0 * nn);  // Energy/(2 Nx Ny)
+  out6[1] = s[1] / (2.0 * nn);  // y_Energy/(2 Nx Ny)
+  for (int k = 2; k < 6; ++k) out6[k] = s[k] / nn;  // C0..C3/(Nx Ny)
+  return set_ok();
+}
+
+int tara_coh2d_real_fields(tara_coh2d* h, double* n, double* ux, double* uy, double* omega) {
+  if (!h) return set_error(TARA_ERR_ARGS, "null handle");
+  TARA_CK(cudaSetDevice(h->dev));
+  int rc;
+  if ((rc = coh_grid_fields(h))) return rc;
+  double* outs[4] = {n, ux, uy, omega};
+  std::vector<double> buf(h->rfs);
+  const double nn = (double)h->nx * (double)h->ny;
+  for (int f = 0; f < 4; ++f) {
+    if (!outs[f]) continue;
+    TARA_CK(cudaMemcpyAsync(buf.data(), h->real + f * h->rfs, h->rfs * sizeof(double), cudaMemcpyDeviceToHost,
+                            h->stream));
+    TARA_CK(cudaStreamSynchronize(h->stream));
+    for (int j = 0; j < h->ny; ++j)
+      for (int i = 0; i < h->nx; ++i) outs[f][(size_t)j * h->nx + i] = buf[(size_t)j * h->rpitch + i] / nn;
+  }
+  return set_ok();
+}
 
 int tara_coh2d_launches_per_step(tara_coh2d* h) { return h ? 7 : 0; }
 

@@ -42,6 +42,7 @@ struct tara_com2d {
   double2 *specB = nullptr;  // 4 spectra: ux_k, uy_k, Fx_k, Fy_k
   double *reA = nullptr, *reB = nullptr, *reC = nullptr, *reD = nullptr;  // 8, 4, 2, 7 real fields
   double *kx = nullptr, *ky = nullptr, *sx = nullptr, *sy = nullptr;
+  double* diag = nullptr;  // per-block partial sums of the driver diagnostics
   int* i0 = nullptr;
   void *twx = nullptr, *twy = nullptr;
   unsigned int* flag = nullptr;
@@ -203,6 +204,89 @@ __global__ void k_com_final(const double2* __restrict__ fl, const double2* __res
     }
   }
   if (bad) atomicOr(flag, 1u);
+}
+
+// Driver diagnostics (src/main2com.f95:415-586).
+// The six fields and div B = (0,1) kx Bx_k + (0,1) ky By_k on the grid.
+__global__ void k_com_diag_spec(const double2* __restrict__ st, size_t fs, const double* __restrict__ kx,
+                                const double* __restrict__ ky, int nh, int ny, int pitch,
+                                double2* __restrict__ sp) {
+  const size_t total = (size_t)ny * nh;
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += (size_t)gridDim.x * blockDim.x) {
+    const int y = (int)(t / nh), x = (int)(t % nh);
+    const size_t q = (size_t)y * pitch + x;
+#pragma unroll
+    for (int f = 0; f < 6; ++f) sp[f * fs + q] = st[f * fs + q];
+    const double2 bx = st[4 * fs + q], by = st[5 * fs + q];
+    const double a = kx[x], b = ky[y];
+    sp[6 * fs + q] = make_double2((-a * bx.y) + (-b * by.y), (a * bx.x) + (b * by.x));
+  }
+}
+
+// ux = rho_ux / rho, uy from the normalised fields (:473-488)
+__global__ void k_com_diag_vel(const double* __restrict__ re, size_t rfs, int nx, int ny, int rpitch, double nn,
+                               double* __restrict__ out) {
+  const size_t total = (size_t)ny * nx;
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += (size_t)gridDim.x * blockDim.x) {
+    const size_t r = (t / nx) * rpitch + (t % nx);
+    const double rho = re[r] / nn;
+    out[r] = (re[rfs + r] / nn) / rho;
+    out[rfs + r] = (re[2 * rfs + r] / nn) / rho;
+  }
+}
+
+// omega_k = (0,1) kx uy_k - (0,1) ky ux_k, j_k = (0,1) kx By_k - (0,1) ky Bx_k (:500-520)
+__global__ void k_com_diag_curl(const double2* __restrict__ vk, const double2* __restrict__ st, size_t fs,
+                                const double* __restrict__ kx, const double* __restrict__ ky, int nh, int ny,
+                                int pitch, double2* __restrict__ sp) {
+  const size_t total = (size_t)ny * nh;
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += (size_t)gridDim.x * blockDim.x) {
+    const int y = (int)(t / nh), x = (int)(t % nh);
+    const size_t q = (size_t)y * pitch + x;
+    const double a = kx[x], b = ky[y];
+    const double2 ux = vk[q], uy = vk[fs + q], bx = st[4 * fs + q], by = st[5 * fs + q];
+    sp[q] = make_double2((-a * uy.y) - (-b * ux.y), (a * uy.x) - (b * ux.x));
+    sp[fs + q] = make_double2((-a * by.y) - (-b * bx.y), (a * by.x) - (b * bx.x));
+  }
+}
+
+constexpr int kDiagBlocksM = 304;
+
+// Per-block sums of (ux^2+uy^2)/N^2, (Bx^2+By^2)/N^2, omega^2/N^2, j^2/N^2,
+// divB/N^2 (:560-575); reA holds the six unnormalised fields and div B.
+__global__ void __launch_bounds__(256) k_com_diag_sum(const double* __restrict__ reA, const double* __restrict__ reB,
+                                                      const double* __restrict__ reC, size_t rfs, int nx, int ny,
+                                                      int rpitch, double nn, double* __restrict__ part) {
+  double acc[5] = {0, 0, 0, 0, 0};
+  const size_t total = (size_t)ny * nx;
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += (size_t)gridDim.x * blockDim.x) {
+    const size_t r = (t / nx) * rpitch + (t % nx);
+    const double ux = reB[r], uy = reB[rfs + r];
+    const double bx = reA[4 * rfs + r] / nn, by = reA[5 * rfs + r] / nn, divb = reA[6 * rfs + r] / nn;
+    const double w = reC[r] / nn, jb = reC[rfs + r] / nn;
+    acc[0] += (ux * ux + uy * uy) / nn;
+    acc[1] += (bx * bx + by * by) / nn;
+    acc[2] += pow(w, 2.0) / nn;
+    acc[3] += pow(jb, 2.0) / nn;
+    acc[4] += divb / nn;
+  }
+  __shared__ double sh[5][8];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    double v = acc[k];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) sh[k][threadIdx.x >> 5] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 5) {
+    double v = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v += sh[threadIdx.x][w];
+    part[blockIdx.x * 5 + threadIdx.x] = v;
+  }
 }
 
 int com_copy_in(tara_com2d* h, double2* dst, const double* host) {
@@ -376,8 +460,8 @@ int tara_com2d_destroy(tara_com2d* h) {
   if (!h) return set_ok();
   cudaSetDevice(h->dev);
   if (h->stream) cudaStreamSynchronize(h->stream);
-  void* ptrs[] = {h->st,  h->hist, h->dnew, h->specA, h->specB, h->reA, h->reB, h->reC, h->reD,
-                  h->kx,  h->ky,   h->sx,   h->sy,    h->i0,    h->twx, h->twy, h->flag};
+  void* ptrs[] = {h->st, h->hist, h->dnew, h->specA, h->specB, h->reA, h->reB, h->reC, h->reD,
+                  h->kx, h->ky,   h->sx,   h->sy,    h->diag,  h->i0,  h->twx, h->twy, h->flag};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (h->stream) cudaStreamDestroy(h->stream);
@@ -428,6 +512,7 @@ int tara_com2d_create(const tara_com2d_config* cfg, tara_com2d** out) {
   CKC(cudaMalloc(&h->sy, h->ny * sizeof(double)));
   CKC(cudaMalloc(&h->i0, h->ny * sizeof(int)));
   CKC(cudaMalloc(&h->flag, sizeof(unsigned int)));
+  CKC(cudaMalloc(&h->diag, 5 * kDiagBlocksM * sizeof(double)));
   CKC(cudaMemsetAsync(h->st, 0, 6 * sb, h->stream));
   CKC(cudaMemsetAsync(h->hist, 0, 6 * sb, h->stream));
   CKC(cudaMemsetAsync(h->dnew, 0, 6 * sb, h->stream));
@@ -501,6 +586,83 @@ int tara_com2d_synchronize(tara_com2d* h) {
 }
 
 void* tara_com2d_stream(tara_com2d* h) { return h ? (void*)h->stream : nullptr; }
+
+// The six fields, div B, u, omega and j on the grid: reA[0..6] (unnormalised),
+// reB[0..1] = ux, uy, reC[0..1] = omega, j (unnormalised).
+static int com_grid_fields(tara_com2d* h) {
+  cudaStream_t s = h->stream;
+  const double nn = (double)h->nx * (double)h->ny;
+  int rc;
+  k_com_diag_spec<<<kElemBlocks, kElemThreads, 0, s>>>(h->st, h->fs, h->kx, h->ky, h->nh, h->ny, h->pitch,
+                                                        h->specA);
+  TARA_CK(cudaGetLastError());
+  if ((rc = Launch2D<double>::col_fft(h->ny, h->nh, h->pitch, h->specA, h->specA, true, h->twy, s, 7, h->fs)))
+    return rc;
+  if ((rc = Launch2D<double>::row_c2r(h->nx, h->ny, h->pitch, h->rpitch, h->specA, h->reA, h->twx, s, 7, h->fs,
+                                      h->rfs)))
+    return rc;
+  k_com_diag_vel<<<kElemBlocks, kElemThreads, 0, s>>>(h->reA, h->rfs, h->nx, h->ny, h->rpitch, nn, h->reB);
+  TARA_CK(cudaGetLastError());
+  if ((rc = Launch2D<double>::row_r2c(h->nx, h->ny, h->rpitch, h->pitch, h->reB, h->specB, h->twx, s, 2, h->rfs,
+                                      h->fs)))
+    return rc;
+  if ((rc = Launch2D<double>::col_fft(h->ny, h->nh, h->pitch, h->specB, h->specB, false, h->twy, s, 2, h->fs)))
+    return rc;
+  k_com_diag_curl<<<kElemBlocks, kElemThreads, 0, s>>>(h->specB, h->st, h->fs, h->kx, h->ky, h->nh, h->ny,
+                                                        h->pitch, h->specA);
+  TARA_CK(cudaGetLastError());
+  if ((rc = Launch2D<double>::col_fft(h->ny, h->nh, h->pitch, h->specA, h->specA, true, h->twy, s, 2, h->fs)))
+    return rc;
+  return Launch2D<double>::row_c2r(h->nx, h->ny, h->pitch, h->rpitch, h->specA, h->reC, h->twx, s, 2, h->fs,
+                                   h->rfs);
+}
+
+int tara_com2d_diag(tara_com2d* h, double* out5) {
+  if (!h || !out5) return set_error(TARA_ERR_ARGS, "null argument");
+  TARA_CK(cudaSetDevice(h->dev));
+  int rc;
+  if ((rc = com_grid_fields(h))) return rc;
+  const double nn = (double)h->nx * (double)h->ny;
+  k_com_diag_sum<<<kDiagBlocksM, 256, 0, h->stream>>>(h->reA, h->reB, h->reC, h->rfs, h->nx, h->ny, h->rpitch, nn,
+                                                       h->diag);
+  TARA_CK(cudaGetLastError());
+  std::vector<double> hp(5 * kDiagBlocksM);
+  TARA_CK(cudaMemcpyAsync(hp.data(), h->diag, hp.size() * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  if ((rc = com_check(h))) return rc;
+  for (int k = 0; k < 5; ++k) out5[k] = 0.0;
+  for (int b = 0; b < kDiagBlocksM; ++b)
+    for (int k = 0; k < 5; ++k) out5[k] += hp[b * 5 + k];
+  return set_ok();
+}
+
+// rho, ux, uy, P = CS^2 rho, E, Bx, By on the grid (the driver's snapshot
+// fields, :571-573), each [Ny][Nx]; a null pointer skips a field.
+int tara_com2d_real_fields(tara_com2d* h, double* rho, double* ux, double* uy, double* P, double* E, double* Bx,
+                           double* By) {
+  if (!h) return set_error(TARA_ERR_ARGS, "null handle");
+  TARA_CK(cudaSetDevice(h->dev));
+  int rc;
+  if ((rc = com_grid_fields(h))) return rc;
+  const double nn = (double)h->nx * (double)h->ny, cs2 = h->cfg.cs * h->cfg.cs;
+  std::vector<double> buf(h->rfs);
+  struct F {
+    double* out;
+    const double* src;
+    int mode;  // 0 normalise, 1 as is (ux, uy), 2 CS^2 times the normalised rho
+  } fl[7] = {{rho, h->reA, 0}, {ux, h->reB, 1}, {uy, h->reB + h->rfs, 1}, {P, h->reA, 2},
+             {E, h->reA + 3 * h->rfs, 0}, {Bx, h->reA + 4 * h->rfs, 0}, {By, h->reA + 5 * h->rfs, 0}};
+  for (const F& f : fl) {
+    if (!f.out) continue;
+    TARA_CK(cudaMemcpyAsync(buf.data(), f.src, h->rfs * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    TARA_CK(cudaStreamSynchronize(h->stream));
+    for (int j = 0; j < h->ny; ++j)
+      for (int i = 0; i < h->nx; ++i) {
+        const double v = buf[(size_t)j * h->rpitch + i];
+        f.out[(size_t)j * h->nx + i] = f.mode == 1 ? v : f.mode == 2 ? cs2 * (v / nn) : v / nn;
+      }
+  }
+  return set_ok();
+}
 
 int tara_com2d_launches_per_step(tara_com2d* h) { return h ? 13 : 0; }
 

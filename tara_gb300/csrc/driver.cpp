@@ -1,6 +1,6 @@
 // input.ini driver: the reference program's dispatch (src/main.f95) and the
 // time loops of the solvers on the path (src/main2css.f95, src/main2csh.f95,
-// src/main3com.f95), with their output files.  Host code over the C ABI; every
+// src/main2coh.f95, src/main2com.f95, src/main3com.f95), with their output files.  Host code over the C ABI; every
 // transform and update runs in libtara's kernels.
 #include <cmath>
 #include <cstdio>
@@ -304,6 +304,149 @@ int run_3d(Reader& R, const std::string& out, int max_steps) {
   return set_ok();
 }
 
+// ---------------------------------------------------------------------------
+// tara2dHydOMP (src/main2coh.f95): 2D compressible isothermal hydro
+// ---------------------------------------------------------------------------
+int run_coh(Reader& R, const std::string& out, int max_steps) {
+  int nx = 0, ny = 0;
+  double lx = 0, ly = 0, tmin = 0, tmax = 0, dt = 0, nu = 0;
+  R.i("grid", "Nx", nx);
+  R.i("grid", "Ny", ny);
+  R.d("length", "Lx", lx);
+  R.d("length", "Ly", ly);
+  R.d("time", "time_min", tmin);
+  R.d("time", "time_max", tmax);
+  R.d("time", "dt", dt);
+  R.d("resistivity", "nu", nu);  // read, then replaced by 0.0002 (src/main2coh.f95:119-120)
+  if (!R.ok) return set_error(TARA_ERR_INI, R.err);
+  const double lx_ini = lx, ly_ini = ly;
+  lx = lx * kPi;
+  ly = ly * kPi;
+  const double dx = lx / (double)nx, dy = ly / (double)ny;
+  tara_coh2d_config cfg;
+  tara_coh2d_default_config(&cfg, nx, ny);  // mux = muy = 0.0002, CS = U0/M (:119-133)
+  cfg.kpi = kPi;
+  cfg.lx = lx;
+  cfg.ly = ly;
+  cfg.dt = dt;
+  tara_coh2d* h = nullptr;
+  if (tara_coh2d_create(&cfg, &h)) return fail_rc();
+  struct Guard {
+    tara_coh2d* h;
+    ~Guard() { tara_coh2d_destroy(h); }
+  } guard{h};
+  if (tara_coh2d_init_vortices(h, lx_ini, ly_ini)) return fail_rc();
+  mkdir(out.c_str(), 0755);
+  const size_t nr = (size_t)nx * ny;
+  std::vector<double> xs(nx), ys(ny), dn(nr), ux(nr), uy(nr), om(nr);
+  for (int i = 0; i < nx; ++i) xs[i] = 0.0 + (double)(float)i * dx;  // x(i)=0.0d0+real(i-1)*dx
+  for (int j = 0; j < ny; ++j) ys[j] = 0.0 + (double)(float)j * dy;
+  auto snapshot = [&](const std::string& path) -> int {  // x, y, omega, n, ux, uy
+    if (tara_coh2d_real_fields(h, dn.data(), ux.data(), uy.data(), om.data())) return fail_rc();
+    Out f(path);
+    for (int i = 0; i < nx; ++i)
+      for (int j = 0; j < ny; ++j) {
+        const size_t r = (size_t)j * nx + i;
+        f.rec({xs[i], ys[j], om[r], dn[r], ux[r], uy[r]});
+      }
+    return TARA_OK;
+  };
+  int rc;
+  if ((rc = snapshot(out + "/Initial_Grid_Data_Reproduced.dat"))) return rc;  // (:214-238)
+  Out energy(out + "/Energy.dat");
+  const long n = trip_count(tmin, tmax, dt);
+  const long steps = (max_steps > 0 && max_steps < n) ? max_steps : n;
+  const double every = 1.0 / (10.0 * dt);  // mod(float(t),1.0d0/(10.0d0*dt)) == 0.0 (:407)
+  double time = tmin;
+  for (long it = 0; it < steps; ++it) {
+    const long t = nint(time / dt) - (long)(tmin / dt);
+    if (tara_coh2d_step(h, 1)) return fail_rc();  // derive2coh + ab2coh + rotation (:263-298)
+    double d[6];
+    if (tara_coh2d_diag(h, d)) return fail_rc();
+    if (std::fmod((double)(float)t, every) == 0.0 && (rc = snapshot(fort_name(out, t + 100)))) return rc;
+    energy.rec({time, d[0], d[1], d[2], d[3], d[4], d[5]});
+    time = time + dt;
+  }
+  return set_ok();
+}
+
+// ---------------------------------------------------------------------------
+// tara2dMHDOMP (src/main2com.f95): 2D compressible MHD
+// ---------------------------------------------------------------------------
+int run_com(Reader& R, const std::string& out, int max_steps) {
+  int nx = 0, ny = 0;
+  double lx = 0, ly = 0, tmin = 0, tmax = 0, dt = 0, mu = 0;
+  R.i("grid", "Nx", nx);
+  R.i("grid", "Ny", ny);
+  R.d("length", "Lx", lx);
+  R.d("length", "Ly", ly);
+  R.d("time", "time_min", tmin);
+  R.d("time", "time_max", tmax);
+  R.d("time", "dt", dt);
+  R.d("resistivity", "nu", mu);
+  if (!R.ok) return set_error(TARA_ERR_INI, R.err);
+  const double lx_ini = lx, ly_ini = ly;
+  lx = lx * kPi;
+  ly = ly * kPi;
+  const double dx = lx / (double)nx, dy = ly / (double)ny;
+  // src/main2com.f95:161-215: eta = 1e-4, M = 0.01 -> CS = 100, U0 = M CS = 1,
+  // VA = U0/MA = 1, B0 = VA sqrt(mu_0 rho0) = 1, kf = A = 1
+  const double cs = 1.0 / 0.010, U0 = 0.010 * cs, B0 = (U0 / 1.0) * std::sqrt(1.0 * 1.0);
+  tara_com2d_config cfg;
+  tara_com2d_default_config(&cfg, nx, ny);
+  cfg.kpi = kPi;
+  cfg.lx = lx;
+  cfg.ly = ly;
+  cfg.mu = mu;
+  cfg.eta = 0.000100;
+  cfg.cs = cs;
+  cfg.kf = 1.0;
+  cfg.a = 1.0;
+  cfg.dt = dt;
+  cfg.defined = 0;
+  tara_com2d* h = nullptr;
+  if (tara_com2d_create(&cfg, &h)) return fail_rc();
+  struct Guard {
+    tara_com2d* h;
+    ~Guard() { tara_com2d_destroy(h); }
+  } guard{h};
+  if (tara_com2d_init_reference(h, lx_ini, ly_ini, B0)) return fail_rc();
+  mkdir(out.c_str(), 0755);
+  const size_t nr = (size_t)nx * ny;
+  std::vector<double> xs(nx), ys(ny);
+  for (int i = 0; i < nx; ++i) xs[i] = 0.0 + (double)(float)i * dx;
+  for (int j = 0; j < ny; ++j) ys[j] = 0.0 + (double)(float)j * dy;
+  Out energy(out + "/Energy.dat");
+  const long n = trip_count(tmin, tmax, dt);
+  const long steps = (max_steps > 0 && max_steps < n) ? max_steps : n;
+  double time = tmin;
+  for (long it = 0; it < steps; ++it) {
+    const long t = nint(time / dt) - (long)(tmin / dt);
+    if (tara_com2d_step(h, 1)) return fail_rc();  // derive2com + ab2com + rotation (:360-414)
+    const double tf = (double)(float)t;
+    if (std::fmod(tf, 100000.0) == 0.0) {  // fort.(t+100000): x, y, rho, ux, uy, P, E, Bx, By (:571-573)
+      std::vector<double> f[7];
+      for (auto& v : f) v.resize(nr);
+      if (tara_com2d_real_fields(h, f[0].data(), f[1].data(), f[2].data(), f[3].data(), f[4].data(), f[5].data(),
+                                 f[6].data()))
+        return fail_rc();
+      Out snap(fort_name(out, t + 100000));
+      for (int i = 0; i < nx; ++i)
+        for (int j = 0; j < ny; ++j) {
+          const size_t r = (size_t)j * nx + i;
+          snap.rec({xs[i], ys[j], f[0][r], f[1][r], f[2][r], f[3][r], f[4][r], f[5][r], f[6][r]});
+        }
+    }
+    if (std::fmod(tf, 100.0) == 0.0) {  // Energy.dat every 100 steps (:578-580)
+      double d[5];
+      if (tara_com2d_diag(h, d)) return fail_rc();
+      energy.rec({time, d[0], d[1], d[2], d[3], d[4]});
+    }
+    time = time + dt;
+  }
+  return set_ok();
+}
+
 }  // namespace
 
 extern "C" int tara_run_ini(const char* ini_path, const char* out_dir, int max_steps) {
@@ -332,12 +475,19 @@ extern "C" int tara_run_ini(const char* ini_path, const char* out_dir, int max_s
     std::printf(" tara-gb300: 3D compressible MHD solver on the GPU\n");
     return run_3d(R, out, max_steps);
   }
+  if (dim == 2 && here && mode == "openmp" && domain == "hydro") {
+    std::printf(" tara-gb300: 2D compressible isothermal hydrodynamic solver on the GPU\n");
+    return run_coh(R, out, max_steps);
+  }
+  if (dim == 2 && here && mode == "openmp" && domain == "mhd") {
+    std::printf(" tara-gb300: 2D compressible MHD solver on the GPU\n");
+    return run_com(R, out, max_steps);
+  }
   if (mode == "mpi" || arch == "multi-gpu" || (dim == 3 && mode == "serial")) {
     std::printf(" Under preparation. Please wait!\n");  // src/main.f95:40-85
     return set_ok();
   }
-  if (dim == 1 || (dim == 2 && mode == "openmp"))
-    return set_error(TARA_ERR_ARGS, "the 1D Burgers and 2D compressible solvers are outside this build");
+  if (dim == 1) return set_error(TARA_ERR_ARGS, "the 1D Burgers solver is outside this build");
   std::printf(" Incompatible Input file. Please check TARA user-manual.\n");
   return set_error(TARA_ERR_INI, "incompatible input file");
 }
