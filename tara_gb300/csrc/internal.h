@@ -85,6 +85,7 @@ struct tara2d {
   unsigned int* flag = nullptr;
   const double2* force = nullptr;  // closure forcing spectrum (batch fields), not owned
   void* scratch = nullptr;         // filter / spectrum / real-state work space
+  void* stage = nullptr;           // one dense field for page-locked host copies (lazy)
   size_t scratch_bytes = 0;
   void *twx64 = nullptr, *twy64 = nullptr;  // FP64 twiddles when the solver runs FP32
   tara::Grid2D grid;
