@@ -460,8 +460,7 @@ __global__ void __launch_bounds__(ColCfg<T, N, V>::THREADS_C)
   }
   // Pass 2: the stage update, in chunks whose loads all precede their stores
   // (the state arrays may alias the RHS input, so loads cannot move past stores).
-  constexpr int CHM = sizeof(T) == 8 ? 8 : 8;
-  constexpr int CH = PER < CHM ? PER : CHM;
+  constexpr int CH = PER < 8 ? PER : 8;
   const double dt = p.dt;
 #pragma unroll
   for (int i0 = 0; i0 < PER; i0 += CH) {

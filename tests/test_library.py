@@ -93,3 +93,31 @@ def test_no_silent_fallback_without_gpu():
     with pytest.raises(tg.TaraError) as e:
         tg.Solver2D(64)
     assert e.value.code in (tg.TARA_ERR_CUDA, tg.TARA_ERR_NOMEM)
+
+
+@pytest.mark.parametrize("name,nf", [("derive2coh_", 3), ("derive2com_", 6)])
+def test_compressible_dropins_validate_before_the_gpu(name, nf):
+    """Shape errors of the compressible drop-ins are recorded before any device
+    call (Nh inconsistent with Nx, and a size outside the transforms' range)."""
+    import numpy as np
+
+    L = tg.lib()
+    w = np.zeros((64, 10), np.complex128)
+    fn = getattr(L, name)
+    nout = 2 * nf if name == "derive2com_" else 6
+    for nx, ny, nh in ((64, 64, 10), (24, 24, 13)):
+        args = [ctypes.byref(ctypes.c_int(v)) for v in (nx, ny, nh)]
+        args += [ctypes.byref(ctypes.c_double(v)) for v in (3.14159265358979, 0.0)]
+        args += [w.ctypes.data] * (nf + nout)
+        fn(*args)
+        assert tg.last_error()[0] == tg.TARA_ERR_ARGS
+
+
+def test_compressible_common_views_share_the_block():
+    """The three Fortran layouts of /comm/ read the same storage."""
+    c = tg.coh_common()
+    old = c.Lx
+    c.Lx = 1.25
+    assert tg.com_common().Lx == 1.25
+    assert ctypes.addressof(tg.coh_common()) == ctypes.addressof(tg.com_common()) == ctypes.addressof(tg.mhd_common())
+    c.Lx = old
