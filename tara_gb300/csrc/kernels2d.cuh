@@ -102,15 +102,20 @@ __host__ __device__ constexpr int pick_rp(int n, int csize) {
 
 // V selects a tile variant for the autotuner: 0 the default tile, 1 half of it,
 // 2 one column (one row pair) per CTA, for grids too small to fill the SMs
-// with the larger tiles.
+// with the larger tiles.  In the column passes variant 2 also gives each
+// column 4x the threads (one radix-4 butterfly per thread per stage), so a
+// 16-byte-element CTA at N = 2048 has 512 (1024 in pass A) threads instead of
+// 128: more loads in flight per column where the default tile is already one
+// column.  The butterflies are the same, so the results are too, bit for bit.
 template <typename T, int N, int V = 0> struct ColCfg {
   typedef typename cplx_of<T>::type C;
-  static constexpr int G = fft_group(N);
+  static constexpr int G0 = fft_group(N);
+  static constexpr int G = V == 2 ? 4 * G0 : G0;  // threads per column slot
   static constexpr int S = N + 1;  // smem column stride (one element of padding)
-  static constexpr int TCA0 = pick_tc(2 * S * (int)sizeof(C), 2 * G);  // pass A: 2 slots/column
+  static constexpr int TCA0 = pick_tc(2 * S * (int)sizeof(C), 2 * G0);  // pass A: 2 slots/column
   // pass C: 1 slot/column; a small tile keeps the live (not fully truncated)
   // columns spread evenly over the SMs
-  static constexpr int TCC0 = pick_tc(S * (int)sizeof(C), G, 48 * 1024);
+  static constexpr int TCC0 = pick_tc(S * (int)sizeof(C), G0, 48 * 1024);
   static constexpr int TCA = V == 2 ? 1 : (V == 1 && TCA0 > 1) ? TCA0 / 2 : TCA0;
   static constexpr int TCC = V == 2 ? 1 : (V == 1 && TCC0 > 1) ? TCC0 / 2 : TCC0;
   static constexpr int THREADS_A = 2 * TCA * G;
@@ -227,7 +232,7 @@ __global__ void __launch_bounds__(ColCfg<T, N, V>::THREADS_A,
     sm[(TC + c) * S + y] = fb;
   }
   __syncthreads();
-  fft_slot<T, N, true>(sm + slot * S, lane, true, tw);
+  fft_slot<T, N, true, G>(sm + slot * S, lane, true, tw);
   TARA_ELEM_LOOP(e, N * TC, CF::THREADS_A) {
     const int y = e / TC, c = e % TC, x = x0 + c;
     if (x < g.nh) {
@@ -355,7 +360,7 @@ __global__ void __launch_bounds__(ColCfg<T, N, V>::THREADS_C)
       sm[c * S + y] = (x < g.nh) ? nl[(size_t)y * g.pitch + x] : mkc<T>(T(0), T(0));
     }
     __syncthreads();
-    fft_slot<T, N, false>(sm + (tid / G) * S, tid % G, true, tw);
+    fft_slot<T, N, false, G>(sm + (tid / G) * S, tid % G, true, tw);
   }
   // Pass 1: the right-hand side of every element of this thread (reads only,
   // so the unrolled loop issues all its loads together).
@@ -553,7 +558,7 @@ __global__ void __launch_bounds__(ColCfg<T, N, V>::THREADS_C)
     sm[c * S + y] = (x < nh) ? in[(size_t)y * pitch + x] : mkc<T>(T(0), T(0));
   }
   __syncthreads();
-  fft_slot<T, N, INV>(sm + (tid / G) * S, tid % G, true, tw);
+  fft_slot<T, N, INV, G>(sm + (tid / G) * S, tid % G, true, tw);
   TARA_ELEM_LOOP(e, N * TC, CF::THREADS_C) {
     const int y = e / TC, c = e % TC, x = x0 + c;
     if (x < nh) out[(size_t)y * pitch + x] = sm[c * S + y];
