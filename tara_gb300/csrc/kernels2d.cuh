@@ -327,9 +327,12 @@ struct StepBufs {
   const double2* force;  // optional spectrum added to every right-hand side (nullptr: none)
 };
 
-// blockIdx.y = run of a batch.
+// blockIdx.y = run of a batch.  The double-float form's 512-thread variant asks
+// for two CTAs per SM (64 registers, 90 bytes of spill): its warps wait on the
+// state loads, and a second CTA hides them (115 -> 103 us at 2048^2).
 template <typename T, int N, int V>
-__global__ void __launch_bounds__(ColCfg<T, N, V>::THREADS_C)
+__global__ void __launch_bounds__(ColCfg<T, N, V>::THREADS_C,
+                                  (is_df64<T>() && ColCfg<T, N, V>::THREADS_C == 512) ? 2 : 1)
     k_col_forward(const typename cplx_of<T>::type* __restrict__ nl, StepBufs sb, Grid2D g,
                   RhsParams p, int mode, const typename cplx_of<T>::type* __restrict__ tw) {
   typedef typename cplx_of<T>::type C;
