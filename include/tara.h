@@ -152,9 +152,10 @@ int tara2d_launches_per_step(const tara2d* h);
 /* Tile variants of the three step kernels (column inverse pass, row pass,
  * column forward pass): 0 the default tile, 1 half of it, 2 one column / one
  * row pair per CTA (small grids, whose FP64 work would otherwise sit on a few
- * SMs).  tara2d_autotune times each variant over trial_steps steps, keeps the
+ * SMs; in the column passes also 4x the threads per column).  tara2d_autotune
+ * times each variant over trial_steps steps in two interleaved rounds, keeps the
  * fastest per kernel and restores the state; variants3 and ms9 (per-launch ms,
- * variant-major) may be NULL. */
+ * the faster round, variant-major) may be NULL. */
 int tara2d_autotune(tara2d* h, int trial_steps, int* variants3, double* ms9);
 int tara2d_set_variants(tara2d* h, const int* variants3);
 
@@ -198,8 +199,9 @@ typedef struct tara_ens tara_ens;
 int tara_ens_create(int nruns, const tara_ens_run* runs, int precision, int scheme, double nu,
                     double dt, double energy, tara_ens** out);
 int tara_ens_destroy(tara_ens* e);
-/* Times both tile variants of each kernel on trial_steps steps per size and keeps
- * the faster per kernel and size; the state is saved and restored around it. */
+/* Times the three tile variants of each kernel on trial_steps steps per size (as
+ * tara2d_autotune) and keeps the fastest per kernel and size; the state is saved
+ * and restored around it. */
 int tara_ens_autotune(tara_ens* e, int trial_steps);
 /* Advances every run nsteps steps: one CUDA-graph launch per step (the graph,
  * one parallel branch per size, is captured on first use).  Asynchronous. */
