@@ -331,6 +331,7 @@ def run_ours(args) -> None:
         "fp64_pipe": (fp64_pipe(n, {k: v["ms"] / max(1, v["launches"]) for k, v in ks.items()},
                                 (clocks or {}).get("sm_mhz"), dfma_rate) if prec == tg.PREC_FP64 else None),
         "tile_variants": tuned["variants"],
+        "autotune_ms": tuned["ms"],  # per-launch ms of variants 0, 1, 2 (rows) x the three kernels
         "diag": {"energy": e, "enstrophy": z},
         "cpu_baseline": cpu,
     }
