@@ -153,9 +153,10 @@ int tara2d_launches_per_step(const tara2d* h);
  * column forward pass): 0 the default tile, 1 half of it, 2 one column / one
  * row pair per CTA (small grids, whose FP64 work would otherwise sit on a few
  * SMs; in the column passes also 4x the threads per column).  tara2d_autotune
- * times each variant over trial_steps steps in two interleaved rounds, keeps the
- * fastest per kernel and restores the state; variants3 and ms9 (per-launch ms,
- * the faster round, variant-major) may be NULL. */
+ * times all kernels per variant over trial_steps steps, then each kernel's
+ * variants with the other two at that first choice (one step each), keeps the
+ * fastest per kernel in that context and restores the state; variants3 and ms9
+ * (per-launch ms in context, variant-major) may be NULL. */
 int tara2d_autotune(tara2d* h, int trial_steps, int* variants3, double* ms9);
 int tara2d_set_variants(tara2d* h, const int* variants3);
 

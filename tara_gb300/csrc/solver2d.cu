@@ -769,32 +769,44 @@ int tara2d_autotune(tara2d* h, int trial_steps, int* variants3, double* ms9) {
   if (!rc && (cudaMemcpyAsync(save_w0, h->w0, bytes, cudaMemcpyDeviceToDevice, h->stream) != cudaSuccess ||
               cudaMemcpyAsync(save_fold, h->fold, bytes, cudaMemcpyDeviceToDevice, h->stream) != cudaSuccess))
     rc = set_error(TARA_ERR_CUDA, "state save");
-  // Two interleaved rounds over the variants, each kernel's time the faster
-  // round: a single pass in variant order charged the first variant with the
-  // clock and cache ramp of the first steps after the initial condition.
+  // Round 1: all three kernels in variant v together (a warm step, which also
+  // sets the shared-memory attributes on first use, then trial_steps timed).
+  // Round 2: each kernel's variants with the other two at their round-1 choice,
+  // one timed step each -- a kernel's time depends on its neighbours' tiles
+  // (cache contents, CTA phases), so the choice is made in that context.
   double ms[3][3];
-  for (int v = 0; v < 3; ++v)
-    for (int k = 0; k < 3; ++k) ms[v][k] = 1e300;
-  for (int round = 0; round < 2 && !rc; ++round)
+  int c[3] = {0, 0, 0};
+  for (int v = 0; v < 3 && !rc; ++v) {
+    for (int k = 0; k < 3; ++k) h->var[k] = v;
+    rc = tara2d_step(h, 1);
+    double t[3];
+    int cnt[3];
+    if (!rc) rc = tara2d_step_timed(h, trial_steps, t, cnt, nullptr);
+    if (!rc)
+      for (int k = 0; k < 3; ++k) ms[v][k] = t[k] / (cnt[k] > 0 ? cnt[k] : 1);
+  }
+  if (!rc)
+    for (int k = 0; k < 3; ++k)
+      for (int v = 1; v < 3; ++v)
+        if (ms[v][k] < ms[c[k]][k]) c[k] = v;
+  double ctx[3][3];
+  for (int k = 0; k < 3 && !rc; ++k)
     for (int v = 0; v < 3 && !rc; ++v) {
-      for (int k = 0; k < 3; ++k) h->var[k] = v;
-      rc = tara2d_step(h, 1);  // untimed: shared-memory attributes on first use, warm caches
+      for (int q = 0; q < 3; ++q) h->var[q] = c[q];
+      h->var[k] = v;
       double t[3];
       int cnt[3];
-      if (!rc) rc = tara2d_step_timed(h, trial_steps, t, cnt, nullptr);
-      if (!rc)
-        for (int k = 0; k < 3; ++k) {
-          const double m = t[k] / (cnt[k] > 0 ? cnt[k] : 1);
-          if (m < ms[v][k]) ms[v][k] = m;
-        }
+      rc = tara2d_step_timed(h, 1, t, cnt, nullptr);
+      if (!rc) ctx[k][v] = t[k] / (cnt[k] > 0 ? cnt[k] : 1);
     }
   if (!rc)
     for (int k = 0; k < 3; ++k) {
       int best = 0;
       for (int v = 1; v < 3; ++v)
-        if (ms[v][k] < ms[best][k]) best = v;
+        if (ctx[k][v] < ctx[k][best]) best = v;
       h->var[k] = best;
       if (variants3) variants3[k] = best;
+      for (int v = 0; v < 3; ++v) ms[v][k] = ctx[k][v];  // reported: the in-context times
     }
   if (!rc && ms9)
     for (int v = 0; v < 3; ++v)
