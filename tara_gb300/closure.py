@@ -1,6 +1,6 @@
 """Learned subgrid closure on libtara: training data from the plain fine-grid
 solver, FNO training with the library's own kernels, and the coarse-grid runs
-judged against the box-filtered fine-grid run.
+measured against the box-filtered fine-grid run.
 
 Everything numeric runs in libtara's CUDA kernels (tara2d_*, tara_fno_*,
 tara_closure_*); torch only holds device buffers.  The workflow:
@@ -10,7 +10,7 @@ tara_closure_*); torch only holds device buffers.  The workflow:
   coarse grid, giving the filtered vorticity (network input) and the exact
   subgrid vorticity flux bar(u w) - bar(u) bar(w) (2-channel target).
 * ``train``: Adam on shuffled mini-batches through ``tara_fno_train_step``.
-* ``evaluate``: from a held-out seed, the fine-grid plain run (the judge) and
+* ``evaluate``: from a held-out seed, the fine-grid plain run (the arbiter of the spectrum error) and
   coarse runs with and without the closure; relative L2 errors of the shell
   energy spectra (shells 1..kmax) against the filtered fine run, averaged over
   the samples of the whole interval, and the simulated time per wall-second of
@@ -254,7 +254,7 @@ def evaluate(s: ClosureSetup, net: FNO | None = None, in_scale=1.0, out_scale: f
              nu_extra: float = 0.0, *, closures: dict | None = None, seed: int | None = None,
              runs: int | None = None) -> dict:
     """Held-out runs (seeds seed..seed+eval_runs, default eval_seed) of the fine
-    plain solver (the judge) and of the coarse solver without a closure and with
+    plain solver (the arbiter) and of the coarse solver without a closure and with
     each closure, from the box-filtered fine initial state.  `closures` maps a
     name to (net, in_scale, out_scale[, nu_extra]), each net a separate handle
     whose batch holds eval_runs, nu_extra an eddy viscosity added to the coarse
@@ -295,7 +295,8 @@ def evaluate(s: ClosureSetup, net: FNO | None = None, in_scale=1.0, out_scale: f
     objs = {}
     try:
         fine = handles["fine"] = _solver(s.n_fine, s, s.dt_fine, batch=R)
-        judge = handles["judge"] = _solver(nc, s, s.dt_coarse, precision=s.coarse_precision, batch=R)
+        # coarse-grid handle that holds the filtered fine state to measure its spectrum
+        meter = handles["meter"] = _solver(nc, s, s.dt_coarse, precision=s.coarse_precision, batch=R)
         coarse = {"plain": _solver(nc, s, s.dt_coarse, precision=s.coarse_precision, batch=R)}
         for k in names:
             nu_e = closures[k][3] if len(closures[k]) > 3 else 0.0
@@ -308,9 +309,9 @@ def evaluate(s: ClosureSetup, net: FNO | None = None, in_scale=1.0, out_scale: f
             c.autotune(2)
         for r in range(R):
             fine.filter(r, s.factor, 0, 0, wbar.data_ptr())
-            for c in [judge] + list(coarse.values()):
+            for c in [meter] + list(coarse.values()):
                 c.set_state_real_device(r, wbar.data_ptr())
-        e_init = [judge.diag_run(r)[0] for r in range(R)]
+        e_init = [meter.diag_run(r)[0] for r in range(R)]
         for k in names:
             nk, ik, ok = closures[k][:3]
             objs[k] = Closure(coarse[k], nk, ik, ok)
@@ -322,9 +323,9 @@ def evaluate(s: ClosureSetup, net: FNO | None = None, in_scale=1.0, out_scale: f
                     objs[k].step(stride_c)
             for r in range(R):
                 fine.filter(r, s.factor, 0, 0, wbar.data_ptr())
-                judge.set_state_real_device(r, wbar.data_ptr())
-                Ef = judge.spectrum(r, kmax)
-                ef = judge.diag_run(r)[0]
+                meter.set_state_real_device(r, wbar.data_ptr())
+                Ef = meter.spectrum(r, kmax)
+                ef = meter.diag_run(r)[0]
                 spec_sum["fine"] += Ef
                 energy["fine"][j] += ef / R
                 for k in ["plain"] + names:
