@@ -447,6 +447,13 @@ int run_com(Reader& R, const std::string& out, int max_steps) {
   return set_ok();
 }
 
+// A console line of the driver, flushed at once so that it keeps its place among
+// the caller's own output when stdout is a pipe or a file.
+void say(const char* line) {
+  std::fputs(line, stdout);
+  std::fflush(stdout);
+}
+
 }  // namespace
 
 extern "C" int tara_run_ini(const char* ini_path, const char* out_dir, int max_steps) {
@@ -464,30 +471,30 @@ extern "C" int tara_run_ini(const char* ini_path, const char* out_dir, int max_s
   if (!R.ok) return set_error(TARA_ERR_INI, R.err);
   const bool here = (arch == "cpu" || arch == "single-gpu");
   if (dim == 2 && here && mode == "serial" && hydrotype == "bare") {
-    std::printf(" tara-gb300: 2D serial hydrodynamic vorticity solver on the GPU\n");
+    say(" tara-gb300: 2D serial hydrodynamic vorticity solver on the GPU\n");
     return run_2d(R, out, max_steps, false);
   }
   if (dim == 2 && here && mode == "serial" && hydrotype == "screen") {
-    std::printf(" tara-gb300: 2D serial screened hydrodynamic vorticity solver on the GPU\n");
+    say(" tara-gb300: 2D serial screened hydrodynamic vorticity solver on the GPU\n");
     return run_2d(R, out, max_steps, true);
   }
   if (dim == 3 && here && mode == "openmp" && domain == "mhd") {
-    std::printf(" tara-gb300: 3D compressible MHD solver on the GPU\n");
+    say(" tara-gb300: 3D compressible MHD solver on the GPU\n");
     return run_3d(R, out, max_steps);
   }
   if (dim == 2 && here && mode == "openmp" && domain == "hydro") {
-    std::printf(" tara-gb300: 2D compressible isothermal hydrodynamic solver on the GPU\n");
+    say(" tara-gb300: 2D compressible isothermal hydrodynamic solver on the GPU\n");
     return run_coh(R, out, max_steps);
   }
   if (dim == 2 && here && mode == "openmp" && domain == "mhd") {
-    std::printf(" tara-gb300: 2D compressible MHD solver on the GPU\n");
+    say(" tara-gb300: 2D compressible MHD solver on the GPU\n");
     return run_com(R, out, max_steps);
   }
   if (mode == "mpi" || arch == "multi-gpu" || (dim == 3 && mode == "serial")) {
-    std::printf(" Under preparation. Please wait!\n");  // src/main.f95:40-85
+    say(" Under preparation. Please wait!\n");  // src/main.f95:40-85
     return set_ok();
   }
   if (dim == 1) return set_error(TARA_ERR_ARGS, "the 1D Burgers solver is outside this build");
-  std::printf(" Incompatible Input file. Please check TARA user-manual.\n");
+  say(" Incompatible Input file. Please check TARA user-manual.\n");
   return set_error(TARA_ERR_INI, "incompatible input file");
 }
