@@ -353,50 +353,75 @@ def timed_on_stream(stream_ptr: int, fn):
     return a.elapsed_time(b)
 
 
+def ensemble_runs(per_rank: int, world_size: int = 1) -> list[tuple[int, float, int]]:
+    """The global run list (n, k0, seed) of the ensemble workload: per_rank x
+    world_size runs at each of 128^2, 256^2 and 512^2 in that order, k0 drawn
+    from numpy default_rng(4000) on U[4,10], seed 4000 + r."""
+    import numpy as np
+
+    per = per_rank * world_size
+    k0 = np.random.default_rng(4000).uniform(4.0, 10.0, 3 * per)
+    return [(n, float(k0[r]), 4000 + r) for r, n in enumerate([128] * per + [256] * per + [512] * per)]
+
+
 def run_ensemble(args) -> None:
-    """Ensemble of 384 independent 2D runs (128 each at 128^2, 256^2, 512^2), RK4,
-    nu = 1e-3, dt = 1e-4, FP32 transforms and products with FP64 state,
-    k0 ~ U[4,10] (numpy default_rng(4000)), seed 4000 + r.  One CUDA-graph launch
-    per ensemble step; tile variants picked by the autotuner first."""
+    """Ensemble of independent 2D runs, RK4, nu = 1e-3, dt = 1e-4, FP32
+    transforms and products with FP64 state: per rank 3 x ens_runs_per_size runs
+    (default 128 each at 128^2, 256^2, 512^2; 384 in all on one GPU).  The global
+    list holds N times as many (same size mix), k0 ~ U[4,10] (numpy
+    default_rng(4000)), seed 4000 + r; each rank steps its cost-balanced shard
+    (tara_gb300.shard) with no exchange between ranks, so the scaling is weak.
+    One CUDA-graph launch per ensemble step on each rank; tile variants picked
+    by the autotuner first."""
     import numpy as np
     import torch
 
     import tara_gb300 as tg
+    from tara_gb300 import shard
 
-    torch.cuda.set_device(0)
-    per = args.ens_runs_per_size
-    k0 = np.random.default_rng(4000).uniform(4.0, 10.0, 3 * per)
-    runs = [(n, float(k0[r]), 4000 + r) for r, n in enumerate([128] * per + [256] * per + [512] * per)]
-    e = tg.Ensemble(runs, precision=tg.PREC_FP32, nu=1e-3, dt=1e-4)
+    rank, ws, dist = dist_init()
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    runs = ensemble_runs(args.ens_runs_per_size, ws)
+    per = args.ens_runs_per_size * ws
+    idx, mine = shard.shard_of(runs, rank, ws)
+    e = tg.Ensemble(mine, precision=tg.PREC_FP32, nu=1e-3, dt=1e-4)
     e.autotune(3)
     e.step(args.warmup)
     e.synchronize()
-    ms = timed_on_stream(e.stream, lambda: e.step(args.steps))
+    if dist:
+        dist.barrier()
+    ms = shard.max_over_ranks(timed_on_stream(e.stream, lambda: e.step(args.steps)), dist)
     e.synchronize()
     pts = sum(n * n for n, _, _ in runs)
-    line = {"metric": f"ensemble grid-pt*steps/s ({3 * per} runs: {per} each at 128^2, 256^2, 512^2; RK4)",
-            "value": pts * args.steps / (ms * 1e-3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+    line = {"metric": f"ensemble grid-pt*steps/s ({len(runs)} runs: {per} each at 128^2, 256^2, 512^2; RK4)",
+            "value": pts * args.steps / (ms * 1e-3), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
-            "dtype": "f32 transforms / f64 state", "data": "synthetic (seeded random-phase spectra)",
+            "scaling": "weak", "dtype": "f32 transforms / f64 state",
+            "data": "synthetic (seeded random-phase spectra)",
             "config": {"workload": "ensemble of uneven runs", "graph": "one cudaGraphLaunch per step",
-                       "l2": "working set > L2 (no flush)"},
-            "gpu_launches": e.launches_per_step * args.steps, "autotune": e.groups()}
+                       "l2": "working set > L2 (no flush)",
+                       "parallelism": f"runs sharded x{ws} (cost-balanced, no exchange)"},
+            "gpu_launches": int(shard.sum_over_ranks(e.launches_per_step * args.steps, dist)),
+            "autotune": e.groups()}
     if args.ens_error_steps:
-        e64 = tg.Ensemble(runs, precision=tg.PREC_FP64, nu=1e-3, dt=1e-4)
+        e64 = tg.Ensemble(mine, precision=tg.PREC_FP64, nu=1e-3, dt=1e-4)
         e.step(args.ens_error_steps - args.steps - args.warmup)
         e64.step(args.ens_error_steps)
         e.synchronize()
         e64.synchronize()
-        errs = []
-        for r in range(len(runs)):
+        local = []
+        for r in range(len(mine)):
             a, b = e.get_state(r), e64.get_state(r)
-            errs.append(float(np.linalg.norm(a - b) / np.linalg.norm(b)))
-        line["error_vs_fp64"] = {"steps": args.ens_error_steps, "max": max(errs),
-                                 "median": float(np.median(errs)),
-                                 "per_size_max": {str(n): max(x for (m, _, _), x in zip(runs, errs) if m == n)
-                                                  for n in (128, 256, 512)}}
+            local.append(float(np.linalg.norm(a - b) / np.linalg.norm(b)))
         e64.close()
-    print(json.dumps(line), flush=True)
+        errs = shard.gather_by_index(idx, local, len(runs), dist)
+        if rank == 0:
+            line["error_vs_fp64"] = {"steps": args.ens_error_steps, "max": max(errs),
+                                     "median": float(np.median(errs)),
+                                     "per_size_max": {str(n): max(x for (m, _, _), x in zip(runs, errs) if m == n)
+                                                      for n in (128, 256, 512)}}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
     e.close()
 
 
@@ -746,7 +771,7 @@ def main() -> None:
                              "coh2d", "com2d"],
                     help="rk4-2048 is the headline; the others measure the ensemble, 3D MHD and the learned closure")
     ap.add_argument("--ens-runs-per-size", type=int, default=128,
-                    help="ensemble: runs of each size (the 384-run ensemble uses 128)")
+                    help="ensemble: runs of each size per rank (the 384-run ensemble on one GPU uses 128)")
     ap.add_argument("--ens-error-steps", type=int, default=0,
                     help="ensemble: also report the per-run error vs FP64 after this many steps")
     ap.add_argument("--closure-epochs", type=int, default=20, help="closure: training epochs")

@@ -1,0 +1,55 @@
+"""One rank of the sharded-ensemble host logic over gloo (run by test_shard.py).
+
+Usage: RANK, WORLD_SIZE, MASTER_ADDR, MASTER_PORT in the environment;
+argv = output JSON path, mode ("ok", "duplicate", "missing"), runs per size per rank.
+Each rank takes its shard of the bench's global run list, makes one scalar per
+run from the run itself (so rank 0 can check the gathered order), a
+rank-dependent "time", and rank 0 writes what the collectives returned.
+"""
+from __future__ import annotations
+
+import json
+import sys
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parents[1]
+sys.path.insert(0, str(ROOT))
+
+
+def main() -> None:
+    import torch.distributed as dist
+
+    import bench
+    from tara_gb300 import shard
+
+    out, mode, per = sys.argv[1], sys.argv[2], int(sys.argv[3])
+    dist.init_process_group("gloo", init_method="env://")
+    rank, ws = dist.get_rank(), dist.get_world_size()
+    runs = bench.ensemble_runs(per, ws)
+    idx, mine = shard.shard_of(runs, rank, ws)
+    vals = [n + 1e-6 * seed for n, _, seed in mine]
+    if mode == "duplicate" and rank == ws - 1:  # report rank 0's first run a second time
+        other = shard.partition_runs([r[0] for r in runs], ws)[0][0]
+        idx, vals = idx + [other], vals + [0.0]
+    if mode == "missing" and rank == ws - 1:
+        idx, vals = idx[1:], vals[1:]
+    res = {"rank": rank, "indices": idx,
+           "max_t": shard.max_over_ranks(1.5 + rank, dist),
+           "sum_launches": shard.sum_over_ranks(10 * (rank + 1), dist)}
+    try:
+        g = shard.gather_by_index(idx, vals, len(runs), dist)
+        res["gathered"] = g
+    except ValueError as e:
+        res["error"] = str(e)
+    all_idx = [None] * ws
+    dist.all_gather_object(all_idx, idx)
+    res["all_indices"] = all_idx
+    dist.barrier()
+    dist.destroy_process_group()
+    if rank == 0:
+        res["expected"] = [n + 1e-6 * seed for n, _, seed in runs]
+        Path(out).write_text(json.dumps(res))
+
+
+if __name__ == "__main__":
+    main()
