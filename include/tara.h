@@ -200,9 +200,9 @@ typedef struct tara_ens tara_ens;
 int tara_ens_create(int nruns, const tara_ens_run* runs, int precision, int scheme, double nu,
                     double dt, double energy, tara_ens** out);
 int tara_ens_destroy(tara_ens* e);
-/* Times the three tile variants of each kernel on trial_steps steps per size (as
- * tara2d_autotune) and keeps the fastest per kernel and size; the state is saved
- * and restored around it. */
+/* Runs tara2d_autotune(trial_steps) on each size group (all kernels per variant,
+ * then each kernel's variants in the context of the others' choice) and keeps
+ * the fastest per kernel and size; the state is saved and restored around it. */
 int tara_ens_autotune(tara_ens* e, int trial_steps);
 /* Advances every run nsteps steps: one CUDA-graph launch per step (the graph,
  * one parallel branch per size, is captured on first use).  Asynchronous. */
