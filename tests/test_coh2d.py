@@ -138,7 +138,7 @@ def test_gpu_init_vortices_golden(gcoh):
 
 
 @gpu
-@pytest.mark.parametrize("ny,nx", [(32, 64), (64, 16), (128, 256)])
+@pytest.mark.parametrize("ny,nx", [(32, 64), (64, 16), (128, 256), (16, 2048), (2048, 16)])
 def test_gpu_rhs_rectangular_vs_oracle(oracle, ny, nx):
     tg = _tg()
     st = _smooth(ny, nx, nx + ny)

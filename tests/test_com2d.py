@@ -130,7 +130,8 @@ def test_gpu_init_reference_golden(gcom):
 
 
 @gpu
-@pytest.mark.parametrize("ny,nx,a", [(32, 64, 1.0), (64, 16, 0.0), (128, 256, 0.5)])
+@pytest.mark.parametrize("ny,nx,a", [(32, 64, 1.0), (64, 16, 0.0), (128, 256, 0.5), (16, 2048, 1.0),
+                                      (2048, 16, 1.0)])
 def test_gpu_rhs_rectangular_vs_oracle(oracle, ny, nx, a):
     """Rectangular grids and boxes, forcing on and off, against the oracle."""
     tg = _tg()

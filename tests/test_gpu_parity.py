@@ -36,7 +36,7 @@ def test_fft_golden_vectors(golden):
 
 
 @pytest.mark.parametrize("ny,nx", [(16, 16), (32, 64), (64, 16), (128, 128), (256, 512),
-                                   (1024, 1024), (2048, 2048)])
+                                   (1024, 1024), (2048, 2048), (16, 2048), (2048, 16)])
 def test_fft_vs_oracle(oracle, ny, nx):
     rng = np.random.default_rng(nx * 7 + ny)
     x = rng.standard_normal((ny, nx))
@@ -66,7 +66,7 @@ def test_derive2css_golden(golden):
     assert rel_l2(tg.derive2css(golden["ic_spec"], 1.0, 0.01), golden["rhs_screen_driverL"]) < 1e-12
 
 
-@pytest.mark.parametrize("ny,nx", [(64, 128), (256, 64), (512, 512), (2048, 2048)])
+@pytest.mark.parametrize("ny,nx", [(64, 128), (256, 64), (512, 512), (2048, 2048), (16, 2048), (2048, 16)])
 def test_derive_vs_oracle_sizes(oracle, ny, nx):
     w = oracle.ic_random(nx, ny, 6.0, 0.5, 11) if nx == ny else None
     if w is None:
