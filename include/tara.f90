@@ -116,6 +116,9 @@ module tara_gb300
       import
       real(c_double), value :: lx, ly, lambda
     end subroutine tara_set_css_params
+    integer(c_int) function tara_finalize() bind(C, name="tara_finalize")
+      import
+    end function tara_finalize
 
     ! ---- device-resident 2D vorticity solver ----------------------------------
     subroutine tara2d_default_config(cfg, nx, ny) bind(C, name="tara2d_default_config")

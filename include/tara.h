@@ -88,6 +88,14 @@ void rk42css_(const int* Nx, const int* Ny, const int* Nh, const double* alpha, 
  * (src/main2css.f95:87). */
 void tara_set_css_params(double lx, double ly, double lambda);
 
+/* Frees the device contexts (arrays, tables, streams) that the Fortran drop-ins
+ * keep per grid shape, the owners of the device side of every drop-in call; the
+ * next drop-in call creates its context again.  Handles made by the *_create
+ * calls belong to the caller and are not touched.  Call it while no drop-in call
+ * runs on another thread.  No counterpart in the reference, whose subroutines
+ * allocate their work arrays and FFTW plans per call. */
+int tara_finalize(void);
+
 /* ---- 2. Device-resident solver ------------------------------------------- */
 
 #define TARA_RHS_PLAIN 0   /* derive2csh */

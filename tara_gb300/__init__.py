@@ -125,6 +125,8 @@ def _declare(L: ctypes.CDLL) -> None:
         getattr(L, name).restype = None
     L.tara_set_css_params.argtypes = [c_double, c_double, c_double]
     L.tara_set_css_params.restype = None
+    L.tara_finalize.argtypes = []
+    L.tara_finalize.restype = c_int
     cfgp = ctypes.POINTER(Config2D)
     L.tara2d_default_config.argtypes = [cfgp, c_int, c_int]
     L.tara2d_default_config.restype = None
@@ -352,6 +354,12 @@ def rk42css(omegak, alpha: float, nu: float, dt: float, time: float = 0.0):
 
 def set_css_params(lx: float, ly: float, lam: float) -> None:
     lib().tara_set_css_params(lx, ly, lam)
+
+
+def finalize() -> None:
+    """Free the device contexts the Fortran drop-ins keep per grid shape
+    (tara_finalize); the next drop-in call creates them again."""
+    _check(lib().tara_finalize())
 
 
 def measure_dfma_rate(reps: int = 5) -> float:

@@ -350,3 +350,24 @@ int tara_fft2d_c2r(int nx, int ny, int precision, const double* in, double* out)
 }
 
 }  // extern "C"
+
+namespace tara {
+int release_dropins_2d() {
+  std::lock_guard<std::mutex> lk(g_mu);
+  int rc = TARA_OK;
+  for (auto& kv : g_ctx) {
+    const int r = tara2d_destroy(kv.second);
+    if (r != TARA_OK && rc == TARA_OK) rc = r;
+  }
+  g_ctx.clear();
+  return rc;
+}
+}  // namespace tara
+
+extern "C" int tara_finalize(void) {
+  const int rcs[4] = {release_dropins_2d(), release_dropins_3d(), release_dropins_coh(),
+                      release_dropins_com()};
+  for (int r : rcs)
+    if (r != TARA_OK) return r;
+  return set_ok();
+}

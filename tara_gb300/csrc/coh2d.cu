@@ -678,3 +678,16 @@ void ab2coh_(const int* Nx, const int* Ny, const int* Nh, const double* pi, cons
 }
 
 }  // extern "C"
+
+namespace tara {
+int release_dropins_coh() {
+  std::lock_guard<std::mutex> lk(g_coh_mu);
+  int rc = TARA_OK;
+  for (auto& kv : g_coh_ctx) {
+    const int r = tara_coh2d_destroy(kv.second);
+    if (r != TARA_OK && rc == TARA_OK) rc = r;
+  }
+  g_coh_ctx.clear();
+  return rc;
+}
+}  // namespace tara

@@ -797,3 +797,16 @@ void ab2com_(const int* Nx, const int* Ny, const int* Nh, const double* pi, cons
 }
 
 }  // extern "C"
+
+namespace tara {
+int release_dropins_com() {
+  std::lock_guard<std::mutex> lk(g_com_mu);
+  int rc = TARA_OK;
+  for (auto& kv : g_com_ctx) {
+    const int r = tara_com2d_destroy(kv.second);
+    if (r != TARA_OK && rc == TARA_OK) rc = r;
+  }
+  g_com_ctx.clear();
+  return rc;
+}
+}  // namespace tara

@@ -121,4 +121,10 @@ const tara_fno_config& fno_config(const tara_fno* f);
 float* fno_input(tara_fno* f);  // the handle's input buffer (max_batch samples)
 unsigned long long fno_param_version(const tara_fno* f);
 int fno_prepare(tara_fno* f);
+// Destroy the contexts the Fortran drop-ins keep per grid shape.  Each file
+// that holds such a cache defines its function; tara_finalize calls them all.
+int release_dropins_2d();
+int release_dropins_3d();
+int release_dropins_coh();
+int release_dropins_com();
 }  // namespace tara

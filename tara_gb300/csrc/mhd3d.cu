@@ -808,3 +808,16 @@ void ab3com_(const int* Nx, const int* Ny, const int* Nz, const int* Nh, const d
 }
 
 }  // extern "C"
+
+namespace tara {
+int release_dropins_3d() {
+  std::lock_guard<std::mutex> lk(g_mu3);
+  int rc = TARA_OK;
+  for (auto& kv : g_ctx3) {
+    const int r = tara3d_destroy(kv.second);
+    if (r != TARA_OK && rc == TARA_OK) rc = r;
+  }
+  g_ctx3.clear();
+  return rc;
+}
+}  // namespace tara

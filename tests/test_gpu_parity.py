@@ -77,6 +77,22 @@ def test_derive_vs_oracle_sizes(oracle, ny, nx):
     assert rel_l2(tg.derive2css(w, 0.7, 1e-3), oracle.derive2css(w, 0.7, 1e-3)) < 1e-12
 
 
+def test_finalize_frees_and_recreates_dropin_contexts(golden):
+    """tara_finalize drops the per-shape contexts of the 2D and compressible
+    drop-ins; the next calls build them again and give the same results."""
+    a = tg.derive2csh(golden["ic_spec"], 0.01)
+    c = tg.coh_common()
+    c.Lx, c.Ly, c.mux, c.muy, c.ms, c.CS, c.dt = 2 * PI_R8, 2 * PI_R8, 2e-4, 2e-4, 1.0, 3.77, 1e-3
+    st = np.zeros((3, 32, 17), np.complex128)
+    st[0, 0, 0] = 32 * 32
+    st[1, 1, 2] = 40.0 + 3.0j
+    d0 = tg.derive2coh(st)
+    tg.finalize()
+    assert rel_l2(tg.derive2csh(golden["ic_spec"], 0.01), a) < 1e-15
+    assert rel_l2(tg.derive2coh(st), d0) < 1e-15
+    tg.finalize()
+
+
 def test_ab2_dropin_exact(oracle):
     rng = np.random.default_rng(2)
     shp = (32, 17)

@@ -79,6 +79,14 @@ def test_python_wrapper_raises_on_bad_args():
     assert e.value.code == tg.TARA_ERR_ARGS
 
 
+def test_finalize_without_contexts_is_ok():
+    """With no drop-in context alive (nothing ran on a GPU) finalize frees
+    nothing and reports success, any number of times."""
+    tg.finalize()
+    tg.finalize()
+    assert tg.last_error()[0] == tg.TARA_OK
+
+
 def test_no_silent_fallback_without_gpu():
     """With no usable GPU a valid request fails loudly (CUDA error), never
     computes on the CPU."""
