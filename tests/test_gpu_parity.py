@@ -119,13 +119,15 @@ def test_rk42css_golden(golden):
 
 # ---------------------------------------------------------------- resident solver
 @pytest.mark.parametrize("steps", [1, 10, 2000])
-def test_solver_ab2_plain_golden(golden, steps):
+def test_solver_ab2_plain_golden(oracle, golden, steps):
     with tg.Solver2D(64, nu=0.01, dt=1e-4) as s:
         s.set_state(golden["ic_spec"])
         s.step(steps)
         w, fo = s.get_state(with_history=True)
     assert rel_l2(w, golden[f"ab2_plain_{steps}"]) < 1e-10
     assert rel_l2(fo, golden[f"ab2_plain_{steps}_hist"]) < 1e-10
+    # the parity bar is stated for the vorticity in real space
+    assert rel_l2(oracle.c2r(w), oracle.c2r(golden[f"ab2_plain_{steps}"])) < 1e-10
 
 
 def test_solver_ab2_screen_golden(golden):
