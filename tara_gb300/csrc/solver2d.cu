@@ -769,9 +769,9 @@ int tara2d_autotune(tara2d* h, int trial_steps, int* variants3, double* ms9) {
   if (!rc && (cudaMemcpyAsync(save_w0, h->w0, bytes, cudaMemcpyDeviceToDevice, h->stream) != cudaSuccess ||
               cudaMemcpyAsync(save_fold, h->fold, bytes, cudaMemcpyDeviceToDevice, h->stream) != cudaSuccess))
     rc = set_error(TARA_ERR_CUDA, "state save");
-  // Round 1: all three kernels in variant v together (a warm step, which also
+  // Pass 1: all three kernels in variant v together (a warm step, which also
   // sets the shared-memory attributes on first use, then trial_steps timed).
-  // Round 2: each kernel's variants with the other two at their round-1 choice,
+  // Pass 2: each kernel's variants with the other two at their pass-1 choice,
   // one timed step each -- a kernel's time depends on its neighbours' tiles
   // (cache contents, CTA phases), so the choice is made in that context.
   double ms[3][3];
