@@ -147,9 +147,12 @@ def dist_init():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if ws > 1:
+        import torch
         import torch.distributed as dist
 
-        backend = "nccl"
+        # NCCL on the GPUs; gloo only where no GPU is visible (the CPU tests of the
+        # multi-rank host logic)
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
         dist.init_process_group(backend=backend)
         return rank, ws, dist
     return 0, 1, None

@@ -1,7 +1,9 @@
 """One rank of the sharded-ensemble host logic over gloo (run by test_shard.py).
 
 Usage: RANK, WORLD_SIZE, MASTER_ADDR, MASTER_PORT in the environment;
-argv = output JSON path, mode ("ok", "duplicate", "missing"), runs per size per rank.
+argv = output JSON path, mode ("ok", "duplicate", "missing", or "bench" for
+bench.py's ensemble workload with stand-ins for the GPU objects), runs per size
+per rank.
 Each rank takes its shard of the bench's global run list, makes one scalar per
 run from the run itself (so rank 0 can check the gathered order), a
 rank-dependent "time", and rank 0 writes what the collectives returned.
@@ -9,6 +11,7 @@ rank-dependent "time", and rank 0 writes what the collectives returned.
 from __future__ import annotations
 
 import json
+import os
 import sys
 from pathlib import Path
 
@@ -51,5 +54,59 @@ def main() -> None:
         Path(out).write_text(json.dumps(res))
 
 
+def bench_ensemble() -> None:
+    """bench.py's ensemble workload on this rank with the GPU objects replaced by
+    stand-ins: each run's "FP32" state differs from its "FP64" one by a factor
+    1 + 1e-7 * seed / 4000, and rank r's timed region takes 10 + r ms, so rank 0's
+    line can be checked against the shard logic."""
+    import types
+
+    import numpy as np
+    import torch
+
+    import bench
+    import tara_gb300 as tg
+
+    class Ensemble:
+        def __init__(self, runs, precision, nu, dt):
+            self.runs, self.fp32 = list(runs), precision == tg.PREC_FP32
+
+        def autotune(self, trial_steps):
+            pass
+
+        def step(self, n):
+            pass
+
+        def synchronize(self):
+            pass
+
+        stream = 0
+        launches_per_step = 36
+
+        def groups(self):
+            return []
+
+        def get_state(self, r):
+            n, _, seed = self.runs[r]
+            w = np.full((n, n // 2 + 1), 1.0 + 0.5j)
+            return w * (1.0 + 1e-7 * seed / 4000.0) if self.fp32 else w
+
+        def close(self):
+            pass
+
+    tg.Ensemble = Ensemble
+    torch.cuda.set_device = lambda d: None
+    rank = int(os.environ["RANK"])
+    bench.timed_on_stream = lambda stream, fn: (fn(), 10.0 + rank)[1]
+    per = int(sys.argv[3])
+    bench.run_ensemble(types.SimpleNamespace(ens_runs_per_size=per, warmup=3, steps=2, ens_error_steps=10))
+    import torch.distributed as dist
+
+    dist.destroy_process_group()
+
+
 if __name__ == "__main__":
-    main()
+    if sys.argv[2] == "bench":
+        bench_ensemble()
+    else:
+        main()

@@ -82,7 +82,8 @@ def _free_port() -> int:
         return s.getsockname()[1]
 
 
-def _run_ranks(tmp_path, mode: str, ws: int = 2, per: int = 4) -> dict:
+def _spawn(tmp_path, mode: str, ws: int = 2, per: int = 4):
+    """Start ws ranks of shard_worker.py; returns (rank 0's output file, logs)."""
     out = tmp_path / f"rank0_{mode}.json"
     env = dict(os.environ, MASTER_ADDR="127.0.0.1", MASTER_PORT=str(_free_port()),
                WORLD_SIZE=str(ws), CUDA_VISIBLE_DEVICES="")
@@ -99,6 +100,11 @@ def _run_ranks(tmp_path, mode: str, ws: int = 2, per: int = 4) -> dict:
             if p.poll() is None:
                 p.kill()
     assert all(p.returncode == 0 for p in procs), "\n".join(logs)
+    return out, logs
+
+
+def _run_ranks(tmp_path, mode: str, ws: int = 2, per: int = 4) -> dict:
+    out, _ = _spawn(tmp_path, mode, ws, per)
     return json.loads(out.read_text())
 
 
@@ -116,3 +122,27 @@ def test_gloo_gather_detects_bad_shards(tmp_path, mode):
     res = _run_ranks(tmp_path, mode)
     assert "gathered" not in res
     assert ("twice" in res["error"]) if mode == "duplicate" else ("no rank" in res["error"])
+
+
+def test_gloo_two_ranks_bench_ensemble_line(tmp_path):
+    """bench.py --workload ensemble on two gloo ranks (stand-ins for the GPU
+    objects): one JSON line from rank 0 only, the time the slower rank's, the
+    points of both shards, launches summed, and the per-run errors gathered in
+    global order."""
+    per = 4
+    _, logs = _spawn(tmp_path, "bench", per=per)
+    lines0 = [l for l in logs[0].splitlines() if l.startswith("{")]
+    assert len(lines0) == 1 and not any(l.startswith("{") for l in logs[1].splitlines())
+    line = json.loads(lines0[0])
+    runs = bench.ensemble_runs(per, 2)
+    pts = sum(n * n for n, _, _ in runs)
+    assert line["n_gpus"] == 2 and line["scaling"] == "weak" and line["steps"] == 2
+    assert line["ms_per_step"] == pytest.approx(11.0 / 2)      # max over ranks of 10 + rank ms
+    assert line["value"] == pytest.approx(pts * 2 / 11e-3)
+    assert line["gpu_launches"] == 2 * 36 * 2
+    errs = [1e-7 * seed / 4000.0 for _, _, seed in runs]
+    ev = line["error_vs_fp64"]
+    assert ev["max"] == pytest.approx(max(errs), rel=1e-6)
+    for n in (128, 256, 512):
+        assert ev["per_size_max"][str(n)] == pytest.approx(
+            max(e for (m, _, _), e in zip(runs, errs) if m == n), rel=1e-6)
