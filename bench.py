@@ -228,6 +228,7 @@ def run_ours(args) -> None:
     import torch
 
     import tara_gb300 as tg
+    from tara_gb300 import shard
 
     rank, ws, dist = dist_init()
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -257,11 +258,7 @@ def run_ours(args) -> None:
     if dist:
         dist.barrier()
     clocks = sampler.stop() if sampler else None
-    el_ms = prof["total_ms"]
-    if dist:
-        t = torch.tensor([el_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        el_ms = float(t.item())
+    el_ms = shard.max_over_ranks(prof["total_ms"], dist)
     e, z = s.diag()  # also raises on non-finite values
 
     # ---- end to end through the public API with pinned host buffers
@@ -280,11 +277,7 @@ def run_ours(args) -> None:
         s.get_state_into(host_out)
         host_in, host_out = host_out, host_in
     torch.cuda.synchronize()
-    e2e_el = time.perf_counter() - t0
-    if dist:
-        t = torch.tensor([e2e_el], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_el = float(t.item())
+    e2e_el = shard.max_over_ranks(time.perf_counter() - t0, dist)
 
     if rank != 0:
         s.close()
