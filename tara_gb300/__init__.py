@@ -550,10 +550,13 @@ def mhd_common() -> MhdCommon:
     return MhdCommon.in_dll(lib(), "comm_")
 
 
-def _state8(a) -> np.ndarray:
+def _state8(a, shape=None) -> np.ndarray:
+    """Eight 3D half spectra, C-contiguous complex128; `shape` = (Nz, Ny, Nh) of the
+    handle they go to (the library reads exactly that many values)."""
     a = np.ascontiguousarray(a, dtype=np.complex128)
-    if a.ndim != 4 or a.shape[0] != 8:
-        raise ValueError("expected an (8, Nz, Ny, Nh) state")
+    if a.ndim != 4 or a.shape[0] != 8 or (shape is not None and a.shape[1:] != tuple(shape)):
+        raise ValueError(f"expected an (8, Nz, Ny, Nh) state{'' if shape is None else ' of ' + str(tuple(shape))}, "
+                         f"got {a.shape}")
     return a
 
 
@@ -621,12 +624,15 @@ class Solver3D:
         self.close()
 
     def set_state(self, state, hist=None):
-        st = _state8(state)
-        h = None if hist is None else _state8(hist)
+        st = _state8(state, self.shape)
+        h = None if hist is None else _state8(hist, self.shape)
         _check(lib().tara3d_set_state(self._h, st.ctypes.data, None if h is None else h.ctypes.data))
 
     def set_state_real(self, real8):
         r = np.ascontiguousarray(real8, dtype=np.float64)
+        nz, ny, nh = self.shape
+        if r.shape != (8, nz, ny, 2 * (nh - 1)):
+            raise ValueError(f"expected an (8, {nz}, {ny}, {2 * (nh - 1)}) real state, got {r.shape}")
         _check(lib().tara3d_set_state_real(self._h, r.ctypes.data))
 
     def get_state(self, with_history: bool = False):
@@ -664,10 +670,12 @@ def coh_common() -> CohCommon:
     return CohCommon.from_address(ctypes.addressof(MhdCommon.in_dll(lib(), "comm_")))
 
 
-def _state3(a) -> np.ndarray:
+def _state3(a, shape=None) -> np.ndarray:
+    """(nk, ukx, uky) half spectra; `shape` = (Ny, Nh) of the handle they go to."""
     a = np.ascontiguousarray(a, dtype=np.complex128)
-    if a.ndim != 3 or a.shape[0] != 3:
-        raise ValueError("expected a (3, Ny, Nh) state (nk, ukx, uky)")
+    if a.ndim != 3 or a.shape[0] != 3 or (shape is not None and a.shape[1:] != tuple(shape)):
+        raise ValueError(f"expected a (3, Ny, Nh) state (nk, ukx, uky)"
+                         f"{'' if shape is None else ' of ' + str(tuple(shape))}, got {a.shape}")
     return a
 
 
@@ -730,8 +738,8 @@ class Coh2D:
         self.close()
 
     def set_state(self, state, hist=None):
-        st = _state3(state)
-        h = None if hist is None else _state3(hist)
+        st = _state3(state, self.shape)
+        h = None if hist is None else _state3(hist, self.shape)
         _check(lib().tara_coh2d_set_state(self._h, st.ctypes.data, None if h is None else h.ctypes.data))
 
     def get_state(self, with_history: bool = False):
@@ -777,10 +785,13 @@ def com_common() -> ComCommon:
     return ComCommon.from_address(ctypes.addressof(MhdCommon.in_dll(lib(), "comm_")))
 
 
-def _state6(a) -> np.ndarray:
+def _state6(a, shape=None) -> np.ndarray:
+    """(rho, rho ux, rho uy, E, Bx, By) half spectra; `shape` = (Ny, Nh) of the
+    handle they go to."""
     a = np.ascontiguousarray(a, dtype=np.complex128)
-    if a.ndim != 3 or a.shape[0] != 6:
-        raise ValueError("expected a (6, Ny, Nh) state (rho, rho ux, rho uy, E, Bx, By)")
+    if a.ndim != 3 or a.shape[0] != 6 or (shape is not None and a.shape[1:] != tuple(shape)):
+        raise ValueError(f"expected a (6, Ny, Nh) state (rho, rho ux, rho uy, E, Bx, By)"
+                         f"{'' if shape is None else ' of ' + str(tuple(shape))}, got {a.shape}")
     return a
 
 
@@ -847,8 +858,8 @@ class Com2D:
         self.close()
 
     def set_state(self, state, hist=None):
-        st = _state6(state)
-        h = None if hist is None else _state6(hist)
+        st = _state6(state, self.shape)
+        h = None if hist is None else _state6(hist, self.shape)
         _check(lib().tara_com2d_set_state(self._h, st.ctypes.data, None if h is None else h.ctypes.data))
 
     def get_state(self, with_history: bool = False):

@@ -129,3 +129,22 @@ def test_compressible_common_views_share_the_block():
     assert tg.com_common().Lx == 1.25
     assert ctypes.addressof(tg.coh_common()) == ctypes.addressof(tg.com_common()) == ctypes.addressof(tg.mhd_common())
     c.Lx = old
+
+
+@pytest.mark.parametrize("cls,shape,nf", [("Coh2D", (32, 17), 3), ("Com2D", (32, 17), 6),
+                                          ("Solver3D", (16, 16, 9), 8)])
+def test_handles_reject_states_of_another_shape(cls, shape, nf):
+    """A state whose grid is not the handle's is refused before the library
+    reads it (the C side copies exactly the handle's number of values)."""
+    h = getattr(tg, cls).__new__(getattr(tg, cls))  # no device handle: validation only
+    h._h, h.shape = None, shape
+    bad = np.zeros((nf,) + tuple(s * 2 for s in shape[:-1]) + (shape[-1],), np.complex128)
+    with pytest.raises(ValueError):
+        h.set_state(bad)
+    with pytest.raises(ValueError):
+        h.set_state(np.zeros((nf,) + shape, np.complex128), hist=bad)
+    with pytest.raises(ValueError):
+        h.set_state(np.zeros((nf + 1,) + shape, np.complex128))
+    if cls == "Solver3D":
+        with pytest.raises(ValueError):
+            h.set_state_real(np.zeros((8, 16, 16, 32)))  # nx = 16 for nh = 9
