@@ -529,6 +529,8 @@ class Solver2D:
     def features(self, run: int, nf: int, out_ptr: int, scales=None) -> None:
         """Closure input features (FP32 (Ny, Nx, nf)) of run `run` at a device pointer."""
         sc = None if scales is None else np.ascontiguousarray(np.asarray(scales, np.float64))
+        if sc is not None and sc.size < nf:
+            raise ValueError(f"expected {nf} feature scales, got {sc.size}")
         _check(lib().tara2d_features(self._h, run, nf, None if sc is None else _dp(sc),
                                      ctypes.c_void_p(out_ptr)))
 

@@ -148,3 +148,10 @@ def test_handles_reject_states_of_another_shape(cls, shape, nf):
     if cls == "Solver3D":
         with pytest.raises(ValueError):
             h.set_state_real(np.zeros((8, 16, 16, 32)))  # nx = 16 for nh = 9
+
+
+def test_features_need_one_scale_per_channel():
+    h = tg.Solver2D.__new__(tg.Solver2D)  # no device handle: validation only
+    h._h = None
+    with pytest.raises(ValueError):
+        h.features(0, 3, 0, scales=[1.0, 2.0])
