@@ -73,7 +73,7 @@ def test_df64_error_vs_fp64(oracle):
     assert 0.0 < err < 1e-12
 
 
-@pytest.mark.parametrize("n", [64, 256])
+@pytest.mark.parametrize("n", [64, 256, 128])
 def test_df64_tile_variants_are_bitwise_equal(n):
     out = []
     for v in ((0, 0, 0), (1, 1, 1), (2, 2, 2), (2, 0, 1)):

@@ -71,16 +71,32 @@ def test_ensemble_run_matches_oracle(oracle):
     assert rel_l2(w, ref) < 1e-12
 
 
-@pytest.mark.parametrize("n", [64, 256])
+@pytest.mark.parametrize("n", [64, 256, 32, 128])
 @pytest.mark.parametrize("prec", [tg.PREC_FP64, tg.PREC_FP32])
 def test_tile_variants_are_bitwise_equal(n, prec):
-    """Every tile variant runs the same per-column / per-row arithmetic."""
+    """Every tile variant runs the same per-column / per-row arithmetic (odd
+    log2 n adds the final radix-2 stage)."""
     out = []
     for v in ((0, 0, 0), (1, 1, 1), (2, 2, 2), (2, 0, 1)):
         with tg.Solver2D(n, scheme=tg.SCHEME_RK4, precision=prec, nu=1e-3, dt=1e-4) as s:
             s.init_random(6.0, 0.5, 4100)
             s.set_variants(v)
             s.step(3)
+            s.synchronize()
+            out.append(s.get_state())
+    for o in out[1:]:
+        assert np.array_equal(o, out[0])
+
+
+def test_tile_variants_at_2048_are_bitwise_equal():
+    """At the bench's 2048^2 FP64 RK4 workload the autotuner picks per-kernel
+    variants such as (1, 0, 2); they give the default tiles' results bit for bit."""
+    out = []
+    for v in ((0, 0, 0), (1, 0, 2), (2, 2, 2)):
+        with tg.Solver2D(2048, scheme=tg.SCHEME_RK4, nu=1e-4, dt=5e-5) as s:
+            s.init_random(6.0, 0.5, 20242048)
+            s.set_variants(v)
+            s.step(1)
             s.synchronize()
             out.append(s.get_state())
     for o in out[1:]:
