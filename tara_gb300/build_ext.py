@@ -11,6 +11,7 @@ import hashlib
 import os
 import shutil
 import subprocess
+import sys
 from pathlib import Path
 
 PKG = Path(__file__).resolve().parent
@@ -30,7 +31,7 @@ NVCC_FLAGS = ARCH + [
     "-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
     # host code keeps IEEE double without FMA contraction (wavenumber tables
     # must equal the oracle's on x86 and Arm alike)
-    "-Xcompiler", "-fPIC,-ffp-contract=off",
+    "-Xcompiler", "-fPIC,-ffp-contract=off,-Wall,-Wextra",
 ]
 
 
@@ -50,11 +51,13 @@ def _stamp(paths) -> str:
     return h.hexdigest()
 
 
-def _compile(src: Path, obj: Path) -> None:
+def _compile(src: Path, obj: Path) -> str:
+    """Compile one translation unit; returns the compiler's warnings (if any)."""
     cmd = [nvcc(), *NVCC_FLAGS, "-c", str(src), "-o", str(obj)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed for {src.name}:\n{r.stdout}\n{r.stderr}")
+    return "\n".join(l for l in (r.stdout + r.stderr).splitlines() if "warning" in l.lower())
 
 
 def build_lib(force: bool = False, verbose: bool = False) -> Path:
@@ -70,7 +73,9 @@ def build_lib(force: bool = False, verbose: bool = False) -> Path:
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         futs = [ex.submit(_compile, CSRC / s, o) for s, o in zip(SOURCES, objs)]
         for f in futs:
-            f.result()
+            warn = f.result()
+            if warn:
+                print(warn, file=sys.stderr)
     tmp = LIB.with_suffix(".so.tmp")
     cmd = [nvcc(), *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)

@@ -23,6 +23,7 @@
 // muy d2ux_dy2)/n) and the momentum terms before the forward one: 11 c2r and
 // 3 r2c per RHS instead of 13 and 9, equal up to rounding.
 #include <cmath>
+#include <cstring>
 #include <map>
 #include <mutex>
 #include <tuple>
@@ -266,7 +267,8 @@ std::map<std::tuple<int, int>, tara_coh2d*> g_coh_ctx;
 
 // Context of a shape for the drop-ins, its parameters refreshed per call.
 tara_coh2d* coh_ctx(int nx, int ny, double pi) {
-  const CohCommon& cm = *reinterpret_cast<const CohCommon*>(&comm_);
+  CohCommon cm;  // a copy: the block's storage is declared with the 3D layout
+  std::memcpy(&cm, &comm_, sizeof cm);
   if (!(cm.Lx > 0.0) || !(cm.Ly > 0.0)) {
     set_error(TARA_ERR_ARGS, "/comm/ Lx and Ly must be positive");
     return nullptr;

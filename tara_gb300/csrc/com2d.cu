@@ -25,6 +25,7 @@
 // The forcing's x(i), y(j) are local arrays the reference never sets
 // (:16,109-110): here they are the driver's grid, (i-1) Lx/Nx and (j-1) Ly/Ny.
 #include <cmath>
+#include <cstring>
 #include <map>
 #include <mutex>
 #include <tuple>
@@ -385,7 +386,8 @@ std::mutex g_com_mu;
 std::map<std::tuple<int, int>, tara_com2d*> g_com_ctx;
 
 tara_com2d* com_ctx(int nx, int ny, double pi) {
-  const ComCommon& cm = *reinterpret_cast<const ComCommon*>(&comm_);
+  ComCommon cm;  // a copy: the block's storage is declared with the 3D layout
+  std::memcpy(&cm, &comm_, sizeof cm);
   if (!(cm.Lx > 0.0) || !(cm.Ly > 0.0)) {
     set_error(TARA_ERR_ARGS, "/comm/ Lx and Ly must be positive");
     return nullptr;

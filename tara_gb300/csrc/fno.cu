@@ -638,8 +638,8 @@ __global__ void k_gelu(const float* __restrict__ z, float* __restrict__ v, size_
     v[i] = gelu(z[i]);
 }
 
-__global__ void k_gelu_back(const float* __restrict__ z, const float* __restrict__ dv, float* __restrict__ dz,
-                            size_t n) {
+// dz may be dv (in place), so neither is declared __restrict__
+__global__ void k_gelu_back(const float* __restrict__ z, const float* dv, float* dz, size_t n) {
   for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
     dz[i] = dv[i] * gelu_grad(z[i]);
 }

@@ -384,7 +384,7 @@ static int stage_buffer(tara2d* h, void** out) {
 int copy_in_dense(tara2d* h, double2* dst, const double* host) {
   const size_t bytes = (size_t)h->nh * h->ny * sizeof(double2);
   if (bytes >= (1u << 20) && is_pinned(host)) {
-    void* stage;
+    void* stage = nullptr;
     int rc;
     if ((rc = stage_buffer(h, &stage))) return rc;
     TARA_CK(cudaMemcpyAsync(stage, host, bytes, cudaMemcpyHostToDevice, h->stream));
@@ -400,7 +400,7 @@ int copy_in_dense(tara2d* h, double2* dst, const double* host) {
 int copy_out_dense(tara2d* h, double* host, const double2* src) {
   const size_t bytes = (size_t)h->nh * h->ny * sizeof(double2);
   if (bytes >= (1u << 20) && is_pinned(host)) {
-    void* stage;
+    void* stage = nullptr;
     int rc;
     if ((rc = stage_buffer(h, &stage))) return rc;
     k_repitch<<<152 * 8, 256, 0, h->stream>>>(src, h->pitch, (double2*)stage, h->nh, h->nh, h->ny);
