@@ -10,6 +10,7 @@ import numpy as np
 import pytest
 
 import tara_gb300 as tg
+from tara_gb300.build_ext import REFERENCE
 
 
 def read_d(s: str):
@@ -166,3 +167,37 @@ def test_list_directed_output_round_trips():
         out = ctypes.c_double()
         assert tg.lib().tara_fortran_read_double(text.encode(), ctypes.byref(out)) == tg.TARA_OK
         assert out.value == v, (v, text, out.value)
+
+
+REFERENCE_INI = REFERENCE / "input.ini"  # the reference checkout, where build_ext finds it
+
+
+@pytest.mark.skipif(not REFERENCE_INI.exists(), reason="the reference tree is not on this machine")
+def test_reference_input_ini():
+    """The reference's shipped input.ini, read where the reference tree exists:
+    every key its programs read, through the same parser and list-directed reads
+    (src/main.f95:26-30, src/main2css.f95:29-76).  d = 3.0d0/128.0d0 reads as
+    3.0: the list-directed read stops at the slash."""
+    def val(sec, key):
+        rc, text = ini_get(REFERENCE_INI, sec, key)
+        assert rc == tg.TARA_OK, (sec, key, tg.last_error())
+        return text
+
+    def dbl(sec, key):
+        out = ctypes.c_double()
+        assert tg.lib().tara_fortran_read_double(val(sec, key).encode(), ctypes.byref(out)) == tg.TARA_OK
+        return out.value
+
+    def num(sec, key):
+        out = ctypes.c_longlong()
+        assert tg.lib().tara_fortran_read_int(val(sec, key).encode(), ctypes.byref(out)) == tg.TARA_OK
+        return out.value
+
+    assert (num("dimension", "dim"), val("architecture", "arch"), val("parallel", "mode")) == (2, "cpu", "serial")
+    assert (val("type", "domain"), val("problem", "hydrotype")) == ("hydro", "screen")
+    assert (num("grid", "Nx"), num("grid", "Ny"), num("grid", "Nz"), num("particle", "Np")) == (64, 64, 64, 10)
+    assert (dbl("length", "Lx"), dbl("length", "Ly"), dbl("length", "Lz")) == (2.0, 2.0, 2.0)
+    assert (dbl("resistivity", "nu"), dbl("resistivity", "eta")) == (0.01, 0.0)
+    assert (dbl("time", "time_min"), dbl("time", "time_max"), dbl("time", "dt")) == (0.0, 2.0, 1e-4)
+    assert (dbl("initialProfile", "W0"), dbl("initialProfile", "m0"), dbl("initialProfile", "d")) == (25.0, 2.0, 3.0)
+    assert dbl("initialB", "B0") == 0.0
