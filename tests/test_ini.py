@@ -138,7 +138,7 @@ def test_list_directed_output_style():
                                                             "-0.10000341643993921"]
 
 
-def test_run_ini_dispatch_without_gpu(tmp_path):
+def test_run_ini_dispatch_without_gpu(tmp_path, capfd):
     L = tg.lib()
     p = tmp_path / "a.ini"
     base = ("[dimension]\ndim = {dim}\n[architecture]\narch = cpu\n[parallel]\nmode = {mode}\n"
@@ -146,7 +146,10 @@ def test_run_ini_dispatch_without_gpu(tmp_path):
     p.write_text(base.format(dim=1, mode="serial"))
     assert L.tara_run_ini(str(p).encode(), str(tmp_path / "o").encode(), 0) == tg.TARA_ERR_ARGS
     p.write_text(base.format(dim=2, mode="mpi"))
+    capfd.readouterr()
     assert L.tara_run_ini(str(p).encode(), str(tmp_path / "o").encode(), 0) == tg.TARA_OK
+    # src/main.f95's message, written and flushed before the call returns
+    assert capfd.readouterr().out == " Under preparation. Please wait!\n"
     p.write_text("[dimension]\ndim = 2\n")  # arch missing
     assert L.tara_run_ini(str(p).encode(), str(tmp_path / "o").encode(), 0) == tg.TARA_ERR_INI
     p.write_text(base.format(dim=2, mode="serial").replace("[grid]", ""))  # no grid keys
