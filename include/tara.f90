@@ -180,8 +180,8 @@ module tara_gb300
       import
       type(c_ptr), value :: h
       integer(c_int), value :: nsteps
-      real(c_double), intent(out), optional :: kernel_ms(3)
-      integer(c_int), intent(out), optional :: kernel_launches(3)
+      real(c_double), intent(out) :: kernel_ms(3)
+      integer(c_int), intent(out) :: kernel_launches(3)
       real(c_double), intent(out), optional :: total_ms
     end function tara2d_step_timed
     integer(c_int) function tara2d_rhs(h, dt_omegak) bind(C, name="tara2d_rhs")
