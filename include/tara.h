@@ -143,7 +143,8 @@ int tara2d_step(tara2d* h, int nsteps);
 /* As tara2d_step, with a CUDA event recorded on the handle's stream after every
  * launch; waits for completion and returns, per kernel kind (0 column inverse
  * pass, 1 row pass, 2 column forward + update pass), the summed milliseconds
- * and launch counts, and the total milliseconds of the nsteps steps. */
+ * and launch counts, and the total milliseconds of the nsteps steps (total_ms
+ * may be NULL). */
 int tara2d_step_timed(tara2d* h, int nsteps, double* kernel_ms, int* kernel_launches,
                       double* total_ms);
 /* One RHS evaluation of the current state into a host array (dense Nh*Ny complex). */
