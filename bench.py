@@ -298,6 +298,10 @@ def run_ours(args) -> None:
     traffic = from_profiles("traffic_bytes_per_launch", dom, n) if prec == tg.PREC_FP64 else None
     value = n * n * args.steps * ws / (el_ms * 1e-3)
     cpu = cpu_baseline(n, budget_s=args.cpu_budget) if not args.no_cpu_baseline else None
+    if cpu:
+        # the reference's own 2D path runs on one thread (no OpenMP, no FFTW threads)
+        one = cpu_baseline(n, budget_s=min(args.cpu_budget, 8.0), threads=1)
+        cpu["single_thread"] = {"value": one["value"], "cores": one["cores"], "sample": one["sample"]}
     line = {
         "metric": {tg.PREC_FP64: METRIC, tg.PREC_FP32: METRIC.replace("FP64", "FP32 form"),
                    tg.PREC_DF64: METRIC.replace("FP64", "double-float form")}[prec],

@@ -61,3 +61,12 @@ def test_fft_fp64_instruction_count():
         lg = n.bit_length() - 1
         # about 3 FP64 instructions per point per radix-2 stage, fewer for the untwiddled first stage
         assert 2.0 * n * lg <= bench.fft_fp64_inst(n) <= 3.0 * n * lg
+
+
+def test_cpu_baseline_thread_counts():
+    """The all-core port baseline and the single-thread one (the reference's own
+    2D path is single-threaded) report the threads they used."""
+    one = bench.cpu_baseline(64, budget_s=0.2, threads=1)
+    assert one["cores"] == 1 and one["value"] > 0 and one["kind"] == "port"
+    many = bench.cpu_baseline(64, budget_s=0.2)
+    assert many["cores"] >= 1 and many["unit"] == bench.UNIT
