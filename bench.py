@@ -140,7 +140,7 @@ def cpu_baseline(n: int, budget_s: float = 15.0, threads: int | None = None) -> 
         steps += 1
     return {"value": n * n * steps / elapsed, "unit": UNIT, "cores": O.threads(), "kind": "port",
             "sample": f"{steps} RK4 step(s) at {n}^2 in {elapsed:.2f} s (oracle C restatement, "
-                      f"own radix-2 FFT, {O.threads()} OpenMP threads)"}
+                      f"own radix-2 FFT, {O.threads()} OpenMP thread{'s' if O.threads() != 1 else ''})"}
 
 
 def dist_init():
