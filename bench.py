@@ -39,6 +39,12 @@ SEED = {512: 20240512, 2048: 20242048}
 NU, DT, K0, ENERGY = 1e-4, 5e-5, 6.0, 0.5
 
 
+def workload(n: int) -> str:
+    """The workload string both arms print in config.workload."""
+    return (f"2D vorticity plain RHS (derive2csh), classic RK4, {n}x{n}, "
+            f"2pi box, nu={NU}, dt={DT}, k0={K0}, E=0.5, seed {SEED.get(n, 1)}")
+
+
 def peaks() -> tuple[float, str]:
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -181,8 +187,9 @@ def run_reference(args) -> None:
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded random-phase spectrum)",
-        "config": {"workload": f"2D vorticity plain RHS, RK4, {n}^2, nu={NU}, dt={DT}",
-                   "note": "reference Fortran not buildable (no Fortran compiler); CPU restatement"},
+        "config": {"workload": workload(n), "l2": "working set > L2 (no flush)",
+                   "parallelism": "host CPU cores, rank 0 only"},
+        "note": "reference Fortran not buildable (no Fortran compiler); CPU restatement",
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": O.threads(), "kind": "port",
                          "sample": f"{args.steps} timed RK4 steps at {n}^2 after {args.warmup} warm-up"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -310,8 +317,7 @@ def run_ours(args) -> None:
         "scaling": "weak", "vs_baseline": None, "dtype": {tg.PREC_FP64: "f64", tg.PREC_FP32: "f32 transforms / f64 state",
                                                   tg.PREC_DF64: "df64 (f32 pair) transforms / f64 state"}[prec],
         "data": "synthetic (seeded random-phase spectrum, Philox4x32-10)",
-        "config": {"workload": f"2D vorticity plain RHS (derive2csh), classic RK4, {n}x{n}, "
-                               f"2pi box, nu={NU}, dt={DT}, k0={K0}, E=0.5, seed {SEED.get(n, 1)}",
+        "config": {"workload": workload(n),
                    "l2": "working set > L2 (no flush)", "parallelism": f"replicas x{ws}"},
         "e2e": {"value": n * n * e2e_steps * ws / e2e_el, "unit": UNIT,
                 "h2d_bytes_per_step": int(F), "d2h_bytes_per_step": int(F),

@@ -591,9 +591,14 @@ int tara_closure_step(tara_closure* c, int nsteps);
  * file-scope static device array of about 2.9 MB that every GPU loading the
  * library holds until exit, so grids are limited to Nx, Ny <= 256 (powers of
  * two); larger ones return TARA_ERR_ARGS.  The first call on a device resolves
- * the array's address and uploads twiddle tables synchronously, so make it
- * before any stream capture.  All calls on a device share the array: calls
- * whose GPU work overlaps race and must be serialised by the caller. */
+ * the array's address, uploads twiddle tables and waits for the device
+ * (cudaDeviceSynchronize), so make it before any stream capture.  All calls on
+ * a device share the array: calls whose GPU work overlaps race and must be
+ * serialised by the caller; calls one after another on one stream are safe.
+ * Non-finite results are not reported: the call returns TARA_OK once its
+ * launches are accepted, even when the output holds NaN or Inf (checking would
+ * need a device-to-host read and a wait), so a caller that needs the check
+ * tests dt_omegak_dev itself. */
 int tara_derive2csh_noalloc(int nx, int ny, double nu, const void* omegak_dev,
                             void* dt_omegak_dev, void* stream);
 

@@ -20,7 +20,9 @@ CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "libtara.so"
 ORACLE = ROOT / "oracle"
-REFERENCE = Path(os.environ.get("TARA_REFERENCE", "/root/reference"))
+# The reference checkout (for the FFTW-backed oracle only): named by the
+# TARA_REFERENCE environment variable; without it oracle/_ref is not built.
+REFERENCE = Path(os.environ["TARA_REFERENCE"]) if os.environ.get("TARA_REFERENCE") else None
 
 SOURCES = ["launch_fp64.cu", "launch_fp32.cu", "launch_df64.cu", "solver2d.cu", "capi.cu", "noalloc.cu", "mhd3d.cu",
            "ensemble.cu", "fno.cu", "closure.cu", "particles.cu", "coh2d.cu", "com2d.cu", "ini.cpp",
@@ -96,11 +98,12 @@ def build_lib(force: bool = False, verbose: bool = False) -> Path:
 
 def build_oracle(verbose: bool = False) -> None:
     """Oracle (test infrastructure): the own-FFT restatement everywhere, and the
-    FFTW-from-reference-sources build only where the reference tree exists."""
+    FFTW-from-reference-sources build only where TARA_REFERENCE names a
+    reference tree that exists."""
     r = subprocess.run(["make", "-s", "-C", str(ORACLE), "port"], capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"oracle build failed:\n{r.stdout}\n{r.stderr}")
-    if (REFERENCE / "lib" / "fftw" / "api" / "fftw3.h").exists():
+    if REFERENCE is not None and (REFERENCE / "lib" / "fftw" / "api" / "fftw3.h").exists():
         jobs = str(os.cpu_count() or 4)
         r = subprocess.run(["make", "-s", "-j", jobs, "-C", str(ORACLE), "ref", f"REF={REFERENCE}"],
                            capture_output=True, text=True)

@@ -13,16 +13,25 @@
 // g_noalloc_scratch, of fixed size (kScratchBytes, about 2.9 MB) that every GPU
 // which loads libtara holds until the process exits.  It carries the four
 // y-inverse spectra, the products' spectrum, the twiddle tables, the
-// wavenumber and 1/k^2 tables and an error flag for grids up to
-// kNoAllocMaxN^2 = 256^2;
-// larger grids are rejected with TARA_ERR_ARGS.
+// wavenumber and 1/k^2 tables and the flag word that the forward column kernel
+// sets on a non-finite value, for grids up to kNoAllocMaxN^2 = 256^2; larger
+// grids are rejected with TARA_ERR_ARGS.
+//
+// Non-finite results are NOT reported: reading the flag back would need a
+// device-to-host copy and a wait on the caller's stream, which this entry
+// point leaves to the caller.  It returns TARA_OK whenever the launches were
+// accepted, even if the right-hand side holds NaN or Inf; a caller that needs
+// the check tests its output array (the regular drop-in derive2csh_ reports
+// TARA_ERR_NONFINITE through tara_last_error instead).
 //
 // Host code cannot use the name g_noalloc_scratch as a device address (on the
 // host it names a shadow variable).  The first call on each device, with that
 // device current, resolves the real address with cudaGetSymbolAddress and
-// uploads the twiddle tables with a synchronous cudaMemcpy; that first call
-// should therefore come before any stream capture.  Later calls only enqueue
-// kernels on the caller's stream.
+// uploads the twiddle tables with cudaMemcpy followed by cudaDeviceSynchronize
+// (a copy from pageable memory may return before its DMA has landed, and a
+// caller's non-blocking stream is not ordered after the legacy stream that
+// carries it); that first call should therefore come before any stream
+// capture.  Later calls only enqueue kernels on the caller's stream.
 //
 // Every call on a device shares the one array, and the array keeps what the last
 // call wrote.  Each call rewrites everything it reads before reading it (the
@@ -123,6 +132,9 @@ static int noalloc_setup(unsigned char** out) {
       }
     e = cudaMemcpy((unsigned char*)p + kOffTw, tw, sizeof(tw), cudaMemcpyHostToDevice);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy(twiddles)");
+    // the tables must be in device memory before any stream of the caller reads them
+    e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceSynchronize(twiddles)");
     g_dev_ptr[dev] = (unsigned char*)p;
   }
   *out = g_dev_ptr[dev];
