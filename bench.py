@@ -431,36 +431,6 @@ def run_ensemble(args) -> None:
     e.close()
 
 
-def mhd3d_initial_state(n: int, seed: int = 3):
-    """3D MHD initial condition as real fields (rho, rho u, E, B): u = (-sin y,
-    sin x, 0), B = (-sin y, sin 2x, 0), rho = 1, plus a seeded 1 % random-phase
-    solenoidal perturbation of u and B at |k| <= 4; E = 1 + |u|^2/2 + |B|^2/2."""
-    import numpy as np
-
-    rng = np.random.default_rng(seed)
-    g = np.arange(n) * (2 * np.pi / n)
-    z, y, x = np.meshgrid(g, g, g, indexing="ij")
-    kz, ky, kx = np.meshgrid(np.fft.fftfreq(n, 1 / n), np.fft.fftfreq(n, 1 / n),
-                             np.arange(n // 2 + 1), indexing="ij")
-    k2 = kx**2 + ky**2 + kz**2
-    shell = (k2 > 0) & (k2 <= 16)
-
-    def solenoidal(base):
-        a = [np.where(shell, np.exp(2j * np.pi * rng.random(k2.shape)), 0) for _ in range(3)]
-        kd = (kx * a[0] + ky * a[1] + kz * a[2]) / np.where(k2 > 0, k2, 1)
-        a = [a[0] - kx * kd, a[1] - ky * kd, a[2] - kz * kd]
-        f = [np.fft.irfftn(c, s=(n, n, n), axes=(0, 1, 2)) for c in a]
-        rms = np.sqrt(sum((v**2).mean() for v in f))
-        brms = np.sqrt(sum((v**2).mean() for v in base))
-        return [b + 0.01 * brms / rms * v for b, v in zip(base, f)]
-
-    u = solenoidal([-np.sin(y), np.sin(x), 0 * x])
-    b = solenoidal([-np.sin(y), np.sin(2 * x), 0 * x])
-    rho = np.ones_like(x)
-    e = 1.0 + 0.5 * sum(v**2 for v in u) + 0.5 * sum(v**2 for v in b)
-    return np.stack([rho, u[0], u[1], u[2], e, b[0], b[1], b[2]])
-
-
 def run_coh2d(args) -> None:
     """The 2D compressible solvers, AB2 steps at n^2 from the reference drivers'
     initial states, FP64:
@@ -589,7 +559,7 @@ def run_mhd3d(args) -> None:
     torch.cuda.set_device(0)
     n = 128
     s = tg.Solver3D(n, defined=1, nu_u=0.01, eta_b=0.01, dt=1e-3)
-    s.set_state_real(mhd3d_initial_state(n))
+    s.init_orszag_tang(0.01, 4, 3)  # tara3d_init_orszag_tang: 1 % perturbation at |k| <= 4, seed 3
     s.step(args.warmup)
     s.synchronize()
     ms = timed_on_stream(s.stream, lambda: s.step(args.steps))

@@ -412,6 +412,16 @@ int tara3d_set_state(tara3d* h, const double* state8, const double* hist8);
 int tara3d_get_state(tara3d* h, double* state8, double* hist8);
 /* eight real (Nx,Ny,Nz) fields in the same order, transformed on the GPU */
 int tara3d_set_state_real(tara3d* h, const double* real8);
+/* The 3D MHD benchmark's initial state (no counterpart in the reference, whose
+ * own 3D initial state is the ABC flow of src/main3com.f95:301-319):
+ * rho = 1, u = (-sin y, sin x, 0) + du, B = (-sin y, sin 2x, 0) + dB,
+ * E = 1 + |u|^2/2 + |B|^2/2 on the 2 pi grid x_i = 2 pi i / Nx, where du and dB
+ * are seeded random-phase solenoidal fields on the modes 0 < |k| <= kmax
+ * (Philox4x32-10 phases at counter (i, j, k, 3 f + c), f = 0 for u and 1 for B,
+ * c the component; projected onto k.a = 0; kx = 0 plane Hermitian) scaled to
+ * amp times the base fields' r.m.s. (1).  The benchmark uses amp = 0.01,
+ * kmax = 4, seed 3.  History set to zero.  Needs 2 kmax < Nx, Ny, Nz. */
+int tara3d_init_orszag_tang(tara3d* h, double amp, int kmax, uint64_t seed);
 /* nsteps of derive3com + ab3com + the driver's history rotation (E frozen) */
 int tara3d_step(tara3d* h, int nsteps);
 /* all eight derivatives of the current state (dense spectra), as derive3com */

@@ -107,6 +107,7 @@ class Oracle:
         L.oracle_ab3com.argtypes = [c_int, c_int, c_int, c_double, vp, vp, vp, vp]
         L.oracle_run3d.argtypes = [c_int, c_int, c_int, vp, c_double, c_int, vp, vp]
         L.oracle_ic3d_abc.argtypes = [c_int, c_int, c_int, c_double, c_double, c_double, vp]
+        L.oracle_ic3d_ot.argtypes = [c_int, c_int, c_int, c_double, c_int, ctypes.c_uint64, vp]
         L.oracle_driver_velocity.argtypes = [c_int, c_int, c_double, c_double, vp, vp, vp]
         L.oracle_particles_step.argtypes = [c_int, c_int, c_double, c_double, vp, vp, c_int, vp, vp,
                                             c_double]
@@ -332,6 +333,14 @@ class Oracle:
     def ic3d_abc(self, nx, ny, nz, l_ini=2.0):
         out = np.zeros((8, nz, ny, nx), np.float64)
         self.L.oracle_ic3d_abc(nx, ny, nz, l_ini, l_ini, l_ini, out.ctypes.data)
+        return out
+
+    def ic3d_ot(self, nx, ny=None, nz=None, amp=0.01, kmax=4, seed=3):
+        """The 3D MHD benchmark's initial state as a spectral state (8, Nz, Ny, Nh)."""
+        ny = nx if ny is None else ny
+        nz = nx if nz is None else nz
+        out = np.zeros((8, nz, ny, nx // 2 + 1), np.complex128)
+        self.L.oracle_ic3d_ot(nx, ny, nz, amp, kmax, seed, out.ctypes.data)
         return out
 
     def state_from_real(self, real8):

@@ -1134,6 +1134,87 @@ void oracle_ic3d_abc(int nx, int ny, int nz, double lx_ini, double ly_ini, doubl
   }
 }
 
+/* The 3D MHD benchmark's initial state (the library's tara3d_init_orszag_tang;
+ * no counterpart in the reference, whose 3D driver starts from the ABC flow
+ * above): rho = 1, u = (-sin y, sin x, 0) + du, B = (-sin y, sin 2x, 0) + dB,
+ * E = 1 + |u|^2/2 + |B|^2/2 on the 2 pi grid.  du, dB: for every mode
+ * 0 < |k|^2 <= kmax^2 of the half space (the kx = 0 plane only where ky > 0,
+ * or ky = 0 and kz > 0; the other half is the conjugate) and component c,
+ * phase 2 pi U (U from word 0 of Philox4x32-10 at counter (i, j, k, 3 f + c),
+ * f = 0 for u and 1 for B, key = seed), projected onto k.a = 0 and scaled so
+ * that sum_c <f_c^2> = amp^2 (the base fields' r.m.s. is 1).  Writes the
+ * spectral state (8, Nz, Ny, Nh) in the unnormalised r2c convention: u and B
+ * spectra through c2r (divided by Nx Ny Nz), E and rho formed on the grid, then
+ * r2c of all eight fields. */
+void oracle_ic3d_ot(int nx, int ny, int nz, double amp, int kmax, uint64_t seed, double* state) {
+  const int nh = nx / 2 + 1;
+  const size_t fs = (size_t)nh * ny * nz, nr = (size_t)nx * ny * nz;
+  const double nn = (double)nx * (double)ny * (double)nz;
+  const double two_pi = 2.0 * PI_R8;
+  const uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+  double* spec = (double*)xcalloc(2 * 6 * fs, sizeof(double));
+  for (int f = 0; f < 2; ++f) {
+    double* P = spec + 2 * 3 * f * fs;
+    double norm2 = 0.0;
+    for (int k = 0; k < nz; ++k)
+      for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nh; ++i) {
+          const int kxi = i, kyi = j <= ny / 2 ? j : j - ny, kzi = k <= nz / 2 ? k : k - nz;
+          const int k2i = kxi * kxi + kyi * kyi + kzi * kzi;
+          if (k2i == 0 || k2i > kmax * kmax) continue;
+          if (i == 0 && (kyi < 0 || (kyi == 0 && kzi < 0))) continue;
+          double ar[3], ai[3];
+          for (int c = 0; c < 3; ++c) {
+            const uint32_t ctr[4] = {(uint32_t)i, (uint32_t)j, (uint32_t)k, (uint32_t)(3 * f + c)};
+            uint32_t r[4];
+            oracle_philox4x32_10(ctr, key, r);
+            const double theta = two_pi * ((double)r[0] * (1.0 / 4294967296.0));
+            ar[c] = cos(theta);
+            ai[c] = sin(theta);
+          }
+          const double kv[3] = {(double)kxi, (double)kyi, (double)kzi};
+          const double k2 = (double)k2i;
+          const double dr = (kv[0] * ar[0] + kv[1] * ar[1] + kv[2] * ar[2]) / k2;
+          const double di = (kv[0] * ai[0] + kv[1] * ai[1] + kv[2] * ai[2]) / k2;
+          for (int c = 0; c < 3; ++c) {
+            const double pr = ar[c] - kv[c] * dr, pim = ai[c] - kv[c] * di;
+            const size_t q = c * fs + ((size_t)k * ny + j) * nh + i;
+            P[2 * q] = pr;
+            P[2 * q + 1] = pim;
+            if (i == 0) {
+              const int jm = (ny - j) % ny, km = (nz - k) % nz;
+              const size_t qm = c * fs + ((size_t)km * ny + jm) * nh;
+              P[2 * qm] = pr;
+              P[2 * qm + 1] = -pim;
+            }
+            norm2 += 2.0 * (pr * pr + pim * pim);
+          }
+        }
+    const double sc = norm2 > 0.0 ? amp * nn / sqrt(norm2) : 0.0;
+    for (size_t q = 0; q < 2 * 3 * fs; ++q) P[q] *= sc;
+    const double h = 0.5 * nn;
+    P[2 * ((size_t)1 * nh) + 1] += h;                 /* -sin y: F(0, 1, 0) = +i N/2 */
+    P[2 * ((size_t)(ny - 1) * nh) + 1] -= h;          /*         F(0, -1, 0) = -i N/2 */
+    P[2 * (fs + (size_t)(f == 0 ? 1 : 2)) + 1] -= h;  /* sin(m x): F(m, 0, 0) = -i N/2 */
+  }
+  double* real = (double*)xcalloc(8 * nr, sizeof(double));
+  const int slot[6] = {F_RUX, F_RUY, F_RUZ, F_BX, F_BY, F_BZ};
+  for (int f = 0; f < 6; ++f) {
+    oracle_c2r_3d(nx, ny, nz, spec + 2 * f * fs, real + slot[f] * nr);
+    for (size_t r = 0; r < nr; ++r) real[slot[f] * nr + r] *= 1.0 / nn;
+  }
+  for (size_t r = 0; r < nr; ++r) {
+    const double ux = real[F_RUX * nr + r], uy = real[F_RUY * nr + r], uz = real[F_RUZ * nr + r];
+    const double bx = real[F_BX * nr + r], by = real[F_BY * nr + r], bz = real[F_BZ * nr + r];
+    const double u2 = (ux * ux + uy * uy) + uz * uz, b2 = (bx * bx + by * by) + bz * bz;
+    real[F_RHO * nr + r] = 1.0;
+    real[F_E * nr + r] = (1.0 + 0.5 * u2) + 0.5 * b2;
+  }
+  for (int f = 0; f < 8; ++f) oracle_r2c_3d(nx, ny, nz, real + f * nr, state + 2 * f * fs);
+  free(real);
+  free(spec);
+}
+
 /* ------------------------------------------------------------------------- */
 /* derive2coh -- src/derive2coh.f95:6-265                                     */
 /* ------------------------------------------------------------------------- */

@@ -135,6 +135,9 @@ void oracle_run3d(int nx, int ny, int nz, const oracle_mhd_params* p, double dt,
  * fields in the state order. */
 void oracle_ic3d_abc(int nx, int ny, int nz, double lx_ini, double ly_ini, double lz_ini,
                      double* real8);
+/* The 3D MHD benchmark's Orszag-Tang-type initial state with a seeded
+ * solenoidal perturbation (spectral state (8, Nz, Ny, Nh); see tara_oracle.c). */
+void oracle_ic3d_ot(int nx, int ny, int nz, double amp, int kmax, uint64_t seed, double* state);
 
 /* ---- 2D compressible isothermal hydro (src/derive2coh.f95, src/ab2coh.f95) ---- */
 typedef struct {

@@ -154,6 +154,7 @@ def _declare(L: ctypes.CDLL) -> None:
     L.tara3d_set_state.argtypes = [vp, vp, vp]
     L.tara3d_get_state.argtypes = [vp, vp, vp]
     L.tara3d_set_state_real.argtypes = [vp, vp]
+    L.tara3d_init_orszag_tang.argtypes = [vp, ctypes.c_double, c_int, ctypes.c_uint64]
     L.tara3d_step.argtypes = [vp, c_int]
     L.tara3d_rhs.argtypes = [vp, vp]
     L.tara3d_synchronize.argtypes = [vp]
@@ -636,6 +637,13 @@ class Solver3D:
         if r.shape != (8, nz, ny, 2 * (nh - 1)):
             raise ValueError(f"expected an (8, {nz}, {ny}, {2 * (nh - 1)}) real state, got {r.shape}")
         _check(lib().tara3d_set_state_real(self._h, r.ctypes.data))
+
+    def init_orszag_tang(self, amp: float = 0.01, kmax: int = 4, seed: int = 3):
+        """The 3D MHD benchmark's initial state (tara3d_init_orszag_tang): rho = 1,
+        u = (-sin y, sin x, 0), B = (-sin y, sin 2x, 0), each plus a seeded
+        random-phase solenoidal perturbation of relative r.m.s. `amp` on the modes
+        0 < |k| <= kmax; E = 1 + |u|^2/2 + |B|^2/2; zero history."""
+        _check(lib().tara3d_init_orszag_tang(self._h, float(amp), int(kmax), int(seed)))
 
     def get_state(self, with_history: bool = False):
         st = np.zeros((8,) + self.shape, np.complex128)

@@ -1,6 +1,7 @@
 // Internal host-side declarations shared by the translation units of libtara.
 #pragma once
 #include <cuda_runtime.h>
+#include <cstdint>
 
 #include <string>
 
@@ -25,6 +26,30 @@ int cuda_fail(cudaError_t e, const char* what);
 constexpr int kMaxN = 2048;
 inline bool is_pow2_in_range(int n) { return n >= 16 && n <= kMaxN && (n & (n - 1)) == 0; }
 inline int round_up(int v, int m) { return (v + m - 1) / m * m; }
+
+// Tile variants per step kernel (column inverse pass, row pass, column forward
+// pass) and the most any kernel has.
+constexpr int kVariants[3] = {3, 4, 3};
+constexpr int kMaxVariants = 4;
+
+// Philox4x32-10 on the host (Salmon et al., SC'11): ten rounds with the
+// published multipliers and Weyl key increments, for the seeded phases of the
+// random initial states.
+inline void philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
+  uint32_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3], k0 = key[0], k1 = key[1];
+  for (int r = 0; r < 10; ++r) {
+    const uint64_t p0 = (uint64_t)0xD2511F53u * c0, p1 = (uint64_t)0xCD9E8D57u * c2;
+    const uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+    const uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+    c0 = hi1 ^ c1 ^ k0;
+    c1 = lo1;
+    c2 = hi0 ^ c3 ^ k1;
+    c3 = lo0;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
 
 // Host tables shared with the oracle's arithmetic: kx = 2*kpi*i/lx etc.
 void make_wavenumbers(int nx, int ny, double kpi, double lx, double ly, double* kx, double* ky,

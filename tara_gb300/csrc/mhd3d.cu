@@ -93,6 +93,31 @@ __global__ void k3_energy(const double* __restrict__ rl, double* __restrict__ pr
   }
 }
 
+// The Orszag-Tang-type initial state on the grid: rl holds the unnormalised c2r
+// of the u and B spectra in the rho u and B slots; normalise them (rho = 1, so
+// rho u = u) and fill rho = 1 and E = 1 + |u|^2/2 + |B|^2/2.
+__global__ void k3_ot_fill(double* __restrict__ rl, Grid3D g, double inv_n) {
+  const size_t total = (size_t)g.nz * g.ny * g.nx;
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += (size_t)gridDim.x * blockDim.x) {
+    const size_t r = (t / g.nx) * g.rpitch + (t % g.nx);
+    const double ux = rl[S_RUX * g.rfs + r] * inv_n, uy = rl[S_RUY * g.rfs + r] * inv_n,
+                 uz = rl[S_RUZ * g.rfs + r] * inv_n;
+    const double bx = rl[S_BX * g.rfs + r] * inv_n, by = rl[S_BY * g.rfs + r] * inv_n,
+                 bz = rl[S_BZ * g.rfs + r] * inv_n;
+    rl[S_RHO * g.rfs + r] = 1.0;
+    rl[S_RUX * g.rfs + r] = ux;
+    rl[S_RUY * g.rfs + r] = uy;
+    rl[S_RUZ * g.rfs + r] = uz;
+    rl[S_BX * g.rfs + r] = bx;
+    rl[S_BY * g.rfs + r] = by;
+    rl[S_BZ * g.rfs + r] = bz;
+    const double u2 = __dadd_rn(__dadd_rn(__dmul_rn(ux, ux), __dmul_rn(uy, uy)), __dmul_rn(uz, uz));
+    const double b2 = __dadd_rn(__dadd_rn(__dmul_rn(bx, bx), __dmul_rn(by, by)), __dmul_rn(bz, bz));
+    rl[S_E * g.rfs + r] = __dadd_rn(__dadd_rn(1.0, __dmul_rn(0.5, u2)), __dmul_rn(0.5, b2));
+  }
+}
+
 __device__ __forceinline__ double2 ik(double k, double2 f) { return make_double2(-k * f.y, k * f.x); }
 
 __global__ void k3_derivs(const double2* __restrict__ st, const double2* __restrict__ pk,
@@ -418,6 +443,73 @@ int r2c3(tara3d* h, const double* in, double2* out, int nf) {
                h->stream);
 }
 
+// Spectra of u and B of the Orszag-Tang-type initial state, in the r2c
+// convention of the state (unnormalised: F(k) = sum_x f(x) exp(-i k.x)), six
+// dense (Nh,Ny,Nz) arrays in the order ux, uy, uz, Bx, By, Bz.
+//   u = (-sin y, sin x, 0) + du,  B = (-sin y, sin 2x, 0) + dB  (2 pi box)
+// du and dB are random-phase solenoidal fields on the modes 0 < |k| <= kmax
+// (integer wavenumbers): for each such mode of the half space and component c,
+// phase theta = 2 pi U with U = word 0 of Philox4x32-10 at counter
+// (i, j, k, 3 f + c) (f = 0 for u, 1 for B; (i, j, k) the array indices of the
+// mode) and key (seed low, seed high), a_c = exp(i theta); then
+// a <- a - k (k.a)/|k|^2.  On the kx = 0 plane only the half with ky > 0, or
+// ky = 0 and kz > 0, is drawn and the other half is its conjugate, so the field
+// is real.  Each perturbation is scaled so that its r.m.s. (sum over the
+// components of <f_c^2>) is amp times that of the base field, which is 1 for
+// both u and B.
+static void ot_spectra(int nx, int ny, int nz, double amp, int kmax, uint64_t seed,
+                       std::vector<double2>& out) {
+  const int nh = nx / 2 + 1;
+  const size_t fs = (size_t)nh * ny * nz;
+  const double nn = (double)nx * (double)ny * (double)nz;
+  const double two_pi = 2.0 * 3.14159265358979323846;
+  out.assign(6 * fs, make_double2(0.0, 0.0));
+  const uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+  auto sgn = [](int j, int n) { return j <= n / 2 ? j : j - n; };
+  for (int f = 0; f < 2; ++f) {
+    double2* P = out.data() + 3 * f * fs;
+    double norm2 = 0.0;
+    for (int k = 0; k < nz; ++k)
+      for (int j = 0; j < ny; ++j)
+        for (int i = 0; i < nh; ++i) {
+          const int kxi = i, kyi = sgn(j, ny), kzi = sgn(k, nz);
+          const int k2i = kxi * kxi + kyi * kyi + kzi * kzi;
+          if (k2i == 0 || k2i > kmax * kmax) continue;
+          if (i == 0 && (kyi < 0 || (kyi == 0 && kzi < 0))) continue;  // the conjugate half
+          double ar[3], ai[3];
+          for (int c = 0; c < 3; ++c) {
+            const uint32_t ctr[4] = {(uint32_t)i, (uint32_t)j, (uint32_t)k, (uint32_t)(3 * f + c)};
+            uint32_t r[4];
+            philox4x32_10(ctr, key, r);
+            const double theta = two_pi * ((double)r[0] * (1.0 / 4294967296.0));
+            ar[c] = std::cos(theta);
+            ai[c] = std::sin(theta);
+          }
+          const double kv[3] = {(double)kxi, (double)kyi, (double)kzi};
+          const double k2 = (double)k2i;
+          const double dr = (kv[0] * ar[0] + kv[1] * ar[1] + kv[2] * ar[2]) / k2;
+          const double di = (kv[0] * ai[0] + kv[1] * ai[1] + kv[2] * ai[2]) / k2;
+          for (int c = 0; c < 3; ++c) {
+            const double pr = ar[c] - kv[c] * dr, pi = ai[c] - kv[c] * di;
+            P[c * fs + ((size_t)k * ny + j) * nh + i] = make_double2(pr, pi);
+            if (i == 0) {
+              const int jm = (ny - j) % ny, km = (nz - k) % nz;
+              P[c * fs + ((size_t)km * ny + jm) * nh] = make_double2(pr, -pi);
+            }
+            // the mode and its conjugate at -k both count in the full spectrum
+            norm2 += 2.0 * (pr * pr + pi * pi);
+          }
+        }
+    const double s = norm2 > 0.0 ? amp * nn / std::sqrt(norm2) : 0.0;
+    for (size_t q = 0; q < 3 * fs; ++q) P[q] = make_double2(P[q].x * s, P[q].y * s);
+    // base modes: -sin y at ky = +-1 (kx = 0), sin(m x) at kx = m (m = 1 for u, 2 for B)
+    const double h = 0.5 * nn;
+    P[0 * fs + (size_t)1 * nh].y += h;         // x component: -sin y, F(0, 1, 0) = +i N/2
+    P[0 * fs + (size_t)(ny - 1) * nh].y -= h;  // F(0, -1, 0) = -i N/2
+    P[1 * fs + (size_t)(f == 0 ? 1 : 2)].y -= h;  // y component: sin(m x), F(m, 0, 0) = -i N/2
+  }
+}
+
 constexpr int kPwBlocks = 152 * 4, kPwThreads = 256;
 
 int rhs3(tara3d* h, int mode, int with_energy) {
@@ -597,6 +689,30 @@ int tara3d_set_state_real(tara3d* h, const double* real8) {
     TARA_CK(cudaMemcpy2DAsync(h->rl + f * h->rfs, rp, real8 + f * dense, rowb, rowb, rows,
                               cudaMemcpyHostToDevice, h->stream));
   int rc;
+  if ((rc = r2c3(h, h->rl, h->st, S_N))) return rc;
+  TARA_CK(cudaMemsetAsync(h->hist, 0, S_N * h->fs * sizeof(double2), h->stream));
+  TARA_CK(cudaStreamSynchronize(h->stream));
+  return set_ok();
+}
+
+int tara3d_init_orszag_tang(tara3d* h, double amp, int kmax, uint64_t seed) {
+  if (!h || !(amp >= 0.0) || kmax < 0) return set_error(TARA_ERR_ARGS, "bad arguments");
+  if (2 * kmax >= h->nx || 2 * kmax >= h->ny || 2 * kmax >= h->nz || h->nx < 8)
+    return set_error(TARA_ERR_ARGS, "kmax must stay below the Nyquist modes (2 kmax < Nx, Ny, Nz)");
+  TARA_CK(cudaSetDevice(h->dev));
+  std::vector<double2> spec;
+  ot_spectra(h->nx, h->ny, h->nz, amp, kmax, seed, spec);
+  const size_t fs = (size_t)h->nh * h->ny * h->nz;
+  int rc;
+  const int slot[6] = {S_RUX, S_RUY, S_RUZ, S_BX, S_BY, S_BZ};
+  for (int f = 0; f < 6; ++f)
+    if ((rc = copy3(h, h->st + slot[f] * h->fs, (const double*)(spec.data() + f * fs),
+                    cudaMemcpyHostToDevice, nullptr)))
+      return rc;
+  if ((rc = c2r3(h, h->st + S_RUX * h->fs, h->rl + S_RUX * h->rfs, 3))) return rc;
+  if ((rc = c2r3(h, h->st + S_BX * h->fs, h->rl + S_BX * h->rfs, 3))) return rc;
+  k3_ot_fill<<<kPwBlocks, kPwThreads, 0, h->stream>>>(h->rl, h->g, h->p.inv_n);
+  TARA_CK(cudaGetLastError());
   if ((rc = r2c3(h, h->rl, h->st, S_N))) return rc;
   TARA_CK(cudaMemsetAsync(h->hist, 0, S_N * h->fs * sizeof(double2), h->stream));
   TARA_CK(cudaStreamSynchronize(h->stream));

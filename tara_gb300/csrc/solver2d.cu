@@ -758,7 +758,7 @@ int tara2d_step_timed(tara2d* h, int nsteps, double* kernel_ms, int* kernel_laun
   return rc ? rc : set_ok();
 }
 
-int tara2d_autotune(tara2d* h, int trial_steps, int* variants3, double* ms9) {
+int tara2d_autotune(tara2d* h, int trial_steps, int* variants3, double* ms12) {
   if (!h || trial_steps <= 0) return set_error(TARA_ERR_ARGS, "bad arguments");
   TARA_CK(cudaSetDevice(h->dev));
   const size_t bytes = (size_t)h->batch * h->ny * h->pitch * sizeof(double2);
@@ -769,48 +769,58 @@ int tara2d_autotune(tara2d* h, int trial_steps, int* variants3, double* ms9) {
   if (!rc && (cudaMemcpyAsync(save_w0, h->w0, bytes, cudaMemcpyDeviceToDevice, h->stream) != cudaSuccess ||
               cudaMemcpyAsync(save_fold, h->fold, bytes, cudaMemcpyDeviceToDevice, h->stream) != cudaSuccess))
     rc = set_error(TARA_ERR_CUDA, "state save");
-  // Pass 1: all three kernels in variant v together (a warm step, which also
-  // sets the shared-memory attributes on first use, then trial_steps timed).
+  // Pass 1: every kernel in variant v (the last variant of a kernel that has
+  // fewer), one settling step (which also sets the shared-memory attributes on
+  // first use), then trial_steps timed.
   // Pass 2: each kernel's variants with the other two at their pass-1 choice,
-  // one timed step each -- a kernel's time depends on its neighbours' tiles
-  // (cache contents, CTA phases), so the choice is made in that context.
-  double ms[3][3];
+  // again one settling step and trial_steps timed -- a kernel's time depends
+  // on its neighbours' tiles (cache contents, CTA phases), and a variant timed
+  // right after a switch, without the settling step, read up to 15 % slow.
+  double ms[kMaxVariants][3];
+  for (int v = 0; v < kMaxVariants; ++v)
+    for (int k = 0; k < 3; ++k) ms[v][k] = 0.0;
   int c[3] = {0, 0, 0};
-  for (int v = 0; v < 3 && !rc; ++v) {
-    for (int k = 0; k < 3; ++k) h->var[k] = v;
-    rc = tara2d_step(h, 1);
-    double t[3];
+  auto timed = [&](double* t) {
+    int r = tara2d_step(h, 1);
     int cnt[3];
-    if (!rc) rc = tara2d_step_timed(h, trial_steps, t, cnt, nullptr);
+    if (!r) r = tara2d_step_timed(h, trial_steps, t, cnt, nullptr);
+    if (!r)
+      for (int k = 0; k < 3; ++k) t[k] /= (cnt[k] > 0 ? cnt[k] : 1);
+    return r;
+  };
+  for (int v = 0; v < kMaxVariants && !rc; ++v) {
+    for (int k = 0; k < 3; ++k) h->var[k] = v < kVariants[k] ? v : kVariants[k] - 1;
+    double t[3];
+    rc = timed(t);
     if (!rc)
-      for (int k = 0; k < 3; ++k) ms[v][k] = t[k] / (cnt[k] > 0 ? cnt[k] : 1);
+      for (int k = 0; k < 3; ++k)
+        if (v < kVariants[k]) ms[v][k] = t[k];
   }
   if (!rc)
     for (int k = 0; k < 3; ++k)
-      for (int v = 1; v < 3; ++v)
+      for (int v = 1; v < kVariants[k]; ++v)
         if (ms[v][k] < ms[c[k]][k]) c[k] = v;
-  double ctx[3][3];
+  double ctx[3][kMaxVariants];
   for (int k = 0; k < 3 && !rc; ++k)
-    for (int v = 0; v < 3 && !rc; ++v) {
+    for (int v = 0; v < kVariants[k] && !rc; ++v) {
       for (int q = 0; q < 3; ++q) h->var[q] = c[q];
       h->var[k] = v;
       double t[3];
-      int cnt[3];
-      rc = tara2d_step_timed(h, 1, t, cnt, nullptr);
-      if (!rc) ctx[k][v] = t[k] / (cnt[k] > 0 ? cnt[k] : 1);
+      rc = timed(t);
+      if (!rc) ctx[k][v] = t[k];
     }
   if (!rc)
     for (int k = 0; k < 3; ++k) {
       int best = 0;
-      for (int v = 1; v < 3; ++v)
+      for (int v = 1; v < kVariants[k]; ++v)
         if (ctx[k][v] < ctx[k][best]) best = v;
       h->var[k] = best;
       if (variants3) variants3[k] = best;
-      for (int v = 0; v < 3; ++v) ms[v][k] = ctx[k][v];  // reported: the in-context times
+      for (int v = 0; v < kVariants[k]; ++v) ms[v][k] = ctx[k][v];  // reported: the in-context times
     }
-  if (!rc && ms9)
-    for (int v = 0; v < 3; ++v)
-      for (int k = 0; k < 3; ++k) ms9[3 * v + k] = ms[v][k];
+  if (!rc && ms12)
+    for (int v = 0; v < kMaxVariants; ++v)
+      for (int k = 0; k < 3; ++k) ms12[3 * v + k] = ms[v][k];
   if (!rc && (cudaMemcpyAsync(h->w0, save_w0, bytes, cudaMemcpyDeviceToDevice, h->stream) != cudaSuccess ||
               cudaMemcpyAsync(h->fold, save_fold, bytes, cudaMemcpyDeviceToDevice, h->stream) != cudaSuccess ||
               cudaStreamSynchronize(h->stream) != cudaSuccess))
@@ -823,7 +833,8 @@ int tara2d_autotune(tara2d* h, int trial_steps, int* variants3, double* ms9) {
 int tara2d_set_variants(tara2d* h, const int* variants3) {
   if (!h || !variants3) return set_error(TARA_ERR_ARGS, "null argument");
   for (int k = 0; k < 3; ++k)
-    if (variants3[k] < 0 || variants3[k] > 2) return set_error(TARA_ERR_ARGS, "variants are 0, 1 or 2");
+    if (variants3[k] < 0 || variants3[k] >= kVariants[k])
+      return set_error(TARA_ERR_ARGS, "variants: column passes 0-2, row pass 0-3");
   for (int k = 0; k < 3; ++k) h->var[k] = variants3[k];
   return set_ok();
 }
@@ -976,23 +987,6 @@ int tara2d_real_fields(tara2d* h, const tara2d_diag_params* dp, double* psi, dou
   cudaFree(tx);
   cudaFree(ty);
   return rc ? rc : set_ok();
-}
-
-// Philox4x32-10 on the host (Salmon et al., SC'11), for the seeded phases.
-static void philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
-  uint32_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3], k0 = key[0], k1 = key[1];
-  for (int r = 0; r < 10; ++r) {
-    const uint64_t p0 = (uint64_t)0xD2511F53u * c0, p1 = (uint64_t)0xCD9E8D57u * c2;
-    const uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
-    const uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
-    c0 = hi1 ^ c1 ^ k0;
-    c1 = lo1;
-    c2 = hi0 ^ c3 ^ k1;
-    c3 = lo0;
-    k0 += 0x9E3779B9u;
-    k1 += 0xBB67AE85u;
-  }
-  out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
 }
 
 int tara2d_init_random(tara2d* h, double k0, double energy, uint64_t seed) {
