@@ -244,7 +244,11 @@ def run_ours(args) -> None:
     prec = {"fp32": tg.PREC_FP32, "df64": tg.PREC_DF64}.get(args.precision, tg.PREC_FP64)
     s = tg.Solver2D(n, scheme=tg.SCHEME_RK4, nu=NU, dt=DT, precision=prec)
     s.init_random(K0, ENERGY, SEED.get(n, 1))
-    tuned = s.autotune(2)  # tile variant per kernel (the state is restored)
+    if args.variants:
+        tuned = {"variants": [int(v) for v in args.variants.split(",")], "ms": None}
+        s.set_variants(tuned["variants"])
+    else:
+        tuned = s.autotune(2)  # configuration per kernel (the state is restored)
     dfma_rate = tg.measure_dfma_rate(5) if prec == tg.PREC_FP64 and rank == 0 else None
     s.step(args.warmup)
     s.synchronize()
@@ -337,7 +341,7 @@ def run_ours(args) -> None:
         "fp64_pipe": (fp64_pipe(n, {k: v["ms"] / max(1, v["launches"]) for k, v in ks.items()},
                                 (clocks or {}).get("sm_mhz"), dfma_rate) if prec == tg.PREC_FP64 else None),
         "tile_variants": tuned["variants"],
-        "autotune_ms": tuned["ms"],  # per-launch ms of variants 0, 1, 2 (rows) x the three kernels
+        "autotune_ms": tuned["ms"],  # per-launch ms in context: configurations 0-7 (rows) x the three kernels
         "diag": {"energy": e, "enstrophy": z},
         "cpu_baseline": cpu,
     }
@@ -391,7 +395,10 @@ def run_ensemble(args) -> None:
     per = args.ens_runs_per_size * ws
     idx, mine = shard.shard_of(runs, rank, ws)
     e = tg.Ensemble(mine, precision=tg.PREC_FP32, nu=1e-3, dt=1e-4)
-    e.autotune(3)
+    e.autotune(3)  # tiles and radix per kernel and size, then graph vs persistent
+    if args.ens_form != "auto":
+        e.set_form({"graph": tg.ENS_GRAPH, "persistent4": tg.ENS_PERSISTENT4,
+                    "persistent8": tg.ENS_PERSISTENT8}[args.ens_form])
     e.step(args.warmup)
     e.synchronize()
     if dist:
@@ -399,16 +406,27 @@ def run_ensemble(args) -> None:
     ms = shard.max_over_ranks(timed_on_stream(e.stream, lambda: e.step(args.steps)), dist)
     e.synchronize()
     pts = sum(n * n for n, _, _ in runs)
+    form = e.form()
+    persistent = form["form"] != "graph"
+    groups = e.groups()
     line = {"metric": f"ensemble grid-pt*steps/s ({len(runs)} runs: {per} each at 128^2, 256^2, 512^2; RK4)",
             "value": pts * args.steps / (ms * 1e-3), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "dtype": "f32 transforms / f64 state",
             "data": "synthetic (seeded random-phase spectra)",
-            "config": {"workload": "ensemble of uneven runs", "graph": "one cudaGraphLaunch per step",
+            "config": {"workload": "ensemble of uneven runs",
+                       "launch": ("one cooperative launch for all timed steps" if persistent
+                                  else "one cudaGraphLaunch per step"),
                        "l2": "working set > L2 (no flush)",
                        "parallelism": f"runs sharded x{ws} (cost-balanced, no exchange)"},
-            "gpu_launches": int(shard.sum_over_ranks(e.launches_per_step * args.steps, dist)),
-            "autotune": e.groups()}
+            # the persistent form is one kernel launch per step() call; the graph
+            # replays every pass kernel of every size per step
+            "gpu_launches": int(shard.sum_over_ranks(1 if persistent else e.launches_per_step * args.steps,
+                                                     dist)),
+            "persistent": persistent, "form": form["form"], "form_ms_per_step": form["ms_per_step"],
+            "radix": {str(g["n"]): ["radix-8" if v & 4 else "radix-4" for v in g["variants"]]
+                      for g in groups},
+            "autotune": groups}
     if args.ens_error_steps:
         e64 = tg.Ensemble(mine, precision=tg.PREC_FP64, nu=1e-3, dt=1e-4)
         e.step(args.ens_error_steps - args.steps - args.warmup)
@@ -751,6 +769,11 @@ def main() -> None:
     ap.add_argument("--ens-error-steps", type=int, default=0,
                     help="ensemble: also report the per-run error vs FP64 after this many steps")
     ap.add_argument("--closure-epochs", type=int, default=20, help="closure: training epochs")
+    ap.add_argument("--variants", default=None,
+                    help="fixed configurations 'a,b,c' of the three step kernels (tile variant, "
+                         "+4 for the radix-8 path) instead of the autotuner, for profiling")
+    ap.add_argument("--ens-form", default="auto", choices=["auto", "graph", "persistent4", "persistent8"],
+                    help="ensemble: the autotuner's fastest form, or a fixed one")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32", "df64"],
                     help="rk4-2048: fp32 runs the FP32 form (FP32 transforms, FP64 state), df64 the "
                          "double-float form (transforms in FP32 pairs, FP64 state); the headline is fp64")

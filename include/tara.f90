@@ -32,6 +32,7 @@ module tara_gb300
   integer(c_int), parameter :: TARA_RHS_PLAIN = 0, TARA_RHS_SCREEN = 1
   integer(c_int), parameter :: TARA_SCHEME_AB2 = 0, TARA_SCHEME_RK4 = 1
   integer(c_int), parameter :: TARA_PREC_FP64 = 0, TARA_PREC_FP32 = 1, TARA_PREC_DF64 = 2
+  integer(c_int), parameter :: TARA_ENS_GRAPH = 0, TARA_ENS_PERSISTENT4 = 1, TARA_ENS_PERSISTENT8 = 2
   integer(c_int), parameter :: TARA_FNO_BF16 = 0, TARA_FNO_FP32 = 1
 
   type, bind(C) :: tara2d_config
@@ -212,12 +213,12 @@ module tara_gb300
       import
       type(c_ptr), value :: h
     end function tara2d_launches_per_step
-    integer(c_int) function tara2d_autotune(h, trial_steps, variants3, ms9) bind(C, name="tara2d_autotune")
+    integer(c_int) function tara2d_autotune(h, trial_steps, variants3, ms24) bind(C, name="tara2d_autotune")
       import
       type(c_ptr), value :: h
       integer(c_int), value :: trial_steps
       integer(c_int), intent(out), optional :: variants3(3)
-      real(c_double), intent(out), optional :: ms9(9)
+      real(c_double), intent(out), optional :: ms24(24)
     end function tara2d_autotune
     integer(c_int) function tara2d_set_variants(h, variants3) bind(C, name="tara2d_set_variants")
       import
@@ -274,6 +275,17 @@ module tara_gb300
       type(c_ptr), value :: e
       integer(c_int), value :: nsteps
     end function tara_ens_step
+    integer(c_int) function tara_ens_set_form(e, form) bind(C, name="tara_ens_set_form")
+      import
+      type(c_ptr), value :: e
+      integer(c_int), value :: form
+    end function tara_ens_set_form
+    integer(c_int) function tara_ens_form(e, form, ms3) bind(C, name="tara_ens_form")
+      import
+      type(c_ptr), value :: e
+      integer(c_int), intent(out), optional :: form
+      real(c_double), intent(out), optional :: ms3(3)
+    end function tara_ens_form
     integer(c_int) function tara_ens_synchronize(e) bind(C, name="tara_ens_synchronize")
       import
       type(c_ptr), value :: e
@@ -304,14 +316,14 @@ module tara_gb300
       import
       type(c_ptr), value :: e
     end function tara_ens_groups
-    integer(c_int) function tara_ens_group_info(e, group, n, runs, variants3, tuned_ms9) &
+    integer(c_int) function tara_ens_group_info(e, group, n, runs, variants3, tuned_ms24) &
         bind(C, name="tara_ens_group_info")
       import
       type(c_ptr), value :: e
       integer(c_int), value :: group
       integer(c_int), intent(out), optional :: n, runs
       integer(c_int), intent(out), optional :: variants3(3)
-      real(c_double), intent(out), optional :: tuned_ms9(9)
+      real(c_double), intent(out), optional :: tuned_ms24(24)
     end function tara_ens_group_info
     integer(c_int) function tara_ens_launches_per_step(e) bind(C, name="tara_ens_launches_per_step")
       import
@@ -486,6 +498,14 @@ module tara_gb300
       type(c_ptr), value :: h
       real(c_double), intent(in) :: real8(*)
     end function tara3d_set_state_real
+    integer(c_int) function tara3d_init_orszag_tang(h, amp, kmax, seed) &
+        bind(C, name="tara3d_init_orszag_tang")
+      import
+      type(c_ptr), value :: h
+      real(c_double), value :: amp
+      integer(c_int), value :: kmax
+      integer(c_int64_t), value :: seed
+    end function tara3d_init_orszag_tang
     integer(c_int) function tara3d_step(h, nsteps) bind(C, name="tara3d_step")
       import
       type(c_ptr), value :: h

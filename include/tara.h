@@ -158,15 +158,23 @@ int tara2d_synchronize(tara2d* h);
 void* tara2d_stream(tara2d* h);
 /* Number of kernel launches a single step issues (for launch accounting). */
 int tara2d_launches_per_step(const tara2d* h);
-/* Tile variants of the three step kernels (column inverse pass, row pass,
- * column forward pass): 0 the default tile, 1 half of it, 2 one column / one
- * row pair per CTA (small grids, whose FP64 work would otherwise sit on a few
- * SMs; in the column passes also 4x the threads per column).  tara2d_autotune
- * times all kernels per variant over trial_steps steps, then each kernel's
- * variants with the other two at that first choice (one step each), keeps the
- * fastest per kernel in that context and restores the state; variants3 and ms9
- * (per-launch ms in context, variant-major) may be NULL. */
-int tara2d_autotune(tara2d* h, int trial_steps, int* variants3, double* ms9);
+/* Configurations of the three step kernels (column inverse pass, row pass,
+ * column forward pass): an index c = tile variant + 4 * radix-8 path.  Tile
+ * variants: 0 the default tile, 1 half of it, 2 one column / one row pair per
+ * CTA (small grids, whose FP64 work would otherwise sit on a few SMs; in the
+ * column passes also 4x the threads per column); the row pass also has 3, one
+ * row pair in three shared-memory slots with half the threads (two CTAs share
+ * an SM).  Radix path: the transforms run radix-4 stages (c < 4) or radix-8
+ * stages first (c >= 4; FP64 and FP32 only) -- the same transform, rounded
+ * differently, so the two paths agree to rounding, not bit for bit; tile
+ * variants on one path agree bit for bit.  tara2d_autotune times all kernels
+ * per candidate (a settling step, then trial_steps timed steps), then each
+ * kernel's candidates with the other two at that first choice (again a
+ * settling step and trial_steps timed), keeps the fastest per kernel in that
+ * context and restores the state; variants3 and ms24 (per-launch ms in
+ * context, candidate-major: 8 candidates x 3 kernels, 0 where a kernel has no
+ * such candidate) may be NULL. */
+int tara2d_autotune(tara2d* h, int trial_steps, int* variants3, double* ms24);
 int tara2d_set_variants(tara2d* h, const int* variants3);
 
 /* Driver diagnostics in the reference's form.  Wavenumbers kx = 2*kpi*i/lx
@@ -209,13 +217,29 @@ typedef struct tara_ens tara_ens;
 int tara_ens_create(int nruns, const tara_ens_run* runs, int precision, int scheme, double nu,
                     double dt, double energy, tara_ens** out);
 int tara_ens_destroy(tara_ens* e);
-/* Runs tara2d_autotune(trial_steps) on each size group (all kernels per variant,
- * then each kernel's variants in the context of the others' choice) and keeps
- * the fastest per kernel and size; the state is saved and restored around it. */
+/* Runs tara2d_autotune(trial_steps) on each size group (all kernels per
+ * candidate, then each kernel's candidates in the context of the others'
+ * choice) and keeps the fastest per kernel and size, then times the graph
+ * against the persistent form (both radix paths) and keeps the fastest form;
+ * the state is saved and restored around it. */
 int tara_ens_autotune(tara_ens* e, int trial_steps);
-/* Advances every run nsteps steps: one CUDA-graph launch per step (the graph,
- * one parallel branch per size, is captured on first use).  Asynchronous. */
+/* Advances every run nsteps steps, asynchronously, in the ensemble's form:
+ * TARA_ENS_GRAPH, one CUDA-graph launch per step (the graph, one parallel
+ * branch per size, is captured on first use); TARA_ENS_PERSISTENT4 / 8, one
+ * cooperative launch for all nsteps steps of every size (grid-wide barriers
+ * between the passes, work items taken from a counter), with the transforms
+ * on the radix-4 or radix-8 path -- FP32 form, RK4 and square grids whose
+ * tiles fit the kernel's 256-thread CTAs (128, 256, 512) only.
+ * tara_ens_autotune times the three and keeps the fastest; tara_ens_set_form
+ * fixes one.  No counterpart in the reference. */
+#define TARA_ENS_GRAPH 0
+#define TARA_ENS_PERSISTENT4 1
+#define TARA_ENS_PERSISTENT8 2
 int tara_ens_step(tara_ens* e, int nsteps);
+int tara_ens_set_form(tara_ens* e, int form);
+/* The current form and the autotuner's milliseconds per step of each form
+ * (graph, persistent radix-4, persistent radix-8; 0 where not timed). */
+int tara_ens_form(tara_ens* e, int* form, double* ms3);
 int tara_ens_synchronize(tara_ens* e);
 /* The stream the graph launches on (cudaStream_t). */
 void* tara_ens_stream(tara_ens* e);
@@ -223,10 +247,11 @@ int tara_ens_get_state(tara_ens* e, int run, double* omegak);
 int tara_ens_set_state(tara_ens* e, int run, const double* omegak);
 int tara_ens_diag(tara_ens* e, int run, double* energy, double* enstrophy);
 int tara_ens_groups(tara_ens* e);
-/* Size group info: n, number of runs, chosen variants of the three kernels, and
- * the autotuner's per-launch milliseconds (variants 0, 1, 2, three kernels each). */
+/* Size group info: n, number of runs, chosen configurations of the three
+ * kernels, and the autotuner's per-launch milliseconds (8 candidates x three
+ * kernels, as tara2d_autotune's ms24). */
 int tara_ens_group_info(tara_ens* e, int group, int* n, int* runs, int* variants3,
-                        double* tuned_ms9);
+                        double* tuned_ms24);
 /* Kernel launches one ensemble step contains (inside its graph). */
 int tara_ens_launches_per_step(tara_ens* e);
 

@@ -26,6 +26,7 @@ TARA_ERR_TIMEOUT = 5
 TARA_ERR_INI = 6
 
 RHS_PLAIN, RHS_SCREEN = 0, 1
+ENS_GRAPH, ENS_PERSISTENT4, ENS_PERSISTENT8 = 0, 1, 2
 SCHEME_AB2, SCHEME_RK4 = 0, 1
 PREC_FP64, PREC_FP32, PREC_DF64 = 0, 1, 2
 
@@ -213,6 +214,8 @@ def _declare(L: ctypes.CDLL) -> None:
                                   ctypes.POINTER(vp)]
     L.tara_ens_destroy.argtypes = [vp]
     L.tara_ens_autotune.argtypes = [vp, c_int]
+    L.tara_ens_set_form.argtypes = [vp, c_int]
+    L.tara_ens_form.argtypes = [vp, ip, dp]
     L.tara_ens_step.argtypes = [vp, c_int]
     L.tara_ens_synchronize.argtypes = [vp]
     L.tara_ens_stream.argtypes = [vp]
@@ -499,9 +502,11 @@ class Solver2D:
     def autotune(self, trial_steps: int = 3) -> dict:
         """Pick the fastest tile variant per step kernel (state restored)."""
         v = (ctypes.c_int * 3)()
-        ms = (ctypes.c_double * 9)()
+        ms = (ctypes.c_double * 24)()
         _check(lib().tara2d_autotune(self._h, int(trial_steps), v, ms))
-        return {"variants": list(v), "ms": [list(ms[3 * i:3 * i + 3]) for i in range(3)]}
+        # per-launch ms in context: rows are the configurations 0-7 (tile variant +
+        # 4 for the radix-8 path), columns the three kernels; 0 = not available
+        return {"variants": list(v), "ms": [list(ms[3 * i:3 * i + 3]) for i in range(8)]}
 
     def set_variants(self, variants) -> None:
         v = (ctypes.c_int * 3)(*[int(x) for x in variants])
@@ -949,6 +954,18 @@ class Ensemble:
     def step(self, n: int = 1):
         _check(lib().tara_ens_step(self._h, int(n)))
 
+    def set_form(self, form: int) -> None:
+        """ENS_GRAPH (one graph launch per step) or ENS_PERSISTENT4 / 8 (one
+        cooperative launch per step() call, radix-4 or radix-8 transforms)."""
+        _check(lib().tara_ens_set_form(self._h, int(form)))
+
+    def form(self) -> dict:
+        f = ctypes.c_int()
+        ms = (ctypes.c_double * 3)()
+        _check(lib().tara_ens_form(self._h, ctypes.byref(f), ms))
+        return {"form": ["graph", "persistent radix-4", "persistent radix-8"][f.value],
+                "ms_per_step": {"graph": ms[0], "persistent radix-4": ms[1], "persistent radix-8": ms[2]}}
+
     def synchronize(self):
         _check(lib().tara_ens_synchronize(self._h))
 
@@ -981,7 +998,7 @@ class Ensemble:
         for g in range(lib().tara_ens_groups(self._h)):
             n, r = ctypes.c_int(), ctypes.c_int()
             v = (ctypes.c_int * 3)()
-            ms = (ctypes.c_double * 9)()
+            ms = (ctypes.c_double * 24)()
             _check(lib().tara_ens_group_info(self._h, g, ctypes.byref(n), ctypes.byref(r), v, ms))
             out.append({"n": n.value, "runs": r.value, "variants": list(v), "tuned_ms": list(ms)})
         return out

@@ -9,6 +9,12 @@
 // the three tile variants of each of the three kernels on the real batch
 // (tara2d_step_timed reports per-kernel CUDA-event times) and keeps the fastest
 // per kernel and size; the state is saved before and restored after the trials.
+//
+// The persistent form (ens_persistent.cu) replaces the graph by one cooperative
+// launch per tara_ens_step call: every size, every RK stage, every step, with a
+// grid-wide barrier between passes.  tara_ens_autotune times the graph and the
+// persistent form on both radix paths and keeps the fastest; tara_ens_set_form
+// fixes a form.
 #include <algorithm>
 #include <cstring>
 #include <map>
@@ -23,7 +29,7 @@ struct tara_ens {
     std::vector<int> runs;  // global run index of each slot
     double2* save_w0 = nullptr;
     double2* save_fold = nullptr;
-    double tuned_ms[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};  // [variant][kernel]
+    double tuned_ms[24] = {};  // [candidate][kernel]
   };
   int nruns = 0;
   std::vector<int> group_of, slot_of;
@@ -34,11 +40,51 @@ struct tara_ens {
   cudaGraphExec_t exec = nullptr;
   cudaGraph_t graph = nullptr;
   int dev = 0;
+  int form = TARA_ENS_GRAPH;           // TARA_ENS_GRAPH / _PERSISTENT4 / _PERSISTENT8
+  double form_ms[3] = {0, 0, 0};       // autotuner: ms per step of each form (0: not timed)
+  void* pdesc = nullptr;               // device descriptors of the groups (persistent form)
+  unsigned long long* pctr = nullptr;  // its work counter
 };
 
 using namespace tara;
 
+namespace tara {
+bool ens_persistent_supports(int n);
+int ens_persistent_launch(tara2d* const* hs, int ngroups, int nsteps, bool radix8, void* desc,
+                          unsigned long long* ctr, cudaStream_t stream);
+size_t ens_desc_bytes(int ngroups);
+}  // namespace tara
+
 namespace {
+
+bool persistent_ok(const tara_ens* e) {
+  for (const auto& g : e->groups)
+    if (!ens_persistent_supports(g.n) || g.h->cfg.precision != TARA_PREC_FP32 ||
+        g.h->cfg.scheme != TARA_SCHEME_RK4)
+      return false;
+  return !e->groups.empty();
+}
+
+// nsteps of the persistent form on e->main, ordered after and before the
+// groups' own streams.
+int persistent_steps(tara_ens* e, int nsteps) {
+  if (!e->pdesc) {
+    TARA_CK(cudaMalloc(&e->pdesc, ens_desc_bytes((int)e->groups.size())));
+    TARA_CK(cudaMalloc((void**)&e->pctr, sizeof(unsigned long long)));
+  }
+  std::vector<tara2d*> hs;
+  for (size_t g = 0; g < e->groups.size(); ++g) {
+    hs.push_back(e->groups[g].h);
+    TARA_CK(cudaEventRecord(e->join[g], e->groups[g].h->stream));
+    TARA_CK(cudaStreamWaitEvent(e->main, e->join[g], 0));
+  }
+  int rc = ens_persistent_launch(hs.data(), (int)hs.size(), nsteps, e->form == TARA_ENS_PERSISTENT8,
+                                 e->pdesc, e->pctr, e->main);
+  if (rc) return rc;
+  TARA_CK(cudaEventRecord(e->fork, e->main));
+  for (auto& g : e->groups) TARA_CK(cudaStreamWaitEvent(g.h->stream, e->fork, 0));
+  return TARA_OK;
+}
 
 int save_or_restore(tara_ens* e, bool save) {
   for (auto& g : e->groups) {
@@ -104,6 +150,8 @@ int tara_ens_destroy(tara_ens* e) {
     cudaFree(g.save_w0);
     cudaFree(g.save_fold);
   }
+  cudaFree(e->pdesc);
+  cudaFree(e->pctr);
   for (cudaEvent_t ev : e->join)
     if (ev) cudaEventDestroy(ev);
   if (e->fork) cudaEventDestroy(e->fork);
@@ -167,20 +215,7 @@ int tara_ens_create(int nruns, const tara_ens_run* runs, int precision, int sche
   return set_ok();
 }
 
-int tara_ens_autotune(tara_ens* e, int trial_steps) {
-  if (!e || trial_steps <= 0) return set_error(TARA_ERR_ARGS, "bad arguments");
-  TARA_CK(cudaSetDevice(e->dev));
-  TARA_CK(cudaStreamSynchronize(e->main));
-  int rc;
-  for (auto& g : e->groups)  // each group saves and restores its own state
-    if ((rc = tara2d_autotune(g.h, trial_steps, nullptr, g.tuned_ms))) return rc;
-  drop_graph(e);  // the graph bakes in the launch shapes
-  return set_ok();
-}
-
-int tara_ens_step(tara_ens* e, int nsteps) {
-  if (!e || nsteps < 0) return set_error(TARA_ERR_ARGS, "bad arguments");
-  TARA_CK(cudaSetDevice(e->dev));
+static int graph_steps(tara_ens* e, int nsteps) {
   int rc;
   if (!e->exec) {
     // one untimed pass sets every kernel's shared-memory attribute outside the
@@ -192,6 +227,75 @@ int tara_ens_step(tara_ens* e, int nsteps) {
     if ((rc = capture(e))) return rc;
   }
   for (int s = 0; s < nsteps; ++s) TARA_CK(cudaGraphLaunch(e->exec, e->main));
+  return TARA_OK;
+}
+
+int tara_ens_step(tara_ens* e, int nsteps) {
+  if (!e || nsteps < 0) return set_error(TARA_ERR_ARGS, "bad arguments");
+  TARA_CK(cudaSetDevice(e->dev));
+  int rc = e->form == TARA_ENS_GRAPH ? graph_steps(e, nsteps) : persistent_steps(e, nsteps);
+  return rc ? rc : set_ok();
+}
+
+int tara_ens_set_form(tara_ens* e, int form) {
+  if (!e || form < TARA_ENS_GRAPH || form > TARA_ENS_PERSISTENT8)
+    return set_error(TARA_ERR_ARGS, "form: TARA_ENS_GRAPH, TARA_ENS_PERSISTENT4 or TARA_ENS_PERSISTENT8");
+  if (form != TARA_ENS_GRAPH && !persistent_ok(e))
+    return set_error(TARA_ERR_ARGS,
+                     "the persistent form needs the FP32 form, RK4 and square grids of 128, 256 or 512");
+  TARA_CK(cudaSetDevice(e->dev));
+  TARA_CK(cudaStreamSynchronize(e->main));
+  e->form = form;
+  return set_ok();
+}
+
+int tara_ens_form(tara_ens* e, int* form, double* ms3) {
+  if (!e) return set_error(TARA_ERR_ARGS, "null handle");
+  if (form) *form = e->form;
+  if (ms3)
+    for (int i = 0; i < 3; ++i) ms3[i] = e->form_ms[i];
+  return set_ok();
+}
+
+int tara_ens_autotune(tara_ens* e, int trial_steps) {
+  if (!e || trial_steps <= 0) return set_error(TARA_ERR_ARGS, "bad arguments");
+  TARA_CK(cudaSetDevice(e->dev));
+  TARA_CK(cudaStreamSynchronize(e->main));
+  int rc;
+  for (auto& g : e->groups)  // each group saves and restores its own state
+    if ((rc = tara2d_autotune(g.h, trial_steps, nullptr, g.tuned_ms))) return rc;
+  drop_graph(e);  // the graph bakes in the launch shapes
+  // Form: the graph (with the tiles just chosen) against the persistent launch
+  // on both radix paths, each after one settling step, timed over trial_steps
+  // steps with CUDA events on the main stream; the state is restored after.
+  for (int f = 0; f < 3; ++f) e->form_ms[f] = 0.0;
+  const int nforms = persistent_ok(e) ? 3 : 1;
+  if ((rc = save_or_restore(e, true))) return rc;
+  cudaEvent_t a = nullptr, b = nullptr;
+  TARA_CK(cudaEventCreate(&a));
+  TARA_CK(cudaEventCreate(&b));
+  const int keep = e->form;
+  for (int f = 0; f < nforms && !rc; ++f) {
+    e->form = f;
+    rc = tara_ens_step(e, 1);
+    if (!rc && cudaEventRecord(a, e->main) != cudaSuccess) rc = set_error(TARA_ERR_CUDA, "event");
+    if (!rc) rc = tara_ens_step(e, trial_steps);
+    if (!rc && (cudaEventRecord(b, e->main) != cudaSuccess || cudaEventSynchronize(b) != cudaSuccess))
+      rc = set_error(TARA_ERR_CUDA, "event");
+    float ms = 0.f;
+    if (!rc && cudaEventElapsedTime(&ms, a, b) != cudaSuccess) rc = set_error(TARA_ERR_CUDA, "event time");
+    if (!rc) e->form_ms[f] = ms / trial_steps;
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  e->form = keep;
+  if (rc) return rc;
+  int best = 0;
+  for (int f = 1; f < nforms; ++f)
+    if (e->form_ms[f] < e->form_ms[best]) best = f;
+  e->form = best;
+  if ((rc = tara_ens_synchronize(e))) return rc;
+  if ((rc = save_or_restore(e, false))) return rc;
   return set_ok();
 }
 
@@ -230,15 +334,15 @@ int tara_ens_diag(tara_ens* e, int run, double* energy, double* enstrophy) {
 }
 
 int tara_ens_group_info(tara_ens* e, int group, int* n, int* runs, int* variants3,
-                        double* tuned_ms9) {
+                        double* tuned_ms24) {
   if (!e || group < 0 || group >= (int)e->groups.size()) return set_error(TARA_ERR_ARGS, "bad group");
   const auto& g = e->groups[group];
   if (n) *n = g.n;
   if (runs) *runs = (int)g.runs.size();
   if (variants3)
     for (int k = 0; k < 3; ++k) variants3[k] = g.h->var[k];
-  if (tuned_ms9)
-    for (int i = 0; i < 9; ++i) tuned_ms9[i] = g.tuned_ms[i];
+  if (tuned_ms24)
+    for (int i = 0; i < 24; ++i) tuned_ms24[i] = g.tuned_ms[i];
   return set_ok();
 }
 

@@ -21,6 +21,7 @@
 // stages.  The first stage has unit twiddles and uses 16 adds.
 #pragma once
 #include <cuda_runtime.h>
+#include <type_traits>
 
 namespace tara {
 
@@ -56,7 +57,38 @@ __host__ __device__ constexpr int fft_group(int n) { return n >= 16 ? n / 16 : 1
 // [(r - 1) Ns + k] for r = 1, 2, 3 and k < Ns, so the lanes of a warp (consecutive
 // k) read consecutive entries.
 __host__ __device__ constexpr int tw_stage_span(int n) { return (1 << (2 * (ilog2c(n) / 2))) - 4; }
-__host__ __device__ constexpr int tw_count(int n) { return n + 2 * tw_stage_span(n); }
+
+// Radix-8 path (the autotuner's alternative to the radix-4 one): radix-8
+// stages first, then zero, one or two radix-4 stages -- 2048 = 8^3 * 4 runs
+// four passes through shared memory instead of six.  The first stage has unit
+// twiddles; a twiddled radix-8 stage at sub-transform length Ns owns 4 Ns
+// entries, W^m, W^2m, W^4m and W^(m + n/8) (= W8 W^m) for m = k n/(8 Ns), each
+// run consecutive in k; a twiddled radix-4 stage owns 3 Ns, as above.  The
+// forward stage tables follow the radix-4 path's two copies, then the
+// inverse copy (conjugated).
+__host__ __device__ constexpr int r8_stages8(int n) {
+  return (ilog2c(n) % 3 == 1 && ilog2c(n) >= 4) ? ilog2c(n) / 3 - 1 : ilog2c(n) / 3;
+}
+__host__ __device__ constexpr int r8_stages4(int n) {
+  return ilog2c(n) % 3 == 1 ? 2 : ilog2c(n) % 3 == 2 ? 1 : 0;
+}
+// radix and sub-transform length of stage i of the radix-8 path
+__host__ __device__ constexpr int r8_radix(int n, int i) { return i < r8_stages8(n) ? 8 : 4; }
+__host__ __device__ constexpr int r8_ns(int n, int i) {
+  return i <= r8_stages8(n) ? (1 << (3 * i)) : (1 << (3 * r8_stages8(n))) << (2 * (i - r8_stages8(n)));
+}
+__host__ __device__ constexpr int r8_stage_size(int n, int i) {
+  return i == 0 ? 0 : (r8_radix(n, i) == 8 ? 4 : 3) * r8_ns(n, i);
+}
+__host__ __device__ constexpr int r8_stage_off(int n, int i) {
+  return i <= 1 ? 0 : r8_stage_off(n, i - 1) + r8_stage_size(n, i - 1);
+}
+__host__ __device__ constexpr int r8_span(int n) {
+  return r8_stage_off(n, r8_stages8(n) + r8_stages4(n) - 1) +
+         r8_stage_size(n, r8_stages8(n) + r8_stages4(n) - 1);
+}
+__host__ __device__ constexpr int tw_r8_base(int n) { return n + 2 * tw_stage_span(n); }
+__host__ __device__ constexpr int tw_count(int n) { return tw_r8_base(n) + 2 * r8_span(n); }
 
 // Untwiddled radix-4 DFT (first stage).  Forward: y1 = a1 - i a3, y3 = a1 + i a3.
 template <bool INV, typename C>
@@ -275,6 +307,194 @@ __device__ __forceinline__ void fft_slot(typename cplx_of<T>::type* buf, int lan
     }
     __syncthreads();
   }
+}
+
+// ---------------------------------------------------------------------------
+// Radix-8 (FP64 and FP32 only)
+// ---------------------------------------------------------------------------
+// a' = a + t b, b' = a - t b in the two-sided FMA form (6 FMA-pipe instructions).
+template <typename C>
+__device__ __forceinline__ void pair_t(C& a, C& b, const C t) {
+  typedef decltype(a.x) T;
+  const T xr = fma(b.x, t.x, fma(-b.y, t.y, a.x));
+  const T xi = fma(b.x, t.y, fma(b.y, t.x, a.y));
+  b.x = fma(T(2), a.x, -xr);
+  b.y = fma(T(2), a.y, -xi);
+  a.x = xr;
+  a.y = xi;
+}
+
+// t times W4 (W4 = -i forward, +i inverse): a swap and a sign, no arithmetic.
+template <bool INV, typename C>
+__device__ __forceinline__ C mul_w4(const C t) {
+  C r;
+  if (!INV) {
+    r.x = t.y;
+    r.y = -t.x;
+  } else {
+    r.x = -t.y;
+    r.y = t.x;
+  }
+  return r;
+}
+
+// a +- b, a +- W4 b (untwiddled pairs: 4 adds)
+template <typename C>
+__device__ __forceinline__ void pair_1(C& a, C& b) {
+  const C s = mkc<decltype(a.x)>(a.x + b.x, a.y + b.y);
+  b = mkc<decltype(a.x)>(a.x - b.x, a.y - b.y);
+  a = s;
+}
+template <bool INV, typename C>
+__device__ __forceinline__ void pair_w4(C& a, C& b) {
+  const C q = mul_w4<INV>(b);
+  const C s = mkc<decltype(a.x)>(a.x + q.x, a.y + q.y);
+  b = mkc<decltype(a.x)>(a.x - q.x, a.y - q.y);
+  a = s;
+}
+// a +- W8^e b for e = 1 or 3 (W8 = (1 -+ i)/sqrt(2)): two adds form the rotated
+// pair up to the factor 1/sqrt(2), which four FMAs then apply (6 instructions).
+template <bool INV, int E, typename C>
+__device__ __forceinline__ void pair_w8(C& a, C& b) {
+  typedef decltype(a.x) T;
+  const T c = T(0.70710678118654752440);
+  T p, q;  // W8^E b = c (p, q)
+  if (!INV) {
+    if (E == 1) { p = b.x + b.y; q = b.y - b.x; }    // (1 - i)(x + iy)
+    else        { p = b.y - b.x; q = -(b.x + b.y); }  // (-1 - i)(x + iy)
+  } else {
+    if (E == 1) { p = b.x - b.y; q = b.x + b.y; }    // (1 + i)(x + iy)
+    else        { p = -(b.x + b.y); q = b.x - b.y; }  // (-1 + i)(x + iy)
+  }
+  const C s = mkc<T>(fma(c, p, a.x), fma(c, q, a.y));
+  b = mkc<T>(fma(-c, p, a.x), fma(-c, q, a.y));
+  a = s;
+}
+
+// Untwiddled 8-point DFT (52 FP64-pipe instructions).  In: v[r] = x[r];
+// out: v[] holds X in the order 0, 4, 2, 6, 1, 5, 3, 7.
+template <bool INV, typename C>
+__device__ __forceinline__ void dft8(C* v) {
+  pair_1(v[0], v[4]); pair_1(v[1], v[5]); pair_1(v[2], v[6]); pair_1(v[3], v[7]);
+  pair_1(v[0], v[2]); pair_1(v[1], v[3]);
+  pair_w4<INV>(v[4], v[6]); pair_w4<INV>(v[5], v[7]);
+  pair_1(v[0], v[1]);
+  pair_w4<INV>(v[2], v[3]);
+  pair_w8<INV, 1>(v[4], v[5]);
+  pair_w8<INV, 3>(v[6], v[7]);
+}
+
+// Twiddled 8-point DFT of x[r] W^(r m): X_q = sum_r x_r W^(rm) W8^(rq), with the
+// twiddles folded into the three pair levels (w = W^m, w2 = W^2m, w4 = W^4m,
+// w8 = W8 W^m; 12 pairs, 72 FP64-pipe instructions).  Output order as dft8.
+template <bool INV, typename C>
+__device__ __forceinline__ void dft8_tw(C* v, const C w, const C w2, const C w4, const C w8) {
+  pair_t(v[0], v[4], w4); pair_t(v[1], v[5], w4); pair_t(v[2], v[6], w4); pair_t(v[3], v[7], w4);
+  pair_t(v[0], v[2], w2); pair_t(v[1], v[3], w2);
+  const C w2q = mul_w4<INV>(w2);
+  pair_t(v[4], v[6], w2q); pair_t(v[5], v[7], w2q);
+  pair_t(v[0], v[1], w);
+  pair_t(v[2], v[3], mul_w4<INV>(w));
+  pair_t(v[4], v[5], w8);
+  pair_t(v[6], v[7], mul_w4<INV>(w8));
+}
+
+// In-place length-N transform along the radix-8 path (same contract and result
+// layout as fft_slot).  G threads share it; in radix-8 stages lanes beyond the
+// N/8 butterflies idle.
+template <typename T, int N, bool INV, int G = fft_group(N)>
+__device__ __forceinline__ void fft_slot_r8(typename cplx_of<T>::type* buf, int lane, bool active,
+                                            const typename cplx_of<T>::type* __restrict__ tw) {
+  typedef typename cplx_of<T>::type C;
+  constexpr int S8 = r8_stages8(N), S4 = r8_stages4(N);
+  constexpr int B8 = N / 8, Q = N / 4;
+  constexpr int BPT8 = (B8 + G - 1) / G, BPT4 = (Q + G - 1) / G;
+  static_assert((1 << ilog2c(N)) == N && N >= 16, "power-of-two length >= 16");
+  const C* tb = tw + tw_r8_base(N) + (INV ? r8_span(N) : 0);
+  constexpr int OUTQ[8] = {0, 4, 2, 6, 1, 5, 3, 7};  // v[i] holds X_OUTQ[i]
+#pragma unroll
+  for (int s = 0; s < S8; ++s) {
+    const int Ns = 1 << (3 * s);
+    C v[BPT8][8];
+    if (active) {
+#pragma unroll
+      for (int b = 0; b < BPT8; ++b) {
+        const int j = lane + b * G;
+        if (j < B8) {
+#pragma unroll
+          for (int r = 0; r < 8; ++r) v[b][r] = buf[j + r * B8];
+        }
+      }
+    }
+    __syncthreads();
+    if (active) {
+#pragma unroll
+      for (int b = 0; b < BPT8; ++b) {
+        const int j = lane + b * G;
+        if (j < B8) {
+          const int k = j & (Ns - 1);
+          if (s == 0) {
+            dft8<INV>(v[b]);
+          } else {
+            const C* ts = tb + r8_stage_off(N, s);
+            dft8_tw<INV>(v[b], load_tw_raw(ts, k), load_tw_raw(ts, Ns + k), load_tw_raw(ts, 2 * Ns + k),
+                         load_tw_raw(ts, 3 * Ns + k));
+          }
+          const int base = ((j - k) << 3) + k;
+#pragma unroll
+          for (int i = 0; i < 8; ++i) buf[base + OUTQ[i] * Ns] = v[b][i];
+        }
+      }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int s = 0; s < S4; ++s) {
+    const int Ns = (1 << (3 * S8)) << (2 * s);
+    C v[BPT4][4];
+    if (active) {
+#pragma unroll
+      for (int b = 0; b < BPT4; ++b) {
+        const int j = lane + b * G;
+        if (j < Q) {
+#pragma unroll
+          for (int r = 0; r < 4; ++r) v[b][r] = buf[j + r * Q];
+        }
+      }
+    }
+    __syncthreads();
+    if (active) {
+#pragma unroll
+      for (int b = 0; b < BPT4; ++b) {
+        const int j = lane + b * G;
+        if (j < Q) {
+          const int k = j & (Ns - 1);
+          if (S8 == 0 && s == 0) {
+            dft4<INV>(v[b][0], v[b][1], v[b][2], v[b][3]);
+          } else {
+            const C* ts = tb + r8_stage_off(N, S8 + s);
+            dft4_tw<INV>(v[b][0], v[b][1], v[b][2], v[b][3], load_tw_raw(ts, k), load_tw_raw(ts, Ns + k),
+                         load_tw_raw(ts, 2 * Ns + k));
+          }
+          const int base = ((j - k) << 2) + k;
+#pragma unroll
+          for (int r = 0; r < 4; ++r) buf[base + r * Ns] = v[b][r];
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// The transform of a step kernel along the path R (4 or 8; the double-float
+// form has only the radix-4 path).
+template <typename T, int N, bool INV, int G, int R>
+__device__ __forceinline__ void fft_path(typename cplx_of<T>::type* buf, int lane, bool active,
+                                         const typename cplx_of<T>::type* __restrict__ tw) {
+  if constexpr (R == 8 && !std::is_same<T, df64>::value)
+    fft_slot_r8<T, N, INV, G>(buf, lane, active, tw);
+  else
+    fft_slot<T, N, INV, G>(buf, lane, active, tw);
 }
 
 }  // namespace tara

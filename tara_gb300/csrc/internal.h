@@ -28,9 +28,10 @@ inline bool is_pow2_in_range(int n) { return n >= 16 && n <= kMaxN && (n & (n - 
 inline int round_up(int v, int m) { return (v + m - 1) / m * m; }
 
 // Tile variants per step kernel (column inverse pass, row pass, column forward
-// pass) and the most any kernel has.
+// pass).  A kernel's configuration index is its tile variant in bits 0-1 and
+// the radix-8 path in bit 2, so the autotuner weighs kCandidates indices.
 constexpr int kVariants[3] = {3, 4, 3};
-constexpr int kMaxVariants = 4;
+constexpr int kCandidates = 8;
 
 // Philox4x32-10 on the host (Salmon et al., SC'11): ten rounds with the
 // published multipliers and Weyl key increments, for the seeded phases of the

@@ -124,14 +124,21 @@ template <typename T, int N, int V = 0> struct ColCfg {
   static constexpr int SMEM_C = TCC * S * (int)sizeof(C);
 };
 
+// Row pass tiles.  Variants 0-2 hold RP row pairs in four slots each (the two
+// inverse transforms of both rows run together).  Variant 3 holds one row pair
+// in three slots with half the threads: the two inverse transforms of row a,
+// then of row b, each leaving its products in the third slot, then the forward
+// transform of that slot.  Its 96 KB of shared memory (FP64, N = 2048) and
+// 256 threads let two CTAs share an SM, so one CTA's loads, stores and stage
+// barriers overlap the other's butterflies.  Same arithmetic, same results.
 template <typename T, int N, int V = 0> struct RowCfg {
   typedef typename cplx_of<T>::type C;
   static constexpr int G = fft_group(N);
   static constexpr int RP0 = pick_rp(N, (int)sizeof(C));
-  static constexpr int RP = V == 2 ? 1 : (V == 1 && RP0 > 1) ? RP0 / 2 : RP0;
-  static constexpr int THREADS = 4 * RP * G;
+  static constexpr int RP = V >= 2 ? 1 : (V == 1 && RP0 > 1) ? RP0 / 2 : RP0;
+  static constexpr int THREADS = V == 3 ? 2 * G : 4 * RP * G;
   static constexpr int SL = N;  // smem stride between row slots
-  static constexpr int SMEM = RP * 4 * SL * (int)sizeof(C);
+  static constexpr int SMEM = (V == 3 ? 3 : RP * 4) * SL * (int)sizeof(C);
 };
 
 // ---------------------------------------------------------------------------
@@ -145,24 +152,24 @@ template <typename T, int N, int V = 0> struct RowCfg {
 // (measured 255 -> 240 us at 2048^2); the FP64 form gains nothing from it.  The
 // FP32 form keeps two 512-thread CTAs per SM (64 registers; at 80 registers one
 // CTA per SM took 113 instead of 95 us at 2048^2).
-template <typename T, int N, int V>
-__global__ void __launch_bounds__(ColCfg<T, N, V>::THREADS_A,
-                                  (is_df64<T>() && ColCfg<T, N, V>::THREADS_A == 256)       ? 3
-                                  : (sizeof(T) == 4 && ColCfg<T, N, V>::THREADS_A == 512) ? 2
-                                                                                          : 1)
-    k_col_inverse(const double2* __restrict__ win, typename cplx_of<T>::type* __restrict__ u,
-                  Grid2D g, RhsParams p, const typename cplx_of<T>::type* __restrict__ tw) {
+// The CTA body (block coordinates given explicitly, so that the ensemble's
+// persistent kernel can run it for any run and tile): tile bx, field pair
+// `pair`, run `run`.
+template <typename T, int N, int V, int R>
+__device__ __forceinline__ void col_inverse_cta(int bx, int pair, int run, const double2* __restrict__ win,
+                                                typename cplx_of<T>::type* __restrict__ u, const Grid2D& g,
+                                                const RhsParams& p,
+                                                const typename cplx_of<T>::type* __restrict__ tw) {
   typedef typename cplx_of<T>::type C;
   typedef ColCfg<T, N, V> CF;
   constexpr int TC = CF::TCA, S = CF::S, G = CF::G;
   extern __shared__ __align__(16) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);  // [2][TC][S]
-  const int x0 = blockIdx.x * TC;
-  const int pair = blockIdx.y;
+  const int x0 = bx * TC;
   const int tid = threadIdx.x;
   const size_t fsz = (size_t)g.ny * g.pitch;
-  win += blockIdx.z * fsz;
-  u += blockIdx.z * 4 * fsz;
+  win += run * fsz;
+  u += run * 4 * fsz;
   const int slot = tid / G, lane = tid % G;
   TARA_ELEM_LOOP(e, N * TC, CF::THREADS_A) {
     const int y = e / TC, c = e % TC, x = x0 + c;
@@ -232,7 +239,7 @@ __global__ void __launch_bounds__(ColCfg<T, N, V>::THREADS_A,
     sm[(TC + c) * S + y] = fb;
   }
   __syncthreads();
-  fft_slot<T, N, true, G>(sm + slot * S, lane, true, tw);
+  fft_path<T, N, true, G, R>(sm + slot * S, lane, true, tw);
   TARA_ELEM_LOOP(e, N * TC, CF::THREADS_A) {
     const int y = e / TC, c = e % TC, x = x0 + c;
     if (x < g.nh) {
@@ -243,6 +250,16 @@ __global__ void __launch_bounds__(ColCfg<T, N, V>::THREADS_A,
   }
 }
 
+template <typename T, int N, int V, int R = 4>
+__global__ void __launch_bounds__(ColCfg<T, N, V>::THREADS_A,
+                                  (is_df64<T>() && ColCfg<T, N, V>::THREADS_A == 256)       ? 3
+                                  : (sizeof(T) == 4 && ColCfg<T, N, V>::THREADS_A == 512) ? 2
+                                                                                          : 1)
+    k_col_inverse(const double2* __restrict__ win, typename cplx_of<T>::type* __restrict__ u,
+                  Grid2D g, RhsParams p, const typename cplx_of<T>::type* __restrict__ tw) {
+  col_inverse_cta<T, N, V, R>(blockIdx.x, blockIdx.y, blockIdx.z, win, u, g, p, tw);
+}
+
 // ---------------------------------------------------------------------------
 // Pass B
 // ---------------------------------------------------------------------------
@@ -251,66 +268,119 @@ __global__ void __launch_bounds__(ColCfg<T, N, V>::THREADS_A,
 // Z[k] = A[k] + i B[k] (k <= N/2), Z[N-k] = conj(A[k]) + i conj(B[k]), with the
 // imaginary parts of the k = 0 and k = N/2 bins dropped first.
 // blockIdx.y = run of a batch.
-template <typename T, int N, int V>
-__global__ void __launch_bounds__(RowCfg<T, N, V>::THREADS, (sizeof(T) == 4 && RowCfg<T, N, V>::THREADS >= 512) ? 2 : 1)
-    k_row_nl(const typename cplx_of<T>::type* __restrict__ u,
-             typename cplx_of<T>::type* __restrict__ nl, Grid2D g,
-             const typename cplx_of<T>::type* __restrict__ tw) {
+// Hermitian extension of the half rows A, B (two spectra of one ky row) into
+// slot entry k of Z = A + i B (see above).
+template <typename T, int N, typename C>
+__device__ __forceinline__ C row_pair_entry(const C* __restrict__ fa, const C* __restrict__ fb, int k) {
+  constexpr int H = N / 2;
+  const int kk = k <= H ? k : N - k;
+  C A = fa[kk], B = fb[kk];
+  if (kk == 0 || kk == H) {
+    A.y = T(0);
+    B.y = T(0);
+  }
+  return (k <= H) ? mkc<T>(A.x - B.y, A.y + B.x) : mkc<T>(A.x + B.y, -A.y + B.x);
+}
+
+// The CTA body: row-pair tile bx of run `run`.
+template <typename T, int N, int V, int R>
+__device__ __forceinline__ void row_nl_cta(int bx, int run, const typename cplx_of<T>::type* __restrict__ u,
+                                           typename cplx_of<T>::type* __restrict__ nl, const Grid2D& g,
+                                           const typename cplx_of<T>::type* __restrict__ tw) {
   typedef typename cplx_of<T>::type C;
   typedef RowCfg<T, N, V> RC;
   constexpr int G = RC::G, H = N / 2, RP = RC::RP, SL = RC::SL;
   extern __shared__ __align__(16) unsigned char smraw[];
-  C* sm = reinterpret_cast<C*>(smraw);  // [RP][4][N]
+  C* sm = reinterpret_cast<C*>(smraw);  // [RP][4][N], or [3][N] in variant 3
   const int tid = threadIdx.x;
   const int slot = tid / G, lane = tid % G;
-  const int y_base = blockIdx.x * (2 * RP);
+  const int y_base = bx * (2 * RP);
   const size_t fsz = (size_t)g.ny * g.pitch;
-  u += blockIdx.y * 4 * fsz;
-  nl += blockIdx.y * fsz;
-  TARA_ELEM_LOOP(e, RP * 4 * N, RC::THREADS) {
-    const int k = e % N, sl = e / N;
-    const int pp = sl >> 2, s = sl & 3;
-    const int y = y_base + 2 * pp + (s >> 1);
-    C z = mkc<T>(T(0), T(0));
-    if (y < g.ny) {
-      const C* fa = u + (size_t)(2 * (s & 1)) * fsz + (size_t)y * g.pitch;
-      const C* fb = fa + fsz;
-      const int kk = k <= H ? k : N - k;
-      C A = fa[kk], B = fb[kk];
-      if (kk == 0 || kk == H) {
-        A.y = T(0);
-        B.y = T(0);
+  u += run * 4 * fsz;
+  nl += run * fsz;
+  if constexpr (V == 3) {
+    C* pk = sm + 2 * SL;  // products of rows a (real part) and b (imaginary part)
+#pragma unroll 1
+    for (int r = 0; r < 2; ++r) {
+      const int y = y_base + r;
+      TARA_ELEM_LOOP(e, 2 * N, RC::THREADS) {
+        const int k = e % N, s = e / N;  // s = 0: u_x + i u_y, 1: w_x + i w_y
+        C z = mkc<T>(T(0), T(0));
+        if (y < g.ny) {
+          const C* fa = u + (size_t)(2 * s) * fsz + (size_t)y * g.pitch;
+          z = row_pair_entry<T, N>(fa, fa + fsz, k);
+        }
+        sm[s * SL + k] = z;
       }
-      z = (k <= H) ? mkc<T>(A.x - B.y, A.y + B.x) : mkc<T>(A.x + B.y, -A.y + B.x);
+      __syncthreads();
+      fft_path<T, N, true, G, R>(sm + slot * SL, lane, true, tw);
+      TARA_ELEM_LOOP(e, N, RC::THREADS) {
+        const C c1 = sm[e], c2 = sm[SL + e];
+        const T v = fma(c1.x, c2.x, c1.y * c2.y);
+        if (r == 0)
+          pk[e].x = v;
+        else
+          pk[e].y = v;
+      }
+      __syncthreads();
     }
-    sm[sl * SL + k] = z;
-  }
-  __syncthreads();
-  fft_slot<T, N, true>(sm + slot * SL, lane, true, tw);
-  // products u_x w_x + u_y w_y for rows a and b, packed as a + i b
-  TARA_ELEM_LOOP(e, RP * N, RC::THREADS) {
-    const int x = e % N, pp = e / N;
-    C* b = sm + (size_t)pp * 4 * SL;
-    const C c1a = b[x], c2a = b[SL + x], c1b = b[2 * SL + x], c2b = b[3 * SL + x];
-    const T na = fma(c1a.x, c2a.x, c1a.y * c2a.y);
-    const T nb = fma(c1b.x, c2b.x, c1b.y * c2b.y);
-    b[x] = mkc<T>(na, nb);
-  }
-  __syncthreads();
-  // forward transform of each pair's packed products (its first slot), shared
-  // by all 4 G threads of the pair so that no thread idles through it
-  fft_slot<T, N, false, 4 * G>(sm + (tid / (4 * G)) * 4 * SL, tid % (4 * G), true, tw);
-  // split: 2 X_a[k] = Z[k] + conj Z[N-k], 2 X_b[k] = -i (Z[k] - conj Z[N-k])
-  TARA_ELEM_LOOP(e, RP * (H + 1), RC::THREADS) {
-    const int k = e % (H + 1), pp = e / (H + 1);
-    const int ya = y_base + 2 * pp;
-    if (ya < g.ny) {
-      const C* b = sm + (size_t)pp * 4 * SL;
-      const C z = b[k], m = b[(N - k) & (N - 1)];
-      nl[(size_t)ya * g.pitch + k] = mkc<T>(z.x + m.x, z.y - m.y);
-      nl[(size_t)(ya + 1) * g.pitch + k] = mkc<T>(z.y + m.y, -(z.x - m.x));
+    fft_path<T, N, false, 2 * G, R>(pk, tid, true, tw);
+    TARA_ELEM_LOOP(e, H + 1, RC::THREADS) {
+      const int k = e;
+      if (y_base < g.ny) {
+        const C z = pk[k], m = pk[(N - k) & (N - 1)];
+        nl[(size_t)y_base * g.pitch + k] = mkc<T>(z.x + m.x, z.y - m.y);
+        nl[(size_t)(y_base + 1) * g.pitch + k] = mkc<T>(z.y + m.y, -(z.x - m.x));
+      }
+    }
+  } else {
+    TARA_ELEM_LOOP(e, RP * 4 * N, RC::THREADS) {
+      const int k = e % N, sl = e / N;
+      const int pp = sl >> 2, s = sl & 3;
+      const int y = y_base + 2 * pp + (s >> 1);
+      C z = mkc<T>(T(0), T(0));
+      if (y < g.ny) {
+        const C* fa = u + (size_t)(2 * (s & 1)) * fsz + (size_t)y * g.pitch;
+        z = row_pair_entry<T, N>(fa, fa + fsz, k);
+      }
+      sm[sl * SL + k] = z;
+    }
+    __syncthreads();
+    fft_path<T, N, true, G, R>(sm + slot * SL, lane, true, tw);
+    // products u_x w_x + u_y w_y for rows a and b, packed as a + i b
+    TARA_ELEM_LOOP(e, RP * N, RC::THREADS) {
+      const int x = e % N, pp = e / N;
+      C* b = sm + (size_t)pp * 4 * SL;
+      const C c1a = b[x], c2a = b[SL + x], c1b = b[2 * SL + x], c2b = b[3 * SL + x];
+      const T na = fma(c1a.x, c2a.x, c1a.y * c2a.y);
+      const T nb = fma(c1b.x, c2b.x, c1b.y * c2b.y);
+      b[x] = mkc<T>(na, nb);
+    }
+    __syncthreads();
+    // forward transform of each pair's packed products (its first slot), shared
+    // by all 4 G threads of the pair so that no thread idles through it
+    fft_path<T, N, false, 4 * G, R>(sm + (tid / (4 * G)) * 4 * SL, tid % (4 * G), true, tw);
+    // split: 2 X_a[k] = Z[k] + conj Z[N-k], 2 X_b[k] = -i (Z[k] - conj Z[N-k])
+    TARA_ELEM_LOOP(e, RP * (H + 1), RC::THREADS) {
+      const int k = e % (H + 1), pp = e / (H + 1);
+      const int ya = y_base + 2 * pp;
+      if (ya < g.ny) {
+        const C* b = sm + (size_t)pp * 4 * SL;
+        const C z = b[k], m = b[(N - k) & (N - 1)];
+        nl[(size_t)ya * g.pitch + k] = mkc<T>(z.x + m.x, z.y - m.y);
+        nl[(size_t)(ya + 1) * g.pitch + k] = mkc<T>(z.y + m.y, -(z.x - m.x));
+      }
     }
   }
+}
+
+template <typename T, int N, int V, int R = 4>
+__global__ void __launch_bounds__(RowCfg<T, N, V>::THREADS,
+                                  (V == 3 || (sizeof(T) == 4 && RowCfg<T, N, V>::THREADS >= 512)) ? 2 : 1)
+    k_row_nl(const typename cplx_of<T>::type* __restrict__ u,
+             typename cplx_of<T>::type* __restrict__ nl, Grid2D g,
+             const typename cplx_of<T>::type* __restrict__ tw) {
+  row_nl_cta<T, N, V, R>(blockIdx.x, blockIdx.y, u, nl, g, tw);
 }
 
 // ---------------------------------------------------------------------------
@@ -330,20 +400,19 @@ struct StepBufs {
 // blockIdx.y = run of a batch.  The double-float form's 512-thread variant asks
 // for two CTAs per SM (64 registers, 90 bytes of spill): its warps wait on the
 // state loads, and a second CTA hides them (115 -> 103 us at 2048^2).
-template <typename T, int N, int V>
-__global__ void __launch_bounds__(ColCfg<T, N, V>::THREADS_C,
-                                  (is_df64<T>() && ColCfg<T, N, V>::THREADS_C == 512) ? 2 : 1)
-    k_col_forward(const typename cplx_of<T>::type* __restrict__ nl, StepBufs sb, Grid2D g,
-                  RhsParams p, int mode, const typename cplx_of<T>::type* __restrict__ tw) {
+template <typename T, int N, int V, int R>
+__device__ __forceinline__ void col_forward_cta(int bx, int run, const typename cplx_of<T>::type* __restrict__ nl,
+                                                StepBufs sb, const Grid2D& g, const RhsParams& p, int mode,
+                                                const typename cplx_of<T>::type* __restrict__ tw) {
   typedef typename cplx_of<T>::type C;
   typedef ColCfg<T, N, V> CF;
   constexpr int TC = CF::TCC, S = CF::S, G = CF::G;
   extern __shared__ __align__(16) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);  // [TC][S]
-  const int x0 = blockIdx.x * TC;
+  const int x0 = bx * TC;
   const int tid = threadIdx.x;
   {
-    const size_t off = blockIdx.y * (size_t)g.ny * g.pitch;
+    const size_t off = run * (size_t)g.ny * g.pitch;
     nl += off;
     sb.win += off;
     if (sb.w0) sb.w0 += off;
@@ -363,7 +432,7 @@ __global__ void __launch_bounds__(ColCfg<T, N, V>::THREADS_C,
       sm[c * S + y] = (x < g.nh) ? nl[(size_t)y * g.pitch + x] : mkc<T>(T(0), T(0));
     }
     __syncthreads();
-    fft_slot<T, N, false, G>(sm + (tid / G) * S, tid % G, true, tw);
+    fft_path<T, N, false, G, R>(sm + (tid / G) * S, tid % G, true, tw);
   }
   // Pass 1: the right-hand side of every element of this thread (reads only,
   // so the unrolled loop issues all its loads together).
@@ -538,6 +607,14 @@ __global__ void __launch_bounds__(ColCfg<T, N, V>::THREADS_C,
     }
   }
   if (bad) atomicOr(sb.flag, 1u);
+}
+
+template <typename T, int N, int V, int R = 4>
+__global__ void __launch_bounds__(ColCfg<T, N, V>::THREADS_C,
+                                  (is_df64<T>() && ColCfg<T, N, V>::THREADS_C == 512) ? 2 : 1)
+    k_col_forward(const typename cplx_of<T>::type* __restrict__ nl, StepBufs sb, Grid2D g,
+                  RhsParams p, int mode, const typename cplx_of<T>::type* __restrict__ tw) {
+  col_forward_cta<T, N, V, R>(blockIdx.x, blockIdx.y, nl, sb, g, p, mode, tw);
 }
 
 // ---------------------------------------------------------------------------

@@ -26,41 +26,41 @@ static cudaError_t allow_smem(K kernel, int bytes) {
     default: return set_error(TARA_ERR_ARGS, "grid size must be a power of two in [16, 2048]"); \
   }
 
-template <typename T, int N, int V>
+template <typename T, int N, int V, int R>
 static int launch_col_inverse(int nh, const double2* win, void* u, const Grid2D& g,
                               const RhsParams& p, const void* tw, cudaStream_t s, int nb) {
   typedef typename cplx_of<T>::type C;
   typedef ColCfg<T, N, V> CF;
-  static cudaError_t attr = allow_smem(k_col_inverse<T, N, V>, CF::SMEM_A);
+  static cudaError_t attr = allow_smem(k_col_inverse<T, N, V, R>, CF::SMEM_A);
   TARA_CK(attr);
   const dim3 blocks((nh + CF::TCA - 1) / CF::TCA, 2, nb);
-  k_col_inverse<T, N, V><<<blocks, CF::THREADS_A, CF::SMEM_A, s>>>(win, (C*)u, g, p, (const C*)tw);
+  k_col_inverse<T, N, V, R><<<blocks, CF::THREADS_A, CF::SMEM_A, s>>>(win, (C*)u, g, p, (const C*)tw);
   TARA_CK(cudaGetLastError());
   return TARA_OK;
 }
 
-template <typename T, int N, int V>
+template <typename T, int N, int V, int R>
 static int launch_row_nl(int ny, const void* u, void* nl, const Grid2D& g, const void* tw,
                          cudaStream_t s, int nb) {
   typedef typename cplx_of<T>::type C;
   typedef RowCfg<T, N, V> RC;
-  static cudaError_t attr = allow_smem(k_row_nl<T, N, V>, RC::SMEM);
+  static cudaError_t attr = allow_smem(k_row_nl<T, N, V, R>, RC::SMEM);
   TARA_CK(attr);
   const dim3 blocks((ny + 2 * RC::RP - 1) / (2 * RC::RP), nb);
-  k_row_nl<T, N, V><<<blocks, RC::THREADS, RC::SMEM, s>>>((const C*)u, (C*)nl, g, (const C*)tw);
+  k_row_nl<T, N, V, R><<<blocks, RC::THREADS, RC::SMEM, s>>>((const C*)u, (C*)nl, g, (const C*)tw);
   TARA_CK(cudaGetLastError());
   return TARA_OK;
 }
 
-template <typename T, int N, int V>
+template <typename T, int N, int V, int R>
 static int launch_col_forward(int nh, const void* nl, const StepBufs& sb, const Grid2D& g,
                               const RhsParams& p, int mode, const void* tw, cudaStream_t s, int nb) {
   typedef typename cplx_of<T>::type C;
   typedef ColCfg<T, N, V> CF;
-  static cudaError_t attr = allow_smem(k_col_forward<T, N, V>, CF::SMEM_C);
+  static cudaError_t attr = allow_smem(k_col_forward<T, N, V, R>, CF::SMEM_C);
   TARA_CK(attr);
   const dim3 blocks((nh + CF::TCC - 1) / CF::TCC, nb);
-  k_col_forward<T, N, V><<<blocks, CF::THREADS_C, CF::SMEM_C, s>>>((const C*)nl, sb, g, p, mode,
+  k_col_forward<T, N, V, R><<<blocks, CF::THREADS_C, CF::SMEM_C, s>>>((const C*)nl, sb, g, p, mode,
                                                                     (const C*)tw);
   TARA_CK(cudaGetLastError());
   return TARA_OK;
@@ -124,45 +124,86 @@ static bool small_row(int ny, int nf) {
   return nf * ((ny + 2 * RowXCfg<T, N, 0>::NP - 1) / (2 * RowXCfg<T, N, 0>::NP)) < kFewCtas;
 }
 
+// The step kernels along radix path R, tile variant v (0-2; 3 for the row pass).
+template <typename T, int R>
+int step_col_inverse(int ny, int nh, const double2* win, void* u, const Grid2D& g, const RhsParams& p,
+                     const void* twy, cudaStream_t s, int nb, int v) {
+  if (v == 2) {
+    TARA_SWITCH_N(ny, return (launch_col_inverse<T, N, 2, R>(nh, win, u, g, p, twy, s, nb)));
+  } else if (v == 1) {
+    TARA_SWITCH_N(ny, return (launch_col_inverse<T, N, 1, R>(nh, win, u, g, p, twy, s, nb)));
+  } else {
+    TARA_SWITCH_N(ny, return (launch_col_inverse<T, N, 0, R>(nh, win, u, g, p, twy, s, nb)));
+  }
+  return TARA_OK;
+}
+
+template <typename T, int R>
+int step_row_nl(int nx, int ny, const void* u, void* nl, const Grid2D& g, const void* twx, cudaStream_t s,
+                int nb, int v) {
+  if (v == 3) {
+    TARA_SWITCH_N(nx, return (launch_row_nl<T, N, 3, R>(ny, u, nl, g, twx, s, nb)));
+  } else if (v == 2) {
+    TARA_SWITCH_N(nx, return (launch_row_nl<T, N, 2, R>(ny, u, nl, g, twx, s, nb)));
+  } else if (v == 1) {
+    TARA_SWITCH_N(nx, return (launch_row_nl<T, N, 1, R>(ny, u, nl, g, twx, s, nb)));
+  } else {
+    TARA_SWITCH_N(nx, return (launch_row_nl<T, N, 0, R>(ny, u, nl, g, twx, s, nb)));
+  }
+  return TARA_OK;
+}
+
+template <typename T, int R>
+int step_col_forward(int ny, int nh, const void* nl, const StepBufs& sb, const Grid2D& g, const RhsParams& p,
+                     int mode, const void* twy, cudaStream_t s, int nb, int v) {
+  if (v == 2) {
+    TARA_SWITCH_N(ny, return (launch_col_forward<T, N, 2, R>(nh, nl, sb, g, p, mode, twy, s, nb)));
+  } else if (v == 1) {
+    TARA_SWITCH_N(ny, return (launch_col_forward<T, N, 1, R>(nh, nl, sb, g, p, mode, twy, s, nb)));
+  } else {
+    TARA_SWITCH_N(ny, return (launch_col_forward<T, N, 0, R>(nh, nl, sb, g, p, mode, twy, s, nb)));
+  }
+  return TARA_OK;
+}
+
+// The variant index of the step launchers carries the radix path in bit 2
+// (v | 4: radix-8 path, FP64 and FP32 only; the double-float form ignores the
+// bit) and the tile variant in bits 0-1.
 template <typename T>
 int Launch2D<T>::col_inverse(int ny, int nh, const double2* win, void* u, const Grid2D& g,
                              const RhsParams& p, const void* twy, cudaStream_t s, int nb, int v) {
-  if (v == 2) {
-    TARA_SWITCH_N(ny, return (launch_col_inverse<T, N, 2>(nh, win, u, g, p, twy, s, nb)));
-  } else if (v == 1) {
-    TARA_SWITCH_N(ny, return (launch_col_inverse<T, N, 1>(nh, win, u, g, p, twy, s, nb)));
-  } else {
-    TARA_SWITCH_N(ny, return (launch_col_inverse<T, N, 0>(nh, win, u, g, p, twy, s, nb)));
-  }
-  return TARA_OK;
+  if constexpr (!is_df64<T>())
+    if (v & 4) return step_col_inverse<T, 8>(ny, nh, win, u, g, p, twy, s, nb, v & 3);
+  return step_col_inverse<T, 4>(ny, nh, win, u, g, p, twy, s, nb, v & 3);
 }
 
 template <typename T>
 int Launch2D<T>::row_nl(int nx, int ny, const void* u, void* nl, const Grid2D& g, const void* twx,
                         cudaStream_t s, int nb, int v) {
-  if (v == 2) {
-    TARA_SWITCH_N(nx, return (launch_row_nl<T, N, 2>(ny, u, nl, g, twx, s, nb)));
-  } else if (v == 1) {
-    TARA_SWITCH_N(nx, return (launch_row_nl<T, N, 1>(ny, u, nl, g, twx, s, nb)));
-  } else {
-    TARA_SWITCH_N(nx, return (launch_row_nl<T, N, 0>(ny, u, nl, g, twx, s, nb)));
-  }
-  return TARA_OK;
+  if constexpr (!is_df64<T>())
+    if (v & 4) return step_row_nl<T, 8>(nx, ny, u, nl, g, twx, s, nb, v & 3);
+  return step_row_nl<T, 4>(nx, ny, u, nl, g, twx, s, nb, v & 3);
 }
 
 template <typename T>
 int Launch2D<T>::col_forward(int ny, int nh, const void* nl, const StepBufs& sb, const Grid2D& g,
                              const RhsParams& p, int mode, const void* twy, cudaStream_t s, int nb,
                              int v) {
-  if (v == 2) {
-    TARA_SWITCH_N(ny, return (launch_col_forward<T, N, 2>(nh, nl, sb, g, p, mode, twy, s, nb)));
-  } else if (v == 1) {
-    TARA_SWITCH_N(ny, return (launch_col_forward<T, N, 1>(nh, nl, sb, g, p, mode, twy, s, nb)));
-  } else {
-    TARA_SWITCH_N(ny, return (launch_col_forward<T, N, 0>(nh, nl, sb, g, p, mode, twy, s, nb)));
-  }
-  return TARA_OK;
+  if constexpr (!is_df64<T>())
+    if (v & 4) return step_col_forward<T, 8>(ny, nh, nl, sb, g, p, mode, twy, s, nb, v & 3);
+  return step_col_forward<T, 4>(ny, nh, nl, sb, g, p, mode, twy, s, nb, v & 3);
 }
+
+// Explicit instantiations of the radix-8 step launchers live in their own
+// translation units (launch_fp64_r8.cu, launch_fp32_r8.cu), which compile in
+// parallel with the radix-4 ones.
+#define TARA_STEP_R8_INSTANCES(EXT, T)                                                              \
+  EXT template int step_col_inverse<T, 8>(int, int, const double2*, void*, const Grid2D&,            \
+                                          const RhsParams&, const void*, cudaStream_t, int, int);    \
+  EXT template int step_row_nl<T, 8>(int, int, const void*, void*, const Grid2D&, const void*,       \
+                                     cudaStream_t, int, int);                                        \
+  EXT template int step_col_forward<T, 8>(int, int, const void*, const StepBufs&, const Grid2D&,     \
+                                          const RhsParams&, int, const void*, cudaStream_t, int, int);
 
 template <typename T>
 int Launch2D<T>::col_fft(int ny, int nh, int pitch, const void* in, void* out, bool inverse,

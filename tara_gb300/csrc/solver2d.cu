@@ -96,6 +96,26 @@ void twiddle_entry(int n, int idx, double* re, double* im) {
     twiddle(n, idx, re, im);
     return;
   }
+  if (idx >= tw_r8_base(n)) {  // radix-8 path stage tables (layout in fft.cuh)
+    int t = idx - tw_r8_base(n);
+    const int span = r8_span(n);
+    const bool inv = t >= span;
+    if (inv) t -= span;
+    int i = 1;
+    while (t >= r8_stage_off(n, i) + r8_stage_size(n, i)) ++i;
+    const int off = t - r8_stage_off(n, i), ns = r8_ns(n, i);
+    const int run = off / ns, k = off % ns;
+    int e;
+    if (r8_radix(n, i) == 8) {
+      const int m = k * (n / (8 * ns));
+      e = run == 0 ? m : run == 1 ? 2 * m : run == 2 ? 4 * m : m + n / 8;
+    } else {
+      e = (run + 1) * k * (n / (4 * ns));
+    }
+    twiddle(n, e, re, im);
+    if (inv) *im = -*im;
+    return;
+  }
   int t = idx - n;
   const int span = tw_stage_span(n);
   const bool inv = t >= span;
@@ -758,7 +778,13 @@ int tara2d_step_timed(tara2d* h, int nsteps, double* kernel_ms, int* kernel_laun
   return rc ? rc : set_ok();
 }
 
-int tara2d_autotune(tara2d* h, int trial_steps, int* variants3, double* ms12) {
+// Is configuration index c (tile variant | 4 for the radix-8 path) available
+// for step kernel k of handle h?
+static bool candidate_ok(const tara2d* h, int k, int c) {
+  return (c & 3) < kVariants[k] && (!(c & 4) || h->cfg.precision != TARA_PREC_DF64);
+}
+
+int tara2d_autotune(tara2d* h, int trial_steps, int* variants3, double* ms24) {
   if (!h || trial_steps <= 0) return set_error(TARA_ERR_ARGS, "bad arguments");
   TARA_CK(cudaSetDevice(h->dev));
   const size_t bytes = (size_t)h->batch * h->ny * h->pitch * sizeof(double2);
@@ -769,17 +795,19 @@ int tara2d_autotune(tara2d* h, int trial_steps, int* variants3, double* ms12) {
   if (!rc && (cudaMemcpyAsync(save_w0, h->w0, bytes, cudaMemcpyDeviceToDevice, h->stream) != cudaSuccess ||
               cudaMemcpyAsync(save_fold, h->fold, bytes, cudaMemcpyDeviceToDevice, h->stream) != cudaSuccess))
     rc = set_error(TARA_ERR_CUDA, "state save");
-  // Pass 1: every kernel in variant v (the last variant of a kernel that has
-  // fewer), one settling step (which also sets the shared-memory attributes on
-  // first use), then trial_steps timed.
-  // Pass 2: each kernel's variants with the other two at their pass-1 choice,
+  // Candidates: every tile variant on both radix paths (radix 4 only for the
+  // double-float form).
+  // Pass 1: every kernel in candidate c (a kernel without it keeps its default),
+  // one settling step (which also sets the shared-memory attributes on first
+  // use), then trial_steps timed.
+  // Pass 2: each kernel's candidates with the other two at their pass-1 choice,
   // again one settling step and trial_steps timed -- a kernel's time depends
   // on its neighbours' tiles (cache contents, CTA phases), and a variant timed
   // right after a switch, without the settling step, read up to 15 % slow.
-  double ms[kMaxVariants][3];
-  for (int v = 0; v < kMaxVariants; ++v)
-    for (int k = 0; k < 3; ++k) ms[v][k] = 0.0;
-  int c[3] = {0, 0, 0};
+  double ms[kCandidates][3];
+  for (int c = 0; c < kCandidates; ++c)
+    for (int k = 0; k < 3; ++k) ms[c][k] = 0.0;
+  int best1[3] = {0, 0, 0};
   auto timed = [&](double* t) {
     int r = tara2d_step(h, 1);
     int cnt[3];
@@ -788,39 +816,47 @@ int tara2d_autotune(tara2d* h, int trial_steps, int* variants3, double* ms12) {
       for (int k = 0; k < 3; ++k) t[k] /= (cnt[k] > 0 ? cnt[k] : 1);
     return r;
   };
-  for (int v = 0; v < kMaxVariants && !rc; ++v) {
-    for (int k = 0; k < 3; ++k) h->var[k] = v < kVariants[k] ? v : kVariants[k] - 1;
+  for (int c = 0; c < kCandidates && !rc; ++c) {
+    bool any = false;
+    for (int k = 0; k < 3; ++k) {
+      const bool ok = candidate_ok(h, k, c);
+      h->var[k] = ok ? c : 0;
+      any |= ok;
+    }
+    if (!any) continue;
     double t[3];
     rc = timed(t);
     if (!rc)
       for (int k = 0; k < 3; ++k)
-        if (v < kVariants[k]) ms[v][k] = t[k];
+        if (candidate_ok(h, k, c)) ms[c][k] = t[k];
   }
   if (!rc)
     for (int k = 0; k < 3; ++k)
-      for (int v = 1; v < kVariants[k]; ++v)
-        if (ms[v][k] < ms[c[k]][k]) c[k] = v;
-  double ctx[3][kMaxVariants];
+      for (int c = 1; c < kCandidates; ++c)
+        if (candidate_ok(h, k, c) && ms[c][k] < ms[best1[k]][k]) best1[k] = c;
+  double ctx[3][kCandidates];
   for (int k = 0; k < 3 && !rc; ++k)
-    for (int v = 0; v < kVariants[k] && !rc; ++v) {
-      for (int q = 0; q < 3; ++q) h->var[q] = c[q];
-      h->var[k] = v;
+    for (int c = 0; c < kCandidates && !rc; ++c) {
+      if (!candidate_ok(h, k, c)) continue;
+      for (int q = 0; q < 3; ++q) h->var[q] = best1[q];
+      h->var[k] = c;
       double t[3];
       rc = timed(t);
-      if (!rc) ctx[k][v] = t[k];
+      if (!rc) ctx[k][c] = t[k];
     }
   if (!rc)
     for (int k = 0; k < 3; ++k) {
       int best = 0;
-      for (int v = 1; v < kVariants[k]; ++v)
-        if (ctx[k][v] < ctx[k][best]) best = v;
+      for (int c = 1; c < kCandidates; ++c)
+        if (candidate_ok(h, k, c) && ctx[k][c] < ctx[k][best]) best = c;
       h->var[k] = best;
       if (variants3) variants3[k] = best;
-      for (int v = 0; v < kVariants[k]; ++v) ms[v][k] = ctx[k][v];  // reported: the in-context times
+      for (int c = 0; c < kCandidates; ++c)
+        ms[c][k] = candidate_ok(h, k, c) ? ctx[k][c] : 0.0;  // reported: the in-context times
     }
-  if (!rc && ms12)
-    for (int v = 0; v < kMaxVariants; ++v)
-      for (int k = 0; k < 3; ++k) ms12[3 * v + k] = ms[v][k];
+  if (!rc && ms24)
+    for (int c = 0; c < kCandidates; ++c)
+      for (int k = 0; k < 3; ++k) ms24[3 * c + k] = ms[c][k];
   if (!rc && (cudaMemcpyAsync(h->w0, save_w0, bytes, cudaMemcpyDeviceToDevice, h->stream) != cudaSuccess ||
               cudaMemcpyAsync(h->fold, save_fold, bytes, cudaMemcpyDeviceToDevice, h->stream) != cudaSuccess ||
               cudaStreamSynchronize(h->stream) != cudaSuccess))
@@ -833,8 +869,10 @@ int tara2d_autotune(tara2d* h, int trial_steps, int* variants3, double* ms12) {
 int tara2d_set_variants(tara2d* h, const int* variants3) {
   if (!h || !variants3) return set_error(TARA_ERR_ARGS, "null argument");
   for (int k = 0; k < 3; ++k)
-    if (variants3[k] < 0 || variants3[k] >= kVariants[k])
-      return set_error(TARA_ERR_ARGS, "variants: column passes 0-2, row pass 0-3");
+    if (variants3[k] < 0 || variants3[k] >= kCandidates || !candidate_ok(h, k, variants3[k]))
+      return set_error(TARA_ERR_ARGS,
+                       "variants: tile 0-2 (row pass 0-3), plus 4 for the radix-8 path (not in the "
+                       "double-float form)");
   for (int k = 0; k < 3; ++k) h->var[k] = variants3[k];
   return set_ok();
 }
