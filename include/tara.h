@@ -20,7 +20,7 @@
  *    many steps per call, plus batched ensembles (tara_ens_*).  These return an
  *    int status (TARA_OK = 0).
  *
- * Grid sizes: Nx and Ny powers of two from 16 to 2048.
+ * Grid sizes: Nx and Ny powers of two from 16 to 4096 (the 2D paths; 3D: 16 to 256).
  */
 #ifndef TARA_H
 #define TARA_H
@@ -107,7 +107,7 @@ int tara_finalize(void);
 #define TARA_PREC_DF64 2   /* double-float (FP32 pair) FFTs and products; FP64 state */
 
 typedef struct tara2d_config {
-  int nx, ny;      /* powers of two, 16..2048 */
+  int nx, ny;      /* powers of two, 16..4096 */
   int rhs;         /* TARA_RHS_* */
   int scheme;      /* TARA_SCHEME_* */
   int precision;   /* TARA_PREC_* */
@@ -201,7 +201,7 @@ int tara2d_init_random_run(tara2d* h, int run, double k0, double energy, uint64_
 
 /* ---- ensembles of runs of uneven sizes ------------------------------------ */
 
-/* One run: grid n x n (power of two in [16, 2048]) with a seeded random-phase
+/* One run: grid n x n (power of two in [16, 4096]) with a seeded random-phase
  * initial spectrum (tara2d_init_random's recipe with this k0 and seed). */
 typedef struct tara_ens_run {
   int n;
@@ -296,7 +296,7 @@ void ab3com_(const int* Nx, const int* Ny, const int* Nz, const int* Nh, const d
  * (complex(8) (Nh,Ny)); the *_old arrays and time are unused.  Lx, Ly, mux, muy,
  * CS come from the caller's common block /comm/ (comm_, the layout
  * Lx,Ly,mux,muy,ms,CS,dt of src/derive2coh.f95:30); wavenumbers use the pi
- * argument.  Sizes: powers of two in [16, 2048]. */
+ * argument.  Sizes: powers of two in [16, 4096]. */
 void derive2coh_(const int* Nx, const int* Ny, const int* Nh, const double* pi, const double* time,
                  const double* nk, const double* ukx, const double* uky, double* dn_dt_old,
                  double* dux_dt_old, double* duy_dt_old, double* dn_dt_new, double* dux_dt_new,
@@ -311,7 +311,7 @@ void ab2coh_(const int* Nx, const int* Ny, const int* Nh, const double* pi, cons
              const double* duy_dt_new);
 
 typedef struct tara_coh2d_config {
-  int nx, ny;        /* powers of two, 16..2048 */
+  int nx, ny;        /* powers of two, 16..4096 */
   double kpi;        /* the pi of kx = 2*pi*(i-1)/Lx */
   double lx, ly;     /* box lengths */
   double mux, muy;   /* viscosities (the reference driver: 0.0002) */
@@ -355,7 +355,7 @@ int tara_coh2d_real_fields(tara_coh2d* h, double* n, double* ux, double* uy, dou
  * caller's /comm/ (comm_, the layout Lx,Ly,spheat,mu,ms,CS,mu_0,eta,dt,kf,A of
  * src/derive2com.f95:43).  Faithful to the reference's curl B (built from
  * d_ux_dx and d_uy_dy, :186-187); the forcing uses the grid coordinates the
- * reference leaves unset.  Sizes: powers of two in [16, 2048]. */
+ * reference leaves unset.  Sizes: powers of two in [16, 4096]. */
 void derive2com_(const int* Nx, const int* Ny, const int* Nh, const double* pi, const double* time,
                  const double* rho_k, const double* rho_ux_k, const double* rho_uy_k,
                  const double* E_k, const double* Bx_k, const double* By_k, double* d_rho_k_dt_old,
@@ -377,7 +377,7 @@ void ab2com_(const int* Nx, const int* Ny, const int* Nh, const double* pi, cons
              const double* d_Bx_k_dt_new, const double* d_By_k_dt_old, const double* d_By_k_dt_new);
 
 typedef struct tara_com2d_config {
-  int nx, ny;      /* powers of two, 16..2048 */
+  int nx, ny;      /* powers of two, 16..4096 */
   int defined;     /* 0: curl B as the reference (from d_ux_dx, d_uy_dy); 1: from dB/dx, dB/dy */
   double kpi;      /* the pi of kx = 2*pi*(i-1)/Lx */
   double lx, ly;   /* box lengths */

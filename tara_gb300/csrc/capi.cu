@@ -48,7 +48,7 @@ bool check_dims(const int* Nx, const int* Ny, const int* Nh) {
     return false;
   }
   if (!is_pow2_in_range(*Nx) || !is_pow2_in_range(*Ny) || *Nh != *Nx / 2 + 1) {
-    set_error(TARA_ERR_ARGS, "Nx, Ny must be powers of two in [16, 2048] and Nh = Nx/2+1");
+    set_error(TARA_ERR_ARGS, "Nx, Ny must be powers of two in [16, 4096] and Nh = Nx/2+1");
     return false;
   }
   return true;

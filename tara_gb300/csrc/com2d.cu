@@ -428,7 +428,7 @@ bool com_dims(const int* Nx, const int* Ny, const int* Nh, const double* pi) {
     return false;
   }
   if (!is_pow2_in_range(*Nx) || !is_pow2_in_range(*Ny) || *Nh != *Nx / 2 + 1) {
-    set_error(TARA_ERR_ARGS, "Nx, Ny must be powers of two in [16, 2048] and Nh = Nx/2+1");
+    set_error(TARA_ERR_ARGS, "Nx, Ny must be powers of two in [16, 4096] and Nh = Nx/2+1");
     return false;
   }
   return true;
@@ -475,7 +475,7 @@ int tara_com2d_create(const tara_com2d_config* cfg, tara_com2d** out) {
   if (!cfg || !out) return set_error(TARA_ERR_ARGS, "null argument");
   *out = nullptr;
   if (!is_pow2_in_range(cfg->nx) || !is_pow2_in_range(cfg->ny))
-    return set_error(TARA_ERR_ARGS, "nx and ny must be powers of two in [16, 2048]");
+    return set_error(TARA_ERR_ARGS, "nx and ny must be powers of two in [16, 4096]");
   if (!(cfg->lx > 0.0) || !(cfg->ly > 0.0) || !(cfg->kpi > 0.0))
     return set_error(TARA_ERR_ARGS, "box lengths and kpi must be positive");
   tara_com2d* h = new tara_com2d();

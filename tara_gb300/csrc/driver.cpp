@@ -85,6 +85,25 @@ std::string fort_name(const std::string& dir, long unit) {
 
 int fail_rc() { return tara_last_error() ? tara_last_error() : TARA_ERR_CUDA; }
 
+// The reference reads any Nx, Ny (, Nz) (src/main2csh.f95:35-38) and FFTW takes
+// any length; these kernels take powers of two, 16 to 4096 in 2D and 16 to 256
+// in 3D.  Refuse anything else before allocating, naming the supported set.
+int check_grid(const char* program, int dims, int nx, int ny, int nz) {
+  const int hi = dims == 2 ? 4096 : 256;
+  const int n[3] = {nx, ny, nz};
+  const char* name[3] = {"Nx", "Ny", "Nz"};
+  for (int d = 0; d < dims; ++d)
+    if (n[d] < 16 || n[d] > hi || (n[d] & (n[d] - 1))) {
+      char msg[256];
+      std::snprintf(msg, sizeof msg,
+                    "%s: %s = %d is not supported; grid sizes here are powers of two from 16 to %d "
+                    "(16, 32, 64, ..., %d)",
+                    program, name[d], n[d], hi, hi);
+      return set_error(TARA_ERR_ARGS, msg);
+    }
+  return TARA_OK;
+}
+
 // ---------------------------------------------------------------------------
 // tara2dScrSer (src/main2css.f95) and tara2dHydSer (src/main2csh.f95)
 // ---------------------------------------------------------------------------
@@ -104,6 +123,7 @@ int run_2d(Reader& R, const std::string& out, int max_steps, bool screened) {
   R.d("initialProfile", "m0", m0);
   R.d("initialProfile", "d", d);
   if (!R.ok) return set_error(TARA_ERR_INI, R.err);
+  if (int rc = check_grid(screened ? "tara2dScrSer" : "tara2dHydSer", 2, nx, ny, 0)) return rc;
   lx = lx * kPi;
   ly = ly * kPi;
   const double dx = lx / (double)nx, dy = ly / (double)ny;
@@ -245,6 +265,7 @@ int run_3d(Reader& R, const std::string& out, int max_steps) {
   R.d("time", "dt", dt);
   R.d("resistivity", "nu", mu);
   if (!R.ok) return set_error(TARA_ERR_INI, R.err);
+  if (int rc = check_grid("tara3dMHDOMP", 3, nx, ny, nz)) return rc;
   lx = lx * kPi;
   ly = ly * kPi;
   lz = lz * kPi;
@@ -319,6 +340,7 @@ int run_coh(Reader& R, const std::string& out, int max_steps) {
   R.d("time", "dt", dt);
   R.d("resistivity", "nu", nu);  // read, then replaced by 0.0002 (src/main2coh.f95:119-120)
   if (!R.ok) return set_error(TARA_ERR_INI, R.err);
+  if (int rc = check_grid("tara2dHydOMP", 2, nx, ny, 0)) return rc;
   const double lx_ini = lx, ly_ini = ly;
   lx = lx * kPi;
   ly = ly * kPi;
@@ -385,6 +407,7 @@ int run_com(Reader& R, const std::string& out, int max_steps) {
   R.d("time", "dt", dt);
   R.d("resistivity", "nu", mu);
   if (!R.ok) return set_error(TARA_ERR_INI, R.err);
+  if (int rc = check_grid("tara2dMHDOMP", 2, nx, ny, 0)) return rc;
   const double lx_ini = lx, ly_ini = ly;
   lx = lx * kPi;
   ly = ly * kPi;

@@ -177,7 +177,7 @@ int tara_ens_create(int nruns, const tara_ens_run* runs, int precision, int sche
   for (int r = 0; r < nruns; ++r) {
     const int n = runs[r].n;
     if (!is_pow2_in_range(n) || !(runs[r].k0 > 0.0))
-      return fail(set_error(TARA_ERR_ARGS, "run sizes must be powers of two in [16, 2048], k0 > 0"));
+      return fail(set_error(TARA_ERR_ARGS, "run sizes must be powers of two in [16, 4096], k0 > 0"));
     auto it = by_n.find(n);
     if (it == by_n.end()) {
       it = by_n.emplace(n, (int)e->groups.size()).first;

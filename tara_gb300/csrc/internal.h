@@ -21,9 +21,10 @@ int cuda_fail(cudaError_t e, const char* what);
     if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
   } while (0)
 
-// Largest transform length: one FP64 row pass of 2048 points fills 128 KB of
-// shared memory with four slots; longer rows would need a split transform.
-constexpr int kMaxN = 2048;
+// Largest transform length: a 4096-point FP64 row pair fits the three-slot row
+// tile (192 KB of shared memory), a column the one-column tiles (128 KB with
+// its two field slots); longer lines would need a split transform.
+constexpr int kMaxN = 4096;
 inline bool is_pow2_in_range(int n) { return n >= 16 && n <= kMaxN && (n & (n - 1)) == 0; }
 inline int round_up(int v, int m) { return (v + m - 1) / m * m; }
 
@@ -79,6 +80,9 @@ struct Launch2D {
                      const void* twx, cudaStream_t s, int nf = 1, size_t fs_in = 0, size_t fs_out = 0);
   static int row_r2c(int nx, int ny, int rpitch, int pitch, const void* in, void* out,
                      const void* twx, cudaStream_t s, int nf = 1, size_t fs_in = 0, size_t fs_out = 0);
+  // whether step kernel k (0 column inverse, 1 row pass, 2 column forward) has
+  // tile variant v at length n (a tile must fit one CTA)
+  static bool tile_fits(int k, int n, int v);
 };
 
 // Twiddle exp(-2 pi i m/n) in FP64 with tw[n - m] = conj(tw[m]) exactly.

@@ -85,6 +85,9 @@ struct RhsParams {
 template <typename T>
 constexpr bool is_df64() { return std::is_same<T, df64>::value; }
 
+// Dynamic shared memory one CTA may use on sm_103a (227 KB).
+constexpr int kMaxSmem = 227 * 1024;
+
 // Largest power-of-two column tile with tile smem <= budget and <= 512 threads.
 __host__ __device__ constexpr int pick_tc(int bytes_per_col, int threads_per_col,
                                           int budget = 100 * 1024) {
@@ -122,6 +125,10 @@ template <typename T, int N, int V = 0> struct ColCfg {
   static constexpr int THREADS_C = TCC * G;
   static constexpr int SMEM_A = 2 * TCA * S * (int)sizeof(C);
   static constexpr int SMEM_C = TCC * S * (int)sizeof(C);
+  // a tile exists when it fits one CTA (at 4096 points variant 2 of pass A
+  // would need 2048 threads)
+  static constexpr bool VALID_A = THREADS_A <= 1024 && SMEM_A <= kMaxSmem;
+  static constexpr bool VALID_C = THREADS_C <= 1024 && SMEM_C <= kMaxSmem;
 };
 
 // Row pass tiles.  Variants 0-2 hold RP row pairs in four slots each (the two
@@ -139,6 +146,16 @@ template <typename T, int N, int V = 0> struct RowCfg {
   static constexpr int THREADS = V == 3 ? 2 * G : 4 * RP * G;
   static constexpr int SL = N;  // smem stride between row slots
   static constexpr int SMEM = (V == 3 ? 3 : RP * 4) * SL * (int)sizeof(C);
+  // four FP64 slots of 4096 points (256 KB) do not fit a CTA: variant 3 only
+  static constexpr bool VALID = THREADS <= 1024 && SMEM <= kMaxSmem;
+  // CTAs per SM the row kernel asks for: two for variant 3 and the 512-thread
+  // FP32 tiles, three for the 256-thread FP32 tiles (at 84 registers a
+  // 256-thread FP32 row CTA fitted only twice per SM, and the 512^2 row pass
+  // took 670 instead of 364 us) -- as far as shared memory allows
+  static constexpr int MINB0 = (V == 3 || (sizeof(T) == 4 && THREADS >= 512)) ? 2
+                               : (sizeof(T) == 4 && THREADS == 256)            ? 3
+                                                                               : 1;
+  static constexpr int MINB = MINB0 * SMEM <= kMaxSmem ? MINB0 : 1;
 };
 
 // ---------------------------------------------------------------------------
@@ -375,8 +392,7 @@ __device__ __forceinline__ void row_nl_cta(int bx, int run, const typename cplx_
 }
 
 template <typename T, int N, int V, int R = 4>
-__global__ void __launch_bounds__(RowCfg<T, N, V>::THREADS,
-                                  (V == 3 || (sizeof(T) == 4 && RowCfg<T, N, V>::THREADS >= 512)) ? 2 : 1)
+__global__ void __launch_bounds__(RowCfg<T, N, V>::THREADS, RowCfg<T, N, V>::MINB)
     k_row_nl(const typename cplx_of<T>::type* __restrict__ u,
              typename cplx_of<T>::type* __restrict__ nl, Grid2D g,
              const typename cplx_of<T>::type* __restrict__ tw) {
@@ -647,8 +663,15 @@ __global__ void __launch_bounds__(ColCfg<T, N, V>::THREADS_C)
 
 // Row pairs per CTA of the plain row transforms (one slot per pair): four per
 // row pair of the RHS row pass, or a single pair for the small-grid variant.
+// Largest power-of-two count of row pairs, at most np, whose slots fit `budget`.
+__host__ __device__ constexpr int fit_pairs(int np, int slot_bytes, int budget = 128 * 1024) {
+  return (np > 1 && np * slot_bytes > budget) ? fit_pairs(np / 2, slot_bytes, budget) : np;
+}
+
 template <typename T, int N, int V> struct RowXCfg {
-  static constexpr int NP = V == 2 ? 1 : 4 * RowCfg<T, N, V>::RP;
+  static constexpr int NP = V == 2 ? 1
+                                   : fit_pairs(4 * RowCfg<T, N, V>::RP,
+                                               N * (int)sizeof(typename cplx_of<T>::type));
   static constexpr int THREADS = NP * fft_group(N);
   static constexpr int SMEM = NP * N * (int)sizeof(typename cplx_of<T>::type);
 };

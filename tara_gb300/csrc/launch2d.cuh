@@ -23,20 +23,29 @@ static cudaError_t allow_smem(K kernel, int bytes) {
     case 512: { constexpr int N = 512; CALL; } break;   \
     case 1024: { constexpr int N = 1024; CALL; } break; \
     case 2048: { constexpr int N = 2048; CALL; } break; \
-    default: return set_error(TARA_ERR_ARGS, "grid size must be a power of two in [16, 2048]"); \
+    case 4096: { constexpr int N = 4096; CALL; } break; \
+    default: return set_error(TARA_ERR_ARGS, "grid size must be a power of two in [16, 4096]"); \
   }
+
+static inline int no_tile() {
+  return set_error(TARA_ERR_ARGS, "this tile variant does not fit one CTA at this length");
+}
 
 template <typename T, int N, int V, int R>
 static int launch_col_inverse(int nh, const double2* win, void* u, const Grid2D& g,
                               const RhsParams& p, const void* tw, cudaStream_t s, int nb) {
   typedef typename cplx_of<T>::type C;
   typedef ColCfg<T, N, V> CF;
-  static cudaError_t attr = allow_smem(k_col_inverse<T, N, V, R>, CF::SMEM_A);
-  TARA_CK(attr);
-  const dim3 blocks((nh + CF::TCA - 1) / CF::TCA, 2, nb);
-  k_col_inverse<T, N, V, R><<<blocks, CF::THREADS_A, CF::SMEM_A, s>>>(win, (C*)u, g, p, (const C*)tw);
-  TARA_CK(cudaGetLastError());
-  return TARA_OK;
+  if constexpr (!CF::VALID_A) {
+    return no_tile();
+  } else {
+    static cudaError_t attr = allow_smem(k_col_inverse<T, N, V, R>, CF::SMEM_A);
+    TARA_CK(attr);
+    const dim3 blocks((nh + CF::TCA - 1) / CF::TCA, 2, nb);
+    k_col_inverse<T, N, V, R><<<blocks, CF::THREADS_A, CF::SMEM_A, s>>>(win, (C*)u, g, p, (const C*)tw);
+    TARA_CK(cudaGetLastError());
+    return TARA_OK;
+  }
 }
 
 template <typename T, int N, int V, int R>
@@ -44,12 +53,16 @@ static int launch_row_nl(int ny, const void* u, void* nl, const Grid2D& g, const
                          cudaStream_t s, int nb) {
   typedef typename cplx_of<T>::type C;
   typedef RowCfg<T, N, V> RC;
-  static cudaError_t attr = allow_smem(k_row_nl<T, N, V, R>, RC::SMEM);
-  TARA_CK(attr);
-  const dim3 blocks((ny + 2 * RC::RP - 1) / (2 * RC::RP), nb);
-  k_row_nl<T, N, V, R><<<blocks, RC::THREADS, RC::SMEM, s>>>((const C*)u, (C*)nl, g, (const C*)tw);
-  TARA_CK(cudaGetLastError());
-  return TARA_OK;
+  if constexpr (!RC::VALID) {
+    return no_tile();
+  } else {
+    static cudaError_t attr = allow_smem(k_row_nl<T, N, V, R>, RC::SMEM);
+    TARA_CK(attr);
+    const dim3 blocks((ny + 2 * RC::RP - 1) / (2 * RC::RP), nb);
+    k_row_nl<T, N, V, R><<<blocks, RC::THREADS, RC::SMEM, s>>>((const C*)u, (C*)nl, g, (const C*)tw);
+    TARA_CK(cudaGetLastError());
+    return TARA_OK;
+  }
 }
 
 template <typename T, int N, int V, int R>
@@ -57,13 +70,17 @@ static int launch_col_forward(int nh, const void* nl, const StepBufs& sb, const 
                               const RhsParams& p, int mode, const void* tw, cudaStream_t s, int nb) {
   typedef typename cplx_of<T>::type C;
   typedef ColCfg<T, N, V> CF;
-  static cudaError_t attr = allow_smem(k_col_forward<T, N, V, R>, CF::SMEM_C);
-  TARA_CK(attr);
-  const dim3 blocks((nh + CF::TCC - 1) / CF::TCC, nb);
-  k_col_forward<T, N, V, R><<<blocks, CF::THREADS_C, CF::SMEM_C, s>>>((const C*)nl, sb, g, p, mode,
-                                                                    (const C*)tw);
-  TARA_CK(cudaGetLastError());
-  return TARA_OK;
+  if constexpr (!CF::VALID_C) {
+    return no_tile();
+  } else {
+    static cudaError_t attr = allow_smem(k_col_forward<T, N, V, R>, CF::SMEM_C);
+    TARA_CK(attr);
+    const dim3 blocks((nh + CF::TCC - 1) / CF::TCC, nb);
+    k_col_forward<T, N, V, R><<<blocks, CF::THREADS_C, CF::SMEM_C, s>>>((const C*)nl, sb, g, p, mode,
+                                                                         (const C*)tw);
+    TARA_CK(cudaGetLastError());
+    return TARA_OK;
+  }
 }
 
 template <typename T, int N, bool INV, int V>
@@ -164,6 +181,36 @@ int step_col_forward(int ny, int nh, const void* nl, const StepBufs& sb, const G
     TARA_SWITCH_N(ny, return (launch_col_forward<T, N, 0, R>(nh, nl, sb, g, p, mode, twy, s, nb)));
   }
   return TARA_OK;
+}
+
+// Whether step kernel k (0 column inverse, 1 row, 2 column forward) has tile
+// variant v (0-3) at length n.
+template <typename T, int N>
+static bool tile_fits_n(int k, int v) {
+  if (k == 0)
+    return v == 0 ? ColCfg<T, N, 0>::VALID_A : v == 1 ? ColCfg<T, N, 1>::VALID_A
+           : v == 2 ? ColCfg<T, N, 2>::VALID_A : false;
+  if (k == 1)
+    return v == 0 ? RowCfg<T, N, 0>::VALID : v == 1 ? RowCfg<T, N, 1>::VALID
+           : v == 2 ? RowCfg<T, N, 2>::VALID : v == 3 ? RowCfg<T, N, 3>::VALID : false;
+  return v == 0 ? ColCfg<T, N, 0>::VALID_C : v == 1 ? ColCfg<T, N, 1>::VALID_C
+         : v == 2 ? ColCfg<T, N, 2>::VALID_C : false;
+}
+
+template <typename T>
+bool Launch2D<T>::tile_fits(int k, int n, int v) {
+  switch (n) {
+    case 16: return tile_fits_n<T, 16>(k, v);
+    case 32: return tile_fits_n<T, 32>(k, v);
+    case 64: return tile_fits_n<T, 64>(k, v);
+    case 128: return tile_fits_n<T, 128>(k, v);
+    case 256: return tile_fits_n<T, 256>(k, v);
+    case 512: return tile_fits_n<T, 512>(k, v);
+    case 1024: return tile_fits_n<T, 1024>(k, v);
+    case 2048: return tile_fits_n<T, 2048>(k, v);
+    case 4096: return tile_fits_n<T, 4096>(k, v);
+    default: return false;
+  }
 }
 
 // The variant index of the step launchers carries the radix path in bit 2

@@ -11,4 +11,5 @@ template int Launch2D<df64>::row_nl(int, int, const void*, void*, const Grid2D&,
                                     int);
 template int Launch2D<df64>::col_forward(int, int, const void*, const StepBufs&, const Grid2D&, const RhsParams&,
                                          int, const void*, cudaStream_t, int, int);
+template bool Launch2D<df64>::tile_fits(int, int, int);
 }  // namespace tara

@@ -566,11 +566,23 @@ int tara2d_destroy(tara2d* h) {
   return set_ok();
 }
 
+// Is configuration index c (tile variant | 4 for the radix-8 path) available
+// for step kernel k of handle h?
+static bool candidate_ok(const tara2d* h, int k, int c) {
+  if ((c & 3) >= kVariants[k] || ((c & 4) && h->cfg.precision == TARA_PREC_DF64)) return false;
+  const int n = k == 1 ? h->nx : h->ny;  // the row pass transforms along x, the others along y
+  switch (h->cfg.precision) {
+    case TARA_PREC_FP32: return Launch2D<float>::tile_fits(k, n, c & 3);
+    case TARA_PREC_DF64: return Launch2D<df64>::tile_fits(k, n, c & 3);
+    default: return Launch2D<double>::tile_fits(k, n, c & 3);
+  }
+}
+
 int tara2d_create(const tara2d_config* cfg, tara2d** out) {
   if (!cfg || !out) return set_error(TARA_ERR_ARGS, "null argument");
   *out = nullptr;
   if (!is_pow2_in_range(cfg->nx) || !is_pow2_in_range(cfg->ny))
-    return set_error(TARA_ERR_ARGS, "nx and ny must be powers of two in [16, 2048]");
+    return set_error(TARA_ERR_ARGS, "nx and ny must be powers of two in [16, 4096]");
   if (cfg->rhs != TARA_RHS_PLAIN && cfg->rhs != TARA_RHS_SCREEN)
     return set_error(TARA_ERR_ARGS, "unknown rhs kind");
   if (cfg->scheme != TARA_SCHEME_AB2 && cfg->scheme != TARA_SCHEME_RK4)
@@ -588,6 +600,14 @@ int tara2d_create(const tara2d_config* cfg, tara2d** out) {
   h->ny = cfg->ny;
   h->nh = cfg->nx / 2 + 1;
   h->pitch = round_up(h->nh, 8);
+  // default tiles: variant 0, or the first that fits a CTA (at 4096 points the
+  // FP64 row pass has only the three-slot tile)
+  for (int k = 0; k < 3; ++k)
+    for (int v = 0; v < kVariants[k]; ++v)
+      if (candidate_ok(h, k, v)) {
+        h->var[k] = v;
+        break;
+      }
   int rc = TARA_OK;
   auto fail = [&](int code) {
     tara2d_destroy(h);
@@ -776,12 +796,6 @@ int tara2d_step_timed(tara2d* h, int nsteps, double* kernel_ms, int* kernel_laun
   for (cudaEvent_t e : ev)
     if (e) cudaEventDestroy(e);
   return rc ? rc : set_ok();
-}
-
-// Is configuration index c (tile variant | 4 for the radix-8 path) available
-// for step kernel k of handle h?
-static bool candidate_ok(const tara2d* h, int k, int c) {
-  return (c & 3) < kVariants[k] && (!(c & 4) || h->cfg.precision != TARA_PREC_DF64);
 }
 
 int tara2d_autotune(tara2d* h, int trial_steps, int* variants3, double* ms24) {

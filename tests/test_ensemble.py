@@ -115,7 +115,8 @@ def test_solver_autotune_restores_state():
         w2, fo2 = s.get_state(with_history=True)
         assert np.array_equal(w, w2) and np.array_equal(fo, fo2)
         assert all(0 <= v < 8 for v in r["variants"])
-        assert all(t > 0 for row in r["ms"] for t in row)
+        for c, row in enumerate(r["ms"]):  # the column passes have no tile variant 3
+            assert [t > 0 for t in row] == [c & 3 < 3, True, c & 3 < 3], (c, row)
 
 
 @pytest.mark.parametrize("n", [16, 32, 64, 128, 256, 512, 1024, 2048])

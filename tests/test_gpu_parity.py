@@ -36,7 +36,8 @@ def test_fft_golden_vectors(golden):
 
 
 @pytest.mark.parametrize("ny,nx", [(16, 16), (32, 64), (64, 16), (128, 128), (256, 512),
-                                   (1024, 1024), (2048, 2048), (16, 2048), (2048, 16)])
+                                   (1024, 1024), (2048, 2048), (16, 2048), (2048, 16), (4096, 4096),
+                                   (16, 4096), (4096, 32)])
 def test_fft_vs_oracle(oracle, ny, nx):
     rng = np.random.default_rng(nx * 7 + ny)
     x = rng.standard_normal((ny, nx))
@@ -66,7 +67,8 @@ def test_derive2css_golden(golden):
     assert rel_l2(tg.derive2css(golden["ic_spec"], 1.0, 0.01), golden["rhs_screen_driverL"]) < 1e-12
 
 
-@pytest.mark.parametrize("ny,nx", [(64, 128), (256, 64), (512, 512), (2048, 2048), (16, 2048), (2048, 16)])
+@pytest.mark.parametrize("ny,nx", [(64, 128), (256, 64), (512, 512), (2048, 2048), (16, 2048), (2048, 16),
+                                   (4096, 4096), (4096, 64), (32, 4096)])
 def test_derive_vs_oracle_sizes(oracle, ny, nx):
     w = oracle.ic_random(nx, ny, 6.0, 0.5, 11) if nx == ny else None
     if w is None:
@@ -249,3 +251,39 @@ def test_pinned_host_round_trip():
         s.set_state(w)                           # pageable write
         s.get_state_into(pin_out)
         assert np.array_equal(pin_out, w)
+
+
+def test_4096_rk4_steps_and_configurations(oracle):
+    """4096^2 (a grid the reference's input.ini can name): the resident RK4
+    solver's right-hand side against the oracle, every configuration the
+    autotuner may pick (tile variants that fit a CTA, both radix paths) giving
+    the default's result (bitwise on one radix path), and RK4 steps that keep
+    Hermitian symmetry and dissipate energy at dE/dt = -2 nu Z."""
+    n, nu, dt = 4096, 1e-4, 2.5e-5
+    with tg.Solver2D(n, scheme=tg.SCHEME_RK4, nu=nu, dt=dt) as s:
+        s.init_random(6.0, 0.5, 4096)
+        w0 = s.get_state()
+        assert rel_l2(s.rhs(), oracle.derive2csh(w0, nu)) < 1e-12
+        e0, z0 = s.diag()
+        s.step(2)
+        e1, z1 = s.diag()
+        w1 = s.get_state()
+        r = s.autotune(1)
+    assert e1 < e0 and z1 < z0
+    rate = (e1 - e0) / (2 * dt)
+    assert abs(rate + 2 * nu * 0.5 * (z0 + z1)) < 1e-3 * abs(rate)
+    col = w1[:, 0]
+    assert np.allclose(col[1:], np.conj(col[1:][::-1]), atol=1e-12 * np.abs(col).max())
+    # the FP64 row pass fits one CTA only in the three-slot tile at 4096 points
+    assert r["variants"][1] & 3 == 3
+    for c in range(8):
+        assert r["ms"][c][1] > 0 if c & 3 == 3 else r["ms"][c][1] == 0
+    with tg.Solver2D(n, scheme=tg.SCHEME_RK4, nu=nu, dt=dt) as s:
+        s.set_state(w0)
+        s.set_variants(r["variants"])
+        s.step(2)
+        w2 = s.get_state()
+    if all(v & 4 == 0 for v in r["variants"]):
+        assert np.array_equal(w2, w1)
+    else:
+        assert rel_l2(w2, w1) < 1e-13

@@ -155,3 +155,27 @@ def test_features_need_one_scale_per_channel():
     h._h = None
     with pytest.raises(ValueError):
         h.features(0, 3, 0, scales=[1.0, 2.0])
+
+
+@pytest.mark.parametrize("grid,dim,program,bad", [
+    ("Nx = 96\nNy = 64\nNz = 64", 2, "tara2dHydSer", "Nx = 96"),
+    ("Nx = 64\nNy = 8192\nNz = 64", 2, "tara2dHydSer", "Ny = 8192"),
+    ("Nx = 64\nNy = 64\nNz = 384", 3, "tara3dMHDOMP", "Nz = 384"),
+])
+def test_driver_refuses_unsupported_grids(tmp_path, grid, dim, program, bad):
+    """The reference's input.ini may name any Nx, Ny, Nz (src/main2csh.f95:35-38);
+    the `tara` driver refuses sizes its kernels do not take before touching a
+    GPU, and says which sizes it takes."""
+    import tara_gb300 as tg
+
+    ini = (f"[dimension]\ndim = {dim}\n[architecture]\narch = cpu\n[parallel]\n"
+           f"mode = {'serial' if dim == 2 else 'openmp'}\n[type]\ndomain = {'hydro' if dim == 2 else 'mhd'}\n"
+           f"[problem]\nhydrotype = bare\n[particle]\nNp = 0\n[grid]\n{grid}\n"
+           "[length]\nLx = 2.0d0\nLy = 2.0d0\nLz = 2.0d0\n[resistivity]\nnu = 0.01d0\neta = 0.0d0\n"
+           "[time]\ntime_min = 0.0d0\ntime_max = 1.0d0\ndt = 0.001d0\n"
+           "[initialProfile]\nW0 = 25.0d0\nm0 = 2.0d0\nd = 0.0234375d0\n")
+    (tmp_path / "input.ini").write_text(ini)
+    rc = tg.lib().tara_run_ini(str(tmp_path / "input.ini").encode(), str(tmp_path / "out").encode(), 1)
+    code, msg = tg.last_error()
+    assert rc == tg.TARA_ERR_ARGS and code == tg.TARA_ERR_ARGS
+    assert program in msg and bad in msg and "powers of two" in msg
