@@ -46,7 +46,7 @@ def _cfg(nx, ny):
     return c
 
 
-@pytest.mark.parametrize("nx,ny", [(100, 64), (64, 8), (4096, 64), (0, 0), (64, 3)])
+@pytest.mark.parametrize("nx,ny", [(100, 64), (64, 8), (8192, 64), (0, 0), (64, 3)])
 def test_create_rejects_bad_sizes(nx, ny):
     h = ctypes.c_void_p()
     rc = tg.lib().tara2d_create(ctypes.byref(_cfg(nx, ny)), ctypes.byref(h))
