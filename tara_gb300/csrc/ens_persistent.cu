@@ -85,7 +85,8 @@ __device__ __forceinline__ void ens_item(const EnsGroupDev& G, int pass, int mod
     col_inverse_cta<float, N, VA, R>(t % G.ta, t / G.ta, run, win, (float2*)G.u, G.g, G.p,
                                      (const float2*)G.twy);
   } else if (pass == 1) {
-    row_nl_cta<float, N, VB, R>(rem % G.tb, rem / G.tb, (const float2*)G.u, (float2*)G.nl, G.g,
+    // coherent loads: this launch wrote u in the previous phase
+    row_nl_cta<float, N, VB, R, false>(rem % G.tb, rem / G.tb, (const float2*)G.u, (float2*)G.nl, G.g,
                                 (const float2*)G.twx);
   } else {
     StepBufs sb;

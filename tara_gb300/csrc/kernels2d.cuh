@@ -173,7 +173,8 @@ template <typename T, int N, int V = 0> struct RowCfg {
 // persistent kernel can run it for any run and tile): tile bx, field pair
 // `pair`, run `run`.
 template <typename T, int N, int V, int R>
-__device__ __forceinline__ void col_inverse_cta(int bx, int pair, int run, const double2* __restrict__ win,
+__device__ __forceinline__ void col_inverse_cta(unsigned bx, unsigned pair, unsigned run,
+                                                const double2* __restrict__ win,
                                                 typename cplx_of<T>::type* __restrict__ u, const Grid2D& g,
                                                 const RhsParams& p,
                                                 const typename cplx_of<T>::type* __restrict__ tw) {
@@ -285,13 +286,37 @@ __global__ void __launch_bounds__(ColCfg<T, N, V>::THREADS_A,
 // Z[k] = A[k] + i B[k] (k <= N/2), Z[N-k] = conj(A[k]) + i conj(B[k]), with the
 // imaginary parts of the k = 0 and k = N/2 bins dropped first.
 // blockIdx.y = run of a batch.
+// Load of a spectral value through the non-coherent (read-only) path, for data
+// that no thread of the running kernel writes.
+template <typename C>
+__device__ __forceinline__ C ldg_c(const C* p) {
+  return __ldg(p);
+}
+__device__ __forceinline__ df64c ldg_c(const df64c* p) {
+  const float4 v = __ldg(reinterpret_cast<const float4*>(p));
+  df64c w;
+  w.x = df64(v.x, v.y);
+  w.y = df64(v.z, v.w);
+  return w;
+}
+
 // Hermitian extension of the half rows A, B (two spectra of one ky row) into
-// slot entry k of Z = A + i B (see above).
-template <typename T, int N, typename C>
+// slot entry k of Z = A + i B (see above).  NC: read through the non-coherent
+// path -- the per-pass row kernel does (a plain load there, once the body sat
+// in a device function, cost the FP32 512^2 row pass 40 %); the persistent
+// ensemble kernel must not, since it wrote the rows itself earlier in the launch.
+template <typename T, int N, bool NC, typename C>
 __device__ __forceinline__ C row_pair_entry(const C* __restrict__ fa, const C* __restrict__ fb, int k) {
   constexpr int H = N / 2;
   const int kk = k <= H ? k : N - k;
-  C A = fa[kk], B = fb[kk];
+  C A, B;
+  if constexpr (NC) {
+    A = ldg_c(fa + kk);
+    B = ldg_c(fb + kk);
+  } else {
+    A = fa[kk];
+    B = fb[kk];
+  }
   if (kk == 0 || kk == H) {
     A.y = T(0);
     B.y = T(0);
@@ -299,9 +324,12 @@ __device__ __forceinline__ C row_pair_entry(const C* __restrict__ fa, const C* _
   return (k <= H) ? mkc<T>(A.x - B.y, A.y + B.x) : mkc<T>(A.x + B.y, -A.y + B.x);
 }
 
-// The CTA body: row-pair tile bx of run `run`.
-template <typename T, int N, int V, int R>
-__device__ __forceinline__ void row_nl_cta(int bx, int run, const typename cplx_of<T>::type* __restrict__ u,
+// The CTA body: row-pair tile bx of run `run` (NC: see row_pair_entry).  The
+// block coordinates are unsigned, as blockIdx is: with int coordinates the
+// 64-bit address arithmetic took 84 instead of 80 registers in the FP32 row
+// tile, which then fitted two CTAs per SM instead of three.
+template <typename T, int N, int V, int R, bool NC = true>
+__device__ __forceinline__ void row_nl_cta(unsigned bx, unsigned run, const typename cplx_of<T>::type* __restrict__ u,
                                            typename cplx_of<T>::type* __restrict__ nl, const Grid2D& g,
                                            const typename cplx_of<T>::type* __restrict__ tw) {
   typedef typename cplx_of<T>::type C;
@@ -325,7 +353,7 @@ __device__ __forceinline__ void row_nl_cta(int bx, int run, const typename cplx_
         C z = mkc<T>(T(0), T(0));
         if (y < g.ny) {
           const C* fa = u + (size_t)(2 * s) * fsz + (size_t)y * g.pitch;
-          z = row_pair_entry<T, N>(fa, fa + fsz, k);
+          z = row_pair_entry<T, N, NC>(fa, fa + fsz, k);
         }
         sm[s * SL + k] = z;
       }
@@ -358,7 +386,7 @@ __device__ __forceinline__ void row_nl_cta(int bx, int run, const typename cplx_
       C z = mkc<T>(T(0), T(0));
       if (y < g.ny) {
         const C* fa = u + (size_t)(2 * (s & 1)) * fsz + (size_t)y * g.pitch;
-        z = row_pair_entry<T, N>(fa, fa + fsz, k);
+        z = row_pair_entry<T, N, NC>(fa, fa + fsz, k);
       }
       sm[sl * SL + k] = z;
     }
@@ -417,7 +445,7 @@ struct StepBufs {
 // for two CTAs per SM (64 registers, 90 bytes of spill): its warps wait on the
 // state loads, and a second CTA hides them (115 -> 103 us at 2048^2).
 template <typename T, int N, int V, int R>
-__device__ __forceinline__ void col_forward_cta(int bx, int run, const typename cplx_of<T>::type* __restrict__ nl,
+__device__ __forceinline__ void col_forward_cta(unsigned bx, unsigned run, const typename cplx_of<T>::type* __restrict__ nl,
                                                 StepBufs sb, const Grid2D& g, const RhsParams& p, int mode,
                                                 const typename cplx_of<T>::type* __restrict__ tw) {
   typedef typename cplx_of<T>::type C;

@@ -821,7 +821,11 @@ int tara2d_autotune(tara2d* h, int trial_steps, int* variants3, double* ms24) {
   double ms[kCandidates][3];
   for (int c = 0; c < kCandidates; ++c)
     for (int k = 0; k < 3; ++k) ms[c][k] = 0.0;
-  int best1[3] = {0, 0, 0};
+  int dflt[3] = {0, 0, 0};  // the first candidate each kernel has (variant 0 may not fit a CTA)
+  for (int k = 0; k < 3; ++k)
+    for (int c = kCandidates - 1; c >= 0; --c)
+      if (candidate_ok(h, k, c)) dflt[k] = c;
+  int best1[3] = {dflt[0], dflt[1], dflt[2]};
   auto timed = [&](double* t) {
     int r = tara2d_step(h, 1);
     int cnt[3];
@@ -834,7 +838,7 @@ int tara2d_autotune(tara2d* h, int trial_steps, int* variants3, double* ms24) {
     bool any = false;
     for (int k = 0; k < 3; ++k) {
       const bool ok = candidate_ok(h, k, c);
-      h->var[k] = ok ? c : 0;
+      h->var[k] = ok ? c : dflt[k];
       any |= ok;
     }
     if (!any) continue;
@@ -846,7 +850,7 @@ int tara2d_autotune(tara2d* h, int trial_steps, int* variants3, double* ms24) {
   }
   if (!rc)
     for (int k = 0; k < 3; ++k)
-      for (int c = 1; c < kCandidates; ++c)
+      for (int c = 0; c < kCandidates; ++c)
         if (candidate_ok(h, k, c) && ms[c][k] < ms[best1[k]][k]) best1[k] = c;
   double ctx[3][kCandidates];
   for (int k = 0; k < 3 && !rc; ++k)
@@ -860,8 +864,8 @@ int tara2d_autotune(tara2d* h, int trial_steps, int* variants3, double* ms24) {
     }
   if (!rc)
     for (int k = 0; k < 3; ++k) {
-      int best = 0;
-      for (int c = 1; c < kCandidates; ++c)
+      int best = dflt[k];
+      for (int c = 0; c < kCandidates; ++c)
         if (candidate_ok(h, k, c) && ctx[k][c] < ctx[k][best]) best = c;
       h->var[k] = best;
       if (variants3) variants3[k] = best;
