@@ -149,12 +149,10 @@ template <typename T, int N, int V = 0> struct RowCfg {
   // four FP64 slots of 4096 points (256 KB) do not fit a CTA: variant 3 only
   static constexpr bool VALID = THREADS <= 1024 && SMEM <= kMaxSmem;
   // CTAs per SM the row kernel asks for: two for variant 3 and the 512-thread
-  // FP32 tiles, three for the 256-thread FP32 tiles (at 84 registers a
-  // 256-thread FP32 row CTA fitted only twice per SM, and the 512^2 row pass
-  // took 670 instead of 364 us) -- as far as shared memory allows
-  static constexpr int MINB0 = (V == 3 || (sizeof(T) == 4 && THREADS >= 512)) ? 2
-                               : (sizeof(T) == 4 && THREADS == 256)            ? 3
-                                                                               : 1;
+  // FP32 tiles -- as far as shared memory allows.  (Asking three of the
+  // 256-thread FP32 tiles held them to 80 registers but scheduled them worse:
+  // the 512^2 row pass took 503 instead of 364 us.)
+  static constexpr int MINB0 = (V == 3 || (sizeof(T) == 4 && THREADS >= 512)) ? 2 : 1;
   static constexpr int MINB = MINB0 * SMEM <= kMaxSmem ? MINB0 : 1;
 };
 
@@ -419,12 +417,70 @@ __device__ __forceinline__ void row_nl_cta(unsigned bx, unsigned run, const type
   }
 }
 
+// The per-pass row kernel.  Variant 3 runs the CTA body above; variants 0-2
+// spell the same body out in the kernel itself: compiled through the device
+// function, the FP32 256-thread tile at 512 points ran 500 instead of 364 us
+// (same arithmetic and register count, a different schedule).
 template <typename T, int N, int V, int R = 4>
 __global__ void __launch_bounds__(RowCfg<T, N, V>::THREADS, RowCfg<T, N, V>::MINB)
     k_row_nl(const typename cplx_of<T>::type* __restrict__ u,
              typename cplx_of<T>::type* __restrict__ nl, Grid2D g,
              const typename cplx_of<T>::type* __restrict__ tw) {
-  row_nl_cta<T, N, V, R>(blockIdx.x, blockIdx.y, u, nl, g, tw);
+  if constexpr (V == 3) {
+    row_nl_cta<T, N, V, R>(blockIdx.x, blockIdx.y, u, nl, g, tw);
+  } else {
+    typedef typename cplx_of<T>::type C;
+    typedef RowCfg<T, N, V> RC;
+    constexpr int G = RC::G, H = N / 2, RP = RC::RP, SL = RC::SL;
+    extern __shared__ __align__(16) unsigned char smraw[];
+    C* sm = reinterpret_cast<C*>(smraw);  // [RP][4][N]
+    const int tid = threadIdx.x;
+    const int slot = tid / G, lane = tid % G;
+    const int y_base = blockIdx.x * (2 * RP);
+    const size_t fsz = (size_t)g.ny * g.pitch;
+    u += blockIdx.y * 4 * fsz;
+    nl += blockIdx.y * fsz;
+    TARA_ELEM_LOOP(e, RP * 4 * N, RC::THREADS) {
+      const int k = e % N, sl = e / N;
+      const int pp = sl >> 2, s = sl & 3;
+      const int y = y_base + 2 * pp + (s >> 1);
+      C z = mkc<T>(T(0), T(0));
+      if (y < g.ny) {
+        const C* fa = u + (size_t)(2 * (s & 1)) * fsz + (size_t)y * g.pitch;
+        const C* fb = fa + fsz;
+        const int kk = k <= H ? k : N - k;
+        C A = fa[kk], B = fb[kk];
+        if (kk == 0 || kk == H) {
+          A.y = T(0);
+          B.y = T(0);
+        }
+        z = (k <= H) ? mkc<T>(A.x - B.y, A.y + B.x) : mkc<T>(A.x + B.y, -A.y + B.x);
+      }
+      sm[sl * SL + k] = z;
+    }
+    __syncthreads();
+    fft_path<T, N, true, G, R>(sm + slot * SL, lane, true, tw);
+    TARA_ELEM_LOOP(e, RP * N, RC::THREADS) {
+      const int x = e % N, pp = e / N;
+      C* b = sm + (size_t)pp * 4 * SL;
+      const C c1a = b[x], c2a = b[SL + x], c1b = b[2 * SL + x], c2b = b[3 * SL + x];
+      const T na = fma(c1a.x, c2a.x, c1a.y * c2a.y);
+      const T nb = fma(c1b.x, c2b.x, c1b.y * c2b.y);
+      b[x] = mkc<T>(na, nb);
+    }
+    __syncthreads();
+    fft_path<T, N, false, 4 * G, R>(sm + (tid / (4 * G)) * 4 * SL, tid % (4 * G), true, tw);
+    TARA_ELEM_LOOP(e, RP * (H + 1), RC::THREADS) {
+      const int k = e % (H + 1), pp = e / (H + 1);
+      const int ya = y_base + 2 * pp;
+      if (ya < g.ny) {
+        const C* b = sm + (size_t)pp * 4 * SL;
+        const C z = b[k], m = b[(N - k) & (N - 1)];
+        nl[(size_t)ya * g.pitch + k] = mkc<T>(z.x + m.x, z.y - m.y);
+        nl[(size_t)(ya + 1) * g.pitch + k] = mkc<T>(z.y + m.y, -(z.x - m.x));
+      }
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------
