@@ -20,7 +20,7 @@
  *    many steps per call, plus batched ensembles (tara_ens_*).  These return an
  *    int status (TARA_OK = 0).
  *
- * Grid sizes: Nx and Ny powers of two from 16 to 4096 (the 2D paths; 3D: 16 to 256).
+ * Grid sizes: Nx and Ny powers of two from 16 to 4096 (the 2D paths; 3D: 16 to 512).
  */
 #ifndef TARA_H
 #define TARA_H
@@ -263,7 +263,7 @@ int tara_ens_launches_per_step(tara_ens* e);
  * (Nh,Ny,Nz).  Lx, Ly, Lz, mu, eta, CS are read from the caller's common block
  * /comm/ (comm_), wavenumbers use the pi argument; viscosity and resistivity are
  * the reference's hard-coded 1/450.  The forcing the reference transforms but
- * never uses is not computed.  Sizes: powers of two in [16, 256]. */
+ * never uses is not computed.  Sizes: powers of two in [16, 512]. */
 void derive3com_(const int* Nx, const int* Ny, const int* Nz, const int* Nh, const double* pi,
                  const double* time, const double* rho_k, const double* rho_ux_k,
                  const double* rho_uy_k, const double* rho_uz_k, const double* E_k,
@@ -414,7 +414,7 @@ int tara_com2d_real_fields(tara_com2d* h, double* rho, double* ux, double* uy, d
                            double* Bx, double* By);
 
 typedef struct tara3d_config {
-  int nx, ny, nz;      /* powers of two, 16..256 */
+  int nx, ny, nz;      /* powers of two, 16..512 */
   int defined;         /* 0: k^2 f / 450 as the reference; 1: nu_u k^2 u and eta_b k^2 B */
   double kpi;          /* the pi of kx = 2*pi*(i-1)/Lx */
   double lx, ly, lz;   /* box lengths (the reference driver uses Lx = Lx_ini * pi) */

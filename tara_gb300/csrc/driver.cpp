@@ -86,10 +86,10 @@ std::string fort_name(const std::string& dir, long unit) {
 int fail_rc() { return tara_last_error() ? tara_last_error() : TARA_ERR_CUDA; }
 
 // The reference reads any Nx, Ny (, Nz) (src/main2csh.f95:35-38) and FFTW takes
-// any length; these kernels take powers of two, 16 to 4096 in 2D and 16 to 256
+// any length; these kernels take powers of two, 16 to 4096 in 2D and 16 to 512
 // in 3D.  Refuse anything else before allocating, naming the supported set.
 int check_grid(const char* program, int dims, int nx, int ny, int nz) {
-  const int hi = dims == 2 ? 4096 : 256;
+  const int hi = dims == 2 ? 4096 : 512;
   const int n[3] = {nx, ny, nz};
   const char* name[3] = {"Nx", "Ny", "Nz"};
   for (int d = 0; d < dims; ++d)

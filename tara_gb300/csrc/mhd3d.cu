@@ -27,7 +27,8 @@
 
 namespace tara {
 
-constexpr int kMax3D = 256;
+// Largest 3D length: 512^3 holds about 85 GB of FP64 state and work fields.
+constexpr int kMax3D = 512;
 
 // ---------------------------------------------------------------------------
 // pointwise kernels
@@ -284,7 +285,8 @@ static cudaError_t allow_smem3(K kernel, int bytes) {
     case 64: { constexpr int N = 64; CALL; } break;        \
     case 128: { constexpr int N = 128; CALL; } break;      \
     case 256: { constexpr int N = 256; CALL; } break;      \
-    default: return set_error(TARA_ERR_ARGS, "3D sizes must be powers of two in [16, 256]"); \
+    case 512: { constexpr int N = 512; CALL; } break;      \
+    default: return set_error(TARA_ERR_ARGS, "3D sizes must be powers of two in [16, 512]"); \
   }
 
 template <int N, bool INV>
@@ -433,7 +435,8 @@ int r2c3(tara3d* h, const double* in, double2* out, int nf) {
     case 64: rc = rows_r2c_n<64>(in, out, h->ny * h->nz, h->rpitch, h->pitch, h->rfs, h->fs, nf, (const double2*)h->twx, h->stream); break;
     case 128: rc = rows_r2c_n<128>(in, out, h->ny * h->nz, h->rpitch, h->pitch, h->rfs, h->fs, nf, (const double2*)h->twx, h->stream); break;
     case 256: rc = rows_r2c_n<256>(in, out, h->ny * h->nz, h->rpitch, h->pitch, h->rfs, h->fs, nf, (const double2*)h->twx, h->stream); break;
-    default: return set_error(TARA_ERR_ARGS, "3D sizes must be powers of two in [16, 256]");
+    case 512: rc = rows_r2c_n<512>(in, out, h->ny * h->nz, h->rpitch, h->pitch, h->rfs, h->fs, nf, (const double2*)h->twx, h->stream); break;
+    default: return set_error(TARA_ERR_ARGS, "3D sizes must be powers of two in [16, 512]");
   }
   if (rc) return rc;
   if ((rc = lines(h->ny, false, out, out, h->nh, pitch, ny * pitch, h->nz, h->fs, h->fs, nf, h->twy,
@@ -580,7 +583,7 @@ int tara3d_create(const tara3d_config* cfg, tara3d** out) {
   *out = nullptr;
   auto ok = [](int n) { return n >= 16 && n <= kMax3D && (n & (n - 1)) == 0; };
   if (!ok(cfg->nx) || !ok(cfg->ny) || !ok(cfg->nz))
-    return set_error(TARA_ERR_ARGS, "3D sizes must be powers of two in [16, 256]");
+    return set_error(TARA_ERR_ARGS, "3D sizes must be powers of two in [16, 512]");
   if (!(cfg->lx > 0 && cfg->ly > 0 && cfg->lz > 0 && cfg->kpi > 0))
     return set_error(TARA_ERR_ARGS, "box lengths and kpi must be positive");
   tara3d* h = new tara3d();
@@ -825,7 +828,7 @@ tara3d* ctx3(int nx, int ny, int nz, double pi) {
 bool dims3(const int* Nx, const int* Ny, const int* Nz, const int* Nh) {
   auto ok = [](int n) { return n >= 16 && n <= kMax3D && (n & (n - 1)) == 0; };
   if (!Nx || !Ny || !Nz || !Nh || !ok(*Nx) || !ok(*Ny) || !ok(*Nz) || *Nh != *Nx / 2 + 1) {
-    set_error(TARA_ERR_ARGS, "Nx, Ny, Nz must be powers of two in [16, 256] and Nh = Nx/2+1");
+    set_error(TARA_ERR_ARGS, "Nx, Ny, Nz must be powers of two in [16, 512] and Nh = Nx/2+1");
     return false;
   }
   return true;

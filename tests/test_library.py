@@ -161,6 +161,7 @@ def test_features_need_one_scale_per_channel():
     ("Nx = 96\nNy = 64\nNz = 64", 2, "tara2dHydSer", "Nx = 96"),
     ("Nx = 64\nNy = 8192\nNz = 64", 2, "tara2dHydSer", "Ny = 8192"),
     ("Nx = 64\nNy = 64\nNz = 384", 3, "tara3dMHDOMP", "Nz = 384"),
+    ("Nx = 1024\nNy = 64\nNz = 64", 3, "tara3dMHDOMP", "Nx = 1024"),
 ])
 def test_driver_refuses_unsupported_grids(tmp_path, grid, dim, program, bad):
     """The reference's input.ini may name any Nx, Ny, Nz (src/main2csh.f95:35-38);
