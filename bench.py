@@ -197,17 +197,25 @@ def run_reference(args) -> None:
     print(json.dumps(line), flush=True)
 
 
-def fft_fp64_inst(n: int) -> int:
+def fft_fp64_inst(n: int, radix8: bool = False) -> int:
     """FP64 instructions of one length-n transform of fft.cuh, counted from its
-    butterflies: an untwiddled radix-4 first stage (16 adds per butterfly),
-    twiddled radix-4 stages (24 per butterfly) and, for odd log2 n, a twiddled
-    radix-2 stage (6 per butterfly)."""
+    butterflies.  Radix-4 path: an untwiddled radix-4 first stage (16 adds per
+    butterfly), twiddled radix-4 stages (24 per butterfly) and, for odd log2 n,
+    a twiddled radix-2 stage (6 per butterfly).  Radix-8 path: an untwiddled
+    radix-8 first stage (52 per butterfly), twiddled radix-8 stages (72), then
+    zero to two twiddled radix-4 stages (24; untwiddled, 16, when they come first)."""
     lg = n.bit_length() - 1
     q = n // 4
-    return q * 16 + q * 24 * (lg // 2 - 1) + ((n // 2) * 6 if lg % 2 else 0)
+    if not radix8:
+        return q * 16 + q * 24 * (lg // 2 - 1) + ((n // 2) * 6 if lg % 2 else 0)
+    s8 = lg // 3 - 1 if (lg % 3 == 1 and lg >= 4) else lg // 3
+    s4 = 2 if lg % 3 == 1 else 1 if lg % 3 == 2 else 0
+    b8 = n // 8
+    inst = (b8 * 52 + b8 * 72 * (s8 - 1)) if s8 else 0
+    return inst + sum(q * (16 if (s8 == 0 and i == 0) else 24) for i in range(s4))
 
 
-def fp64_pipe(n: int, per_kernel_ms: dict, sm_mhz, probe_tinst) -> dict:
+def fp64_pipe(n: int, per_kernel_ms: dict, sm_mhz, probe_tinst, variants=(0, 0, 0)) -> dict:
     """FP64-pipe roofline of the three kernels at n x n: the transforms' FP64
     instructions per launch (element work excluded, so the fractions are lower
     bounds) over the measured launch time, against the nominal rate (2 FP64
@@ -218,8 +226,8 @@ def fp64_pipe(n: int, per_kernel_ms: dict, sm_mhz, probe_tinst) -> dict:
     import torch
     nh = n // 2 + 1
     live = math.ceil((n + n) / 2.0 / 3.0)  # columns below the 2/3 cut (integer wavenumbers)
-    f = fft_fp64_inst(n)
-    inst = {"k_col_inverse": 4 * nh * f, "k_row_nl": (n // 2) * 5 * f, "k_col_forward": live * f}
+    f = [fft_fp64_inst(n, bool(v & 4)) for v in variants]  # per kernel: its radix path
+    inst = {"k_col_inverse": 4 * nh * f[0], "k_row_nl": (n // 2) * 5 * f[1], "k_col_forward": live * f[2]}
     sms = torch.cuda.get_device_properties(0).multi_processor_count
     nominal = 2.0 * sms * (sm_mhz or 2070.0) * 1e6
     ach = {k: inst[k] / (per_kernel_ms[k] * 1e-3) for k in inst if k in per_kernel_ms}
@@ -313,6 +321,21 @@ def run_ours(args) -> None:
         # the reference's own 2D path runs on one thread (no OpenMP, no FFTW threads)
         one = cpu_baseline(n, budget_s=min(args.cpu_budget, 8.0), threads=1)
         cpu["single_thread"] = {"value": one["value"], "cores": one["cores"], "sample": one["sample"]}
+    fp64 = (fp64_pipe(n, {k: v["ms"] / max(1, v["launches"]) for k, v in ks.items()},
+                      (clocks or {}).get("sm_mhz"), dfma_rate, tuned["variants"])
+            if prec == tg.PREC_FP64 else None)
+    roof64 = None
+    if fp64:
+        # the FP64-pipe roofline beside the HBM one: the transforms' algorithmic
+        # FP64 instructions (element work excluded) over the measured DFMA rate,
+        # for the dominant kernel and for the whole RK4 step (4 RHS evaluations)
+        pk = fp64["measured_dfma_inst_per_s"] or fp64["nominal_inst_per_s"]
+        step_inst = 4 * sum(fp64["inst_per_launch"].values())
+        step_rate = step_inst / (el_ms / args.steps * 1e-3)
+        roof64 = {"bound": "fp64", "kernel": dom, "achieved": fp64["achieved_inst_per_s"][dom], "peak": pk,
+                  "peak_kind": "measured DFMA rate" if fp64["measured_dfma_inst_per_s"] else "nominal",
+                  "unit": "FP64 inst/s", "frac": fp64["achieved_inst_per_s"][dom] / pk,
+                  "step": {"inst_per_step": step_inst, "achieved": step_rate, "frac": step_rate / pk}}
     line = {
         "metric": {tg.PREC_FP64: METRIC, tg.PREC_FP32: METRIC.replace("FP64", "FP32 form"),
                    tg.PREC_DF64: METRIC.replace("FP64", "double-float form")}[prec],
@@ -338,8 +361,8 @@ def run_ours(args) -> None:
                                                 if prec == tg.PREC_FP64 else None),
                      "per_kernel_ms": {k: v["ms"] / max(1, v["launches"]) for k, v in ks.items()}},
         "clocks": clocks,
-        "fp64_pipe": (fp64_pipe(n, {k: v["ms"] / max(1, v["launches"]) for k, v in ks.items()},
-                                (clocks or {}).get("sm_mhz"), dfma_rate) if prec == tg.PREC_FP64 else None),
+        "fp64_pipe": fp64,
+        "roofline_fp64": roof64,
         "tile_variants": tuned["variants"],
         "autotune_ms": tuned["ms"],  # per-launch ms in context: configurations 0-7 (rows) x the three kernels
         "diag": {"energy": e, "enstrophy": z},
