@@ -368,8 +368,33 @@ def run_ours(args) -> None:
         "diag": {"energy": e, "enstrophy": z},
         "cpu_baseline": cpu,
     }
+    if ws == 1 and not args.no_side:
+        line["other_configs"] = side_workloads(args)
     print(json.dumps(line), flush=True)
     s.close()
+
+
+def side_workloads(args) -> dict:
+    """Short measurements of the other benchmark configurations in the same run
+    (one GPU): the 384-run ensemble (FP32 form, RK4; autotuned form and tiles),
+    the 128^3 3D MHD AB2 step, and the closure network's training step.  Each
+    reports its own metric; a failure is recorded, not raised."""
+    import copy
+
+    out = {}
+    for name, fn in (("ensemble_384_runs", run_ensemble), ("mhd3d_128", run_mhd3d),
+                     ("fno_train_batch32", run_fno_train)):
+        a = copy.copy(args)
+        a.steps, a.warmup, a.ens_error_steps, a.ens_form = 10, 3, 0, "auto"
+        try:
+            ln = fn(a, emit=False)
+            out[name] = {k: ln[k] for k in ("metric", "value", "unit", "ms_per_step", "dtype") if k in ln}
+            for k in ("form", "persistent", "form_ms_per_step", "radix"):
+                if k in ln:
+                    out[name][k] = ln[k]
+        except Exception as exc:  # reported beside the headline, never hides it
+            out[name] = {"error": f"{type(exc).__name__}: {exc}"}
+    return out
 
 
 def timed_on_stream(stream_ptr: int, fn):
@@ -397,7 +422,7 @@ def ensemble_runs(per_rank: int, world_size: int = 1) -> list[tuple[int, float, 
     return [(n, float(k0[r]), 4000 + r) for r, n in enumerate([128] * per + [256] * per + [512] * per)]
 
 
-def run_ensemble(args) -> None:
+def run_ensemble(args, emit: bool = True) -> dict | None:
     """Ensemble of independent 2D runs, RK4, nu = 1e-3, dt = 1e-4, FP32
     transforms and products with FP64 state: per rank 3 x ens_runs_per_size runs
     (default 128 each at 128^2, 256^2, 512^2; 384 in all on one GPU).  The global
@@ -468,8 +493,10 @@ def run_ensemble(args) -> None:
                                      "per_size_max": {str(n): max(x for (m, _, _), x in zip(runs, errs) if m == n)
                                                       for n in (128, 256, 512)}}
     if rank == 0:
-        print(json.dumps(line), flush=True)
+        if emit:
+            print(json.dumps(line), flush=True)
     e.close()
+    return line if rank == 0 else None
 
 
 def run_coh2d(args) -> None:
@@ -591,7 +618,7 @@ def run_coh2d(args) -> None:
     print(json.dumps(line), flush=True)
 
 
-def run_mhd3d(args) -> None:
+def run_mhd3d(args, emit: bool = True) -> dict:
     """128^3 compressible MHD, FP64, AB2, nu = eta = 0.01, dt = 1e-3."""
     import torch
 
@@ -613,8 +640,10 @@ def run_mhd3d(args) -> None:
             "config": {"workload": "3D MHD 128^3, nu=eta=0.01, dt=1e-3, AB2, 20 transforms/step"},
             "gpu_launches": None, "diag": {"pressure": d[0], "kinetic": d[1], "total_E": d[2],
                                            "magnetic": d[3]}}
-    print(json.dumps(line), flush=True)
+    if emit:
+        print(json.dumps(line), flush=True)
     s.close()
+    return line
 
 
 def run_closure(args) -> None:
@@ -706,7 +735,7 @@ def run_cufft(args) -> None:
     print(json.dumps(line), flush=True)
 
 
-def run_fno_train(args) -> None:
+def run_fno_train(args, emit: bool = True) -> dict:
     """Training step of the closure network: 128^2, 6 input channels, 4 Fourier
     layers, 32 channels, 16 modes per axis, projection 128, batch 32, BF16
     tensor-core GEMMs with FP32 accumulation, Adam (lr 1e-4) on seeded random
@@ -736,8 +765,10 @@ def run_fno_train(args) -> None:
             "vs_baseline": None, "dtype": "bf16 GEMM operands / f32 accumulation and activations",
             "data": "synthetic (seeded normal inputs and targets)",
             "config": {"workload": "FNO train step", "batch": B, "params": net.num_params}}
-    print(json.dumps(line), flush=True)
+    if emit:
+        print(json.dumps(line), flush=True)
     net.close()
+    return line
 
 
 def run_closure_step(args) -> None:
@@ -783,6 +814,8 @@ def main() -> None:
     ap.add_argument("--n", type=int, default=2048)
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-side", action="store_true",
+                    help="skip the short runs of the other benchmark configurations")
     ap.add_argument("--workload", default="rk4-2048",
                     choices=["rk4-2048", "ensemble", "mhd3d", "closure", "fno-train", "closure-step", "cufft",
                              "coh2d", "com2d"],
