@@ -170,36 +170,37 @@ def test_gpu_128_cubed_rhs_and_steps(oracle):
 
 
 @gpu
-def test_gpu_512_cubed_rhs_equals_64_cubed_on_shared_modes(oracle):
-    """512^3 (the largest 3D grid here, about 85 GB on the GPU).  The
-    Orszag-Tang-type state holds modes |k| <= 4 only, and every product in the
-    right-hand side is at most cubic, so its RHS lives on |k| <= 12 -- inside
-    the dealiasing sphere of 64^3 and of 512^3.  The two grids must then give
-    the same RHS on those modes (spectra divided by N^3), and the 64^3 one
-    equals the oracle's."""
+@pytest.mark.parametrize("shape", [(512, 16, 16), (16, 512, 16), (16, 16, 512)])
+def test_gpu_512_lines_rhs_vs_oracle(oracle, shape):
+    """512-point transforms along each axis (the rows along x, the strided
+    line passes along y and z) in a full right-hand side against the oracle,
+    from the Orszag-Tang-type state (kmax 4 fits every axis of 16)."""
     tg = _tg()
     p = orc.mhd_params(defined=1, nu_u=0.01, eta_b=0.01)
-    kw = dict(defined=1, nu_u=0.01, eta_b=0.01, dt=1e-3)
-    with tg.Solver3D(64, **kw) as s:
+    with tg.Solver3D(*shape, defined=1, nu_u=0.01, eta_b=0.01, dt=1e-3) as s:
         s.init_orszag_tang(0.01, 4, 3)
-        st64 = s.get_state()
-        d64 = s.rhs()
-    assert rel_l2(d64, oracle.derive3com(st64, p)) < 1e-11
-    kz = np.r_[0:13, -12:0]
-    with tg.Solver3D(512, **kw) as s:
+        st = s.get_state()
+        d = s.rhs()
+    assert rel_l2(st, oracle.ic3d_ot(*shape, amp=0.01, kmax=4, seed=3)) < 1e-13
+    assert rel_l2(d, oracle.derive3com(st, p)) < 1e-11
+
+
+@gpu
+def test_gpu_512_cubed_steps():
+    """512^3 (the largest 3D grid here, about 85 GB on the GPU): the
+    benchmark's initial state, then AB2 steps stay finite and keep the mean
+    density (the k = 0 mode of d rho/dt vanishes), and the magnetic and
+    kinetic energies move by what a few steps of nu = eta = 0.01 allow."""
+    tg = _tg()
+    with tg.Solver3D(512, defined=1, nu_u=0.01, eta_b=0.01, dt=1e-3) as s:
         s.init_orszag_tang(0.01, 4, 3)
-        d512 = s.rhs()  # 8.6 GB on the host
-        b = d512[:, kz][:, :, kz][:, :, :, :13] / 512.0**3
-        top = np.abs(b).max()
-        # a slab of kz far outside |k| <= 12: round-off only
-        outside = np.abs(d512[:, 100:110]).max() / 512.0**3
-        del d512
-        s.step(2)
+        d0 = s.diag()
+        s.step(3)
         s.synchronize()
+        d1 = s.diag()
         st = s.get_state()
         assert np.all(np.isfinite(st[:, ::7, ::7, ::7]))
-        assert abs(st[0, 0, 0, 0] / 512.0**3 - 1.0) < 1e-12  # mean density kept
+        assert abs(st[0, 0, 0, 0] / 512.0**3 - 1.0) < 1e-12
         del st
-    a = d64[:, kz][:, :, kz][:, :, :, :13] / 64.0**3
-    assert rel_l2(b, a) < 1e-11
-    assert outside < 1e-12 * top
+    assert all(np.isfinite(d1))
+    assert abs(d1[1] - d0[1]) < 0.05 * d0[1] and abs(d1[3] - d0[3]) < 0.05 * d0[3]
