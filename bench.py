@@ -759,12 +759,20 @@ def run_fno_train(args, emit: bool = True) -> dict:
             net.train_step(x.data_ptr(), t.data_ptr(), B, lr=1e-4, want_loss=False)
 
     ms = timed_on_stream(net.stream, steps)
+    # the same step with the channel GEMMs on tcgen05 (accumulators in tensor memory)
+    net.set_mode(tg.FNO_BF16_TMEM)
+    for _ in range(args.warmup):
+        net.train_step(x.data_ptr(), t.data_ptr(), B, lr=1e-4, want_loss=False)
+    ms_tc = timed_on_stream(net.stream, steps)
+    net.train_step(x.data_ptr(), t.data_ptr(), B, lr=0.0)  # reports a tensor-memory wait that gave up
+    net.set_mode(tg.FNO_BF16)
     line = {"metric": "closure-network training samples/s (128^2, 6->32 ch, 4 layers, 16 modes, batch 32)",
             "value": B * args.steps / (ms * 1e-3), "unit": "samples/s", "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
             "vs_baseline": None, "dtype": "bf16 GEMM operands / f32 accumulation and activations",
             "data": "synthetic (seeded normal inputs and targets)",
-            "config": {"workload": "FNO train step", "batch": B, "params": net.num_params}}
+            "config": {"workload": "FNO train step", "batch": B, "params": net.num_params},
+            "gemm_forms_ms_per_step": {"mma.sync (value)": ms / args.steps, "tcgen05 + TMEM": ms_tc / args.steps}}
     if emit:
         print(json.dumps(line), flush=True)
     net.close()

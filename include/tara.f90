@@ -33,7 +33,7 @@ module tara_gb300
   integer(c_int), parameter :: TARA_SCHEME_AB2 = 0, TARA_SCHEME_RK4 = 1
   integer(c_int), parameter :: TARA_PREC_FP64 = 0, TARA_PREC_FP32 = 1, TARA_PREC_DF64 = 2
   integer(c_int), parameter :: TARA_ENS_GRAPH = 0, TARA_ENS_PERSISTENT4 = 1, TARA_ENS_PERSISTENT8 = 2
-  integer(c_int), parameter :: TARA_FNO_BF16 = 0, TARA_FNO_FP32 = 1
+  integer(c_int), parameter :: TARA_FNO_BF16 = 0, TARA_FNO_FP32 = 1, TARA_FNO_BF16_TMEM = 2
 
   type, bind(C) :: tara2d_config
     integer(c_int) :: nx, ny

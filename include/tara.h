@@ -536,6 +536,8 @@ int tara_fft2d_c2r(int nx, int ny, int precision, const double* in, double* out)
 typedef struct tara_fno tara_fno;
 #define TARA_FNO_BF16 0  /* channel mixing on BF16 tensor cores, FP32 accumulators */
 #define TARA_FNO_FP32 1  /* the same GEMMs on FP32 CUDA cores (gradient checks)    */
+#define TARA_FNO_BF16_TMEM 2  /* as BF16, the tall-skinny channel GEMMs on tcgen05 with
+                               * accumulators in tensor memory */
 typedef struct tara_fno_config {
   int h, w;           /* grid (rows, columns) */
   int ci, c, co;      /* input, hidden and output channels */

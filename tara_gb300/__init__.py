@@ -92,7 +92,7 @@ class FnoConfig(ctypes.Structure):
                                             "max_batch", "mode")] + [("seed", ctypes.c_uint64)]
 
 
-FNO_BF16, FNO_FP32 = 0, 1
+FNO_BF16, FNO_FP32, FNO_BF16_TMEM = 0, 1, 2
 
 _lib = None
 

@@ -14,6 +14,8 @@
 // the per-mode complex mixing (as a 2C x 2C real block matrix) in forward and
 // backward, and the weight gradients -- runs through gemm_bf16: operands
 // rounded to BF16 in shared memory, mma.sync.m16n8k16 with FP32 accumulators.
+// In mode TARA_FNO_BF16_TMEM the tall-skinny GEMMs run on the 5th-generation
+// tensor cores instead (fno_tc.cu: tcgen05.mma, accumulators in tensor memory).
 // The same GEMM has an FP32 CUDA-core path (mode TARA_FNO_FP32) used to check
 // gradients against the FP64 oracle.  The truncated DFTs (16 and 32 modes of a
 // 128-point axis) run on FP32 CUDA cores, and so does the per-mode mixing of
@@ -28,6 +30,10 @@
 #include "internal.h"
 
 namespace tara {
+
+// fno_tc.cu: the tall-skinny GEMMs on tcgen05 with TMEM accumulators.
+bool ts_gemm_tc_launch(const float* A, long long M, int K, int N, const float* Bw, int transB, const float* bias,
+                       float* C, int accumulate, float* act, int act_mode, unsigned int* err, cudaStream_t s);
 
 // ---------------------------------------------------------------------------
 // strided batched GEMM:  C[b](m,n) = alpha * sum_k A[b](m,k) B[b](k,n)
@@ -824,6 +830,9 @@ namespace {
 
 constexpr int kPw = 152 * 4, kTh = 256;
 
+// BF16 operands on the tensor cores (either form of the tall-skinny GEMMs).
+bool bf16_mode(const tara_fno* f) { return f->cfg.mode == TARA_FNO_BF16 || f->cfg.mode == TARA_FNO_BF16_TMEM; }
+
 int gemm(tara_fno* f, const GemmArgs& a) {
   const dim3 grid((a.N + GT_N - 1) / GT_N, (a.M + GT_M - 1) / GT_M, a.batch);
   if (f->cfg.mode == TARA_FNO_FP32)
@@ -840,6 +849,8 @@ constexpr int kTsCtas = 152 * 2;
 // in BF16 mode for the shapes it is instantiated for; false when not handled.
 bool ts_gemm(tara_fno* f, const float* A, long long M, int K, int N, const float* Bw, int transB,
              const float* bias, float* C, int accumulate, float* act, int act_mode) {
+  if (f->cfg.mode == TARA_FNO_BF16_TMEM)
+    return ts_gemm_tc_launch(A, M, K, N, Bw, transB, bias, C, accumulate, act, act_mode, f->bad, f->stream);
   if (f->cfg.mode != TARA_FNO_BF16) return false;
   const long long tiles = (M + kTsRows - 1) / kTsRows;
   const int grid = (int)std::min<long long>(tiles, kTsCtas * 2);
@@ -858,7 +869,7 @@ bool ts_gemm(tara_fno* f, const float* A, long long M, int K, int N, const float
 // dW (K x N) = A^T B over M rows (+ bias gradient = column sums of B) with the
 // tensor-core reduction kernel in BF16 mode; false when not handled.
 bool ts_wgrad(tara_fno* f, const float* A, int K, const float* B, int N, long long M, float* dW, float* dbias) {
-  if (f->cfg.mode != TARA_FNO_BF16) return false;
+  if (!bf16_mode(f)) return false;
   const int ctas = (int)std::min<long long>(kTsCtas, (M + 63) / 64);
   const long long per = ((M + ctas - 1) / ctas + 63) / 64 * 64;
   float* bias_part = f->part + (size_t)ctas * K * N;
@@ -999,7 +1010,7 @@ int spectral_fwd(tara_fno* f, const float* v, float* out, float* Xsave, const fl
   int rc;
   if (B <= kMixB && 2 * C <= 128) {
     k_mode_mix<<<MY * MX, 128, 0, f->stream>>>(Xsave, Rb, f->Y, B, 2 * C, (long long)MY * MX * 2 * C,
-                                               f->cfg.mode == TARA_FNO_BF16);
+                                               bf16_mode(f));
     TARA_CK(cudaGetLastError());
   } else if ((rc = gemm(f, a))) {
     return rc;
@@ -1426,7 +1437,8 @@ int tara_fno_get_grads(tara_fno* f, float* host) {
 }
 
 int tara_fno_set_mode(tara_fno* f, int mode) {
-  if (!f || (mode != TARA_FNO_BF16 && mode != TARA_FNO_FP32)) return set_error(TARA_ERR_ARGS, "bad mode");
+  if (!f || (mode != TARA_FNO_BF16 && mode != TARA_FNO_FP32 && mode != TARA_FNO_BF16_TMEM))
+    return set_error(TARA_ERR_ARGS, "bad mode");
   f->cfg.mode = mode;
   return set_ok();
 }
@@ -1437,10 +1449,14 @@ int tara_fno_forward(tara_fno* f, const float* x_dev, float* y_dev, int B) {
   TARA_CK(cudaSetDevice(f->dev));
   int rc;
   const float* y = nullptr;
+  TARA_CK(cudaMemsetAsync(f->bad, 0, sizeof(unsigned int), f->stream));
   if ((rc = fno_forward_async(f, x_dev, B, &y))) return rc;
   const size_t n = (size_t)B * f->cfg.h * f->cfg.w * f->cfg.co;
   TARA_CK(cudaMemcpyAsync(y_dev, y, n * sizeof(float), cudaMemcpyDeviceToDevice, f->stream));
+  unsigned int bad = 0;
+  TARA_CK(cudaMemcpyAsync(&bad, f->bad, sizeof(bad), cudaMemcpyDeviceToHost, f->stream));
   TARA_CK(cudaStreamSynchronize(f->stream));
+  if (bad & 2u) return set_error(TARA_ERR_TIMEOUT, "a tensor-memory GEMM wait gave up");
   return set_ok();
 }
 
@@ -1479,6 +1495,7 @@ int tara_fno_train_step(tara_fno* f, const float* x_dev, const float* t_dev, con
     TARA_CK(cudaMemcpyAsync(lp.data(), f->lpart, kPw * sizeof(double), cudaMemcpyDeviceToHost, f->stream));
   TARA_CK(cudaMemcpyAsync(&bad, f->bad, sizeof(bad), cudaMemcpyDeviceToHost, f->stream));
   TARA_CK(cudaStreamSynchronize(f->stream));
+  if (bad & 2u) return set_error(TARA_ERR_TIMEOUT, "a tensor-memory GEMM wait gave up");
   if (bad) return set_error(TARA_ERR_ARGS, "sample index outside the dataset");
   if (loss) {
     double s = 0.0;

@@ -151,12 +151,15 @@ def test_training_reduces_loss():
 CLOSURE_CH = dict(h=32, w=32, ci=6, c=32, co=2, mx=8, my=16, layers=2, p=128, max_batch=8)
 
 
+@pytest.mark.parametrize("mode", [tg.FNO_BF16, tg.FNO_BF16_TMEM])
 @pytest.mark.parametrize("batch", [2, 6])
-def test_tensor_core_kernels_match_oracle(batch):
-    """BF16 mode at the closure's channel counts (6 -> 32 -> 128 -> 2), where the
-    tall-skinny tensor-core GEMMs (pointwise mixing, head, input gradients) and
-    the weight-gradient reductions (with the fused bias gradients) run."""
+def test_tensor_core_kernels_match_oracle(batch, mode):
+    """BF16 modes at the closure's channel counts (6 -> 32 -> 128 -> 2), where the
+    tall-skinny tensor-core GEMMs (pointwise mixing, head, input gradients; on
+    mma.sync or on tcgen05 with tensor-memory accumulators) and the
+    weight-gradient reductions (with the fused bias gradients) run."""
     cfg = tg.fno_default_config(**CLOSURE_CH)
+    cfg.mode = mode
     with tg.FNO(cfg) as net:
         s = fo.FnoShape.of(cfg)
         x, t = _data(net, batch, 20 + batch)
@@ -174,3 +177,31 @@ def test_tensor_core_kernels_match_oracle(batch):
             assert rel_l2(gb[name], rb[name]) < 4e-2, name
         cos = float(np.dot(g, ref_g) / (np.linalg.norm(g) * np.linalg.norm(ref_g)))
         assert cos > 0.996
+
+
+def test_tcgen05_gemms_match_mma_sync():
+    """The tcgen05 form of the channel GEMMs (TARA_FNO_BF16_TMEM) against the
+    mma.sync form at the production shape (128^2, 6 -> 32 -> 128 -> 2, batch 8:
+    1024 row tiles per GEMM, several per CTA): both multiply the same BF16-rounded
+    operands with FP32 accumulation, so outputs, loss and gradients agree to
+    FP32 summation-order differences."""
+    cfg = tg.fno_default_config(ci=6, max_batch=8)
+    with tg.FNO(cfg) as net:
+        x = np.random.default_rng(31).standard_normal((8, 128, 128, 6)).astype(np.float32)
+        t = np.random.default_rng(32).standard_normal((8, 128, 128, 2)).astype(np.float32)
+        y0 = _forward_gpu(net, x, 8)
+        xd, td = _dev(x), _dev(t)
+        l0 = net.train_step(xd.data_ptr(), td.data_ptr(), 8, lr=0.0)
+        g0 = net.get_grads()
+        net.set_mode(tg.FNO_BF16_TMEM)
+        y1 = _forward_gpu(net, x, 8)
+        l1 = net.train_step(xd.data_ptr(), td.data_ptr(), 8, lr=0.0)
+        g1 = net.get_grads()
+        assert rel_l2(y1, y0) < 1e-5
+        assert abs(l1 - l0) < 1e-5 * l0
+        assert rel_l2(g1, g0) < 1e-4
+        # training in the tcgen05 form: Adam steps keep the loss finite and decreasing
+        for _ in range(20):
+            net.train_step(xd.data_ptr(), td.data_ptr(), 8, lr=1e-3, want_loss=False)
+        l2 = net.train_step(xd.data_ptr(), td.data_ptr(), 8, lr=0.0)
+        assert np.isfinite(l2) and l2 < l1
