@@ -444,9 +444,10 @@ def run_ensemble(args, emit: bool = True) -> dict | None:
     idx, mine = shard.shard_of(runs, rank, ws)
     e = tg.Ensemble(mine, precision=tg.PREC_FP32, nu=1e-3, dt=1e-4)
     e.autotune(3)  # tiles and radix per kernel and size, then graph vs persistent
-    if args.ens_form != "auto":
+    form = getattr(args, "ens_form", "auto")
+    if form != "auto":
         e.set_form({"graph": tg.ENS_GRAPH, "persistent4": tg.ENS_PERSISTENT4,
-                    "persistent8": tg.ENS_PERSISTENT8}[args.ens_form])
+                    "persistent8": tg.ENS_PERSISTENT8}[form])
     e.step(args.warmup)
     e.synchronize()
     if dist:

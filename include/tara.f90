@@ -642,6 +642,11 @@ module tara_gb300
       type(c_ptr), value :: f
       integer(c_int), value :: mode
     end function tara_fno_set_mode
+    integer(c_int) function tara_fno_set_fused(f, enable) bind(C, name="tara_fno_set_fused")
+      import
+      type(c_ptr), value :: f
+      integer(c_int), value :: enable
+    end function tara_fno_set_fused
     integer(c_int) function tara_fno_forward(f, x_dev, y_dev, nb) bind(C, name="tara_fno_forward")
       import
       type(c_ptr), value :: f, x_dev, y_dev

@@ -557,6 +557,14 @@ int tara_fno_set_params(tara_fno* f, const float* host);
 /* Gradients of the last tara_fno_train_step (same layout as the parameters). */
 int tara_fno_get_grads(tara_fno* f, float* host);
 int tara_fno_set_mode(tara_fno* f, int mode);
+/* Inference path of tara_fno_forward and the closure (enable != 0, the default):
+ * in the BF16 modes, batches of at most 4 samples at W = 128, 32 channels,
+ * p in {32, 64, 128, 256}, co <= 4, H <= 256, mx <= 16 and mx * my <= 512 run through fused
+ * per-row and per-column kernels (lift + 2 launches per Fourier layer, the
+ * pointwise and projection products on tcgen05); enable = 0 keeps the
+ * layer-by-layer forward of the training step.  Same arithmetic up to the
+ * order of FP32 sums. */
+int tara_fno_set_fused(tara_fno* f, int enable);
 /* y_dev (B,H,W,co) = FNO(x_dev (B,H,W,ci)); device FP32 arrays; synchronous. */
 int tara_fno_forward(tara_fno* f, const float* x_dev, float* y_dev, int B);
 /* Forward, loss = mean((y - t)^2), backward, then one Adam step (beta 0.9,

@@ -242,6 +242,7 @@ def _declare(L: ctypes.CDLL) -> None:
     L.tara_fno_set_params.argtypes = [vp, fp]
     L.tara_fno_get_grads.argtypes = [vp, fp]
     L.tara_fno_set_mode.argtypes = [vp, c_int]
+    L.tara_fno_set_fused.argtypes = [vp, c_int]
     L.tara_fno_forward.argtypes = [vp, vp, vp, c_int]
     L.tara_fno_train_step.argtypes = [vp, vp, vp, vp, c_int, c_int, ctypes.c_float, dp]
     L.tara_fno_adam_steps.argtypes = [vp]
@@ -1063,6 +1064,10 @@ class FNO:
 
     def set_mode(self, mode: int) -> None:
         _check(lib().tara_fno_set_mode(self._h, mode))
+
+    def set_fused(self, enable: bool) -> None:
+        """Fused small-batch inference forward (default on; see tara_fno_set_fused)."""
+        _check(lib().tara_fno_set_fused(self._h, int(bool(enable))))
 
     def forward(self, x_ptr: int, y_ptr: int, batch: int) -> None:
         _check(lib().tara_fno_forward(self._h, ctypes.c_void_p(x_ptr), ctypes.c_void_p(y_ptr), batch))

@@ -281,7 +281,9 @@ int closure_step_once(tara_closure* c) {
   if ((rc = features(h, 0, B, c->nf, c->spec, c->real, c->rpitch, c->in_scale, fno_input(c->f)))) return rc;
   const float* y = nullptr;
   fno_bind_stream(c->f, h->stream);
+  fno_bind_error(c->f, h->flag);  // reported by the solver's synchronize
   rc = fno_forward_async(c->f, nullptr, B, &y);
+  fno_bind_error(c->f, nullptr);
   fno_bind_stream(c->f, nullptr);
   if (rc) return rc;
   k_output_to_real<<<kBlocks, kThreads, 0, h->stream>>>(y, h->nx, h->ny, c->rpitch, rfs, B, c->out_scale,

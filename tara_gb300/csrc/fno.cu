@@ -27,6 +27,7 @@
 
 #include <cuda_bf16.h>
 
+#include "fno_fused.h"
 #include "internal.h"
 
 namespace tara {
@@ -824,6 +825,9 @@ struct tara_fno {
   size_t part_n = 0;
   double* lpart = nullptr;
   unsigned int* bad = nullptr;
+  unsigned int* errw = nullptr;  // where tensor-core waits that gave up are flagged (value 4): bad, or a
+                                 // word of the caller the handle is bound to (the closure's solver flag)
+  bool fused = true;             // inference forward of small batches through fno_fused.cu
 };
 
 namespace {
@@ -850,7 +854,7 @@ constexpr int kTsCtas = 152 * 2;
 bool ts_gemm(tara_fno* f, const float* A, long long M, int K, int N, const float* Bw, int transB,
              const float* bias, float* C, int accumulate, float* act, int act_mode) {
   if (f->cfg.mode == TARA_FNO_BF16_TMEM)
-    return ts_gemm_tc_launch(A, M, K, N, Bw, transB, bias, C, accumulate, act, act_mode, f->bad, f->stream);
+    return ts_gemm_tc_launch(A, M, K, N, Bw, transB, bias, C, accumulate, act, act_mode, f->errw, f->stream);
   if (f->cfg.mode != TARA_FNO_BF16) return false;
   const long long tiles = (M + kTsRows - 1) / kTsRows;
   const int grid = (int)std::min<long long>(tiles, kTsCtas * 2);
@@ -1250,12 +1254,55 @@ namespace tara {
 
 // Forward pass on the handle's current stream, leaving the output in the
 // handle (valid until the next call); x is copied in first.
+// Inference forward (nothing kept for a backward pass): the fused kernels of
+// fno_fused.cu for small batches of the shapes they take, in the BF16 modes;
+// otherwise the layer-by-layer forward.
+int forward_infer(tara_fno* f, int B) {
+  const auto& c = f->cfg;
+  if (!f->fused || !bf16_mode(f) || c.layers > kFusedMaxLayers ||
+      !fused_forward_supported(B, c.h, c.w, c.c, c.mx, c.my, c.ci, c.p, c.co))
+    return forward(f, B);
+  int rc;
+  if ((rc = refresh_rb(f))) return rc;
+  FusedFwdArgs a{};
+  a.B = B;
+  a.H = c.h;
+  a.MX = c.mx;
+  a.MY = c.my;
+  a.CI = c.ci;
+  a.P = c.p;
+  a.CO = c.co;
+  a.layers = c.layers;
+  a.bf16 = 1;
+  a.x = f->x;
+  a.Pw = f->p + f->off_Pw;
+  a.Pb = f->p + f->off_Pb;
+  for (int l = 1; l <= c.layers; ++l) {
+    a.Wl[l] = f->p + f->off_W[l - 1];
+    a.bl[l] = f->p + f->off_b[l - 1];
+    a.Rb[l] = layer_rb(f, l);
+  }
+  for (int l = 0; l < c.layers; ++l) a.v[l] = act_v(f, l);
+  a.Q1 = f->p + f->off_Q1;
+  a.q1 = f->p + f->off_q1;
+  a.Q2 = f->p + f->off_Q2;
+  a.q2 = f->p + f->off_q2;
+  a.csx = f->csx;
+  a.csy = f->csy;
+  a.wx = f->wx;
+  a.A = f->A;
+  a.Y = f->Y;
+  a.y = f->y;
+  a.err = f->errw;
+  return fused_forward_launch(a, f->stream);
+}
+
 int fno_forward_async(tara_fno* f, const float* x_dev, int B, const float** y) {
   if (!f || B < 1 || B > f->bmax) return set_error(TARA_ERR_ARGS, "bad arguments");
   const size_t n = (size_t)B * f->cfg.h * f->cfg.w * f->cfg.ci;
   if (x_dev && x_dev != f->x)
     TARA_CK(cudaMemcpyAsync(f->x, x_dev, n * sizeof(float), cudaMemcpyDeviceToDevice, f->stream));
-  const int rc = forward(f, B);
+  const int rc = forward_infer(f, B);
   if (rc) return rc;
   *y = f->y;
   return TARA_OK;
@@ -1263,6 +1310,8 @@ int fno_forward_async(tara_fno* f, const float* x_dev, int B, const float** y) {
 
 // Launch the network's work on `s` (nullptr: back to its own stream).
 void fno_bind_stream(tara_fno* f, cudaStream_t s) { f->stream = s ? s : f->own_stream; }
+// Flag tensor-core waits that gave up in `w` (nullptr: back to the handle's own word).
+void fno_bind_error(tara_fno* f, unsigned int* w) { f->errw = w ? w : f->bad; }
 
 const tara_fno_config& fno_config(const tara_fno* f) { return f->cfg; }
 float* fno_input(tara_fno* f) { return f->x; }
@@ -1369,6 +1418,7 @@ int tara_fno_create(const tara_fno_config* cfg, tara_fno** out) {
   FA(f->part, f->part_n);
   FA(f->lpart, kPw);
   FA(f->bad, 1);
+  f->errw = f->bad;
 #undef FA
   // tables
   std::vector<float> cs;
@@ -1436,6 +1486,12 @@ int tara_fno_get_grads(tara_fno* f, float* host) {
   return set_ok();
 }
 
+int tara_fno_set_fused(tara_fno* f, int enable) {
+  if (!f) return set_error(TARA_ERR_ARGS, "null handle");
+  f->fused = enable != 0;
+  return set_ok();
+}
+
 int tara_fno_set_mode(tara_fno* f, int mode) {
   if (!f || (mode != TARA_FNO_BF16 && mode != TARA_FNO_FP32 && mode != TARA_FNO_BF16_TMEM))
     return set_error(TARA_ERR_ARGS, "bad mode");
@@ -1456,7 +1512,7 @@ int tara_fno_forward(tara_fno* f, const float* x_dev, float* y_dev, int B) {
   unsigned int bad = 0;
   TARA_CK(cudaMemcpyAsync(&bad, f->bad, sizeof(bad), cudaMemcpyDeviceToHost, f->stream));
   TARA_CK(cudaStreamSynchronize(f->stream));
-  if (bad & 2u) return set_error(TARA_ERR_TIMEOUT, "a tensor-memory GEMM wait gave up");
+  if (bad & 4u) return set_error(TARA_ERR_TIMEOUT, "a tensor-memory GEMM wait gave up");
   return set_ok();
 }
 
@@ -1495,7 +1551,7 @@ int tara_fno_train_step(tara_fno* f, const float* x_dev, const float* t_dev, con
     TARA_CK(cudaMemcpyAsync(lp.data(), f->lpart, kPw * sizeof(double), cudaMemcpyDeviceToHost, f->stream));
   TARA_CK(cudaMemcpyAsync(&bad, f->bad, sizeof(bad), cudaMemcpyDeviceToHost, f->stream));
   TARA_CK(cudaStreamSynchronize(f->stream));
-  if (bad & 2u) return set_error(TARA_ERR_TIMEOUT, "a tensor-memory GEMM wait gave up");
+  if (bad & 4u) return set_error(TARA_ERR_TIMEOUT, "a tensor-memory GEMM wait gave up");
   if (bad) return set_error(TARA_ERR_ARGS, "sample index outside the dataset");
   if (loss) {
     double s = 0.0;

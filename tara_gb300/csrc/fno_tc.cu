@@ -13,7 +13,7 @@
 // output -- exactly as the mma.sync kernel of the BF16 mode does.  The weight
 // matrix is staged once per CTA; the CTAs loop over tiles.
 //
-// Every wait is bounded: a wait that gives up sets bit 1 (value 2) of *err, the
+// Every wait is bounded: a wait that gives up sets bit 2 (value 4) of *err, the
 // CTA stops taking tiles, and the host reports TARA_ERR_TIMEOUT.
 #include <cstdint>
 
@@ -125,7 +125,7 @@ __global__ void __launch_bounds__(128) k_ts_gemm_tc(const float* __restrict__ A,
     umma::fence_before_sync();
     __syncthreads();  // TMEM read and As consumed before the next tile's MMA and loads
   }
-  if (failed && tid == 0) atomicOr(err, 2u);
+  if (failed && tid == 0) atomicOr(err, 4u);
   __syncthreads();
   umma::fence_after_sync();
   if (warp == 0) umma::dealloc(tmem, kCols);

@@ -147,6 +147,7 @@ int twiddles64(tara2d* h, const void** twx, const void** twy);
 // Learned-closure internals (fno.cu).
 int fno_forward_async(tara_fno* f, const float* x_dev, int B, const float** y);
 void fno_bind_stream(tara_fno* f, cudaStream_t s);
+void fno_bind_error(tara_fno* f, unsigned int* w);  // nullptr: the handle's own word
 const tara_fno_config& fno_config(const tara_fno* f);
 float* fno_input(tara_fno* f);  // the handle's input buffer (max_batch samples)
 unsigned long long fno_param_version(const tara_fno* f);

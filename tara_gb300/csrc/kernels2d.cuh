@@ -756,7 +756,10 @@ template <typename T, int N, int V> struct RowXCfg {
   static constexpr int NP = V == 2 ? 1
                                    : fit_pairs(4 * RowCfg<T, N, V>::RP,
                                                N * (int)sizeof(typename cplx_of<T>::type));
-  static constexpr int THREADS = NP * fft_group(N);
+  // the single-pair tile gives its transform 4x the threads (one radix-4
+  // butterfly per thread per stage), as the one-column tile of the column pass does
+  static constexpr int G = V == 2 ? 4 * fft_group(N) : fft_group(N);
+  static constexpr int THREADS = NP * G;
   static constexpr int SMEM = NP * N * (int)sizeof(typename cplx_of<T>::type);
 };
 
@@ -769,7 +772,7 @@ __global__ void __launch_bounds__(RowXCfg<T, N, V>::THREADS)
               const typename cplx_of<T>::type* __restrict__ tw) {
   typedef typename cplx_of<T>::type C;
   typedef RowXCfg<T, N, V> RC;
-  constexpr int G = fft_group(N), H = N / 2, NP = RC::NP, SL = N;  // NP row pairs per CTA
+  constexpr int G = RC::G, H = N / 2, NP = RC::NP, SL = N;  // NP row pairs per CTA
   extern __shared__ __align__(16) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);  // [NP][N]
   const int tid = threadIdx.x, y_base = blockIdx.x * (2 * NP);
@@ -790,7 +793,7 @@ __global__ void __launch_bounds__(RowXCfg<T, N, V>::THREADS)
     sm[pp * SL + k] = z;
   }
   __syncthreads();
-  fft_slot<T, N, true>(sm + (tid / G) * SL, tid % G, true, tw);
+  fft_slot<T, N, true, G>(sm + (tid / G) * SL, tid % G, true, tw);
   TARA_ELEM_LOOP(e, NP * N, RC::THREADS) {
     const int x = e % N, pp = e / N, ya = y_base + 2 * pp;
     if (ya < ny) {
@@ -809,7 +812,7 @@ __global__ void __launch_bounds__(RowXCfg<T, N, V>::THREADS)
               const typename cplx_of<T>::type* __restrict__ tw) {
   typedef typename cplx_of<T>::type C;
   typedef RowXCfg<T, N, V> RC;
-  constexpr int G = fft_group(N), H = N / 2, NP = RC::NP, SL = N;
+  constexpr int G = RC::G, H = N / 2, NP = RC::NP, SL = N;
   extern __shared__ __align__(16) unsigned char smraw[];
   C* sm = reinterpret_cast<C*>(smraw);
   const int tid = threadIdx.x, y_base = blockIdx.x * (2 * NP);
@@ -821,7 +824,7 @@ __global__ void __launch_bounds__(RowXCfg<T, N, V>::THREADS)
                                : mkc<T>(T(0), T(0));
   }
   __syncthreads();
-  fft_slot<T, N, false>(sm + (tid / G) * SL, tid % G, true, tw);
+  fft_slot<T, N, false, G>(sm + (tid / G) * SL, tid % G, true, tw);
   TARA_ELEM_LOOP(e, NP * (H + 1), RC::THREADS) {
     const int k = e % (H + 1), pp = e / (H + 1), ya = y_base + 2 * pp;
     if (ya < ny) {

@@ -86,6 +86,9 @@ def bench_ensemble() -> None:
         def groups(self):
             return []
 
+        def form(self):
+            return {"form": "graph", "ms_per_step": {"graph": 1.0}}
+
         def get_state(self, r):
             n, _, seed = self.runs[r]
             w = np.full((n, n // 2 + 1), 1.0 + 0.5j)

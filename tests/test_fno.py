@@ -205,3 +205,33 @@ def test_tcgen05_gemms_match_mma_sync():
             net.train_step(xd.data_ptr(), td.data_ptr(), 8, lr=1e-3, want_loss=False)
         l2 = net.train_step(xd.data_ptr(), td.data_ptr(), 8, lr=0.0)
         assert np.isfinite(l2) and l2 < l1
+
+
+@pytest.mark.parametrize("mode", [tg.FNO_BF16, tg.FNO_BF16_TMEM])
+@pytest.mark.parametrize("kw,batches", [
+    (dict(ci=6), (1, 3)),                       # the closure's network (p = 128, co = 2)
+    (dict(ci=1, h=64, p=64, co=1), (2,)),       # 64 grid rows, a narrower projection
+    (dict(ci=3, p=256, co=4, my=16, mx=8), (4,)),
+])
+def test_fused_inference_matches_layer_by_layer(mode, kw, batches):
+    """The fused small-batch inference forward (lift + 2 launches per layer,
+    tcgen05 pointwise and projection products) against the layer-by-layer
+    forward of the training step on the same BF16-rounded operands, and against
+    the FP64 oracle at BF16 tolerance.  The two forwards sum in different orders
+    in FP32; where that moves an activation across a BF16 rounding boundary the
+    next layer's operand differs by one BF16 unit (2^-8 relative), so they agree
+    to about 1e-4, not to FP32 precision."""
+    cfg = tg.fno_default_config(max_batch=4, **kw)
+    cfg.mode = mode
+    with tg.FNO(cfg) as net:
+        s = fo.FnoShape.of(cfg)
+        for B in batches:
+            x = np.random.default_rng(40 + B).standard_normal((B, cfg.h, cfg.w, cfg.ci)).astype(np.float32)
+            net.set_fused(True)
+            y_fused = _forward_gpu(net, x, B)
+            net.set_fused(False)
+            y_layers = _forward_gpu(net, x, B)
+            assert rel_l2(y_fused, y_layers) < 1e-3, B
+            ref = fo.forward(torch.tensor(net.get_params(), dtype=torch.float64),
+                             torch.tensor(x, dtype=torch.float64), s)
+            assert rel_l2(y_fused, ref.numpy()) < 2e-2, B
