@@ -399,17 +399,26 @@ def side_workloads(args) -> dict:
     return out
 
 
+PROFILE_RANGE = False  # --profile-range: the timed regions run inside cudaProfilerStart/Stop
+
+
 def timed_on_stream(stream_ptr: int, fn):
-    """CUDA-event time (ms) of fn() on the library stream stream_ptr."""
+    """CUDA-event time (ms) of fn() on the library stream stream_ptr (with
+    --profile-range, inside a profiler range, so that `ncu --profile-from-start
+    off` captures the timed launches only)."""
     import torch
 
     st = torch.cuda.ExternalStream(stream_ptr)
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
+    if PROFILE_RANGE:
+        torch.cuda.profiler.start()
     a.record(st)
     fn()
     b.record(st)
     b.synchronize()
+    if PROFILE_RANGE:
+        torch.cuda.profiler.stop()
     return a.elapsed_time(b)
 
 
@@ -842,6 +851,8 @@ def main() -> None:
     ap.add_argument("--n", type=int, default=2048)
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-range", action="store_true",
+                    help="bracket the timed regions with cudaProfilerStart/Stop (for ncu --profile-from-start off)")
     ap.add_argument("--no-side", action="store_true",
                     help="skip the short runs of the other benchmark configurations")
     ap.add_argument("--workload", default="rk4-2048",
@@ -862,6 +873,8 @@ def main() -> None:
                     help="rk4-2048: fp32 runs the FP32 form (FP32 transforms, FP64 state), df64 the "
                          "double-float form (transforms in FP32 pairs, FP64 state); the headline is fp64")
     args = ap.parse_args()
+    global PROFILE_RANGE
+    PROFILE_RANGE = args.profile_range
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

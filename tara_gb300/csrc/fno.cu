@@ -32,6 +32,15 @@
 
 namespace tara {
 
+// fno_dft_tc.cu: the truncated DFTs on tcgen05 (split-BF16 operands).
+bool x2m_tc_launch(const float* v, float* out, long long rows, int W, int C, int MX, const float* cs,
+                   const float* scale, unsigned int* err, cudaStream_t s);
+bool m2x_tc_launch(const float* a, float* out, long long rows, int W, int C, int MX, const float* cs,
+                   const float* scale, int accumulate, unsigned int* err, cudaStream_t s);
+bool y2m_tc_launch(const float* a, float* out, int B, int H, int C, int MX, int MY, const float* cs,
+                   unsigned int* err, cudaStream_t s);
+bool m2y_tc_launch(const float* v, float* out, int B, int H, int C, int MX, int MY, const float* cs,
+                   unsigned int* err, cudaStream_t s);
 // fno_tc.cu: the tall-skinny GEMMs on tcgen05 with TMEM accumulators.
 bool ts_gemm_tc_launch(const float* A, long long M, int K, int N, const float* Bw, int transB, const float* bias,
                        float* C, int accumulate, float* act, int act_mode, unsigned int* err, cudaStream_t s);
@@ -837,6 +846,48 @@ constexpr int kPw = 152 * 4, kTh = 256;
 // BF16 operands on the tensor cores (either form of the tall-skinny GEMMs).
 bool bf16_mode(const tara_fno* f) { return f->cfg.mode == TARA_FNO_BF16 || f->cfg.mode == TARA_FNO_BF16_TMEM; }
 
+// The truncated DFTs along x over `rows` grid rows: on the tensor cores in the
+// BF16 modes where the shape allows (fno_dft_tc.cu), else on FP32 CUDA cores.
+int x_to_modes(tara_fno* f, const float* v, float* out, int rows, const float* scale) {
+  const auto& c = f->cfg;
+  if (bf16_mode(f) && x2m_tc_launch(v, out, rows, c.w, c.c, c.mx, f->csx, scale, f->errw, f->stream))
+    return TARA_OK;
+  const size_t sx = (size_t)(c.w * c.c + 2 * c.w) * sizeof(float);
+  k_x_to_modes<<<rows, 256, sx, f->stream>>>(v, out, c.w, c.c, c.mx, f->csx, scale);
+  TARA_CK(cudaGetLastError());
+  return TARA_OK;
+}
+int modes_to_x(tara_fno* f, const float* a, float* out, int rows, const float* scale, int accumulate) {
+  const auto& c = f->cfg;
+  if (bf16_mode(f) && m2x_tc_launch(a, out, rows, c.w, c.c, c.mx, f->csx, scale, accumulate, f->errw, f->stream))
+    return TARA_OK;
+  const size_t smx = (size_t)(c.mx * 2 * c.c + 2 * c.w) * sizeof(float);
+  k_modes_to_x<<<rows, 256, smx, f->stream>>>(a, out, c.w, c.c, c.mx, f->csx, scale, accumulate);
+  TARA_CK(cudaGetLastError());
+  return TARA_OK;
+}
+
+// The truncated DFTs along y (forward: sign -1 into the modes; inverse: +1 back
+// to the rows), likewise.
+int y_to_modes(tara_fno* f, const float* a, float* out, int B) {
+  const auto& c = f->cfg;
+  if (bf16_mode(f) && y2m_tc_launch(a, out, B, c.h, c.c, c.mx, c.my, f->csy, f->errw, f->stream)) return TARA_OK;
+  const dim3 gy(B * c.mx, c.c / kCpb);
+  const size_t sy = (size_t)(c.h * 2 * kCpb + 2 * c.h) * sizeof(float);
+  k_y_to_modes<<<gy, 256, sy, f->stream>>>(a, out, c.h, c.c, c.mx, c.my, f->csy, -1.f);
+  TARA_CK(cudaGetLastError());
+  return TARA_OK;
+}
+int modes_to_y(tara_fno* f, const float* v, float* out, int B) {
+  const auto& c = f->cfg;
+  if (bf16_mode(f) && m2y_tc_launch(v, out, B, c.h, c.c, c.mx, c.my, f->csy, f->errw, f->stream)) return TARA_OK;
+  const dim3 gy(B * c.mx, c.c / kCpb);
+  const size_t smy = (size_t)(c.my * 2 * kCpb + 2 * c.h) * sizeof(float);
+  k_modes_to_y<<<gy, 256, smy, f->stream>>>(v, out, c.h, c.c, c.mx, c.my, f->csy, 1.f);
+  TARA_CK(cudaGetLastError());
+  return TARA_OK;
+}
+
 int gemm(tara_fno* f, const GemmArgs& a) {
   const dim3 grid((a.N + GT_N - 1) / GT_N, (a.M + GT_M - 1) / GT_M, a.batch);
   if (f->cfg.mode == TARA_FNO_FP32)
@@ -983,15 +1034,10 @@ float* act_X(tara_fno* f, int l) {  // spectral input of layer l
 // the layer's block weights Rb; the mode coefficients go to Xsave.
 int spectral_fwd(tara_fno* f, const float* v, float* out, float* Xsave, const float* Rb, int B) {
   const auto& c = f->cfg;
-  const int C = c.c, H = c.h, W = c.w, MX = c.mx, MY = c.my;
-  const dim3 gy(B * MX, C / kCpb);
-  const size_t sx = (size_t)(W * C + 2 * W) * sizeof(float), sy = (size_t)(H * 2 * kCpb + 2 * H) * sizeof(float);
-  const size_t smy = (size_t)(MY * 2 * kCpb + 2 * H) * sizeof(float);
-  const size_t smx = (size_t)(MX * 2 * C + 2 * W) * sizeof(float);
-  k_x_to_modes<<<B * H, 256, sx, f->stream>>>(v, f->A, W, C, MX, f->csx, nullptr);
-  TARA_CK(cudaGetLastError());
-  k_y_to_modes<<<gy, 256, sy, f->stream>>>(f->A, Xsave, H, C, MX, MY, f->csy, -1.f);
-  TARA_CK(cudaGetLastError());
+  const int C = c.c, H = c.h, MX = c.mx, MY = c.my;
+  int rc;
+  if ((rc = x_to_modes(f, v, f->A, B * H, nullptr))) return rc;
+  if ((rc = y_to_modes(f, f->A, Xsave, B))) return rc;
   // per-mode complex mixing: Y[b, m, :] = X[b, m, :] Rb[m]  (M = B, K = N = 2C)
   GemmArgs a{};
   a.M = B;
@@ -1011,7 +1057,6 @@ int spectral_fwd(tara_fno* f, const float* v, float* out, float* Xsave, const fl
   a.scm = (long long)MY * MX * 2 * C;
   a.scn = 1;
   a.alpha = 1.f;
-  int rc;
   if (B <= kMixB && 2 * C <= 128) {
     k_mode_mix<<<MY * MX, 128, 0, f->stream>>>(Xsave, Rb, f->Y, B, 2 * C, (long long)MY * MX * 2 * C,
                                                bf16_mode(f));
@@ -1019,10 +1064,8 @@ int spectral_fwd(tara_fno* f, const float* v, float* out, float* Xsave, const fl
   } else if ((rc = gemm(f, a))) {
     return rc;
   }
-  k_modes_to_y<<<gy, 256, smy, f->stream>>>(f->Y, f->U, H, C, MX, MY, f->csy, 1.f);
-  TARA_CK(cudaGetLastError());
-  k_modes_to_x<<<B * H, 256, smx, f->stream>>>(f->U, out, W, C, MX, f->csx, f->wx, 0);
-  TARA_CK(cudaGetLastError());
+  if ((rc = modes_to_y(f, f->Y, f->U, B))) return rc;
+  if ((rc = modes_to_x(f, f->U, out, B * H, f->wx, 0))) return rc;
   return TARA_OK;
 }
 
@@ -1185,12 +1228,8 @@ int backward(tara_fno* f, int B) {
       if ((rc = gemm(f, a))) return rc;
     }
     // spectral part: adjoints in reverse order
-    const dim3 gy(B * MX, C / kCpb);
-    const size_t sx = (size_t)(W * C + 2 * W) * sizeof(float), sy = (size_t)(H * 2 * kCpb + 2 * H) * sizeof(float);
-    const size_t smy = (size_t)(MY * 2 * kCpb + 2 * H) * sizeof(float);
-    const size_t smx = (size_t)(MX * 2 * C + 2 * W) * sizeof(float);
-    k_x_to_modes<<<B * H, 256, sx, f->stream>>>(dz, f->A, W, C, MX, f->csx, f->wx);
-    k_y_to_modes<<<gy, 256, sy, f->stream>>>(f->A, f->Y, H, C, MX, MY, f->csy, -1.f);
+    if ((rc = x_to_modes(f, dz, f->A, B * H, f->wx))) return rc;
+    if ((rc = y_to_modes(f, f->A, f->Y, B))) return rc;
     TARA_CK(cudaGetLastError());
     {
       GemmArgs a{};  // dRb[m] = X[:, m, :]^T dY[:, m, :]   (M = N = 2C, K = B)
@@ -1234,8 +1273,8 @@ int backward(tara_fno* f, int B) {
       t.alpha = 1.f;
       if ((rc = gemm(f, t))) return rc;
     }
-    k_modes_to_y<<<gy, 256, smy, f->stream>>>(f->U, f->A, H, C, MX, MY, f->csy, 1.f);
-    k_modes_to_x<<<B * H, 256, smx, f->stream>>>(f->A, f->dv, W, C, MX, f->csx, nullptr, 1);
+    if ((rc = modes_to_y(f, f->U, f->A, B))) return rc;
+    if ((rc = modes_to_x(f, f->A, f->dv, B * H, nullptr, 1))) return rc;
     TARA_CK(cudaGetLastError());
   }
   // lifting

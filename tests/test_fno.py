@@ -235,3 +235,34 @@ def test_fused_inference_matches_layer_by_layer(mode, kw, batches):
             ref = fo.forward(torch.tensor(net.get_params(), dtype=torch.float64),
                              torch.tensor(x, dtype=torch.float64), s)
             assert rel_l2(y_fused, ref.numpy()) < 2e-2, B
+
+
+@pytest.mark.parametrize("mode", [tg.FNO_BF16, tg.FNO_BF16_TMEM])
+def test_tensor_core_dfts_at_production_shape(mode):
+    """At the closure's network shape (W = 128, 32 channels, 16 kx modes) the
+    truncated DFTs along x run as tcgen05 products with split-BF16 operands in
+    the BF16 modes (forward and the adjoints of the backward pass): the
+    layer-by-layer forward, the loss and every parameter block's gradient
+    against the FP64 oracle at the BF16 tolerances, at batch 2 and 6 (the
+    per-mode GEMV and the batched mixing GEMM)."""
+    cfg = tg.fno_default_config(ci=6, max_batch=6)
+    cfg.mode = mode
+    with tg.FNO(cfg) as net:
+        net.set_fused(False)
+        s = fo.FnoShape.of(cfg)
+        p = net.get_params()
+        for B in (2, 6):
+            x, t = _data(net, B, 60 + B)
+            y = _forward_gpu(net, x, B)
+            ref = fo.forward(torch.tensor(p, dtype=torch.float64), torch.tensor(x, dtype=torch.float64), s)
+            assert rel_l2(y, ref.numpy()) < 2e-2, B
+            xd, td = _dev(x), _dev(t)
+            loss = net.train_step(xd.data_ptr(), td.data_ptr(), B, lr=0.0)
+            g = net.get_grads()
+            ref_loss, ref_g = fo.loss_and_grad(p, x, t, s)
+            assert abs(loss - ref_loss) < 2e-2 * ref_loss, B
+            gb, rb = _blocks(s, g), _blocks(s, ref_g)
+            for name in gb:
+                assert rel_l2(gb[name], rb[name]) < 4e-2, (B, name)
+            cos = float(np.dot(g, ref_g) / (np.linalg.norm(g) * np.linalg.norm(ref_g)))
+            assert cos > 0.996, B
