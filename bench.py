@@ -809,7 +809,7 @@ def run_closure_step(args, emit: bool = True) -> dict:
     s = tg.Solver2D(128, scheme=tg.SCHEME_RK4, precision=tg.PREC_FP32, nu=5e-5, dt=4e-3,
                     kpi=np.pi, lx=2 * np.pi, ly=2 * np.pi)
     s.init_random(8.0, 0.5, 9000)
-    s.autotune(2)
+    tuned = s.autotune(2)
     net = tg.FNO(tg.fno_default_config(ci=6, max_batch=1))
     c = tg.Closure(s, net, np.full(6, 0.05), 0.01)
     c.step(args.warmup)
@@ -835,6 +835,7 @@ def run_closure_step(args, emit: bool = True) -> dict:
             "vs_baseline": None, "dtype": "bf16 GEMMs / f32 network / f64 state",
             "data": "synthetic (seeded random-phase state, random network)",
             "config": {"workload": "closure step", "graph": "one cudaGraphLaunch per step"},
+            "coarse_tile_variants": tuned["variants"],
             "fine_1024_fp64_ms_per_step": fms,
             "simtime_speedup_vs_fine_1024": (4e-3 / cms) / (5e-4 / fms)}
     if emit:

@@ -41,6 +41,14 @@ bool y2m_tc_launch(const float* a, float* out, int B, int H, int C, int MX, int 
                    unsigned int* err, cudaStream_t s);
 bool m2y_tc_launch(const float* v, float* out, int B, int H, int C, int MX, int MY, const float* cs,
                    unsigned int* err, cudaStream_t s);
+// fno_head_tc.cu: the projection head fused on tcgen05 (forward without stored
+// hidden activations; backward recomputing them, with the weight gradients).
+bool head_tc_supported(int C, int P, int CO);
+bool head_fwd_tc_launch(const float* v, long long rows, const float* Q1, const float* q1, const float* Q2,
+                        const float* q2, int CO, float* y, unsigned int* err, cudaStream_t s);
+int head_bwd_tc_grid(long long rows);
+bool head_bwd_tc_launch(const float* v, const float* dy, long long rows, const float* Q1, const float* q1,
+                        const float* Q2, int CO, float* dv, float* part, unsigned int* err, cudaStream_t s);
 // fno_tc.cu: the tall-skinny GEMMs on tcgen05 with TMEM accumulators.
 bool ts_gemm_tc_launch(const float* A, long long M, int K, int N, const float* Bw, int transB, const float* bias,
                        float* C, int accumulate, float* act, int act_mode, unsigned int* err, cudaStream_t s);
@@ -888,6 +896,11 @@ int modes_to_y(tara_fno* f, const float* v, float* out, int B) {
   return TARA_OK;
 }
 
+// The fused head (fno_head_tc.cu) replaces the stored zh, h of the projection in
+// the BF16 modes at 32 channels and 128 hidden units; forward and backward
+// decide the same way.
+bool head_fused(const tara_fno* f) { return bf16_mode(f) && head_tc_supported(f->cfg.c, f->cfg.p, f->cfg.co); }
+
 int gemm(tara_fno* f, const GemmArgs& a) {
   const dim3 grid((a.N + GT_N - 1) / GT_N, (a.M + GT_M - 1) / GT_M, a.batch);
   if (f->cfg.mode == TARA_FNO_FP32)
@@ -1124,6 +1137,12 @@ int forward(tara_fno* f, int B) {
     a.act_mode = l < c.layers ? 1 : 2;
     if (!ts_gemm(f, a.A, rows, C, C, a.B, 0, a.bias, z, 1, a.act, a.act_mode) && (rc = gemm(f, a))) return rc;
   }
+  if (head_fused(f)) {  // y = GELU(v_L Q1 + q1) Q2 + q2, nothing else stored
+    if (!head_fwd_tc_launch(act_v(f, c.layers), rows, f->p + f->off_Q1, f->p + f->off_q1, f->p + f->off_Q2,
+                            f->p + f->off_q2, c.co, f->y, f->errw, f->stream))
+      return set_error(TARA_ERR_CUDA, "fused head launch");
+    return TARA_OK;
+  }
   GemmArgs a{};  // zh = v_L Q1 + q1 ; h = GELU(zh)
   a.M = (int)rows;
   a.N = c.p;
@@ -1160,6 +1179,21 @@ int backward(tara_fno* f, int B) {
   TARA_CK(cudaMemsetAsync(f->g, 0, f->np * sizeof(float), f->stream));
   // projection
   if ((rc = colsum(f, f->dy, rows, c.co, f->g + f->off_q2))) return rc;
+  if (head_fused(f)) {
+    // dv = dh Q1^T and the partial dQ1, dq1, dQ2 of every CTA, then their sums
+    const int parts = head_bwd_tc_grid(rows);
+    const size_t nq1 = (size_t)C * c.p;
+    if ((size_t)parts * (nq1 + c.p + (size_t)c.p * c.co) > f->part_n)
+      return set_error(TARA_ERR_ARGS, "partial-sum buffer too small for the fused head");
+    if (!head_bwd_tc_launch(act_v(f, c.layers), f->dy, rows, f->p + f->off_Q1, f->p + f->off_q1,
+                            f->p + f->off_Q2, c.co, f->dv, f->part, f->errw, f->stream))
+      return set_error(TARA_ERR_CUDA, "fused head backward launch");
+    k_sum_parts<<<64, dim3(32, 8), 0, f->stream>>>(f->part, parts, (int)nq1, f->g + f->off_Q1, 0);
+    k_sum_parts<<<64, dim3(32, 8), 0, f->stream>>>(f->part + parts * nq1, parts, c.p, f->g + f->off_q1, 0);
+    k_sum_parts<<<64, dim3(32, 8), 0, f->stream>>>(f->part + parts * (nq1 + c.p), parts, c.p * c.co,
+                                                   f->g + f->off_Q2, 0);
+    TARA_CK(cudaGetLastError());
+  } else {
   if (c.p * c.co <= 1024) {
     if ((rc = wgrad_small(f, f->h, c.p, f->dy, c.co, rows, f->g + f->off_Q2))) return rc;
   } else if ((rc = gemm_tn_long(f, f->h, c.p, f->dy, c.co, f->g + f->off_Q2, c.p, c.co, rows, 0))) {
@@ -1196,6 +1230,7 @@ int backward(tara_fno* f, int B) {
     a.alpha = 1.f;
     if ((rc = gemm(f, a))) return rc;
   }
+  }  // layer-by-layer head
   for (int l = c.layers; l >= 1; --l) {
     float* dz = f->dz;
     if (l < c.layers) {

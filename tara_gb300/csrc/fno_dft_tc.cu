@@ -191,7 +191,11 @@ __global__ void __launch_bounds__(256, 1) k_m2x_tc(const float* __restrict__ a, 
   unsigned char* gl = gh + W * K * 2;         // low parts
   unsigned char* bh = gl + W * K * 2;         // [RB][C][K] A'^T of the round's rows, high
   unsigned char* bl = bh + RB * C * K * 2;    // low
-  unsigned long long* mbar = reinterpret_cast<unsigned long long*>(bl + RB * C * K * 2);
+  // the round's output rows [RB][W][C + 4] (FP32), staged so that the stores to
+  // memory go out as contiguous 16-byte runs across the CTA
+  constexpr int SP = C + 4;
+  float* stage = reinterpret_cast<float*>(bl + RB * C * K * 2);
+  unsigned long long* mbar = reinterpret_cast<unsigned long long*>(stage + RB * W * SP);
   uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 1);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   // G[x, (kx, re/im)] = (cos, -sin)(2 pi kx x / W)
@@ -258,25 +262,32 @@ __global__ void __launch_bounds__(256, 1) k_m2x_tc(const float* __restrict__ a, 
     const int x = (warp & 3) * 32 + lane;
     for (int jj = 0; jj < RB / 2; ++jj) {
       const int j = (warp >> 2) * (RB / 2) + jj;
-      const long long row = row0 + j;
       for (int c0 = 0; c0 < C; c0 += 8) {
         float d[8];
         umma::ld_8cols(tmem + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)(j * C + c0), d);
-        if (row < rows) {
-          float4* o = reinterpret_cast<float4*>(out + ((size_t)row * W + x) * C + c0);
-          float4 p0 = make_float4(d[0], d[1], d[2], d[3]), p1 = make_float4(d[4], d[5], d[6], d[7]);
-          if (accumulate) {
-            const float4 q0 = o[0], q1 = o[1];
-            p0.x += q0.x; p0.y += q0.y; p0.z += q0.z; p0.w += q0.w;
-            p1.x += q1.x; p1.y += q1.y; p1.z += q1.z; p1.w += q1.w;
-          }
-          o[0] = p0;
-          o[1] = p1;
-        }
+        float4* st = reinterpret_cast<float4*>(stage + (j * W + x) * SP + c0);
+        st[0] = make_float4(d[0], d[1], d[2], d[3]);
+        st[1] = make_float4(d[4], d[5], d[6], d[7]);
       }
     }
     umma::fence_before_sync();
-    __syncthreads();
+    __syncthreads();  // staged; the accumulators are free again
+    for (int e = tid; e < RB * W * (C / 4); e += 256) {
+      const int c4 = (e % (C / 4)) * 4, xx = (e / (C / 4)) % W, j = e / ((C / 4) * W);
+      const long long row = row0 + j;
+      if (row >= rows) continue;
+      float4 p = *reinterpret_cast<const float4*>(stage + (j * W + xx) * SP + c4);
+      float4* o = reinterpret_cast<float4*>(out + ((size_t)row * W + xx) * C + c4);
+      if (accumulate) {
+        const float4 q = *o;
+        p.x += q.x;
+        p.y += q.y;
+        p.z += q.z;
+        p.w += q.w;
+      }
+      *o = p;
+    }
+    __syncthreads();  // the stage is read before the next round writes it
   }
   if (failed && tid == 0) atomicOr(err, 4u);
   __syncthreads();
@@ -511,7 +522,7 @@ bool m2x_tc_launch(const float* a, float* out, long long rows, int W, int C, int
   if (rows < 1 || W != 128 || K % 16 || K > 64) return false;
   // (padded so that the CTAs resident on an SM hold at most 512 TMEM columns:
   // tcgen05.alloc waits while they are taken)
-  const size_t cols = tmem_cols(4 * C), need = (size_t)(2 * 128 * K + 2 * 4 * C * K) * 2 + 16,
+  const size_t cols = tmem_cols(4 * C), need = (size_t)(2 * 128 * K + 2 * 4 * C * K) * 2 + (size_t)4 * 128 * (C + 4) * 4 + 16,
                floor_bytes = (size_t)228 * 1024 / (512 / cols + 1);
   const size_t smem = need > floor_bytes ? need : floor_bytes;
   const long long rounds = (rows + 3) / 4;

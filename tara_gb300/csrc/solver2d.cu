@@ -829,6 +829,19 @@ int tara2d_autotune(tara2d* h, int trial_steps, int* variants3, double* ms24) {
     for (int c = kCandidates - 1; c >= 0; --c)
       if (candidate_ok(h, k, c)) dflt[k] = c;
   int best1[3] = {dflt[0], dflt[1], dflt[2]};
+  // Warm-up: about 50 ms of steps before anything is timed.  Timed from an idle
+  // GPU, the first candidates ran at lower clocks than the later ones, and at
+  // small grids that reordered the ranking.
+  if (!rc) {
+    for (int k = 0; k < 3; ++k) h->var[k] = dflt[k];
+    double kms[3] = {0.0, 0.0, 0.0}, tot = 0.0;
+    int cnt[3];
+    rc = tara2d_step_timed(h, 1, kms, cnt, &tot);
+    if (!rc) {
+      const int warm = (int)std::min(500.0, std::ceil(50.0 / std::max(tot, 1e-3)));
+      rc = tara2d_step(h, warm);
+    }
+  }
   auto timed = [&](double* t) {
     int r = tara2d_step(h, 1);
     int cnt[3];
@@ -896,8 +909,11 @@ int tara2d_autotune(tara2d* h, int trial_steps, int* variants3, double* ms24) {
     for (int k = 0; k < 3; ++k) est += ctx[k][top[k][0]] * (h->cfg.scheme == TARA_SCHEME_RK4 ? 4 : 1);
     const int reps = std::max(trial_steps, std::min(200, (int)(2.0 / std::max(est, 1e-3)) + 1));
     float best_ms = 0.f;
+    bool have = false;
     int pick[3] = {top[0][0], top[1][0], top[2][0]};
-    for (int m = 0; m < 8 && !rc; ++m) {
+    // every combination twice, the second sweep in reverse order
+    for (int it = 0; it < 16 && !rc; ++it) {
+      const int m = it < 8 ? it : 15 - it;
       const int v[3] = {top[0][m & 1], top[1][(m >> 1) & 1], top[2][(m >> 2) & 1]};
       bool dup = false;  // a kernel with one candidate repeats a combination
       for (int q = 0; q < 3; ++q) dup |= ((m >> q) & 1) && top[q][1] == top[q][0];
@@ -910,7 +926,8 @@ int tara2d_autotune(tara2d* h, int trial_steps, int* variants3, double* ms24) {
       if (!rc && (cudaEventRecord(e1, h->stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
                   cudaEventElapsedTime(&t, e0, e1) != cudaSuccess))
         rc = set_error(TARA_ERR_CUDA, "event timing");
-      if (!rc && (m == 0 || t < best_ms)) {
+      if (!rc && (!have || t < best_ms)) {
+        have = true;
         best_ms = t;
         for (int q = 0; q < 3; ++q) pick[q] = v[q];
       }
