@@ -17,6 +17,7 @@
 #include "tara_oracle.h"
 
 #include <math.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 #ifdef _OPENMP
@@ -96,16 +97,38 @@ void oracle_c2r_3d(int nx, int ny, int nz, const double* in, double* out) {
 int oracle_backend_is_fftw(void) { return 0; }
 
 /* Own FFT: iterative radix-2 decimation in time, twiddles from long-double
- * sin/cos rounded once.  Powers of two only. */
+ * sin/cos rounded once.  Lengths that are not powers of two take a direct DFT
+ * (O(n^2), same twiddle table over all n roots): the test sizes of the
+ * mixed-radix GPU path are small. */
 typedef struct {
   int n;
-  double* w; /* w[2k] = cos(2 pi k/n), w[2k+1] = -sin(2 pi k/n), k < n/2 */
-  int* rev;
+  double* w; /* w[2k] = cos(2 pi k/n), w[2k+1] = -sin(2 pi k/n), k < n/2 (k < n for a direct DFT) */
+  int* rev;  /* NULL: direct DFT */
 } fft_plan;
 
 static fft_plan g_plans[32];
+static fft_plan g_any_plans[64];
 
 static fft_plan* get_plan(int n) {
+  if (n & (n - 1)) { /* not a power of two */
+    for (int i = 0; i < 64; ++i) {
+      fft_plan* q = &g_any_plans[i];
+      if (q->n == n) return q;
+      if (q->n == 0) {
+        q->w = (double*)xcalloc(2 * (size_t)n, sizeof(double));
+        for (int k = 0; k < n; ++k) {
+          long double a = 2.0L * 3.141592653589793238462643383279502884L * (long double)k / (long double)n;
+          q->w[2 * k] = (double)cosl(a);
+          q->w[2 * k + 1] = (double)-sinl(a);
+        }
+        q->rev = NULL;
+        q->n = n;
+        return q;
+      }
+    }
+    fprintf(stderr, "oracle: too many transform lengths\n");
+    abort();
+  }
   int lg = 0;
   while ((1 << lg) < n) ++lg;
   fft_plan* p = &g_plans[lg];
@@ -129,6 +152,23 @@ static fft_plan* get_plan(int n) {
 
 /* in-place complex DFT of z[n] (interleaved); sign -1 forward, +1 backward */
 static void fft1d(double* z, int n, int sign, const fft_plan* p) {
+  if (!p->rev) { /* direct DFT: Z[k] = sum_j z[j] exp(sign 2 pi i j k / n) */
+    double* t = (double*)xcalloc(2 * (size_t)n, sizeof(double));
+    for (int k = 0; k < n; ++k) {
+      double sr = 0.0, si = 0.0;
+      for (int j = 0; j < n; ++j) {
+        const int m = (int)(((long long)j * k) % n);
+        const double wr = p->w[2 * m], wi = sign < 0 ? p->w[2 * m + 1] : -p->w[2 * m + 1];
+        sr += z[2 * j] * wr - z[2 * j + 1] * wi;
+        si += z[2 * j] * wi + z[2 * j + 1] * wr;
+      }
+      t[2 * k] = sr;
+      t[2 * k + 1] = si;
+    }
+    memcpy(z, t, 2 * (size_t)n * sizeof(double));
+    free(t);
+    return;
+  }
   for (int i = 0; i < n; ++i) {
     int r = p->rev[i];
     if (r > i) {

@@ -24,7 +24,7 @@ ORACLE = ROOT / "oracle"
 # TARA_REFERENCE environment variable; without it oracle/_ref is not built.
 REFERENCE = Path(os.environ["TARA_REFERENCE"]) if os.environ.get("TARA_REFERENCE") else None
 
-SOURCES = ["launch_fp64.cu", "launch_fp64_r8.cu", "launch_fp32.cu", "launch_fp32_r8.cu", "launch_df64.cu", "solver2d.cu", "capi.cu", "noalloc.cu", "mhd3d.cu",
+SOURCES = ["launch_fp64.cu", "launch_fp64_r8.cu", "launch_fp32.cu", "launch_fp32_r8.cu", "launch_df64.cu", "solver2d.cu", "generic2d.cu", "capi.cu", "noalloc.cu", "mhd3d.cu",
            "ensemble.cu", "ens_persistent.cu", "fno.cu", "fno_tc.cu", "fno_fused.cu", "fno_dft_tc.cu", "fno_head_tc.cu", "closure.cu", "particles.cu", "coh2d.cu", "com2d.cu", "ini.cpp",
            "driver.cpp"]
 EXE = PKG / "tara"

@@ -47,8 +47,10 @@ bool check_dims(const int* Nx, const int* Ny, const int* Nh) {
     set_error(TARA_ERR_ARGS, "null dimension argument");
     return false;
   }
-  if (!is_pow2_in_range(*Nx) || !is_pow2_in_range(*Ny) || *Nh != *Nx / 2 + 1) {
-    set_error(TARA_ERR_ARGS, "Nx, Ny must be powers of two in [16, 4096] and Nh = Nx/2+1");
+  if (!is_size_2d(*Nx) || !is_size_2d(*Ny) || *Nh != *Nx / 2 + 1) {
+    set_error(TARA_ERR_ARGS,
+              "Nx, Ny must be powers of two in [16, 4096] or even lengths 8 to 2048 with factors 2, 3, 5, "
+              "and Nh = Nx/2+1");
     return false;
   }
   return true;
@@ -254,9 +256,11 @@ int tara_measure_dfma_rate(int reps, double* inst_per_s) {
 }
 
 int tara_fft2d_r2c(int nx, int ny, int precision, const double* in, double* out) {
-  if (!is_pow2_in_range(nx) || !is_pow2_in_range(ny) || !in || !out)
+  if (!is_size_2d(nx) || !is_size_2d(ny) || !in || !out)
     return set_error(TARA_ERR_ARGS, "bad transform arguments");
   const bool f32 = precision == TARA_PREC_FP32;
+  if (f32 && (!is_pow2_in_range(nx) || !is_pow2_in_range(ny)))
+    return set_error(TARA_ERR_ARGS, "FP32 transforms take powers of two only");
   const int nh = nx / 2 + 1, pitch = round_up(nh, 8), rpitch = round_up(nx, 8);
   const size_t cs = f32 ? sizeof(float2) : sizeof(double2), rs = f32 ? sizeof(float) : sizeof(double);
   std::vector<unsigned char> hr((size_t)ny * rpitch * rs, 0), hc((size_t)ny * pitch * cs, 0);
@@ -306,9 +310,11 @@ int tara_fft2d_r2c(int nx, int ny, int precision, const double* in, double* out)
 
 // in: complex (Nh,Ny) interleaved (left untouched); out: real (Nx,Ny).
 int tara_fft2d_c2r(int nx, int ny, int precision, const double* in, double* out) {
-  if (!is_pow2_in_range(nx) || !is_pow2_in_range(ny) || !in || !out)
+  if (!is_size_2d(nx) || !is_size_2d(ny) || !in || !out)
     return set_error(TARA_ERR_ARGS, "bad transform arguments");
   const bool f32 = precision == TARA_PREC_FP32;
+  if (f32 && (!is_pow2_in_range(nx) || !is_pow2_in_range(ny)))
+    return set_error(TARA_ERR_ARGS, "FP32 transforms take powers of two only");
   const int nh = nx / 2 + 1, pitch = round_up(nh, 8), rpitch = round_up(nx, 8);
   const size_t cs = f32 ? sizeof(float2) : sizeof(double2), rs = f32 ? sizeof(float) : sizeof(double);
   std::vector<unsigned char> hr((size_t)ny * rpitch * rs, 0), hc((size_t)ny * pitch * cs, 0);

@@ -87,20 +87,38 @@ int fail_rc() { return tara_last_error() ? tara_last_error() : TARA_ERR_CUDA; }
 
 // The reference reads any Nx, Ny (, Nz) (src/main2csh.f95:35-38) and FFTW takes
 // any length; these kernels take powers of two, 16 to 4096 in 2D and 16 to 512
-// in 3D.  Refuse anything else before allocating, naming the supported set.
-int check_grid(const char* program, int dims, int nx, int ny, int nz) {
+// in 3D, and the incompressible 2D programs (any_ok) also even lengths 8 to
+// 2048 with factors 2, 3, 5 (the mixed-radix FP64 path).  Refuse anything else
+// before allocating, naming the supported set.
+// even, 8 to 2048, no prime factor above 5 (the mixed-radix path's lengths)
+bool mixed_radix_size(int n) {
+  if (n < 8 || n > 2048 || (n & 1)) return false;
+  for (int p : {2, 3, 5})
+    while (n % p == 0) n /= p;
+  return n == 1;
+}
+
+int check_grid(const char* program, int dims, int nx, int ny, int nz, bool any_ok = false) {
   const int hi = dims == 2 ? 4096 : 512;
   const int n[3] = {nx, ny, nz};
   const char* name[3] = {"Nx", "Ny", "Nz"};
-  for (int d = 0; d < dims; ++d)
-    if (n[d] < 16 || n[d] > hi || (n[d] & (n[d] - 1))) {
-      char msg[256];
+  for (int d = 0; d < dims; ++d) {
+    const bool pow2 = n[d] >= 16 && n[d] <= hi && !(n[d] & (n[d] - 1));
+    if (pow2 || (any_ok && mixed_radix_size(n[d]))) continue;
+    char msg[320];
+    if (any_ok)
+      std::snprintf(msg, sizeof msg,
+                    "%s: %s = %d is not supported; grid sizes here are powers of two from 16 to %d "
+                    "(16, 32, 64, ..., %d), or even lengths from 8 to 2048 whose only prime factors are "
+                    "2, 3 and 5 (e.g. 48, 96, 384)",
+                    program, name[d], n[d], hi, hi);
+    else
       std::snprintf(msg, sizeof msg,
                     "%s: %s = %d is not supported; grid sizes here are powers of two from 16 to %d "
                     "(16, 32, 64, ..., %d)",
                     program, name[d], n[d], hi, hi);
-      return set_error(TARA_ERR_ARGS, msg);
-    }
+    return set_error(TARA_ERR_ARGS, msg);
+  }
   return TARA_OK;
 }
 
@@ -123,7 +141,7 @@ int run_2d(Reader& R, const std::string& out, int max_steps, bool screened) {
   R.d("initialProfile", "m0", m0);
   R.d("initialProfile", "d", d);
   if (!R.ok) return set_error(TARA_ERR_INI, R.err);
-  if (int rc = check_grid(screened ? "tara2dScrSer" : "tara2dHydSer", 2, nx, ny, 0)) return rc;
+  if (int rc = check_grid(screened ? "tara2dScrSer" : "tara2dHydSer", 2, nx, ny, 0, true)) return rc;
   lx = lx * kPi;
   ly = ly * kPi;
   const double dx = lx / (double)nx, dy = ly / (double)ny;

@@ -85,6 +85,26 @@ struct Launch2D {
   static bool tile_fits(int k, int n, int v);
 };
 
+// Grid sizes that are not powers of two (generic2d.cu, fft_any.cuh): even,
+// 8 to 2048, factors 2, 3 and 5; FP64 only.  The Launch2D entry points route
+// such lengths there.
+bool any_size_2d(int n);
+inline bool is_size_2d(int n) { return is_pow2_in_range(n) || any_size_2d(n); }
+namespace any2d {
+int col_inverse(int ny, int nh, const double2* win, void* u, const Grid2D& g, const RhsParams& p, const void* twy,
+                cudaStream_t s, int nb);
+int row_nl(int nx, int ny, const void* u, void* nl, const Grid2D& g, const void* twx, cudaStream_t s, int nb);
+int col_forward(int ny, int nh, const void* nl, const StepBufs& sb, const Grid2D& g, const RhsParams& p, int mode,
+                const void* twy, cudaStream_t s, int nb);
+int col_fft(int ny, int nh, int pitch, const void* in, void* out, bool inverse, const void* twy, cudaStream_t s,
+            int nf, size_t fs);
+int row_c2r(int nx, int ny, int pitch, int rpitch, const void* in, void* out, const void* twx, cudaStream_t s, int nf,
+            size_t fs_in, size_t fs_out);
+int row_r2c(int nx, int ny, int rpitch, int pitch, const void* in, void* out, const void* twx, cudaStream_t s, int nf,
+            size_t fs_in, size_t fs_out);
+int make_roots(int n, void** dev);  // exp(-2 pi i t / n), t < n, FP64
+}  // namespace any2d
+
 // Twiddle exp(-2 pi i m/n) in FP64 with tw[n - m] = conj(tw[m]) exactly.
 void twiddle(int n, int m, double* re, double* im);
 // Entry idx < tw_count(n) of the length-n twiddle table (layout in fft.cuh).

@@ -2,6 +2,8 @@
 // length.  Included once per precision (launch_fp64.cu, launch_fp32.cu) so the
 // two instantiation sets compile in parallel.
 #pragma once
+#include <type_traits>
+
 #include "internal.h"
 
 namespace tara {
@@ -197,8 +199,20 @@ static bool tile_fits_n(int k, int v) {
          : v == 2 ? ColCfg<T, N, 2>::VALID_C : false;
 }
 
+// Lengths that are not powers of two go to the mixed-radix FP64 passes
+// (generic2d.cu); they have one configuration (variant 0).
+#define TARA_ANY_2D(n, CALL)                                                                 \
+  if (!is_pow2_in_range(n)) {                                                                \
+    if constexpr (std::is_same<T, double>::value) {                                          \
+      if (any_size_2d(n)) return CALL;                                                       \
+    }                                                                                        \
+    return set_error(TARA_ERR_ARGS, "grid sizes that are not powers of two need FP64, even " \
+                                    "lengths 8 to 2048 with factors 2, 3, 5");               \
+  }
+
 template <typename T>
 bool Launch2D<T>::tile_fits(int k, int n, int v) {
+  if (!is_pow2_in_range(n)) return std::is_same<T, double>::value && any_size_2d(n) && v == 0;
   switch (n) {
     case 16: return tile_fits_n<T, 16>(k, v);
     case 32: return tile_fits_n<T, 32>(k, v);
@@ -219,6 +233,7 @@ bool Launch2D<T>::tile_fits(int k, int n, int v) {
 template <typename T>
 int Launch2D<T>::col_inverse(int ny, int nh, const double2* win, void* u, const Grid2D& g,
                              const RhsParams& p, const void* twy, cudaStream_t s, int nb, int v) {
+  TARA_ANY_2D(ny, any2d::col_inverse(ny, nh, win, u, g, p, twy, s, nb))
   if constexpr (!is_df64<T>())
     if (v & 4) return step_col_inverse<T, 8>(ny, nh, win, u, g, p, twy, s, nb, v & 3);
   return step_col_inverse<T, 4>(ny, nh, win, u, g, p, twy, s, nb, v & 3);
@@ -227,6 +242,7 @@ int Launch2D<T>::col_inverse(int ny, int nh, const double2* win, void* u, const 
 template <typename T>
 int Launch2D<T>::row_nl(int nx, int ny, const void* u, void* nl, const Grid2D& g, const void* twx,
                         cudaStream_t s, int nb, int v) {
+  TARA_ANY_2D(nx, any2d::row_nl(nx, ny, u, nl, g, twx, s, nb))
   if constexpr (!is_df64<T>())
     if (v & 4) return step_row_nl<T, 8>(nx, ny, u, nl, g, twx, s, nb, v & 3);
   return step_row_nl<T, 4>(nx, ny, u, nl, g, twx, s, nb, v & 3);
@@ -236,6 +252,7 @@ template <typename T>
 int Launch2D<T>::col_forward(int ny, int nh, const void* nl, const StepBufs& sb, const Grid2D& g,
                              const RhsParams& p, int mode, const void* twy, cudaStream_t s, int nb,
                              int v) {
+  TARA_ANY_2D(ny, any2d::col_forward(ny, nh, nl, sb, g, p, mode, twy, s, nb))
   if constexpr (!is_df64<T>())
     if (v & 4) return step_col_forward<T, 8>(ny, nh, nl, sb, g, p, mode, twy, s, nb, v & 3);
   return step_col_forward<T, 4>(ny, nh, nl, sb, g, p, mode, twy, s, nb, v & 3);
@@ -255,6 +272,7 @@ int Launch2D<T>::col_forward(int ny, int nh, const void* nl, const StepBufs& sb,
 template <typename T>
 int Launch2D<T>::col_fft(int ny, int nh, int pitch, const void* in, void* out, bool inverse,
                          const void* twy, cudaStream_t s, int nf, size_t fs) {
+  TARA_ANY_2D(ny, any2d::col_fft(ny, nh, pitch, in, out, inverse, twy, s, nf, fs))
   if (inverse) {
     TARA_SWITCH_N(ny, return (small_col<T, N>(nh, nf)
                                   ? launch_col_fft<T, N, true, 2>(nh, pitch, in, out, twy, s, nf, fs)
@@ -270,6 +288,7 @@ int Launch2D<T>::col_fft(int ny, int nh, int pitch, const void* in, void* out, b
 template <typename T>
 int Launch2D<T>::row_c2r(int nx, int ny, int pitch, int rpitch, const void* in, void* out,
                          const void* twx, cudaStream_t s, int nf, size_t fs_in, size_t fs_out) {
+  TARA_ANY_2D(nx, any2d::row_c2r(nx, ny, pitch, rpitch, in, out, twx, s, nf, fs_in, fs_out))
   TARA_SWITCH_N(nx, return (small_row<T, N>(ny, nf)
                                 ? launch_row_c2r<T, N, 2>(ny, pitch, rpitch, in, out, twx, s, nf, fs_in, fs_out)
                                 : launch_row_c2r<T, N, 0>(ny, pitch, rpitch, in, out, twx, s, nf, fs_in, fs_out)));
@@ -279,6 +298,7 @@ int Launch2D<T>::row_c2r(int nx, int ny, int pitch, int rpitch, const void* in, 
 template <typename T>
 int Launch2D<T>::row_r2c(int nx, int ny, int rpitch, int pitch, const void* in, void* out,
                          const void* twx, cudaStream_t s, int nf, size_t fs_in, size_t fs_out) {
+  TARA_ANY_2D(nx, any2d::row_r2c(nx, ny, rpitch, pitch, in, out, twx, s, nf, fs_in, fs_out))
   TARA_SWITCH_N(nx, return (small_row<T, N>(ny, nf)
                                 ? launch_row_r2c<T, N, 2>(ny, rpitch, pitch, in, out, twx, s, nf, fs_in, fs_out)
                                 : launch_row_r2c<T, N, 0>(ny, rpitch, pitch, in, out, twx, s, nf, fs_in, fs_out)));

@@ -130,6 +130,10 @@ void twiddle_entry(int n, int idx, double* re, double* im) {
 }
 
 int make_twiddles(int n, bool fp32, void** dev) {
+  if (!is_pow2_in_range(n)) {  // the mixed-radix path: the n roots, FP64 only
+    if (fp32 || !any_size_2d(n)) return set_error(TARA_ERR_ARGS, "twiddles: unsupported length");
+    return any2d::make_roots(n, dev);
+  }
   const int cnt = tw_count(n);
   if (fp32) {
     std::vector<float2> w(cnt);
@@ -156,6 +160,7 @@ int make_twiddles(int n, bool fp32, void** dev) {
 // The same table as double-float pairs (hi, lo) per component, for the
 // double-float transforms: hi = fl32(w), lo = fl32(w - hi).
 int make_twiddles_df64(int n, void** dev) {
+  if (!is_pow2_in_range(n)) return set_error(TARA_ERR_ARGS, "the double-float form takes powers of two only");
   const int cnt = tw_count(n);
   std::vector<float4> w(cnt);
   for (int m = 0; m < cnt; ++m) {
@@ -572,6 +577,7 @@ int tara2d_destroy(tara2d* h) {
 // for step kernel k of handle h?
 static bool candidate_ok(const tara2d* h, int k, int c) {
   if ((c & 3) >= kVariants[k] || ((c & 4) && h->cfg.precision == TARA_PREC_DF64)) return false;
+  if (!is_pow2_in_range(h->nx) || !is_pow2_in_range(h->ny)) return c == 0;  // mixed-radix path: one form
   const int n = k == 1 ? h->nx : h->ny;  // the row pass transforms along x, the others along y
   switch (h->cfg.precision) {
     case TARA_PREC_FP32: return Launch2D<float>::tile_fits(k, n, c & 3);
@@ -583,8 +589,12 @@ static bool candidate_ok(const tara2d* h, int k, int c) {
 int tara2d_create(const tara2d_config* cfg, tara2d** out) {
   if (!cfg || !out) return set_error(TARA_ERR_ARGS, "null argument");
   *out = nullptr;
-  if (!is_pow2_in_range(cfg->nx) || !is_pow2_in_range(cfg->ny))
-    return set_error(TARA_ERR_ARGS, "nx and ny must be powers of two in [16, 4096]");
+  if (!is_size_2d(cfg->nx) || !is_size_2d(cfg->ny))
+    return set_error(TARA_ERR_ARGS,
+                     "nx and ny must be powers of two in [16, 4096], or (FP64) even lengths 8 to 2048 "
+                     "with factors 2, 3, 5");
+  if ((!is_pow2_in_range(cfg->nx) || !is_pow2_in_range(cfg->ny)) && cfg->precision != TARA_PREC_FP64)
+    return set_error(TARA_ERR_ARGS, "grid sizes that are not powers of two take the FP64 precision only");
   if (cfg->rhs != TARA_RHS_PLAIN && cfg->rhs != TARA_RHS_SCREEN)
     return set_error(TARA_ERR_ARGS, "unknown rhs kind");
   if (cfg->scheme != TARA_SCHEME_AB2 && cfg->scheme != TARA_SCHEME_RK4)

@@ -46,7 +46,7 @@ def _cfg(nx, ny):
     return c
 
 
-@pytest.mark.parametrize("nx,ny", [(100, 64), (64, 8), (8192, 64), (0, 0), (64, 3)])
+@pytest.mark.parametrize("nx,ny", [(98, 64), (64, 7), (8192, 64), (0, 0), (64, 3), (4096 + 2048, 64)])
 def test_create_rejects_bad_sizes(nx, ny):
     h = ctypes.c_void_p()
     rc = tg.lib().tara2d_create(ctypes.byref(_cfg(nx, ny)), ctypes.byref(h))
@@ -75,7 +75,7 @@ def test_dropin_bad_dims_records_error():
 
 def test_python_wrapper_raises_on_bad_args():
     with pytest.raises(tg.TaraError) as e:
-        tg.fft2d_r2c(np.zeros((24, 24)))
+        tg.fft2d_r2c(np.zeros((22, 22)))  # a factor 11: neither path takes it
     assert e.value.code == tg.TARA_ERR_ARGS
 
 
@@ -158,7 +158,7 @@ def test_features_need_one_scale_per_channel():
 
 
 @pytest.mark.parametrize("grid,dim,program,bad", [
-    ("Nx = 96\nNy = 64\nNz = 64", 2, "tara2dHydSer", "Nx = 96"),
+    ("Nx = 98\nNy = 64\nNz = 64", 2, "tara2dHydSer", "Nx = 98"),
     ("Nx = 64\nNy = 8192\nNz = 64", 2, "tara2dHydSer", "Ny = 8192"),
     ("Nx = 64\nNy = 64\nNz = 384", 3, "tara3dMHDOMP", "Nz = 384"),
     ("Nx = 1024\nNy = 64\nNz = 64", 3, "tara3dMHDOMP", "Nx = 1024"),
@@ -180,3 +180,5 @@ def test_driver_refuses_unsupported_grids(tmp_path, grid, dim, program, bad):
     code, msg = tg.last_error()
     assert rc == tg.TARA_ERR_ARGS and code == tg.TARA_ERR_ARGS
     assert program in msg and bad in msg and "powers of two" in msg
+    if dim == 2:
+        assert "factors are 2, 3 and 5" in msg
