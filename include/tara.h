@@ -21,6 +21,10 @@
  *    int status (TARA_OK = 0).
  *
  * Grid sizes: Nx and Ny powers of two from 16 to 4096 (the 2D paths; 3D: 16 to 512).
+ * The incompressible 2D path in FP64 (the derive2csh_ / derive2css_ / ab2csh_ /
+ * ab2css_ / rk42css_ drop-ins, tara2d_* with TARA_PREC_FP64, tara_fft2d_* in
+ * FP64 and the tara2dHydSer / tara2dScrSer programs) also takes even lengths
+ * from 8 to 2048 whose only prime factors are 2, 3 and 5 (mixed-radix passes).
  */
 #ifndef TARA_H
 #define TARA_H
@@ -107,7 +111,7 @@ int tara_finalize(void);
 #define TARA_PREC_DF64 2   /* double-float (FP32 pair) FFTs and products; FP64 state */
 
 typedef struct tara2d_config {
-  int nx, ny;      /* powers of two, 16..4096 */
+  int nx, ny;      /* powers of two, 16..4096; in FP64 also even 8..2048 with factors 2, 3, 5 */
   int rhs;         /* TARA_RHS_* */
   int scheme;      /* TARA_SCHEME_* */
   int precision;   /* TARA_PREC_* */
