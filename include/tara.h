@@ -472,7 +472,7 @@ int tara3d_diag(tara3d* h, double* out4);
  * arch cpu and single-gpu both run on the GPU.  Output files go to out_dir
  * (the reference writes ./output).  max_steps > 0 caps the number of steps
  * (0: the full time_min..time_max loop).  Returns TARA_ERR_INI for a missing or
- * malformed ini key, TARA_ERR_ARGS for a solver outside this build. */
+ * malformed ini key, TARA_ERR_ARGS for a solver this library does not implement. */
 int tara_run_ini(const char* ini_path, const char* out_dir, int max_steps);
 
 /* cfg%gets of the reference's ini parser: the value of section/key with the

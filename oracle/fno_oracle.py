@@ -1,7 +1,7 @@
 """CPU oracle of the learned closure -- TEST INFRASTRUCTURE ONLY.
 
 Only tests/, ``__graft_entry__.smoke()`` and bench.py's checks import this
-module, as the checker of libtara's Fourier neural operator (tara_fno_*) and of
+module, as the oracle of libtara's Fourier neural operator (tara_fno_*) and of
 its closure pieces (box filter, shell spectrum).  Nothing here runs on the
 product path.
 

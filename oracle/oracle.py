@@ -1,7 +1,7 @@
 """ctypes binding of the CPU oracle -- TEST INFRASTRUCTURE ONLY.
 
 Only tests/, ``__graft_entry__.smoke()`` and the CPU-baseline leg of bench.py
-import this module, and only as the checker.  ``load()`` returns the own-FFT
+import this module, and only as the oracle.  ``load()`` returns the own-FFT
 restatement (liboracle.so, builds anywhere); ``load(fftw=True)`` returns the
 same restatement over FFTW 3.3.9 compiled from the reference's vendored sources
 (oracle/_ref/liboracle_fftw.so), which exists only where the reference tree was

@@ -1,7 +1,7 @@
 /* CPU oracle for the TARA 2D pseudo-spectral path -- TEST INFRASTRUCTURE ONLY.
  *
  * Only the test suite, smoke() and the bench's CPU-baseline leg load this
- * library, and only as the checker.  The product library never links it.
+ * library, and only as the oracle.  The product library never links it.
  *
  * Each function restates one reference subroutine; the citation on each names
  * the file:line it follows.  All arithmetic is IEEE double without FMA

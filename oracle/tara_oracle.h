@@ -1,7 +1,7 @@
 /* CPU oracle for the TARA 2D pseudo-spectral path -- TEST INFRASTRUCTURE ONLY.
  *
  * A plain-C restatement of the reference subroutines on the hot path, used by
- * the test suite, smoke() and the bench's CPU-baseline leg as the checker.  It
+ * the test suite, smoke() and the bench's CPU-baseline leg as the oracle.  It
  * is never linked into the product library.
  *
  * Arrays follow the reference's Fortran layout: a half spectrum complex(8)
@@ -22,7 +22,7 @@
 extern "C" {
 #endif
 
-/* 1 when this build routes transforms through FFTW, 0 for the own FFT */
+/* 1 when the loaded library routes transforms through FFTW, 0 for the own FFT */
 int oracle_backend_is_fftw(void);
 /* OpenMP threads used by the own-FFT backend (<=0: all available) */
 void oracle_set_threads(int n);

@@ -535,7 +535,7 @@ extern "C" int tara_run_ini(const char* ini_path, const char* out_dir, int max_s
     say(" Under preparation. Please wait!\n");  // src/main.f95:40-85
     return set_ok();
   }
-  if (dim == 1) return set_error(TARA_ERR_ARGS, "the 1D Burgers solver is outside this build");
+  if (dim == 1) return set_error(TARA_ERR_ARGS, "the 1D Burgers solver is not implemented by this library");
   say(" Incompatible Input file. Please check TARA user-manual.\n");
   return set_error(TARA_ERR_INI, "incompatible input file");
 }

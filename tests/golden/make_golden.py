@@ -1,6 +1,6 @@
 """Generate tests/golden/golden64.npz from the FFTW-backed oracle.
 
-The oracle restates the reference's 2D path in C; this build of it routes every
+The oracle restates the reference's 2D path in C; its FFTW-backed version routes every
 transform through FFTW 3.3.9 compiled from the reference's own vendored sources
 (oracle/_ref, made by ``make -C oracle ref``), planned FFTW_ESTIMATE per
 transform as src/derive2csh.f95:73-106 does.  The fixtures pin the portable

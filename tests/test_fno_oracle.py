@@ -1,7 +1,7 @@
 """CPU tests of the learned-closure oracle (oracle/fno_oracle.py): the rfft2
 form of the spectral convolution equals its explicit-sum restatement, autograd
 gradients equal finite differences, and the box filter / shell spectrum keep
-their defining identities.  These pin the checker the GPU tests rely on."""
+their defining identities.  These pin the oracle the GPU tests rely on."""
 from __future__ import annotations
 
 import numpy as np
