@@ -51,6 +51,68 @@ __device__ __forceinline__ double2 cmul_any(double2 a, double2 b) {
   return make_double2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
 }
 
+// One Stockham stage of radix R (compile-time: the R values stay in registers).
+// The small DFT: radix 2 and 4 by their butterflies, 3 and 5 by the table roots
+// W_R^m = W_n^(m n / R) read once per stage.
+template <int R>
+__device__ __forceinline__ void any_stage(const double2* __restrict__ src, double2* __restrict__ dst, int n, int ns,
+                                          const double2* __restrict__ w, bool inverse, int tid, int nthreads) {
+  const int m = n / R;
+  const int q = n / (ns * R);  // twiddle index step per unit of (j mod ns) and r
+  double2 wr[R];
+#pragma unroll
+  for (int k = 0; k < R; ++k) {
+    wr[k] = w[k * (n / R)];
+    if (inverse) wr[k].y = -wr[k].y;
+  }
+  for (int j = tid; j < m; j += nthreads) {
+    const int jm = j % ns, base = (j / ns) * ns * R + jm;
+    const int tstep = jm * q;
+    double2 v[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      double2 x = src[j + r * m];
+      if (r > 0 && tstep > 0) {
+        double2 t = w[r * tstep];  // r * tstep < n
+        if (inverse) t.y = -t.y;
+        x = cmul_any(x, t);
+      }
+      v[r] = x;
+    }
+    double2 V[R];
+    if constexpr (R == 2) {
+      V[0] = make_double2(v[0].x + v[1].x, v[0].y + v[1].y);
+      V[1] = make_double2(v[0].x - v[1].x, v[0].y - v[1].y);
+    } else if constexpr (R == 4) {
+      // W_4 = -i forward, +i inverse
+      const double2 a = make_double2(v[0].x + v[2].x, v[0].y + v[2].y);
+      const double2 b = make_double2(v[0].x - v[2].x, v[0].y - v[2].y);
+      const double2 c = make_double2(v[1].x + v[3].x, v[1].y + v[3].y);
+      const double2 d = make_double2(v[1].x - v[3].x, v[1].y - v[3].y);
+      // -i d (forward) or +i d (inverse)
+      const double2 e = inverse ? make_double2(-d.y, d.x) : make_double2(d.y, -d.x);
+      V[0] = make_double2(a.x + c.x, a.y + c.y);
+      V[1] = make_double2(b.x + e.x, b.y + e.y);
+      V[2] = make_double2(a.x - c.x, a.y - c.y);
+      V[3] = make_double2(b.x - e.x, b.y - e.y);
+    } else {
+#pragma unroll
+      for (int k = 0; k < R; ++k) {
+        double2 acc = v[0];
+#pragma unroll
+        for (int r = 1; r < R; ++r) {
+          const double2 p = cmul_any(v[r], wr[(r * k) % R]);
+          acc.x += p.x;
+          acc.y += p.y;
+        }
+        V[k] = acc;
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < R; ++k) dst[base + k * ns] = V[k];
+  }
+}
+
 // In-place transform of buf[0, n) with scratch tmp[0, n) (both shared memory),
 // by all `nthreads` threads of the CTA (tid < nthreads).  w: the n roots
 // exp(-2 pi i t / n); inverse: their conjugates.  Ends with a barrier; the
@@ -62,33 +124,12 @@ __device__ inline void fft_any(double2* buf, double2* tmp, const AnyPlan& pl, co
   double2* dst = tmp;
   int ns = 1;
   for (int st = 0; st < pl.stages; ++st) {
-    const int R = pl.radix[st], m = n / R;
-    for (int j = tid; j < m; j += nthreads) {
-      const int jm = j % ns, base = (j / ns) * ns * R + jm;
-      const int tstep = jm * (n / (ns * R));  // twiddle index step per r
-      double2 v[5];
-      for (int r = 0; r < R; ++r) {
-        double2 x = src[j + r * m];
-        if (r > 0 && tstep > 0) {
-          double2 t = w[(r * tstep) % n];
-          if (inverse) t.y = -t.y;
-          x = cmul_any(x, t);
-        }
-        v[r] = x;
-      }
-      // V[k] = sum_r v[r] W_R^(r k)
-      const int q = n / R;
-      for (int k = 0; k < R; ++k) {
-        double2 acc = v[0];
-        for (int r = 1; r < R; ++r) {
-          double2 t = w[((r * k) % R) * q];
-          if (inverse) t.y = -t.y;
-          const double2 p = cmul_any(v[r], t);
-          acc.x += p.x;
-          acc.y += p.y;
-        }
-        dst[base + k * ns] = acc;
-      }
+    const int R = pl.radix[st];
+    switch (R) {
+      case 4: any_stage<4>(src, dst, n, ns, w, inverse, tid, nthreads); break;
+      case 2: any_stage<2>(src, dst, n, ns, w, inverse, tid, nthreads); break;
+      case 3: any_stage<3>(src, dst, n, ns, w, inverse, tid, nthreads); break;
+      default: any_stage<5>(src, dst, n, ns, w, inverse, tid, nthreads); break;
     }
     __syncthreads();
     double2* s = src;
