@@ -52,8 +52,8 @@ __device__ __forceinline__ double2 cmul_any(double2 a, double2 b) {
 }
 
 // One Stockham stage of radix R (compile-time: the R values stay in registers).
-// The small DFT: radix 2 and 4 by their butterflies, 3 and 5 by the table roots
-// W_R^m = W_n^(m n / R) read once per stage.
+// The small DFTs are the standard butterflies; radix 3 and 5 take their cosines
+// and sines from the table roots W_R^m = W_n^(m n / R), read once per stage.
 template <int R>
 __device__ __forceinline__ void any_stage(const double2* __restrict__ src, double2* __restrict__ dst, int n, int ns,
                                           const double2* __restrict__ w, bool inverse, int tid, int nthreads) {
@@ -95,18 +95,31 @@ __device__ __forceinline__ void any_stage(const double2* __restrict__ src, doubl
       V[1] = make_double2(b.x + e.x, b.y + e.y);
       V[2] = make_double2(a.x - c.x, a.y - c.y);
       V[3] = make_double2(b.x - e.x, b.y - e.y);
-    } else {
-#pragma unroll
-      for (int k = 0; k < R; ++k) {
-        double2 acc = v[0];
-#pragma unroll
-        for (int r = 1; r < R; ++r) {
-          const double2 p = cmul_any(v[r], wr[(r * k) % R]);
-          acc.x += p.x;
-          acc.y += p.y;
-        }
-        V[k] = acc;
-      }
+    } else if constexpr (R == 3) {
+      // W_3 = c - i s (forward; the inverse table carries -s)
+      const double c = wr[1].x, sn = -wr[1].y;
+      const double2 t1 = make_double2(v[1].x + v[2].x, v[1].y + v[2].y);
+      const double2 t2 = make_double2(v[1].x - v[2].x, v[1].y - v[2].y);
+      const double2 a = make_double2(fma(c, t1.x, v[0].x), fma(c, t1.y, v[0].y));
+      const double2 b = make_double2(sn * t2.x, sn * t2.y);  // V1 = a - i b, V2 = a + i b
+      V[0] = make_double2(v[0].x + t1.x, v[0].y + t1.y);
+      V[1] = make_double2(a.x + b.y, a.y - b.x);
+      V[2] = make_double2(a.x - b.y, a.y + b.x);
+    } else {  // R == 5: W_5 = c1 - i s1, W_5^2 = c2 - i s2
+      const double c1 = wr[1].x, s1 = -wr[1].y, c2 = wr[2].x, s2 = -wr[2].y;
+      const double2 t1 = make_double2(v[1].x + v[4].x, v[1].y + v[4].y);
+      const double2 t2 = make_double2(v[2].x + v[3].x, v[2].y + v[3].y);
+      const double2 t3 = make_double2(v[1].x - v[4].x, v[1].y - v[4].y);
+      const double2 t4 = make_double2(v[2].x - v[3].x, v[2].y - v[3].y);
+      const double2 a1 = make_double2(fma(c2, t2.x, fma(c1, t1.x, v[0].x)), fma(c2, t2.y, fma(c1, t1.y, v[0].y)));
+      const double2 a2 = make_double2(fma(c1, t2.x, fma(c2, t1.x, v[0].x)), fma(c1, t2.y, fma(c2, t1.y, v[0].y)));
+      const double2 b1 = make_double2(fma(s2, t4.x, s1 * t3.x), fma(s2, t4.y, s1 * t3.y));
+      const double2 b2 = make_double2(fma(-s1, t4.x, s2 * t3.x), fma(-s1, t4.y, s2 * t3.y));
+      V[0] = make_double2(v[0].x + t1.x + t2.x, v[0].y + t1.y + t2.y);
+      V[1] = make_double2(a1.x + b1.y, a1.y - b1.x);  // a1 - i b1
+      V[4] = make_double2(a1.x - b1.y, a1.y + b1.x);  // a1 + i b1
+      V[2] = make_double2(a2.x + b2.y, a2.y - b2.x);
+      V[3] = make_double2(a2.x - b2.y, a2.y + b2.x);
     }
 #pragma unroll
     for (int k = 0; k < R; ++k) dst[base + k * ns] = V[k];
