@@ -41,6 +41,13 @@ constexpr int kW = kFusedW, kC = kFusedC, kThreads = 256, kModeGroup = 4;
 // thread owns one grid point x and kCpt channels, and each 128-thread quarter
 // one quarter of the x range in the row DFT.
 constexpr int kRT = 512, kQ = kRT / 128, kCpt = kC / kQ;
+constexpr int kK2 = 2 * kFusedMaxMX;  // the inverse x-DFT's K: (kx, re/im), padded with zeros past 2 MX
+
+__device__ __forceinline__ void split_store(unsigned char* hi, unsigned char* lo, uint32_t off, float v) {
+  const __nv_bfloat16 h = __float2bfloat16_rn(v);
+  *reinterpret_cast<__nv_bfloat16*>(hi + off) = h;
+  *reinterpret_cast<__nv_bfloat16*>(lo + off) = __float2bfloat16_rn(v - __bfloat162float(h));
+}
 constexpr uint32_t kFwWait = 1u << 20;  // polls of an mbarrier before a wait gives up
 constexpr uint32_t kBulkChunk = 16384;   // bytes per bulk copy instruction
 
@@ -64,8 +71,13 @@ template <int P> struct RowSmem {
   static constexpr int A = 0;                        // 128 x 32 BF16 activations, canonical layout
   static constexpr int BW = A + kW * kC * 2;         // 32 x 32 BF16 pointwise weights (N x K)
   static constexpr int BQ = BW + kC * kC * 2;        // P x 32 BF16 projection weights (N x K)
-  static constexpr int U = BQ + P * kC * 2;          // [MX][2][C] inverse-y modes, scaled
-  static constexpr int TWX = U + kFusedMaxMX * 2 * kC * 4;  // cos, sin (2 pi t / W)
+  // the inverse x-DFT as a product with the same accumulator: G (x, (kx, re/im))
+  // and U ((c), (kx, re/im)), each split into BF16 high and low parts
+  static constexpr int GH = BQ + P * kC * 2;         // 128 x 32 BF16
+  static constexpr int GL = GH + kW * kK2 * 2;
+  static constexpr int UH = GL + kW * kK2 * 2;       // 32 x 32 BF16 (N = channels, K = modes)
+  static constexpr int UL = UH + kC * kK2 * 2;
+  static constexpr int TWX = UL + kC * kK2 * 2;      // cos, sin (2 pi t / W)
   static constexpr int TWY = TWX + 2 * kW * 4;              // cos, sin (2 pi t / H)
   static constexpr int SV = TWY + 2 * kFusedMaxH * 4;       // [W][C] FP32 activations / y partials
   static constexpr int PART = SV + kW * kC * 4;             // [kQ][MX][2][C] DFT partial sums
@@ -232,7 +244,10 @@ __global__ void __launch_bounds__(kRT, 1) k_fused_row(FusedFwdArgs a, int layer)
   __nv_bfloat16* As = reinterpret_cast<__nv_bfloat16*>(fused_sm + L::A);
   __nv_bfloat16* Bw = reinterpret_cast<__nv_bfloat16*>(fused_sm + L::BW);
   __nv_bfloat16* Bq = reinterpret_cast<__nv_bfloat16*>(fused_sm + L::BQ);
-  float* su = reinterpret_cast<float*>(fused_sm + L::U);
+  unsigned char* gh = fused_sm + L::GH;
+  unsigned char* gl = fused_sm + L::GL;
+  unsigned char* uh = fused_sm + L::UH;
+  unsigned char* ul = fused_sm + L::UL;
   float* twx = reinterpret_cast<float*>(fused_sm + L::TWX);
   float* twy = reinterpret_cast<float*>(fused_sm + L::TWY);
   float* sv = reinterpret_cast<float*>(fused_sm + L::SV);
@@ -265,6 +280,21 @@ __global__ void __launch_bounds__(kRT, 1) k_fused_row(FusedFwdArgs a, int layer)
   }
   for (int e = tid; e < 2 * kW; e += kRT) twx[e] = a.csx[e];
   for (int e = tid; e < 2 * H; e += kRT) twy[e] = a.csy[e];
+  // G[x, (kx, re)] = cos, G[x, (kx, im)] = -sin (2 pi kx x / W), zero past 2 MX;
+  // and the U columns past 2 MX, zero
+  for (int e = tid; e < kW * kK2; e += kRT) {
+    const int x = e / kK2, k = e % kK2, kx = k >> 1;
+    float g = 0.f;
+    if (kx < MX) {
+      const int t = (kx * x) & (kW - 1);
+      g = (k & 1) ? -a.csx[2 * t + 1] : a.csx[2 * t];
+    }
+    split_store(gh, gl, umma::elem_offset<kK2>(x, k), g);
+  }
+  for (int e = tid; e < kC * (kK2 - 2 * MX); e += kRT) {
+    const int c = e / (kK2 - 2 * MX), k = 2 * MX + e % (kK2 - 2 * MX);
+    split_store(uh, ul, umma::elem_offset<kK2>(c, k), 0.f);
+  }
   if (warp == 0) umma::alloc(umma::smem_addr(tmem_slot), L::TMEM_COLS);
   // then one thread starts the bulk copies of this sample's mixed modes Y[b]
   // (all rows need all of them) and of v_{l-1}'s row (FP32, into sv)
@@ -298,16 +328,8 @@ __global__ void __launch_bounds__(kRT, 1) k_fused_row(FusedFwdArgs a, int layer)
   umma::fence_after_sync();
   const uint32_t tmem = *tmem_slot;
   constexpr uint32_t kSbo = (kC / 8) * 128;
-  if (ok && tid == 0) {  // z = v W: M = 128 rows (x), N = 32, K = 32 in two K = 16 steps
-    const uint32_t a0 = umma::smem_addr(As), b0 = umma::smem_addr(Bw);
-    const uint32_t idesc = umma::idesc_bf16_f32(kW, kC);
-#pragma unroll
-    for (int s = 0; s < kC / 16; ++s)
-      umma::mma_bf16(tmem, umma::smem_desc(a0 + 2 * s * 128, 128, kSbo), umma::smem_desc(b0 + 2 * s * 128, 128, kSbo),
-                     idesc, s > 0);
-    umma::commit(mb);
-  }
-  // meanwhile: U[kx, c] = w_kx sum_j Y[b, j, kx, c] exp(+2 pi i ky(j) y / H) for this row
+  static_assert(kK2 == kC, "one stride serves both K = 32 operands");
+  // U[kx, c] = w_kx sum_j Y[b, j, kx, c] exp(+2 pi i ky(j) y / H) for this row
   for (int e = tid; e < MX * kC; e += kRT) {
     const int kx = e / kC, c = e % kC;
     float re = 0.f, im = 0.f;
@@ -321,26 +343,32 @@ __global__ void __launch_bounds__(kRT, 1) k_fused_row(FusedFwdArgs a, int layer)
       im = fmaf(vr, si, fmaf(vi, co, im));
     }
     const float s = a.wx[kx];
-    su[(kx * 2) * kC + c] = re * s;
-    su[(kx * 2 + 1) * kC + c] = im * s;
+    split_store(uh, ul, umma::elem_offset<kK2>(c, 2 * kx), re * s);
+    split_store(uh, ul, umma::elem_offset<kK2>(c, 2 * kx + 1), im * s);
   }
+  umma::fence_proxy_async();
+  umma::fence_before_sync();
   __syncthreads();
+  umma::fence_after_sync();
+  // z = v W + G U: M = 128 rows (x), N = 32; v W in BF16 (K = 32 channels) and the
+  // inverse x-DFT G U in split BF16 (G_hi U_hi + G_hi U_lo + G_lo U_hi, K = 32 modes)
+  if (ok && tid == 0) {
+    const uint32_t idesc = umma::idesc_bf16_f32(kW, kC);
+    const uint32_t pa[4] = {umma::smem_addr(As), umma::smem_addr(gh), umma::smem_addr(gh), umma::smem_addr(gl)};
+    const uint32_t pb[4] = {umma::smem_addr(Bw), umma::smem_addr(uh), umma::smem_addr(ul), umma::smem_addr(uh)};
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+#pragma unroll
+      for (int s = 0; s < kC / 16; ++s)
+        umma::mma_bf16(tmem, umma::smem_desc(pa[q] + 2 * s * 128, 128, kSbo),
+                       umma::smem_desc(pb[q] + 2 * s * 128, 128, kSbo), idesc, (q > 0 || s > 0) ? 1u : 0u);
+    umma::commit(mb);
+  }
   // this thread: row x (its TMEM lane) and kCpt channels
   const int lg = warp & 3, x = lg * 32 + lane, c0 = (warp >> 2) * kCpt;
   float z[kCpt];
 #pragma unroll
   for (int i = 0; i < kCpt; ++i) z[i] = 0.f;
-  {
-    int t = 0;
-    for (int kx = 0; kx < MX; ++kx) {
-      const float co = twx[2 * t], si = twx[2 * t + 1];
-      const float* ur = su + (kx * 2) * kC + c0;
-      const float* ui = su + (kx * 2 + 1) * kC + c0;
-#pragma unroll
-      for (int i = 0; i < kCpt; ++i) z[i] = fmaf(ur[i], co, fmaf(-ui[i], si, z[i]));
-      t = (t + x) & (kW - 1);
-    }
-  }
   if (ok) {  // (uniform over the CTA)
     ok = umma::mbar_wait(mb, 0, kFwWait);
     umma::fence_after_sync();
@@ -357,7 +385,7 @@ __global__ void __launch_bounds__(kRT, 1) k_fused_row(FusedFwdArgs a, int layer)
     umma::ld_8cols(tmem + ((uint32_t)(lg * 32) << 16) + (uint32_t)c0, acc);
 #pragma unroll
     for (int i = 0; i < kCpt; ++i) {
-      const float zz = (acc[i] + bl[c0 + i]) + z[i];
+      const float zz = acc[i] + bl[c0 + i];
       z[i] = last ? zz : gelu_f(zz);  // v_l (the last Fourier layer has no activation)
     }
   }
