@@ -182,3 +182,31 @@ def test_driver_refuses_unsupported_grids(tmp_path, grid, dim, program, bad):
     assert program in msg and bad in msg and "powers of two" in msg
     if dim == 2:
         assert "factors are 2, 3 and 5" in msg
+
+
+@pytest.mark.parametrize("prec", [tg.PREC_FP32, tg.PREC_DF64])
+def test_mixed_radix_sizes_need_fp64(prec):
+    """A 96 x 96 grid (factor 3) takes the mixed-radix path, which is FP64 only:
+    the other precisions are refused before any device call."""
+    c = _cfg(96, 96)
+    c.precision = prec
+    h = ctypes.c_void_p()
+    assert tg.lib().tara2d_create(ctypes.byref(c), ctypes.byref(h)) == tg.TARA_ERR_ARGS
+    code, msg = tg.last_error()
+    assert code == tg.TARA_ERR_ARGS and "FP64" in msg
+
+
+def test_mixed_radix_dropin_shape_checks():
+    """The drop-ins take 96 (2^5 3) but still refuse 98 (a factor 7) and odd lengths,
+    recording the error before touching the arrays."""
+    L = tg.lib()
+    for nx, ny in ((98, 96), (96, 99)):
+        nh = nx // 2 + 1
+        w = np.zeros((ny, nh), np.complex128)
+        ints = [ctypes.byref(ctypes.c_int(v)) for v in (nx, ny, nh)]
+        dbl = [ctypes.byref(ctypes.c_double(v)) for v in (0.01, 0.0)]
+        p = w.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        tg.lib().tara_clear_error()
+        L.derive2csh_(*ints, *dbl, p, p, p, p)
+        assert tg.last_error()[0] == tg.TARA_ERR_ARGS
+        assert not w.any()
