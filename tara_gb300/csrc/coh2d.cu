@@ -319,8 +319,10 @@ bool coh_dims(const int* Nx, const int* Ny, const int* Nh, const double* pi) {
     set_error(TARA_ERR_ARGS, "null argument");
     return false;
   }
-  if (!is_pow2_in_range(*Nx) || !is_pow2_in_range(*Ny) || *Nh != *Nx / 2 + 1) {
-    set_error(TARA_ERR_ARGS, "Nx, Ny must be powers of two in [16, 4096] and Nh = Nx/2+1");
+  if (!is_size_2d(*Nx) || !is_size_2d(*Ny) || *Nh != *Nx / 2 + 1) {
+    set_error(TARA_ERR_ARGS,
+              "Nx, Ny must be powers of two in [16, 4096] or even lengths 8 to 2048 with factors 2, 3, 5, "
+              "and Nh = Nx/2+1");
     return false;
   }
   return true;
@@ -363,8 +365,9 @@ int tara_coh2d_destroy(tara_coh2d* h) {
 int tara_coh2d_create(const tara_coh2d_config* cfg, tara_coh2d** out) {
   if (!cfg || !out) return set_error(TARA_ERR_ARGS, "null argument");
   *out = nullptr;
-  if (!is_pow2_in_range(cfg->nx) || !is_pow2_in_range(cfg->ny))
-    return set_error(TARA_ERR_ARGS, "nx and ny must be powers of two in [16, 4096]");
+  if (!is_size_2d(cfg->nx) || !is_size_2d(cfg->ny))
+    return set_error(TARA_ERR_ARGS,
+                     "nx and ny must be powers of two in [16, 4096] or even lengths 8 to 2048 with factors 2, 3, 5");
   if (!(cfg->lx > 0.0) || !(cfg->ly > 0.0) || !(cfg->kpi > 0.0))
     return set_error(TARA_ERR_ARGS, "box lengths and kpi must be positive");
   tara_coh2d* h = new tara_coh2d();

@@ -87,8 +87,8 @@ int fail_rc() { return tara_last_error() ? tara_last_error() : TARA_ERR_CUDA; }
 
 // The reference reads any Nx, Ny (, Nz) (src/main2csh.f95:35-38) and FFTW takes
 // any length; these kernels take powers of two, 16 to 4096 in 2D and 16 to 512
-// in 3D, and the incompressible 2D programs (any_ok) also even lengths 8 to
-// 2048 with factors 2, 3, 5 (the mixed-radix FP64 path).  Refuse anything else
+// in 3D, and the 2D programs (any_ok) also even lengths 8 to 2048 with
+// factors 2, 3, 5 (the mixed-radix FP64 path).  Refuse anything else
 // before allocating, naming the supported set.
 // even, 8 to 2048, no prime factor above 5 (the mixed-radix path's lengths)
 bool mixed_radix_size(int n) {
@@ -358,7 +358,7 @@ int run_coh(Reader& R, const std::string& out, int max_steps) {
   R.d("time", "dt", dt);
   R.d("resistivity", "nu", nu);  // read, then replaced by 0.0002 (src/main2coh.f95:119-120)
   if (!R.ok) return set_error(TARA_ERR_INI, R.err);
-  if (int rc = check_grid("tara2dHydOMP", 2, nx, ny, 0)) return rc;
+  if (int rc = check_grid("tara2dHydOMP", 2, nx, ny, 0, true)) return rc;
   const double lx_ini = lx, ly_ini = ly;
   lx = lx * kPi;
   ly = ly * kPi;
@@ -425,7 +425,7 @@ int run_com(Reader& R, const std::string& out, int max_steps) {
   R.d("time", "dt", dt);
   R.d("resistivity", "nu", mu);
   if (!R.ok) return set_error(TARA_ERR_INI, R.err);
-  if (int rc = check_grid("tara2dMHDOMP", 2, nx, ny, 0)) return rc;
+  if (int rc = check_grid("tara2dMHDOMP", 2, nx, ny, 0, true)) return rc;
   const double lx_ini = lx, ly_ini = ly;
   lx = lx * kPi;
   ly = ly * kPi;

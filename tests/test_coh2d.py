@@ -138,7 +138,8 @@ def test_gpu_init_vortices_golden(gcoh):
 
 
 @gpu
-@pytest.mark.parametrize("ny,nx", [(32, 64), (64, 16), (128, 256), (16, 2048), (2048, 16)])
+@pytest.mark.parametrize("ny,nx", [(32, 64), (64, 16), (128, 256), (16, 2048), (2048, 16),
+                                   (96, 96), (80, 48), (60, 120)])  # (mixed-radix lengths)
 def test_gpu_rhs_rectangular_vs_oracle(oracle, ny, nx):
     tg = _tg()
     st = _smooth(ny, nx, nx + ny)
@@ -187,3 +188,20 @@ def test_gpu_dropin_rejects_bad_common():
     with pytest.raises(tg.TaraError):
         tg.derive2coh(np.zeros((3, 32, 17), np.complex128))
     _set_common(tg)
+
+
+@gpu
+def test_gpu_mixed_radix_96_steps_vs_oracle(oracle):
+    """A 96^2 grid (mixed-radix transforms): the driver's initial state and 20
+    AB2 steps against the oracle (its direct DFT at this length)."""
+    tg = _tg()
+    st0 = oracle.ic_coh(96, 96)
+    p = orc.coh_params()
+    with tg.Coh2D(96, dt=5e-4) as s:
+        s.init_vortices(2.0, 2.0)
+        assert rel_l2(s.get_state(), st0) < 1e-13
+        assert rel_l2(s.rhs(), oracle.derive2coh(st0, p)) < 1e-12
+        s.step(20)
+        st = s.get_state()
+    ref, _ = oracle.run_coh(st0, p, 5e-4, 20)
+    assert rel_l2(st, ref) < 1e-11

@@ -131,7 +131,8 @@ def test_gpu_init_reference_golden(gcom):
 
 @gpu
 @pytest.mark.parametrize("ny,nx,a", [(32, 64, 1.0), (64, 16, 0.0), (128, 256, 0.5), (16, 2048, 1.0),
-                                      (2048, 16, 1.0)])
+                                      (2048, 16, 1.0),
+                                      (96, 96, 1.0), (80, 48, 0.5), (60, 120, 1.0)])  # (mixed-radix lengths)
 def test_gpu_rhs_rectangular_vs_oracle(oracle, ny, nx, a):
     """Rectangular grids and boxes, forcing on and off, against the oracle."""
     tg = _tg()
@@ -159,6 +160,22 @@ def test_gpu_1024_rhs_and_steps_vs_oracle(oracle):
     st0 = oracle.ic_com(1024, 1024)
     p = orc.com_params()
     with tg.Com2D(1024, dt=2e-5) as s:
+        s.init_reference(2.0, 2.0, 1.0)
+        assert rel_l2(s.get_state(), st0) < 1e-13
+        s.step(20)
+        st = s.get_state()
+    ref, _ = oracle.run_com(st0, p, 2e-5, 20)
+    assert rel_l2(st, ref) < 1e-11
+
+
+@gpu
+def test_gpu_mixed_radix_96_steps_vs_oracle(oracle):
+    """A 96^2 grid (mixed-radix transforms) from the driver's initial state: the
+    state after 20 AB2 steps against the oracle (its direct DFT at this length)."""
+    tg = _tg()
+    st0 = oracle.ic_com(96, 96)
+    p = orc.com_params()
+    with tg.Com2D(96, dt=2e-5) as s:
         s.init_reference(2.0, 2.0, 1.0)
         assert rel_l2(s.get_state(), st0) < 1e-13
         s.step(20)

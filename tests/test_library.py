@@ -113,7 +113,7 @@ def test_compressible_dropins_validate_before_the_gpu(name, nf):
     w = np.zeros((64, 10), np.complex128)
     fn = getattr(L, name)
     nout = 2 * nf if name == "derive2com_" else 6
-    for nx, ny, nh in ((64, 64, 10), (24, 24, 13)):
+    for nx, ny, nh in ((64, 64, 10), (98, 98, 50)):  # (98 = 2 * 7^2: no mixed-radix plan)
         args = [ctypes.byref(ctypes.c_int(v)) for v in (nx, ny, nh)]
         args += [ctypes.byref(ctypes.c_double(v)) for v in (3.14159265358979, 0.0)]
         args += [w.ctypes.data] * (nf + nout)
