@@ -1,7 +1,7 @@
-// Complex FFTs of lengths that are not powers of two (n = 2^a 3^b 5^c, even,
-// up to kAnyMaxN), for the grids the reference accepts beyond the power-of-two
-// kernels: a mixed-radix Stockham transform in shared memory, radix 4, 2, 3 and
-// 5 stages, one CTA per transform, FP64.
+// Complex FFTs of lengths that are not powers of two (n = 2^a 3^b 5^c 7^d,
+// even, up to kAnyMaxN), for the grids the reference accepts beyond the
+// power-of-two kernels: a mixed-radix Stockham transform in shared memory,
+// radix 4, 2, 3, 5 and 7 stages, one CTA per transform, FP64.
 //
 // Stage with radix R over the current span Ns (the product of the radices
 // already applied; Govindaraju et al., "High performance discrete Fourier
@@ -26,13 +26,13 @@ struct AnyPlan {
   int radix[kAnyMaxStages];
 };
 
-// Factorisation n = 4^a 2^b 3^c 5^d (radix 4 first); false when n has another factor.
+// Factorisation n = 4^a 2^b 3^c 5^d 7^e (radix 4 first); false when n has another factor.
 inline bool any_plan(int n, AnyPlan* p) {
   if (n < 2 || n > kAnyMaxN) return false;
   p->n = n;
   p->stages = 0;
   int m = n;
-  const int order[4] = {4, 2, 3, 5};
+  const int order[5] = {4, 2, 3, 5, 7};
   for (int r : order)
     while (m % r == 0 && p->stages < kAnyMaxStages) {
       p->radix[p->stages++] = r;
@@ -41,7 +41,7 @@ inline bool any_plan(int n, AnyPlan* p) {
   return m == 1;
 }
 
-// Sizes the mixed-radix path takes: even, 8 to kAnyMaxN, factors 2, 3, 5 only.
+// Sizes the mixed-radix path takes: even, 8 to kAnyMaxN, factors 2, 3, 5, 7 only.
 inline bool any_size_ok(int n) {
   AnyPlan p;
   return n >= 8 && n % 2 == 0 && any_plan(n, &p);
@@ -52,8 +52,11 @@ __device__ __forceinline__ double2 cmul_any(double2 a, double2 b) {
 }
 
 // One Stockham stage of radix R (compile-time: the R values stay in registers).
-// The small DFTs are the standard butterflies; radix 3 and 5 take their cosines
-// and sines from the table roots W_R^m = W_n^(m n / R), read once per stage.
+// The small DFTs are the standard butterflies; radix 3, 5 and 7 take their
+// cosines and sines from the table roots W_R^m = W_n^(m n / R), read once per
+// stage.  Radix 7 pairs the inputs m and R - m: with t_m = v_m + v_(R-m) and
+// d_m = v_m - v_(R-m), V_k = a_k - i b_k and V_(R-k) = a_k + i b_k for
+// a_k = v_0 + sum_m cos(2 pi m k / R) t_m and b_k = sum_m sin(2 pi m k / R) d_m.
 template <int R>
 __device__ __forceinline__ void any_stage(const double2* __restrict__ src, double2* __restrict__ dst, int n, int ns,
                                           const double2* __restrict__ w, bool inverse, int tid, int nthreads) {
@@ -105,6 +108,26 @@ __device__ __forceinline__ void any_stage(const double2* __restrict__ src, doubl
       V[0] = make_double2(v[0].x + t1.x, v[0].y + t1.y);
       V[1] = make_double2(a.x + b.y, a.y - b.x);
       V[2] = make_double2(a.x - b.y, a.y + b.x);
+    } else if constexpr (R == 7) {
+      double2 t[3], d[3];
+#pragma unroll
+      for (int m = 1; m <= 3; ++m) {
+        t[m - 1] = make_double2(v[m].x + v[7 - m].x, v[m].y + v[7 - m].y);
+        d[m - 1] = make_double2(v[m].x - v[7 - m].x, v[m].y - v[7 - m].y);
+      }
+      V[0] = make_double2(v[0].x + t[0].x + t[1].x + t[2].x, v[0].y + t[0].y + t[1].y + t[2].y);
+#pragma unroll
+      for (int k = 1; k <= 3; ++k) {
+        double2 a = v[0], b = make_double2(0.0, 0.0);
+#pragma unroll
+        for (int m = 1; m <= 3; ++m) {
+          const double c = wr[(m * k) % 7].x, sn = -wr[(m * k) % 7].y;
+          a = make_double2(fma(c, t[m - 1].x, a.x), fma(c, t[m - 1].y, a.y));
+          b = make_double2(fma(sn, d[m - 1].x, b.x), fma(sn, d[m - 1].y, b.y));
+        }
+        V[k] = make_double2(a.x + b.y, a.y - b.x);      // a - i b
+        V[7 - k] = make_double2(a.x - b.y, a.y + b.x);  // a + i b
+      }
     } else {  // R == 5: W_5 = c1 - i s1, W_5^2 = c2 - i s2
       const double c1 = wr[1].x, s1 = -wr[1].y, c2 = wr[2].x, s2 = -wr[2].y;
       const double2 t1 = make_double2(v[1].x + v[4].x, v[1].y + v[4].y);
@@ -142,7 +165,8 @@ __device__ inline void fft_any(double2* buf, double2* tmp, const AnyPlan& pl, co
       case 4: any_stage<4>(src, dst, n, ns, w, inverse, tid, nthreads); break;
       case 2: any_stage<2>(src, dst, n, ns, w, inverse, tid, nthreads); break;
       case 3: any_stage<3>(src, dst, n, ns, w, inverse, tid, nthreads); break;
-      default: any_stage<5>(src, dst, n, ns, w, inverse, tid, nthreads); break;
+      case 5: any_stage<5>(src, dst, n, ns, w, inverse, tid, nthreads); break;
+      default: any_stage<7>(src, dst, n, ns, w, inverse, tid, nthreads); break;
     }
     __syncthreads();
     double2* s = src;

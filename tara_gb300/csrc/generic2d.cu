@@ -1,5 +1,5 @@
 // The 2D FP64 passes for grid sizes that are not powers of two (even sizes with
-// factors 2, 3 and 5, up to 2048 per axis): the same three passes per right-hand
+// factors 2, 3, 5 and 7, up to 2048 per axis): the same three passes per right-hand
 // side as kernels2d.cuh -- the y-direction inverse transforms of the four
 // spectral fields, the x-direction c2r / product / r2c per pair of ky rows, the
 // y-direction forward transform with the 2/3 truncation, the nu k^2 term and
@@ -289,7 +289,7 @@ bool any_size_2d(int n) { return !is_pow2_in_range(n) && any_size_ok(n); }
 namespace any2d {
 
 static int plan_of(int n, AnyPlan* p) {
-  if (!any_plan(n, p)) return set_error(TARA_ERR_ARGS, "grid size has a prime factor other than 2, 3, 5");
+  if (!any_plan(n, p)) return set_error(TARA_ERR_ARGS, "grid size has a prime factor other than 2, 3, 5, 7");
   return TARA_OK;
 }
 

@@ -30,14 +30,14 @@ int fortran_style_calls(void) {
   static double _Complex w[NH * NY], wn[NH * NY], d_old[NH * NY], d_new[NH * NY];
   const double _Complex fill = 7.0 + 3.0 * I;
   for (size_t i = 0; i < NH * NY; ++i) w[i] = wn[i] = d_old[i] = d_new[i] = fill;
-  int nx = NX, ny = NY, nh_bad = NH + 1, nx_bad = 98, nh_of_bad = 50;
+  int nx = NX, ny = NY, nh_bad = NH + 1, nx_bad = 88, nh_of_bad = 45;
   double nu = 0.01, t = 0.0, dt = 1e-4, alpha = 1.0;
 
   tara_clear_error();
   derive2csh_(&nx, &ny, &nh_bad, &nu, &t, w, wn, d_old, d_new);  /* Nh != Nx/2+1 */
   if (tara_last_error() != 1) return 1;
   tara_clear_error();
-  derive2csh_(&nx_bad, &ny, &nh_of_bad, &nu, &t, w, wn, d_old, d_new);  /* Nx = 98: factor 7 */
+  derive2csh_(&nx_bad, &ny, &nh_of_bad, &nu, &t, w, wn, d_old, d_new);  /* Nx = 88: factor 11 */
   if (tara_last_error() != 1) return 2;
   tara_clear_error();
   ab2csh_(&nx, &ny, &nh_bad, &nu, &t, &dt, w, wn, d_old, d_new);

@@ -24,7 +24,7 @@ int main(void) {
   tara2d_config c;
   tara2d_default_config(&c, 64, 64);
   CHECK(c.nx == 64 && c.ny == 64);
-  c.nx = 98; /* neither a power of two nor 2, 3, 5-smooth */
+  c.nx = 88; /* neither a power of two nor 2, 3, 5, 7-smooth (a factor 11) */
   tara2d* h = (tara2d*)&c; /* must be reset to NULL on failure */
   CHECK(tara2d_create(&c, &h) == TARA_ERR_ARGS);
   CHECK(h == NULL);

@@ -1,10 +1,11 @@
 """GPU tests of the mixed-radix FP64 path: the grid sizes the reference accepts
 beyond powers of two (src/main2csh.f95:35-38 reads any Nx, Ny; FFTW transforms
-any length), here even lengths up to 2048 whose prime factors are 2, 3 and 5.
+any length), here even lengths up to 2048 whose prime factors are 2, 3, 5 and 7.
 
 Against the FFTW-backed fixtures (tests/golden/make_generic_sizes.py): the RHS
 and 500 AB2 steps from the reference's shear layer at 96^2, the RHS and 200 RK4
-steps from a seeded random-phase state at 48 x 80.  Against the oracle (its
+steps from a seeded random-phase state at 48 x 80, the RHS and 100 RK4 steps
+at 56 x 84 (a factor 7 on both axes).  Against the oracle (its
 direct DFT at these lengths, itself pinned to the same fixtures on the CPU):
 transforms, one RHS of both kinds, and steps at several shapes.  At sizes the
 oracle's direct DFT would take long, properties: the c2r of the r2c returns
@@ -49,9 +50,15 @@ def test_fixtures_rhs_and_runs(gen):
         s.set_state(gen["r48x80_w0"])
         s.step(200)
         assert rel_l2(s.get_state(), gen["r48x80_w200"]) < 1e-10
+    assert rel_l2(tg.derive2csh(gen["r56x84_w0"], 1e-3), gen["r56x84_rhs"]) < 1e-12
+    with tg.Solver2D(56, 84, scheme=tg.SCHEME_RK4, nu=1e-3, dt=1e-3) as s:
+        s.set_state(gen["r56x84_w0"])
+        s.step(100)
+        assert rel_l2(s.get_state(), gen["r56x84_w100"]) < 1e-10
 
 
-@pytest.mark.parametrize("ny,nx", [(96, 96), (80, 48), (40, 30), (90, 120), (384, 384), (50, 200), (8, 12)])
+@pytest.mark.parametrize("ny,nx", [(96, 96), (80, 48), (40, 30), (90, 120), (384, 384), (50, 200), (8, 12),
+                                   (84, 56), (70, 42), (14, 28), (448, 336)])
 def test_transforms_vs_oracle(oracle, ny, nx):
     rng = np.random.default_rng(nx * 3 + ny)
     x = rng.standard_normal((ny, nx))
@@ -60,7 +67,8 @@ def test_transforms_vs_oracle(oracle, ny, nx):
     assert rel_l2(tg.fft2d_c2r(c), oracle.c2r(c)) < 1e-14
 
 
-@pytest.mark.parametrize("ny,nx", [(96, 96), (80, 48), (40, 30), (90, 120), (384, 384), (64, 96), (96, 64)])
+@pytest.mark.parametrize("ny,nx", [(96, 96), (80, 48), (40, 30), (90, 120), (384, 384), (64, 96), (96, 64),
+                                   (84, 56), (112, 112), (64, 98)])
 def test_rhs_vs_oracle(oracle, ny, nx):
     """One RHS of each kind; (64, 96) and (96, 64) mix a power-of-two axis with
     a mixed-radix one (the whole grid takes the mixed-radix path)."""
@@ -91,7 +99,7 @@ def test_dropins_and_rk4_dropin(gen, oracle):
     assert rel_l2(tg.rk42css(w, 1.0, 0.01, 1e-4), oracle.rk42css(w, 1.0, 0.01, 1e-4)) < 1e-12
 
 
-@pytest.mark.parametrize("n", [1536, 2000])
+@pytest.mark.parametrize("n", [1536, 2000, 1792])
 def test_large_mixed_radix_properties(n):
     """Lengths whose oracle DFT would take minutes: the c2r of the r2c is Nx Ny
     times the field, and a plain RK4 run keeps the mean vorticity and loses

@@ -46,7 +46,7 @@ def _cfg(nx, ny):
     return c
 
 
-@pytest.mark.parametrize("nx,ny", [(98, 64), (64, 7), (8192, 64), (0, 0), (64, 3), (4096 + 2048, 64)])
+@pytest.mark.parametrize("nx,ny", [(88, 64), (64, 7), (8192, 64), (0, 0), (64, 3), (4096 + 2048, 64)])
 def test_create_rejects_bad_sizes(nx, ny):
     h = ctypes.c_void_p()
     rc = tg.lib().tara2d_create(ctypes.byref(_cfg(nx, ny)), ctypes.byref(h))
@@ -113,7 +113,7 @@ def test_compressible_dropins_validate_before_the_gpu(name, nf):
     w = np.zeros((64, 10), np.complex128)
     fn = getattr(L, name)
     nout = 2 * nf if name == "derive2com_" else 6
-    for nx, ny, nh in ((64, 64, 10), (98, 98, 50)):  # (98 = 2 * 7^2: no mixed-radix plan)
+    for nx, ny, nh in ((64, 64, 10), (88, 88, 45)):  # (88 = 8 * 11: no mixed-radix plan)
         args = [ctypes.byref(ctypes.c_int(v)) for v in (nx, ny, nh)]
         args += [ctypes.byref(ctypes.c_double(v)) for v in (3.14159265358979, 0.0)]
         args += [w.ctypes.data] * (nf + nout)
@@ -158,7 +158,7 @@ def test_features_need_one_scale_per_channel():
 
 
 @pytest.mark.parametrize("grid,dim,program,bad", [
-    ("Nx = 98\nNy = 64\nNz = 64", 2, "tara2dHydSer", "Nx = 98"),
+    ("Nx = 88\nNy = 64\nNz = 64", 2, "tara2dHydSer", "Nx = 88"),
     ("Nx = 64\nNy = 8192\nNz = 64", 2, "tara2dHydSer", "Ny = 8192"),
     ("Nx = 64\nNy = 64\nNz = 384", 3, "tara3dMHDOMP", "Nz = 384"),
     ("Nx = 1024\nNy = 64\nNz = 64", 3, "tara3dMHDOMP", "Nx = 1024"),
@@ -181,7 +181,7 @@ def test_driver_refuses_unsupported_grids(tmp_path, grid, dim, program, bad):
     assert rc == tg.TARA_ERR_ARGS and code == tg.TARA_ERR_ARGS
     assert program in msg and bad in msg and "powers of two" in msg
     if dim == 2:
-        assert "factors are 2, 3 and 5" in msg
+        assert "factors are 2, 3, 5 and 7" in msg
 
 
 @pytest.mark.parametrize("prec", [tg.PREC_FP32, tg.PREC_DF64])
@@ -197,10 +197,10 @@ def test_mixed_radix_sizes_need_fp64(prec):
 
 
 def test_mixed_radix_dropin_shape_checks():
-    """The drop-ins take 96 (2^5 3) but still refuse 98 (a factor 7) and odd lengths,
+    """The drop-ins take 96 (2^5 3) and 98 (2 7^2) but still refuse 88 (a factor 11) and odd lengths,
     recording the error before touching the arrays."""
     L = tg.lib()
-    for nx, ny in ((98, 96), (96, 99)):
+    for nx, ny in ((88, 96), (96, 99)):
         nh = nx // 2 + 1
         w = np.zeros((ny, nh), np.complex128)
         ints = [ctypes.byref(ctypes.c_int(v)) for v in (nx, ny, nh)]
