@@ -25,7 +25,7 @@
  * rk42css_ / derive2coh_ / derive2com_ drop-ins, tara2d_* with TARA_PREC_FP64,
  * tara_coh2d_* and tara_com2d_*, tara_fft2d_* in FP64 and the tara2dHydSer /
  * tara2dScrSer / tara2dHydOMP / tara2dMHDOMP programs) also take even lengths
- * from 8 to 2048 whose only prime factors are 2, 3, 5 and 7 (mixed-radix passes).
+ * from 8 to 3600 whose only prime factors are 2, 3, 5 and 7 (mixed-radix passes).
  */
 #ifndef TARA_H
 #define TARA_H
@@ -112,7 +112,7 @@ int tara_finalize(void);
 #define TARA_PREC_DF64 2   /* double-float (FP32 pair) FFTs and products; FP64 state */
 
 typedef struct tara2d_config {
-  int nx, ny;      /* powers of two, 16..4096; in FP64 also even 8..2048 with factors 2, 3, 5, 7 */
+  int nx, ny;      /* powers of two, 16..4096; in FP64 also even 8..3600 with factors 2, 3, 5, 7 */
   int rhs;         /* TARA_RHS_* */
   int scheme;      /* TARA_SCHEME_* */
   int precision;   /* TARA_PREC_* */
@@ -301,7 +301,7 @@ void ab3com_(const int* Nx, const int* Ny, const int* Nz, const int* Nh, const d
  * (complex(8) (Nh,Ny)); the *_old arrays and time are unused.  Lx, Ly, mux, muy,
  * CS come from the caller's common block /comm/ (comm_, the layout
  * Lx,Ly,mux,muy,ms,CS,dt of src/derive2coh.f95:30); wavenumbers use the pi
- * argument.  Sizes: powers of two in [16, 4096], or even 8..2048 with factors 2, 3, 5, 7. */
+ * argument.  Sizes: powers of two in [16, 4096], or even 8..3600 with factors 2, 3, 5, 7. */
 void derive2coh_(const int* Nx, const int* Ny, const int* Nh, const double* pi, const double* time,
                  const double* nk, const double* ukx, const double* uky, double* dn_dt_old,
                  double* dux_dt_old, double* duy_dt_old, double* dn_dt_new, double* dux_dt_new,
@@ -316,7 +316,7 @@ void ab2coh_(const int* Nx, const int* Ny, const int* Nh, const double* pi, cons
              const double* duy_dt_new);
 
 typedef struct tara_coh2d_config {
-  int nx, ny;        /* powers of two, 16..4096, or even 8..2048 with factors 2, 3, 5, 7 */
+  int nx, ny;        /* powers of two, 16..4096, or even 8..3600 with factors 2, 3, 5, 7 */
   double kpi;        /* the pi of kx = 2*pi*(i-1)/Lx */
   double lx, ly;     /* box lengths */
   double mux, muy;   /* viscosities (the reference driver: 0.0002) */
@@ -360,7 +360,7 @@ int tara_coh2d_real_fields(tara_coh2d* h, double* n, double* ux, double* uy, dou
  * caller's /comm/ (comm_, the layout Lx,Ly,spheat,mu,ms,CS,mu_0,eta,dt,kf,A of
  * src/derive2com.f95:43).  Faithful to the reference's curl B (built from
  * d_ux_dx and d_uy_dy, :186-187); the forcing uses the grid coordinates the
- * reference leaves unset.  Sizes: powers of two in [16, 4096], or even 8..2048 with
+ * reference leaves unset.  Sizes: powers of two in [16, 4096], or even 8..3600 with
  * factors 2, 3, 5, 7. */
 void derive2com_(const int* Nx, const int* Ny, const int* Nh, const double* pi, const double* time,
                  const double* rho_k, const double* rho_ux_k, const double* rho_uy_k,
@@ -383,7 +383,7 @@ void ab2com_(const int* Nx, const int* Ny, const int* Nh, const double* pi, cons
              const double* d_Bx_k_dt_new, const double* d_By_k_dt_old, const double* d_By_k_dt_new);
 
 typedef struct tara_com2d_config {
-  int nx, ny;      /* powers of two, 16..4096, or even 8..2048 with factors 2, 3, 5, 7 */
+  int nx, ny;      /* powers of two, 16..4096, or even 8..3600 with factors 2, 3, 5, 7 */
   int defined;     /* 0: curl B as the reference (from d_ux_dx, d_uy_dy); 1: from dB/dx, dB/dy */
   double kpi;      /* the pi of kx = 2*pi*(i-1)/Lx */
   double lx, ly;   /* box lengths */

@@ -49,7 +49,7 @@ bool check_dims(const int* Nx, const int* Ny, const int* Nh) {
   }
   if (!is_size_2d(*Nx) || !is_size_2d(*Ny) || *Nh != *Nx / 2 + 1) {
     set_error(TARA_ERR_ARGS,
-              "Nx, Ny must be powers of two in [16, 4096] or even lengths 8 to 2048 with factors 2, 3, 5, 7, "
+              "Nx, Ny must be powers of two in [16, 4096] or even lengths 8 to 3600 with factors 2, 3, 5, 7, "
               "and Nh = Nx/2+1");
     return false;
   }

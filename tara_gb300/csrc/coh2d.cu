@@ -321,7 +321,7 @@ bool coh_dims(const int* Nx, const int* Ny, const int* Nh, const double* pi) {
   }
   if (!is_size_2d(*Nx) || !is_size_2d(*Ny) || *Nh != *Nx / 2 + 1) {
     set_error(TARA_ERR_ARGS,
-              "Nx, Ny must be powers of two in [16, 4096] or even lengths 8 to 2048 with factors 2, 3, 5, 7, "
+              "Nx, Ny must be powers of two in [16, 4096] or even lengths 8 to 3600 with factors 2, 3, 5, 7, "
               "and Nh = Nx/2+1");
     return false;
   }
@@ -367,7 +367,7 @@ int tara_coh2d_create(const tara_coh2d_config* cfg, tara_coh2d** out) {
   *out = nullptr;
   if (!is_size_2d(cfg->nx) || !is_size_2d(cfg->ny))
     return set_error(TARA_ERR_ARGS,
-                     "nx and ny must be powers of two in [16, 4096] or even lengths 8 to 2048 with factors 2, 3, 5, 7");
+                     "nx and ny must be powers of two in [16, 4096] or even lengths 8 to 3600 with factors 2, 3, 5, 7");
   if (!(cfg->lx > 0.0) || !(cfg->ly > 0.0) || !(cfg->kpi > 0.0))
     return set_error(TARA_ERR_ARGS, "box lengths and kpi must be positive");
   tara_coh2d* h = new tara_coh2d();

@@ -87,12 +87,12 @@ int fail_rc() { return tara_last_error() ? tara_last_error() : TARA_ERR_CUDA; }
 
 // The reference reads any Nx, Ny (, Nz) (src/main2csh.f95:35-38) and FFTW takes
 // any length; these kernels take powers of two, 16 to 4096 in 2D and 16 to 512
-// in 3D, and the 2D programs (any_ok) also even lengths 8 to 2048 with
+// in 3D, and the 2D programs (any_ok) also even lengths 8 to 3600 with
 // factors 2, 3, 5, 7 (the mixed-radix FP64 path).  Refuse anything else
 // before allocating, naming the supported set.
-// even, 8 to 2048, no prime factor above 7 (the mixed-radix path's lengths)
+// even, 8 to 3600, no prime factor above 7 (the mixed-radix path's lengths)
 bool mixed_radix_size(int n) {
-  if (n < 8 || n > 2048 || (n & 1)) return false;
+  if (n < 8 || n > 3600 || (n & 1)) return false;
   for (int p : {2, 3, 5, 7})
     while (n % p == 0) n /= p;
   return n == 1;
@@ -109,7 +109,7 @@ int check_grid(const char* program, int dims, int nx, int ny, int nz, bool any_o
     if (any_ok)
       std::snprintf(msg, sizeof msg,
                     "%s: %s = %d is not supported; grid sizes here are powers of two from 16 to %d "
-                    "(16, 32, 64, ..., %d), or even lengths from 8 to 2048 whose only prime factors are "
+                    "(16, 32, 64, ..., %d), or even lengths from 8 to 3600 whose only prime factors are "
                     "2, 3, 5 and 7 (e.g. 48, 96, 384, 448)",
                     program, name[d], n[d], hi, hi);
     else

@@ -17,7 +17,7 @@
 
 namespace tara {
 
-constexpr int kAnyMaxN = 2048;  // longest transform (the row pass holds four of them)
+constexpr int kAnyMaxN = 3600;  // longest transform: the row pass holds four, 4 x 3600 x 16 B = 225 KB
 constexpr int kAnyMaxStages = 16;
 
 struct AnyPlan {

@@ -1,5 +1,5 @@
 // The 2D FP64 passes for grid sizes that are not powers of two (even sizes with
-// factors 2, 3, 5 and 7, up to 2048 per axis): the same three passes per right-hand
+// factors 2, 3, 5 and 7, up to 3600 per axis): the same three passes per right-hand
 // side as kernels2d.cuh -- the y-direction inverse transforms of the four
 // spectral fields, the x-direction c2r / product / r2c per pair of ky rows, the
 // y-direction forward transform with the 2/3 truncation, the nu k^2 term and

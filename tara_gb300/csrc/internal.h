@@ -86,7 +86,7 @@ struct Launch2D {
 };
 
 // Grid sizes that are not powers of two (generic2d.cu, fft_any.cuh): even,
-// 8 to 2048, factors 2, 3, 5 and 7; FP64 only.  The Launch2D entry points route
+// 8 to 3600, factors 2, 3, 5 and 7; FP64 only.  The Launch2D entry points route
 // such lengths there.
 bool any_size_2d(int n);
 inline bool is_size_2d(int n) { return is_pow2_in_range(n) || any_size_2d(n); }

@@ -207,7 +207,7 @@ static bool tile_fits_n(int k, int v) {
       if (any_size_2d(n)) return CALL;                                                       \
     }                                                                                        \
     return set_error(TARA_ERR_ARGS, "grid sizes that are not powers of two need FP64, even " \
-                                    "lengths 8 to 2048 with factors 2, 3, 5, 7");            \
+                                    "lengths 8 to 3600 with factors 2, 3, 5, 7");            \
   }
 
 template <typename T>

@@ -591,7 +591,7 @@ int tara2d_create(const tara2d_config* cfg, tara2d** out) {
   *out = nullptr;
   if (!is_size_2d(cfg->nx) || !is_size_2d(cfg->ny))
     return set_error(TARA_ERR_ARGS,
-                     "nx and ny must be powers of two in [16, 4096], or (FP64) even lengths 8 to 2048 "
+                     "nx and ny must be powers of two in [16, 4096], or (FP64) even lengths 8 to 3600 "
                      "with factors 2, 3, 5, 7");
   if ((!is_pow2_in_range(cfg->nx) || !is_pow2_in_range(cfg->ny)) && cfg->precision != TARA_PREC_FP64)
     return set_error(TARA_ERR_ARGS, "grid sizes that are not powers of two take the FP64 precision only");

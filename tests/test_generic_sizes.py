@@ -1,6 +1,6 @@
 """GPU tests of the mixed-radix FP64 path: the grid sizes the reference accepts
 beyond powers of two (src/main2csh.f95:35-38 reads any Nx, Ny; FFTW transforms
-any length), here even lengths up to 2048 whose prime factors are 2, 3, 5 and 7.
+any length), here even lengths up to 3600 whose prime factors are 2, 3, 5 and 7.
 
 Against the FFTW-backed fixtures (tests/golden/make_generic_sizes.py): the RHS
 and 500 AB2 steps from the reference's shear layer at 96^2, the RHS and 200 RK4
@@ -99,7 +99,7 @@ def test_dropins_and_rk4_dropin(gen, oracle):
     assert rel_l2(tg.rk42css(w, 1.0, 0.01, 1e-4), oracle.rk42css(w, 1.0, 0.01, 1e-4)) < 1e-12
 
 
-@pytest.mark.parametrize("n", [1536, 2000, 1792])
+@pytest.mark.parametrize("n", [1536, 2000, 1792, 3000, 3600])
 def test_large_mixed_radix_properties(n):
     """Lengths whose oracle DFT would take minutes: the c2r of the r2c is Nx Ny
     times the field, and a plain RK4 run keeps the mean vorticity and loses

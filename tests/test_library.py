@@ -46,7 +46,7 @@ def _cfg(nx, ny):
     return c
 
 
-@pytest.mark.parametrize("nx,ny", [(88, 64), (64, 7), (8192, 64), (0, 0), (64, 3), (4096 + 2048, 64)])
+@pytest.mark.parametrize("nx,ny", [(88, 64), (64, 7), (3840, 64), (8192, 64), (0, 0), (64, 3), (4096 + 2048, 64)])
 def test_create_rejects_bad_sizes(nx, ny):
     h = ctypes.c_void_p()
     rc = tg.lib().tara2d_create(ctypes.byref(_cfg(nx, ny)), ctypes.byref(h))
