@@ -200,14 +200,15 @@ def run_reference(args) -> None:
 def fft_fp64_inst(n: int, radix8: bool = False) -> int:
     """FP64 instructions of one length-n transform of fft.cuh, counted from its
     butterflies.  Radix-4 path: an untwiddled radix-4 first stage (16 adds per
-    butterfly), twiddled radix-4 stages (24 per butterfly) and, for odd log2 n,
-    a twiddled radix-2 stage (6 per butterfly).  Radix-8 path: an untwiddled
-    radix-8 first stage (52 per butterfly), twiddled radix-8 stages (72), then
-    zero to two twiddled radix-4 stages (24; untwiddled, 16, when they come first)."""
+    butterfly), twiddled radix-4 stages on ratio-form twiddles (22 FMAs per
+    butterfly) and, for odd log2 n, a twiddled radix-2 stage (6 per butterfly).
+    Radix-8 path: an untwiddled radix-8 first stage (52 per butterfly), twiddled
+    radix-8 stages (72), then zero to two twiddled radix-4 stages on plain
+    complex twiddles (24; untwiddled, 16, when they come first)."""
     lg = n.bit_length() - 1
     q = n // 4
     if not radix8:
-        return q * 16 + q * 24 * (lg // 2 - 1) + ((n // 2) * 6 if lg % 2 else 0)
+        return q * 16 + q * 22 * (lg // 2 - 1) + ((n // 2) * 6 if lg % 2 else 0)
     s8 = lg // 3 - 1 if (lg % 3 == 1 and lg >= 4) else lg // 3
     s4 = 2 if lg % 3 == 1 else 1 if lg % 3 == 2 else 0
     b8 = n // 8
@@ -335,7 +336,20 @@ def run_ours(args) -> None:
         roof64 = {"bound": "fp64", "kernel": dom, "achieved": fp64["achieved_inst_per_s"][dom], "peak": pk,
                   "peak_kind": "measured DFMA rate" if fp64["measured_dfma_inst_per_s"] else "nominal",
                   "unit": "FP64 inst/s", "frac": fp64["achieved_inst_per_s"][dom] / pk,
+                  "count": "transform butterflies only (a lower bound)",
                   "step": {"inst_per_step": step_inst, "achieved": step_rate, "frac": step_rate / pk}}
+        # the same with every FP64 instruction the kernels execute, as ncu
+        # counted them (sm__inst_executed_pipe_fp64 x 32) in the capture summarised
+        # in profiles/rhs2d_fp64_2048_traffic.txt
+        cnt = {k: from_profiles("fp64_thread_inst_per_launch", k, n) for k in fp64["inst_per_launch"]}
+        if all(cnt.values()):
+            per_ms = {k: v["ms"] / max(1, v["launches"]) for k, v in ks.items()}
+            step_all = 4 * sum(cnt.values())
+            roof64["all_fp64_inst"] = {
+                "inst_per_launch": cnt[dom], "achieved": cnt[dom] / (per_ms[dom] * 1e-3),
+                "frac": cnt[dom] / (per_ms[dom] * 1e-3) / pk,
+                "step": {"inst_per_step": step_all, "achieved": step_all / (el_ms / args.steps * 1e-3),
+                         "frac": step_all / (el_ms / args.steps * 1e-3) / pk}}
     line = {
         "metric": {tg.PREC_FP64: METRIC, tg.PREC_FP32: METRIC.replace("FP64", "FP32 form"),
                    tg.PREC_DF64: METRIC.replace("FP64", "double-float form")}[prec],

@@ -109,6 +109,8 @@ int make_roots(int n, void** dev);  // exp(-2 pi i t / n), t < n, FP64
 void twiddle(int n, int m, double* re, double* im);
 // Entry idx < tw_count(n) of the length-n twiddle table (layout in fft.cuh).
 void twiddle_entry(int n, int idx, double* re, double* im);
+// The FP64 table's entry idx: the radix-4 stage entries in ratio form (fft.cuh).
+void twiddle_entry_fp64(int n, int idx, double* a, double* b);
 // Twiddle table exp(-2 pi i m/n), m < n, in precision T, uploaded to device.
 int make_twiddles(int n, bool fp32, void** dev);
 // The same table as double-float (hi, lo) pairs: float4 {re.hi, re.lo, im.hi, im.lo}.

@@ -127,7 +127,7 @@ static int noalloc_setup(unsigned char** out) {
     for (int n = 16; n <= kNoAllocMaxN; n *= 2)
       for (int m = 0; m < tw_count(n); ++m) {
         double c, sn;
-        twiddle_entry(n, m, &c, &sn);
+        twiddle_entry_fp64(n, m, &c, &sn);
         tw[tw_offset(n) + m] = make_double2(c, sn);
       }
     e = cudaMemcpy((unsigned char*)p + kOffTw, tw, sizeof(tw), cudaMemcpyHostToDevice);

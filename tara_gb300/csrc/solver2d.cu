@@ -129,6 +129,40 @@ void twiddle_entry(int n, int idx, double* re, double* im) {
   if (inv) *im = -*im;
 }
 
+// Entry idx of the FP64 table: as twiddle_entry, except the twiddled radix-4
+// stage entries, which take the ratio form of dft4_tw_ratio (fft.cuh):
+// (tau_r, c_r) for r = 1, 2 and (tau_3, c_3 / c_1) for r = 3, tau = s / c.  A
+// zero cosine (the quarter turn, only ever w2 at k = Ns/2) becomes 2^-256 with
+// tau = s 2^256: both exact powers of two, so c tau = s exactly.
+void twiddle_entry_fp64(int n, int idx, double* a, double* b) {
+  const int span = tw_stage_span(n);
+  if (idx < n || idx >= n + 2 * span) {
+    twiddle_entry(n, idx, a, b);
+    return;
+  }
+  int t = idx - n;
+  const int base = t >= span ? n + span : n;
+  if (t >= span) t -= span;
+  int ns = 4;
+  while (4 * ns - 4 <= t) ns *= 4;
+  const int off = t - (ns - 4);
+  const int r = off / ns + 1, k = off % ns;
+  auto entry = [&](int rr, double* c, double* s) {
+    twiddle_entry(n, base + (ns - 4) + (rr - 1) * ns + k, c, s);
+    if (*c == 0.0) *c = std::ldexp(1.0, -256);
+  };
+  double c, s;
+  entry(r, &c, &s);
+  *a = s / c;
+  if (r < 3) {
+    *b = c;
+  } else {
+    double c1, s1;
+    entry(1, &c1, &s1);
+    *b = c / c1;
+  }
+}
+
 int make_twiddles(int n, bool fp32, void** dev) {
   if (!is_pow2_in_range(n)) {  // the mixed-radix path: the n roots, FP64 only
     if (fp32 || !any_size_2d(n)) return set_error(TARA_ERR_ARGS, "twiddles: unsupported length");
@@ -148,7 +182,7 @@ int make_twiddles(int n, bool fp32, void** dev) {
     std::vector<double2> w(cnt);
     for (int m = 0; m < cnt; ++m) {
       double c, s;
-      twiddle_entry(n, m, &c, &s);
+      twiddle_entry_fp64(n, m, &c, &s);
       w[m] = make_double2(c, s);
     }
     TARA_CK(cudaMalloc(dev, cnt * sizeof(double2)));
