@@ -200,15 +200,17 @@ def run_reference(args) -> None:
 def fft_fp64_inst(n: int, radix8: bool = False) -> int:
     """FP64 instructions of one length-n transform of fft.cuh, counted from its
     butterflies.  Radix-4 path: an untwiddled radix-4 first stage (16 adds per
-    butterfly), twiddled radix-4 stages on ratio-form twiddles (22 FMAs per
-    butterfly) and, for odd log2 n, a twiddled radix-2 stage (6 per butterfly).
-    Radix-8 path: an untwiddled radix-8 first stage (52 per butterfly), twiddled
+    butterfly) or, for odd log2 n, an untwiddled radix-8 first stage (52 per
+    butterfly), then twiddled radix-4 stages on ratio-form twiddles (22 FMAs per
+    butterfly).  Radix-8 path: an untwiddled radix-8 first stage (52 per butterfly), twiddled
     radix-8 stages (72), then zero to two twiddled radix-4 stages on plain
     complex twiddles (24; untwiddled, 16, when they come first)."""
     lg = n.bit_length() - 1
     q = n // 4
     if not radix8:
-        return q * 16 + q * 22 * (lg // 2 - 1) + ((n // 2) * 6 if lg % 2 else 0)
+        if lg % 2:
+            return (n // 8) * 52 + q * 22 * ((lg - 3) // 2)
+        return q * 16 + q * 22 * (lg // 2 - 1)
     s8 = lg // 3 - 1 if (lg % 3 == 1 and lg >= 4) else lg // 3
     s4 = 2 if lg % 3 == 1 else 1 if lg % 3 == 2 else 0
     b8 = n // 8

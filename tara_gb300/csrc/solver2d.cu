@@ -97,6 +97,18 @@ void twiddle_entry(int n, int idx, double* re, double* im) {
     twiddle(n, idx, re, im);
     return;
   }
+  if (idx >= tw_m8_base(n)) {  // radix-4 stages after a radix-8 first stage (layout in fft.cuh)
+    int t = idx - tw_m8_base(n);
+    const int span = tw_m8_span(n);
+    const bool inv = t >= span;
+    if (inv) t -= span;
+    int ns = 8;  // stage Ns owns [Ns - 8, 4 Ns - 8)
+    while (4 * ns - 8 <= t) ns *= 4;
+    const int off = t - (ns - 8);
+    twiddle(n, (off / ns + 1) * (off % ns) * (n / (4 * ns)), re, im);
+    if (inv) *im = -*im;
+    return;
+  }
   if (idx >= tw_r8_base(n)) {  // radix-8 path stage tables (layout in fft.cuh)
     int t = idx - tw_r8_base(n);
     const int span = r8_span(n);
@@ -130,25 +142,34 @@ void twiddle_entry(int n, int idx, double* re, double* im) {
 }
 
 // Entry idx of the FP64 table: as twiddle_entry, except the twiddled radix-4
-// stage entries, which take the ratio form of dft4_tw_ratio (fft.cuh):
-// (tau_r, c_r) for r = 1, 2 and (tau_3, c_3 / c_1) for r = 3, tau = s / c.  A
-// zero cosine (the quarter turn, only ever w2 at k = Ns/2) becomes 2^-256 with
-// tau = s 2^256: both exact powers of two, so c tau = s exactly.
+// stage entries (of the radix-4 path and of the radix-8-first path, fft.cuh),
+// which take the ratio form of dft4_tw_ratio: (tau_r, c_r) for r = 1, 2 and
+// (tau_3, c_3 / c_1) for r = 3, tau = s / c.  A zero cosine (the quarter turn,
+// only ever w2 at k = Ns/2) becomes 2^-256 with tau = s 2^256: both exact
+// powers of two, so c tau = s exactly.
 void twiddle_entry_fp64(int n, int idx, double* a, double* b) {
-  const int span = tw_stage_span(n);
-  if (idx < n || idx >= n + 2 * span) {
+  int start, span, first;  // the region, its per-direction size, its first Ns
+  if (idx >= n && idx < n + 2 * tw_stage_span(n)) {
+    start = n;
+    span = tw_stage_span(n);
+    first = 4;
+  } else if (idx >= tw_m8_base(n) && idx < tw_m8_base(n) + 2 * tw_m8_span(n)) {
+    start = tw_m8_base(n);
+    span = tw_m8_span(n);
+    first = 8;
+  } else {
     twiddle_entry(n, idx, a, b);
     return;
   }
-  int t = idx - n;
-  const int base = t >= span ? n + span : n;
+  int t = idx - start;
+  const int base = t >= span ? start + span : start;
   if (t >= span) t -= span;
-  int ns = 4;
-  while (4 * ns - 4 <= t) ns *= 4;
-  const int off = t - (ns - 4);
+  int ns = first;  // stage Ns owns [Ns - first, 4 Ns - first)
+  while (4 * ns - first <= t) ns *= 4;
+  const int off = t - (ns - first);
   const int r = off / ns + 1, k = off % ns;
   auto entry = [&](int rr, double* c, double* s) {
-    twiddle_entry(n, base + (ns - 4) + (rr - 1) * ns + k, c, s);
+    twiddle_entry(n, base + (ns - first) + (rr - 1) * ns + k, c, s);
     if (*c == 0.0) *c = std::ldexp(1.0, -256);
   };
   double c, s;

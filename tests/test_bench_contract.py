@@ -53,10 +53,10 @@ def test_warmup_is_at_least_three():
 
 
 def test_fft_fp64_instruction_count():
-    # 2048 = 4^5 * 2: an untwiddled radix-4 stage, 4 twiddled ones, one radix-2 stage
-    assert bench.fft_fp64_inst(2048) == 512 * 16 + 512 * 24 * 4 + 1024 * 6 == 63488
-    # 1024 = 4^5: no radix-2 stage
-    assert bench.fft_fp64_inst(1024) == 256 * 16 + 256 * 24 * 4
+    # 2048 = 8 * 4^4: an untwiddled radix-8 stage, then 4 ratio-form radix-4 stages
+    assert bench.fft_fp64_inst(2048) == 256 * 52 + 512 * 22 * 4 == 58368
+    # 1024 = 4^5: an untwiddled radix-4 stage, then 4 ratio-form ones
+    assert bench.fft_fp64_inst(1024) == 256 * 16 + 256 * 22 * 4
     for n in (16, 32, 64, 128, 256, 512, 1024, 2048):
         lg = n.bit_length() - 1
         # about 3 FP64 instructions per point per radix-2 stage, fewer for the untwiddled first stage
