@@ -731,6 +731,13 @@ module tara_gb300
       integer(c_int), value :: reps
       real(c_double), intent(out) :: inst_per_s
     end function tara_measure_dfma_rate
+    integer(c_int) function tara_twiddle_table(n, precision, out, capacity, count) &
+        bind(C, name="tara_twiddle_table")
+      import
+      integer(c_int), value :: n, precision, capacity
+      real(c_double), intent(out) :: out(*)
+      integer(c_int), intent(out) :: count
+    end function tara_twiddle_table
     type(c_ptr) function tara_version() bind(C, name="tara_version")
       import
     end function tara_version

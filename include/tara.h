@@ -659,6 +659,14 @@ int tara_derive2csh_noalloc(int nx, int ny, double nu, const void* omegak_dev,
  * The measured denominator of the FP64-pipe roofline. */
 int tara_measure_dfma_rate(int reps, double* inst_per_s);
 
+/* The transforms' twiddle table of a power-of-two length n (16..4096) as the
+ * device reads it, host only (no device call): *count entries of two doubles.
+ * TARA_PREC_FP64 gives the FP64 table, whose twiddled radix-4 stage entries hold
+ * the ratio form (tau, c) and (tau3, c3/c1), tau = s/c; TARA_PREC_FP32 the plain
+ * twiddles (cos, -sin) before their rounding to FP32.  With out NULL only *count
+ * is set; otherwise capacity must be at least *count. */
+int tara_twiddle_table(int n, int precision, double* out, int capacity, int* count);
+
 /* Library version string. */
 const char* tara_version(void);
 

@@ -172,6 +172,7 @@ def _declare(L: ctypes.CDLL) -> None:
     L.tara3d_stream.argtypes = [vp]
     L.tara3d_stream.restype = vp
     L.tara_measure_dfma_rate.argtypes = [c_int, dp]
+    L.tara_twiddle_table.argtypes = [c_int, c_int, dp, c_int, ctypes.POINTER(c_int)]
     L.tara_coh2d_default_config.argtypes = [vp, c_int, c_int]
     L.tara_coh2d_default_config.restype = None
     L.tara_coh2d_create.argtypes = [vp, vp]
@@ -372,6 +373,17 @@ def measure_dfma_rate(reps: int = 5) -> float:
     v = ctypes.c_double()
     _check(lib().tara_measure_dfma_rate(int(reps), ctypes.byref(v)))
     return v.value
+
+
+def twiddle_table(n: int, precision: int = PREC_FP64) -> np.ndarray:
+    """The transforms' twiddle table of length n as the device reads it, (count, 2)
+    doubles (tara_twiddle_table; host only)."""
+    cnt = ctypes.c_int()
+    _check(lib().tara_twiddle_table(int(n), int(precision), None, 0, ctypes.byref(cnt)))
+    out = np.zeros((cnt.value, 2))
+    _check(lib().tara_twiddle_table(int(n), int(precision), out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                    cnt.value, ctypes.byref(cnt)))
+    return out
 
 
 def fft2d_r2c(x: np.ndarray, precision: int = PREC_FP64) -> np.ndarray:

@@ -223,6 +223,22 @@ __global__ void __launch_bounds__(256) k_dfma_probe(double* out, int iters, doub
   if (s == -1.0) out[0] = s;
 }
 
+int tara_twiddle_table(int n, int precision, double* out, int capacity, int* count) {
+  if (!count || !is_pow2_in_range(n) || (precision != TARA_PREC_FP64 && precision != TARA_PREC_FP32))
+    return set_error(TARA_ERR_ARGS, "tara_twiddle_table: n a power of two in [16, 4096], FP64 or FP32");
+  const int cnt = tw_count(n);
+  *count = cnt;
+  if (!out) return TARA_OK;
+  if (capacity < cnt) return set_error(TARA_ERR_ARGS, "tara_twiddle_table: capacity below the entry count");
+  for (int m = 0; m < cnt; ++m) {
+    if (precision == TARA_PREC_FP64)
+      twiddle_entry_fp64(n, m, out + 2 * m, out + 2 * m + 1);
+    else
+      twiddle_entry(n, m, out + 2 * m, out + 2 * m + 1);
+  }
+  return TARA_OK;
+}
+
 int tara_measure_dfma_rate(int reps, double* inst_per_s) {
   if (!inst_per_s || reps < 1) return set_error(TARA_ERR_ARGS, "bad argument");
   int dev, sms;
