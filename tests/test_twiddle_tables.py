@@ -210,3 +210,87 @@ def test_table_export_validates_arguments():
     rc = tg.lib().tara_twiddle_table(64, tg.PREC_FP64, buf.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), 4,
                                      ctypes.byref(cnt))
     assert rc == tg.TARA_ERR_ARGS and cnt.value > 4 and not buf.any()
+
+
+# ---- the 8-point DFT of fft.cuh, single lane (dft8) and split over a lane pair
+C8 = 0.70710678118654752440
+
+
+def _mul_w4(t, inv):  # exact: a swap and a sign
+    return (-t[1], t[0]) if inv else (t[1], -t[0])
+
+
+def _pair_1(a, b):
+    return (a[0] + b[0], a[1] + b[1]), (a[0] - b[0], a[1] - b[1])
+
+
+def _pair_w4(a, b, inv):
+    return _pair_1(a, _mul_w4(b, inv))
+
+
+def _pair_w8(a, b, inv, e):
+    x, y = b
+    if not inv:
+        p, q = (x + y, y - x) if e == 1 else (y - x, -(x + y))
+    else:
+        p, q = (x - y, x + y) if e == 1 else (-(x + y), x - y)
+    return (a[0] + C8 * p, a[1] + C8 * q), (a[0] - C8 * p, a[1] - C8 * q)
+
+
+def _dft8(v, inv):
+    v = list(v)
+    for i in range(4):
+        v[i], v[i + 4] = _pair_1(v[i], v[i + 4])
+    v[0], v[2] = _pair_1(v[0], v[2])
+    v[1], v[3] = _pair_1(v[1], v[3])
+    v[4], v[6] = _pair_w4(v[4], v[6], inv)
+    v[5], v[7] = _pair_w4(v[5], v[7], inv)
+    v[0], v[1] = _pair_1(v[0], v[1])
+    v[2], v[3] = _pair_w4(v[2], v[3], inv)
+    v[4], v[5] = _pair_w8(v[4], v[5], inv, 1)
+    v[6], v[7] = _pair_w8(v[6], v[7], inv, 3)
+    out = [None] * 8
+    for i, q in enumerate((0, 4, 2, 6, 1, 5, 3, 7)):
+        out[q] = v[i]
+    return out
+
+
+def _dft8_lane_pair(v, inv):
+    lanes = []
+    for odd in (0, 1):
+        u = [v[2 * i + odd] for i in range(4)]
+        u[0], u[2] = _pair_1(u[0], u[2])
+        u[1], u[3] = _pair_1(u[1], u[3])
+        u[0], u[1] = _pair_1(u[0], u[1])
+        u[2], u[3] = _pair_w4(u[2], u[3], inv)
+        lanes.append(u)
+    out = [None] * 8
+    for odd in (0, 1):
+        u, w = lanes[odd], lanes[1 - odd]
+        r0, r1 = (w[1], w[3]) if odd else (w[0], w[2])  # what the partner lane sends
+        x0 = r0 if odd else u[0]
+        x1 = _mul_w4(u[1], inv) if odd else r0
+        x4 = r1 if odd else u[2]
+        x5 = _mul_w4(u[3], inv) if odd else r1
+        x0, x1 = _pair_1(x0, x1)
+        x4, x5 = _pair_w8(x4, x5, inv, 1)
+        o = 2 if odd else 0
+        out[o], out[o + 4], out[o + 1], out[o + 5] = x0, x1, x4, x5
+    return out
+
+
+@pytest.mark.parametrize("inv", [False, True])
+def test_lane_pair_8point_dft_gives_the_single_lane_bits(inv):
+    """fft_slot_m8's lane-pair form runs dft8's pairs on the same operands: the odd
+    lane's (x2, W4 x3) and (x6, W4 x7) pairs reproduce pair_w4 and pair_w8<3> bit
+    for bit, and both equal the DFT to rounding."""
+    rng = np.random.default_rng(8 + inv)
+    for _ in range(200):
+        z = rng.standard_normal((8, 2)) * 10.0 ** rng.integers(-5, 6, size=(8, 1))
+        v = [tuple(r) for r in z]
+        a, b = _dft8(v, inv), _dft8_lane_pair(v, inv)
+        assert all(p == q for p, q in zip(a, b))
+        x = z[:, 0] + 1j * z[:, 1]
+        ref = np.fft.ifft(x) * 8 if inv else np.fft.fft(x)
+        got = np.array([complex(*t) for t in a])
+        assert np.abs(got - ref).max() <= 1e-14 * np.abs(x).sum()
