@@ -416,7 +416,9 @@ int tara_closure_create(tara2d* h, tara_fno* f, const double* in_scales, double 
   const void *tx, *ty;
   int rc;
   if ((rc = twiddles64(h, &tx, &ty))) {
+    const ErrorState saved = save_error();
     tara_closure_destroy(c);
+    restore_error(saved);
     return rc;
   }
   *out = c;

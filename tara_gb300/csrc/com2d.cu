@@ -490,8 +490,10 @@ int tara_com2d_create(const tara_com2d_config* cfg, tara_com2d** out) {
   h->rpitch = round_up(h->nx, 8);
   h->fs = (size_t)h->ny * h->pitch;
   h->rfs = (size_t)h->ny * h->rpitch;
-  auto fail = [&](int code) {
+  auto fail = [&](int code) {  // free the half-built handle, keep the error
+    const ErrorState saved = save_error();
     tara_com2d_destroy(h);
+    restore_error(saved);
     return code;
   };
 #define CKC(call)                                              \

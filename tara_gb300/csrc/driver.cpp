@@ -11,15 +11,20 @@
 
 #include "../../include/tara.h"
 #include "ini.h"
-
-namespace tara {
-int set_error(int code, const std::string& msg);
-int set_ok();
-}  // namespace tara
+#include "status.h"
 
 using namespace tara;
 
 namespace {
+
+// A run that leaves on an error frees its handles on the way out; the public
+// destroy records success, so the error is saved and put back around it.
+template <typename F>
+void keep_error_across(F&& cleanup) {
+  const ErrorState saved = save_error();
+  cleanup();
+  restore_error(saved);
+}
 
 const double kPi = 3.14159265358979323846;  // real(kind=8), parameter :: pi (main2css.f95:9)
 
@@ -185,7 +190,7 @@ int run_2d(Reader& R, const std::string& out, int max_steps, bool screened) {
   if (tara2d_create(&cfg, &h)) return fail_rc();
   struct Guard {
     tara2d* h;
-    ~Guard() { tara2d_destroy(h); }
+    ~Guard() { keep_error_across([&] { tara2d_destroy(h); }); }
   } guard{h};
   if (tara2d_set_state(h, wk.data(), nullptr)) return fail_rc();
   const size_t nr = (size_t)nx * ny;
@@ -205,7 +210,7 @@ int run_2d(Reader& R, const std::string& out, int max_steps, bool screened) {
   tara_particles* parts = nullptr;
   struct PGuard {
     tara_particles** p;
-    ~PGuard() { tara_particles_destroy(*p); }
+    ~PGuard() { keep_error_across([&] { tara_particles_destroy(*p); }); }
   } pguard{&parts};
   std::vector<double> xp, yp;
   if (!screened && np > 0) {
@@ -325,7 +330,7 @@ int run_3d(Reader& R, const std::string& out, int max_steps) {
   if (tara3d_create(&cfg, &h)) return fail_rc();
   struct Guard {
     tara3d* h;
-    ~Guard() { tara3d_destroy(h); }
+    ~Guard() { keep_error_across([&] { tara3d_destroy(h); }); }
   } guard{h};
   if (tara3d_set_state_real(h, real.data())) return fail_rc();
   mkdir(out.c_str(), 0755);
@@ -373,7 +378,7 @@ int run_coh(Reader& R, const std::string& out, int max_steps) {
   if (tara_coh2d_create(&cfg, &h)) return fail_rc();
   struct Guard {
     tara_coh2d* h;
-    ~Guard() { tara_coh2d_destroy(h); }
+    ~Guard() { keep_error_across([&] { tara_coh2d_destroy(h); }); }
   } guard{h};
   if (tara_coh2d_init_vortices(h, lx_ini, ly_ini)) return fail_rc();
   mkdir(out.c_str(), 0755);
@@ -449,7 +454,7 @@ int run_com(Reader& R, const std::string& out, int max_steps) {
   if (tara_com2d_create(&cfg, &h)) return fail_rc();
   struct Guard {
     tara_com2d* h;
-    ~Guard() { tara_com2d_destroy(h); }
+    ~Guard() { keep_error_across([&] { tara_com2d_destroy(h); }); }
   } guard{h};
   if (tara_com2d_init_reference(h, lx_ini, ly_ini, B0)) return fail_rc();
   mkdir(out.c_str(), 0755);

@@ -166,8 +166,10 @@ int tara_ens_create(int nruns, const tara_ens_run* runs, int precision, int sche
   *out = nullptr;
   tara_ens* e = new tara_ens();
   e->nruns = nruns;
-  auto fail = [&](int code) {
+  auto fail = [&](int code) {  // free the half-built handle, keep the error
+    const ErrorState saved = save_error();
     tara_ens_destroy(e);
+    restore_error(saved);
     return code;
   };
   if (cudaGetDevice(&e->dev) != cudaSuccess) return fail(set_error(TARA_ERR_CUDA, "cudaGetDevice"));

@@ -1443,8 +1443,10 @@ int tara_fno_create(const tara_fno_config* cfg, tara_fno** out) {
   tara_fno* f = new tara_fno();
   f->cfg = c;
   f->bmax = c.max_batch;
-  auto fail = [&](int code) {
+  auto fail = [&](int code) {  // free the half-built handle, keep the error
+    const ErrorState saved = save_error();
     tara_fno_destroy(f);
+    restore_error(saved);
     return code;
   };
   // parameter layout

@@ -7,12 +7,11 @@
 
 #include "../../include/tara.h"
 #include "kernels2d.cuh"
+#include "status.h"
 
 namespace tara {
 
-// thread-local status (tara_last_error)
-int set_error(int code, const std::string& msg);
-int set_ok();
+// thread-local status (tara_last_error): set_error, set_ok, save/restore_error in status.h
 int cuda_fail(cudaError_t e, const char* what);
 
 #define TARA_CK(call)                                   \

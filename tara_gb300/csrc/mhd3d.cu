@@ -597,8 +597,10 @@ int tara3d_create(const tara3d_config* cfg, tara3d** out) {
   h->fs = (size_t)h->nz * h->ny * h->pitch;
   h->rfs = (size_t)h->nz * h->ny * h->rpitch;
   int rc;
-  auto fail = [&](int code) {
+  auto fail = [&](int code) {  // free the half-built handle, keep the error
+    const ErrorState saved = save_error();
     tara3d_destroy(h);
+    restore_error(saved);
     return code;
   };
 #define CK3(call)                                              \

@@ -138,7 +138,9 @@ int tara_particles_create(tara2d* h, double kpi, double lx, double ly, int np, c
               cudaMemcpy(p->yp, yp, np * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess))
     rc = set_error(TARA_ERR_CUDA, "particle upload");
   if (rc) {
+    const ErrorState saved = save_error();
     tara_particles_destroy(p);
+    restore_error(saved);
     return rc;
   }
   *out = p;

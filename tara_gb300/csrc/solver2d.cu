@@ -27,6 +27,11 @@ int set_ok() {
   g_msg.clear();
   return TARA_OK;
 }
+ErrorState save_error() { return ErrorState{g_err, g_msg}; }
+void restore_error(const ErrorState& s) {
+  g_err = s.code;
+  g_msg = s.msg;
+}
 int cuda_fail(cudaError_t e, const char* what) {
   const int code = (e == cudaErrorMemoryAllocation) ? TARA_ERR_NOMEM : TARA_ERR_CUDA;
   return set_error(code, std::string(what) + ": " + cudaGetErrorString(e));
@@ -676,8 +681,10 @@ int tara2d_create(const tara2d_config* cfg, tara2d** out) {
         break;
       }
   int rc = TARA_OK;
-  auto fail = [&](int code) {
+  auto fail = [&](int code) {  // free the half-built handle, keep the error
+    const ErrorState saved = save_error();
     tara2d_destroy(h);
+    restore_error(saved);
     return code;
   };
 #define CKC(call)                                              \

@@ -103,6 +103,25 @@ def test_no_silent_fallback_without_gpu():
     assert e.value.code in (tg.TARA_ERR_CUDA, tg.TARA_ERR_NOMEM)
 
 
+@pytest.mark.parametrize("cls,args", [("Solver2D", (64,)), ("Solver3D", (16,)), ("Coh2D", (64,)), ("Com2D", (64,))])
+def test_failed_create_keeps_its_error_message(cls, args):
+    """A create that fails after recording an error frees its half-built handle
+    through the public destroy (which records success); the error code and
+    message it recorded are what the caller reads back."""
+    try:
+        import torch
+
+        has_gpu = torch.cuda.is_available()
+    except Exception:
+        has_gpu = False
+    if has_gpu:
+        pytest.skip("a GPU is present")
+    with pytest.raises(tg.TaraError) as e:
+        getattr(tg, cls)(*args)
+    code, msg = tg.last_error()
+    assert code == e.value.code and code in (tg.TARA_ERR_CUDA, tg.TARA_ERR_NOMEM) and msg
+
+
 @pytest.mark.parametrize("name,nf", [("derive2coh_", 3), ("derive2com_", 6)])
 def test_compressible_dropins_validate_before_the_gpu(name, nf):
     """Shape errors of the compressible drop-ins are recorded before any device
@@ -182,6 +201,32 @@ def test_driver_refuses_unsupported_grids(tmp_path, grid, dim, program, bad):
     assert program in msg and bad in msg and "powers of two" in msg
     if dim == 2:
         assert "factors are 2, 3, 5 and 7" in msg
+
+
+@pytest.mark.parametrize("grid,domain,parallel", [
+    ("Nx = 96\nNy = 112", "hydro", "serial"),     # factors 3 and 7
+    ("Nx = 3600\nNy = 64", "hydro", "serial"),    # the longest mixed-radix length
+    ("Nx = 120\nNy = 98", "hydro", "openmp"),     # compressible hydro (tara2dHydOMP)
+    ("Nx = 80\nNy = 48", "mhd", "openmp"),        # compressible MHD (tara2dMHDOMP)
+])
+def test_driver_passes_mixed_radix_grids_to_the_solver(tmp_path, grid, domain, parallel):
+    """Even lengths up to 3600 whose only prime factors are 2, 3, 5, 7 pass the
+    driver's grid check for every 2D program: what follows is the solver (on a
+    machine without a GPU, a device error, whose message survives the driver
+    freeing its handles), never an argument error."""
+    ini = (f"[dimension]\ndim = 2\n[architecture]\narch = cpu\n[parallel]\nmode = {parallel}\n[type]\n"
+           f"domain = {domain}\n[problem]\nhydrotype = bare\n[particle]\nNp = 0\n[grid]\n{grid}\nNz = 64\n"
+           "[length]\nLx = 2.0d0\nLy = 2.0d0\nLz = 2.0d0\n[resistivity]\nnu = 0.01d0\neta = 0.0d0\n"
+           "[time]\ntime_min = 0.0d0\ntime_max = 0.0001d0\ndt = 0.0001d0\n"
+           "[initialProfile]\nW0 = 25.0d0\nm0 = 2.0d0\nd = 0.0234375d0\n")
+    (tmp_path / "input.ini").write_text(ini)
+    tg.lib().tara_clear_error()
+    rc = tg.lib().tara_run_ini(str(tmp_path / "input.ini").encode(), str(tmp_path / "out").encode(), 1)
+    code, msg = tg.last_error()
+    assert rc != tg.TARA_ERR_ARGS and code != tg.TARA_ERR_ARGS, msg
+    assert "not supported" not in msg
+    if rc != tg.TARA_OK:
+        assert code == rc and msg
 
 
 @pytest.mark.parametrize("prec", [tg.PREC_FP32, tg.PREC_DF64])
