@@ -2,9 +2,10 @@
 //
 // One "slot" is a length-N complex vector in shared memory, transformed by a
 // group of G = N/16 threads (16 elements per thread: four radix-4 butterflies
-// per stage, or eight radix-2 butterflies in the final odd stage).  Every thread
-// of the CTA calls the same transform so that the stage barriers line up;
-// `active` masks threads whose slot holds nothing.
+// per stage, or, for odd log2 N, eight radix-2 butterflies in a final stage
+// (FP32, double-float) or two 8-point DFTs in a first stage (FP64)).  Every
+// thread of the CTA calls the same transform so that the stage barriers line
+// up; `active` masks threads whose slot holds nothing.
 //
 // Stockham autosort form (Govindaraju et al., SC'08): at a stage with
 // sub-transform length Ns and radix R, butterfly j reads in[j + r*N/R],
