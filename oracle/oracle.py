@@ -135,10 +135,14 @@ class Oracle:
         self.L.oracle_r2c_2d(nx, ny, x.ctypes.data, out.ctypes.data)
         return out
 
-    def c2r(self, c):
+    def c2r(self, c, nx=None):
+        """Unnormalised c2r of a (Ny, Nh) half spectrum; nx defaults to the even
+        length 2 (Nh - 1) (an odd nx = 2 Nh - 1 has the same Nh)."""
         c = np.ascontiguousarray(c, np.complex128)
         ny, nh = c.shape
-        nx = 2 * (nh - 1)
+        nx = 2 * (nh - 1) if nx is None else int(nx)
+        if nx // 2 + 1 != nh:
+            raise ValueError(f"nx = {nx} does not match Nh = {nh}")
         out = np.zeros((ny, nx), np.float64)
         self.L.oracle_c2r_2d(nx, ny, c.ctypes.data, out.ctypes.data)
         return out

@@ -200,7 +200,8 @@ static void fft1d(double* z, int n, int sign, const fft_plan* p) {
 
 /* rank-2 c2r as FFTW's rank-geq2-rdft2 orders it: complex backward DFTs along y
  * for every kx column, then 1D c2r along x, where the 1D c2r reads only the real
- * parts of the kx=0 and kx=Nx/2 bins.  Two rows share one complex transform. */
+ * parts of the kx=0 bin and, for even Nx, the kx=Nx/2 bin (odd Nx has no
+ * self-conjugate bin but kx=0).  Two rows share one complex transform. */
 void oracle_c2r_2d(int nx, int ny, const double* in, double* out) {
   const int nh = nx / 2 + 1;
   const size_t ns = (size_t)nh * ny;
@@ -230,12 +231,12 @@ void oracle_c2r_2d(int nx, int ny, const double* in, double* out) {
       const double* a = tmp + 2 * (size_t)j * nh;
       const double* b = (j + 1 < ny) ? tmp + 2 * (size_t)(j + 1) * nh : NULL;
       for (int k = 0; k <= nx / 2; ++k) {
-        const int edge = (k == 0 || k == nx / 2);
+        const int edge = (k == 0 || 2 * k == nx); /* self-conjugate bins (Nyquist for even nx only) */
         const double ar = a[2 * k], ai = edge ? 0.0 : a[2 * k + 1];
         const double br = b ? b[2 * k] : 0.0, bi = (b && !edge) ? b[2 * k + 1] : 0.0;
         z[2 * k] = ar - bi; /* A + iB */
         z[2 * k + 1] = ai + br;
-        if (k > 0 && k < nx / 2) {
+        if (!edge) {
           z[2 * (nx - k)] = ar + bi; /* conj(A) + i conj(B) */
           z[2 * (nx - k) + 1] = -ai + br;
         }

@@ -42,3 +42,16 @@ def test_oracle_transforms_invert_at_factor_7_lengths(oracle, ny, nx):
     assert rel_l2(oracle.c2r(oracle.r2c(x)) / (nx * ny), x) < 1e-14
     k = np.fft.rfft2(x)
     assert rel_l2(oracle.r2c(x), k) < 1e-14
+
+
+@pytest.mark.parametrize("ny,nx", [(45, 45), (27, 50), (50, 27), (33, 35), (64, 63)])
+def test_oracle_transforms_at_odd_lengths(oracle, ny, nx):
+    """Odd lengths (which the reference's FFTW takes and the GPU path refuses):
+    the oracle's r2c and c2r against numpy's pocketfft, whose c2r keeps FFTW's
+    semantics (a complex inverse along y, then a c2r along x that reads only the
+    real part of the self-conjugate bins: kx = 0, and kx = Nx/2 for even Nx)."""
+    rng = np.random.default_rng(nx * 100 + ny)
+    x = rng.standard_normal((ny, nx))
+    assert rel_l2(oracle.r2c(x), np.fft.rfft2(x)) < 1e-14
+    c = rng.standard_normal((ny, nx // 2 + 1)) + 1j * rng.standard_normal((ny, nx // 2 + 1))
+    assert rel_l2(oracle.c2r(c, nx), np.fft.irfft2(c, s=(ny, nx)) * (nx * ny)) < 1e-14
