@@ -560,6 +560,13 @@ module tara_gb300
       character(kind=c_char), intent(out) :: buf(*)
       integer(c_int), value :: buflen
     end function tara_fortran_list_record
+    integer(c_int) function tara_write_grid_records(path, nx, ny, xs, ys, fields, nfields) &
+        bind(C, name="tara_write_grid_records")
+      import
+      character(kind=c_char), intent(in) :: path(*)
+      integer(c_int), value :: nx, ny, nfields
+      real(c_double), intent(in) :: xs(*), ys(*), fields(*)
+    end function tara_write_grid_records
 
     ! ---- Lagrangian particles -------------------------------------------------
     integer(c_int) function tara_particles_create(h, kpi, lx, ly, np, xp, yp, p) &

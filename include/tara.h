@@ -486,6 +486,12 @@ int tara_fortran_read_double(const char* s, double* out);
 int tara_fortran_read_int(const char* s, long long* out);
 /* One list-directed output record of n REAL(8) values, gfortran style. */
 int tara_fortran_list_record(const double* v, int n, char* buf, int buflen);
+/* A snapshot file in the reference drivers' fort.* format: one record per grid
+ * point, x outer and y inner, holding xs[i], ys[j] and fields[k*nx*ny + j*nx + i]
+ * for k < nfields (the same records as tara_fortran_list_record), formatted in
+ * parallel on the host's cores. */
+int tara_write_grid_records(const char* path, int nx, int ny, const double* xs, const double* ys,
+                            const double* fields, int nfields);
 
 /* ---- Lagrangian passive particles ------------------------------------------ */
 /* The plain serial driver's particles (src/main2csh.f95:93-96, 187-273): after a

@@ -169,9 +169,10 @@ int run_2d(Reader& R, const std::string& out, int max_steps, bool screened) {
     }
   mkdir(out.c_str(), 0755);
   if (screened) {
-    Out f15(out + "/Initial_Condition_Velocity.dat");
-    for (int i = 0; i < nx; ++i)
-      for (int j = 0; j < ny; ++j) f15.rec({xs[i], ys[j], omega[(size_t)j * nx + i], 0.0, 0.0});
+    const std::vector<double> zero((size_t)nx * ny, 0.0);
+    if (int rc = write_grid_records(out + "/Initial_Condition_Velocity.dat", nx, ny, xs.data(), ys.data(),
+                                    {omega.data(), zero.data(), zero.data()}))
+      return rc;
   }
   std::vector<double> wk(2 * (size_t)nh * ny);
   if (tara_fft2d_r2c(nx, ny, TARA_PREC_FP64, omega.data(), wk.data())) return fail_rc();
@@ -198,12 +199,9 @@ int run_2d(Reader& R, const std::string& out, int max_steps, bool screened) {
   if (screened) {  // initial diagnostics use psi = omega/k^2 (src/main2css.f95:112-179)
     tara2d_diag_params p0 = {kPi, lx, ly, 0.0, 0};
     if (tara2d_real_fields(h, &p0, psi.data(), om.data(), ux.data(), uy.data())) return fail_rc();
-    Out f10(out + "/Initial_Condition_Omega_REP.dat");
-    for (int i = 0; i < nx; ++i)
-      for (int j = 0; j < ny; ++j) {
-        const size_t r = (size_t)j * nx + i;
-        f10.rec({xs[i], ys[j], om[r], psi[r], ux[r], uy[r]});
-      }
+    if (int rc = write_grid_records(out + "/Initial_Condition_Omega_REP.dat", nx, ny, xs.data(), ys.data(),
+                                    {om.data(), psi.data(), ux.data(), uy.data()}))
+      return rc;
   }
   // Lagrangian particles of the plain driver (src/main2csh.f95:93-96, 187-273);
   // the screened driver reads Np but moves none
@@ -238,23 +236,17 @@ int run_2d(Reader& R, const std::string& out, int max_steps, bool screened) {
       y_energy += uysq;  // never reset by the reference (src/main2css.f95:259)
       if (t % every == 0) {
         if (tara2d_real_fields(h, &dp, nullptr, om.data(), ux.data(), uy.data())) return fail_rc();
-        Out snap(fort_name(out, t + 100));
-        for (int i = 0; i < nx; ++i)
-          for (int j = 0; j < ny; ++j) {
-            const size_t r = (size_t)j * nx + i;
-            snap.rec({xs[i], ys[j], ux[r], uy[r], om[r]});
-          }
+        if (int rc = write_grid_records(fort_name(out, t + 100), nx, ny, xs.data(), ys.data(),
+                                        {ux.data(), uy.data(), om.data()}))
+          return rc;
       }
       energy.rec({time, usq, y_energy});
     } else {
       if (t % every == 0) {
         if (tara2d_real_fields(h, &dp, nullptr, om.data(), ux.data(), uy.data())) return fail_rc();
-        Out snap(fort_name(out, t + 100));
-        for (int i = 0; i < nx; ++i)
-          for (int j = 0; j < ny; ++j) {
-            const size_t r = (size_t)j * nx + i;
-            snap.rec({xs[i], ys[j], om[r], ux[r], uy[r]});
-          }
+        if (int rc = write_grid_records(fort_name(out, t + 100), nx, ny, xs.data(), ys.data(),
+                                        {om.data(), ux.data(), uy.data()}))
+          return rc;
       }
       if (parts) {
         if (tara_particles_advance(parts, dt)) return fail_rc();
@@ -388,13 +380,7 @@ int run_coh(Reader& R, const std::string& out, int max_steps) {
   for (int j = 0; j < ny; ++j) ys[j] = 0.0 + (double)(float)j * dy;
   auto snapshot = [&](const std::string& path) -> int {  // x, y, omega, n, ux, uy
     if (tara_coh2d_real_fields(h, dn.data(), ux.data(), uy.data(), om.data())) return fail_rc();
-    Out f(path);
-    for (int i = 0; i < nx; ++i)
-      for (int j = 0; j < ny; ++j) {
-        const size_t r = (size_t)j * nx + i;
-        f.rec({xs[i], ys[j], om[r], dn[r], ux[r], uy[r]});
-      }
-    return TARA_OK;
+    return write_grid_records(path, nx, ny, xs.data(), ys.data(), {om.data(), dn.data(), ux.data(), uy.data()});
   };
   int rc;
   if ((rc = snapshot(out + "/Initial_Grid_Data_Reproduced.dat"))) return rc;  // (:214-238)
@@ -476,12 +462,10 @@ int run_com(Reader& R, const std::string& out, int max_steps) {
       if (tara_com2d_real_fields(h, f[0].data(), f[1].data(), f[2].data(), f[3].data(), f[4].data(), f[5].data(),
                                  f[6].data()))
         return fail_rc();
-      Out snap(fort_name(out, t + 100000));
-      for (int i = 0; i < nx; ++i)
-        for (int j = 0; j < ny; ++j) {
-          const size_t r = (size_t)j * nx + i;
-          snap.rec({xs[i], ys[j], f[0][r], f[1][r], f[2][r], f[3][r], f[4][r], f[5][r], f[6][r]});
-        }
+      if (int rc = write_grid_records(fort_name(out, t + 100000), nx, ny, xs.data(), ys.data(),
+                                      {f[0].data(), f[1].data(), f[2].data(), f[3].data(), f[4].data(),
+                                       f[5].data(), f[6].data()}))
+        return rc;
     }
     if (std::fmod(tf, 100.0) == 0.0) {  // Energy.dat every 100 steps (:578-580)
       double d[5];

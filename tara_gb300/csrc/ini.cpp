@@ -2,13 +2,16 @@
 // list-directed number reads.  Host code only.
 #include "ini.h"
 
+#include <algorithm>
 #include <cctype>
+#include <charconv>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
 #include <sstream>
+#include <thread>
 
 #include "../../include/tara.h"
 
@@ -251,41 +254,118 @@ bool fortran_read_int(const std::string& s, long long& v, std::string& err) {
   return true;
 }
 
-std::string fortran_list_record(const double* v, int n) {
-  std::string rec;
-  char buf[64];
-  for (int k = 0; k < n; ++k) {
-    const double x = v[k];
-    rec += ' ';  // value separator: a 20-character F field must not touch its neighbour
-    if (!std::isfinite(x)) {
-      std::snprintf(buf, sizeof buf, "%25s", std::isnan(x) ? "NaN" : (x > 0 ? "Infinity" : "-Infinity"));
-      rec += buf;
-      continue;
-    }
-    // decimal exponent after rounding to 17 significant digits
-    int e10 = 0;
-    if (x != 0.0) {
-      std::snprintf(buf, sizeof buf, "%.16E", x);
-      e10 = std::atoi(std::strchr(buf, 'E') + 1);
-    }
-    if (x == 0.0 || (e10 >= -1 && e10 < 17)) {
-      const int dec = x == 0.0 ? 16 : 16 - e10;  // F(20).(17 - k) with k = e10 + 1 integer digits
-      char f[48];
-      std::snprintf(f, sizeof f, "%.*f", dec, x);
-      std::snprintf(buf, sizeof buf, "%20s     ", f);
-    } else {
-      char m[48];
-      std::snprintf(m, sizeof m, "%.16E", x);  // d.dddddddddddddddE+xx
-      char* ep = std::strchr(m, 'E');
-      const int ex = std::atoi(ep + 1);
-      *ep = '\0';
-      char f[64];
-      std::snprintf(f, sizeof f, "%sE%c%03d", m, ex < 0 ? '-' : '+', ex < 0 ? -ex : ex);
-      std::snprintf(buf, sizeof buf, "%25s", f);
-    }
-    rec += buf;
+// One REAL(8) item of a list-directed record: a separating blank, then G25.17
+// (F20.(16 - e) plus five blanks for 0.1 <= |x| < 1e17, where e is the decimal
+// exponent after rounding to 17 significant digits; otherwise 1P E25.17 with a
+// three-digit exponent).  Always kItem characters.  The 17 digits come from one
+// correctly rounded conversion (std::to_chars, the digits printf's %.16E gives);
+// the F form places the same digits around the decimal point, which is what
+// printf's %.*f gives at 16 - e decimals, since both round at the 17th
+// significant digit.
+constexpr int kItem = 26;
+
+char* fortran_item(char* out, double x) {
+  char* p = out;
+  *p++ = ' ';
+  if (!std::isfinite(x)) {
+    const char* w = std::isnan(x) ? "NaN" : (x > 0 ? "Infinity" : "-Infinity");
+    const int len = (int)std::strlen(w);
+    std::memset(p, ' ', 25 - len);
+    std::memcpy(p + 25 - len, w, len);
+    return p + 25;
   }
+  char s[48];
+  const std::to_chars_result r = std::to_chars(s, s + sizeof s, x, std::chars_format::scientific, 16);
+  const bool neg = s[0] == '-';
+  const char* d = s + (neg ? 1 : 0);  // d[0] '.' d[2..17] 'e' sign exponent
+  int ex = 0;
+  for (const char* q = d + 20; q < r.ptr; ++q) ex = 10 * ex + (*q - '0');
+  if (d[19] == '-') ex = -ex;
+  char f[32];
+  int n = 0;
+  if (neg) f[n++] = '-';
+  if (x == 0.0 || (ex >= -1 && ex < 17)) {
+    char dig[17];
+    dig[0] = d[0];
+    std::memcpy(dig + 1, d + 2, 16);
+    if (x == 0.0) {
+      f[n++] = '0';
+      f[n++] = '.';
+      std::memset(f + n, '0', 16);
+      n += 16;
+    } else if (ex >= 0) {
+      std::memcpy(f + n, dig, ex + 1);
+      n += ex + 1;
+      f[n++] = '.';
+      std::memcpy(f + n, dig + ex + 1, 16 - ex);
+      n += 16 - ex;
+    } else {  // ex == -1: 0.ddddddddddddddddd
+      f[n++] = '0';
+      f[n++] = '.';
+      std::memcpy(f + n, dig, 17);
+      n += 17;
+    }
+    std::memset(p, ' ', 20 - n);
+    std::memcpy(p + 20 - n, f, n);
+    std::memset(p + 20, ' ', 5);
+    return p + 25;
+  }
+  std::memcpy(f + n, d, 18);  // d.dddddddddddddddd
+  n += 18;
+  f[n++] = 'E';
+  f[n++] = ex < 0 ? '-' : '+';
+  const int a = ex < 0 ? -ex : ex;
+  f[n++] = (char)('0' + a / 100);
+  f[n++] = (char)('0' + a / 10 % 10);
+  f[n++] = (char)('0' + a % 10);
+  std::memset(p, ' ', 25 - n);
+  std::memcpy(p + 25 - n, f, n);
+  return p + 25;
+}
+
+std::string fortran_list_record(const double* v, int n) {
+  std::string rec((size_t)kItem * (n > 0 ? n : 0), ' ');
+  for (int k = 0; k < n; ++k) fortran_item(&rec[(size_t)k * kItem], v[k]);
   return rec;
+}
+
+int write_grid_records(const std::string& path, int nx, int ny, const double* xs, const double* ys,
+                       const std::vector<const double*>& fields) {
+  FILE* fp = std::fopen(path.c_str(), "w");
+  if (!fp) return set_error(TARA_ERR_ARGS, "cannot open " + path + " for writing");
+  const size_t items = 2 + fields.size(), rec = items * kItem + 1;
+  // blocks of whole x columns (ny records each), formatted in parallel into
+  // their final offsets, then written in order; about 64 MB of text per block
+  const int cols = std::max(1, (int)std::min<size_t>((size_t)nx, (64u << 20) / (rec * (size_t)ny)));
+  std::vector<char> buf(rec * (size_t)ny * cols);
+  const int hw = (int)std::thread::hardware_concurrency();
+  const int nthreads = std::max(1, std::min(hw > 0 ? hw : 1, 64));
+  int rc = TARA_OK;
+  for (int i0 = 0; i0 < nx && rc == TARA_OK; i0 += cols) {
+    const int ncol = std::min(cols, nx - i0);
+    auto work = [&](int t) {
+      for (int c = t; c < ncol; c += nthreads) {
+        const int i = i0 + c;
+        char* o = buf.data() + rec * (size_t)ny * c;
+        for (int j = 0; j < ny; ++j) {
+          const size_t q = (size_t)j * nx + i;
+          o = fortran_item(o, xs[i]);
+          o = fortran_item(o, ys[j]);
+          for (const double* fld : fields) o = fortran_item(o, fld[q]);
+          *o++ = '\n';
+        }
+      }
+    };
+    const int nt = std::min(nthreads, ncol);
+    std::vector<std::thread> pool;
+    for (int t = 1; t < nt; ++t) pool.emplace_back(work, t);
+    work(0);
+    for (std::thread& th : pool) th.join();
+    const size_t bytes = rec * (size_t)ny * ncol;
+    if (std::fwrite(buf.data(), 1, bytes, fp) != bytes) rc = set_error(TARA_ERR_ARGS, "short write to " + path);
+  }
+  if (std::fclose(fp) != 0 && rc == TARA_OK) rc = set_error(TARA_ERR_ARGS, "cannot close " + path);
+  return rc;
 }
 
 }  // namespace tara
@@ -316,6 +396,16 @@ int tara_ini_get(const char* path, const char* section, const char* key, char* b
     return set_error(TARA_ERR_INI, err);
   std::snprintf(buf, (size_t)buflen, "%s", val.c_str());
   return set_ok();
+}
+
+int tara_write_grid_records(const char* path, int nx, int ny, const double* xs, const double* ys,
+                            const double* fields, int nfields) {
+  if (!path || !xs || !ys || nx < 1 || ny < 1 || nfields < 0 || (nfields > 0 && !fields))
+    return set_error(TARA_ERR_ARGS, "tara_write_grid_records: bad argument");
+  std::vector<const double*> f;
+  for (int k = 0; k < nfields; ++k) f.push_back(fields + (size_t)k * nx * ny);
+  const int rc = write_grid_records(path, nx, ny, xs, ys, f);
+  return rc ? rc : set_ok();
 }
 
 int tara_fortran_list_record(const double* v, int n, char* buf, int buflen) {

@@ -39,4 +39,11 @@ bool fortran_read_int(const std::string& s, long long& v, std::string& err);
 // three-digit exponent), each item preceded by one separating blank.
 std::string fortran_list_record(const double* v, int n);
 
+// A snapshot file of the reference's drivers: one record per grid point, x
+// outer and y inner (do i = 1, Nx; do j = 1, Ny), holding xs[i], ys[j] and each
+// field's value at index j * nx + i, in fortran_list_record's format.  Records
+// are formatted in parallel on the host's cores and written in order.
+int write_grid_records(const std::string& path, int nx, int ny, const double* xs, const double* ys,
+                       const std::vector<const double*>& fields);
+
 }  // namespace tara

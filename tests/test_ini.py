@@ -206,3 +206,66 @@ def test_reference_input_ini():
     assert (dbl("time", "time_min"), dbl("time", "time_max"), dbl("time", "dt")) == (0.0, 2.0, 1e-4)
     assert (dbl("initialProfile", "W0"), dbl("initialProfile", "m0"), dbl("initialProfile", "d")) == (25.0, 2.0, 3.0)
     assert dbl("initialB", "B0") == 0.0
+
+
+def _g25_17(x: float) -> str:
+    """gfortran's list-directed REAL(8) item built from printf conversions:
+    F20.(16 - e) + 5 blanks for e in [-1, 16], else 1P E25.17 with a three-digit
+    exponent; e from %.16E.  Fortran's F editing always writes the decimal
+    point, also with no fraction digits (e = 16), where %.0f leaves it out."""
+    if x != x or x in (float("inf"), float("-inf")):
+        return " " + ("NaN" if x != x else ("Infinity" if x > 0 else "-Infinity")).rjust(25)
+    e10 = 0 if x == 0.0 else int(("%.16E" % x).split("E")[1])
+    if x == 0.0 or -1 <= e10 < 17:
+        dec = 16 if x == 0.0 else 16 - e10
+        return " " + ("%.*f" % (dec, x) + ("." if dec == 0 else "")).rjust(20) + "     "
+    m, ex = ("%.16E" % x).split("E")
+    ex = int(ex)
+    return " " + ("%sE%s%03d" % (m, "-" if ex < 0 else "+", abs(ex))).rjust(25)
+
+
+def test_list_directed_items_match_the_printf_rules():
+    """The library formats each item from one correctly rounded conversion;
+    over random values of every magnitude and the carry and limit cases it
+    gives the same characters as the printf-based rules (17 integer digits keep
+    their decimal point, as F editing writes it)."""
+    assert record(1.6450126423277086e16) == "   16450126423277086.     "
+    rng = np.random.default_rng(11)
+    vals = list(rng.standard_normal(20000) * 10.0 ** rng.integers(-320, 308, 20000))
+    vals += list(rng.standard_normal(20000) * 10.0 ** rng.integers(-3, 18, 20000))
+    edge = [0.0, -0.0, 0.1, -0.1, 0.09999999999999999, 0.099999999999999999, 1.0, 9.999999999999999,
+            99999999999999990.0, 1e16, 9.999999999999998e16, 1e17, -1e17, 5e-324, -5e-324,
+            2.2250738585072014e-308, 1.7976931348623157e308, -1.7976931348623157e308, 0.5, 123456.78901234567,
+            float("nan"), float("inf"), float("-inf")]
+    for k in range(-20, 20):
+        for m in (1.0, 9.999999999999999, 9.9999999999999996, 9.99999999999999999):
+            edge += [m * 10.0 ** k, -m * 10.0 ** k]
+    vals += edge
+    for chunk in range(0, len(vals), 150):  # 150 items fit record()'s 4096-byte buffer
+        part = vals[chunk:chunk + 150]
+        assert record(*part) == "".join(_g25_17(float(v)) for v in part)
+
+
+def test_grid_records_file_matches_the_records(tmp_path):
+    """tara_write_grid_records: x outer, y inner, fields at j * nx + i, each line
+    one record (checked whole on a small grid; on a grid of several 64 MB
+    blocks, by its size and a sample of records at their fixed offsets)."""
+    rng = np.random.default_rng(3)
+    for nx, ny, nf, full in ((7, 5, 3, True), (1024, 512, 4, False)):
+        xs, ys = rng.standard_normal(nx), rng.standard_normal(ny) * 1e-3
+        fields = rng.standard_normal((nf, ny, nx)) * 10.0 ** rng.integers(-5, 20, (nf, ny, nx))
+        path = tmp_path / f"g{nx}.dat"
+        dp = ctypes.POINTER(ctypes.c_double)
+        assert tg.lib().tara_write_grid_records(str(path).encode(), nx, ny, xs.ctypes.data_as(dp),
+                                                ys.ctypes.data_as(dp), fields.ctypes.data_as(dp), nf) == tg.TARA_OK
+        data = path.read_bytes()
+        rec = 26 * (2 + nf) + 1
+        assert len(data) == nx * ny * rec
+        pts = [(i, j) for i in range(nx) for j in range(ny)] if full else \
+            [(int(i), int(j)) for i, j in zip(rng.integers(0, nx, 300), rng.integers(0, ny, 300))] + [(0, 0), (nx - 1, ny - 1)]
+        for i, j in pts:
+            n = i * ny + j
+            line = data[n * rec:(n + 1) * rec].decode()
+            assert line == record(xs[i], ys[j], *fields[:, j, i]) + "\n"
+    assert tg.lib().tara_write_grid_records(str(tmp_path / "no" / "dir.dat").encode(), 2, 2,
+                                            xs.ctypes.data_as(dp), ys.ctypes.data_as(dp), None, 0) == tg.TARA_ERR_ARGS
