@@ -173,6 +173,7 @@ def _declare(L: ctypes.CDLL) -> None:
     L.tara3d_stream.restype = vp
     L.tara_measure_dfma_rate.argtypes = [c_int, dp]
     L.tara_twiddle_table.argtypes = [c_int, c_int, dp, c_int, ctypes.POINTER(c_int)]
+    L.tara_write_grid_records.argtypes = [ctypes.c_char_p, c_int, c_int, dp, dp, dp, c_int]
     L.tara_coh2d_default_config.argtypes = [vp, c_int, c_int]
     L.tara_coh2d_default_config.restype = None
     L.tara_coh2d_create.argtypes = [vp, vp]
@@ -373,6 +374,22 @@ def measure_dfma_rate(reps: int = 5) -> float:
     v = ctypes.c_double()
     _check(lib().tara_measure_dfma_rate(int(reps), ctypes.byref(v)))
     return v.value
+
+
+def write_grid_records(path, xs, ys, fields) -> None:
+    """A snapshot file in the reference drivers' fort.* format: one record per
+    grid point (x outer, y inner) of xs[i], ys[j] and fields[k][j, i]
+    (tara_write_grid_records; fields: (nfields, Ny, Nx) real arrays)."""
+    xs = np.ascontiguousarray(xs, np.float64)
+    ys = np.ascontiguousarray(ys, np.float64)
+    f = np.ascontiguousarray(fields, np.float64)
+    if f.ndim == 2:
+        f = f[None]
+    if f.shape[1:] != (ys.size, xs.size):
+        raise ValueError(f"fields of shape {f.shape} do not match Ny = {ys.size}, Nx = {xs.size}")
+    dptr = lambda a: a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))  # noqa: E731
+    _check(lib().tara_write_grid_records(str(path).encode(), xs.size, ys.size, dptr(xs), dptr(ys), dptr(f),
+                                         f.shape[0]))
 
 
 def twiddle_table(n: int, precision: int = PREC_FP64) -> np.ndarray:

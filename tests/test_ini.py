@@ -269,3 +269,17 @@ def test_grid_records_file_matches_the_records(tmp_path):
             assert line == record(xs[i], ys[j], *fields[:, j, i]) + "\n"
     assert tg.lib().tara_write_grid_records(str(tmp_path / "no" / "dir.dat").encode(), 2, 2,
                                             xs.ctypes.data_as(dp), ys.ctypes.data_as(dp), None, 0) == tg.TARA_ERR_ARGS
+
+
+def test_write_grid_records_python_wrapper(tmp_path):
+    rng = np.random.default_rng(5)
+    xs, ys = np.arange(4) * 0.5, np.arange(3) * 0.25
+    f = rng.standard_normal((2, 3, 4))
+    tg.write_grid_records(tmp_path / "s.dat", xs, ys, f)
+    lines = (tmp_path / "s.dat").read_text().splitlines()
+    assert len(lines) == 12
+    assert lines[1] + "\n" == record(xs[0], ys[1], f[0, 1, 0], f[1, 1, 0]) + "\n"
+    vals = np.array([[float(v) for v in ln.split()] for ln in lines])
+    assert np.array_equal(vals[:, 2].reshape(4, 3), f[0].T)
+    with pytest.raises(ValueError):
+        tg.write_grid_records(tmp_path / "t.dat", xs, ys, f[:, :, :3])
