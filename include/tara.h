@@ -484,7 +484,9 @@ int tara_ini_get(const char* path, const char* section, const char* key, char* b
  * "0.010d0" -> 0.01 and "3.0d0/128.0d0" -> 3.0 (the slash ends the read). */
 int tara_fortran_read_double(const char* s, double* out);
 int tara_fortran_read_int(const char* s, long long* out);
-/* One list-directed output record of n REAL(8) values, gfortran style. */
+/* One list-directed output record of n REAL(8) values, gfortran style: 26
+ * characters per value and a terminating NUL; a smaller buflen is refused
+ * (TARA_ERR_ARGS, buf set to the empty string). */
 int tara_fortran_list_record(const double* v, int n, char* buf, int buflen);
 /* A snapshot file in the reference drivers' fort.* format: one record per grid
  * point, x outer and y inner, holding xs[i], ys[j] and fields[k*nx*ny + j*nx + i]

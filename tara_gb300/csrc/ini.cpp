@@ -14,11 +14,9 @@
 #include <thread>
 
 #include "../../include/tara.h"
+#include "status.h"
 
 namespace tara {
-
-int set_error(int code, const std::string& msg);
-int set_ok();
 
 namespace {
 
@@ -410,7 +408,13 @@ int tara_write_grid_records(const char* path, int nx, int ny, const double* xs, 
 
 int tara_fortran_list_record(const double* v, int n, char* buf, int buflen) {
   if (!v || n < 0 || !buf || buflen <= 0) return set_error(TARA_ERR_ARGS, "null argument");
-  std::snprintf(buf, (size_t)buflen, "%s", fortran_list_record(v, n).c_str());
+  const std::string rec = fortran_list_record(v, n);
+  if (rec.size() + 1 > (size_t)buflen) {
+    buf[0] = '\0';
+    return set_error(TARA_ERR_ARGS, "tara_fortran_list_record: the record needs " + std::to_string(rec.size() + 1) +
+                                        " bytes, buflen is " + std::to_string(buflen));
+  }
+  std::memcpy(buf, rec.c_str(), rec.size() + 1);
   return set_ok();
 }
 

@@ -283,3 +283,13 @@ def test_write_grid_records_python_wrapper(tmp_path):
     assert np.array_equal(vals[:, 2].reshape(4, 3), f[0].T)
     with pytest.raises(ValueError):
         tg.write_grid_records(tmp_path / "t.dat", xs, ys, f[:, :, :3])
+
+
+def test_list_record_refuses_a_short_buffer():
+    v = (ctypes.c_double * 3)(1.0, 2.0, 3.0)
+    buf = ctypes.create_string_buffer(3 * 26)  # one byte short of the NUL
+    assert tg.lib().tara_fortran_list_record(v, 3, buf, 3 * 26) == tg.TARA_ERR_ARGS
+    assert buf.value == b"" and "needs 79 bytes" in tg.last_error()[1]
+    buf = ctypes.create_string_buffer(3 * 26 + 1)
+    assert tg.lib().tara_fortran_list_record(v, 3, buf, 3 * 26 + 1) == tg.TARA_OK
+    assert len(buf.value) == 78
