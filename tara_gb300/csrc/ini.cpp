@@ -11,6 +11,8 @@
 #include <cstring>
 #include <fstream>
 #include <sstream>
+#include <new>
+#include <stdexcept>
 #include <thread>
 
 #include "../../include/tara.h"
@@ -329,13 +331,18 @@ std::string fortran_list_record(const double* v, int n) {
 
 int write_grid_records(const std::string& path, int nx, int ny, const double* xs, const double* ys,
                        const std::vector<const double*>& fields) {
-  FILE* fp = std::fopen(path.c_str(), "w");
-  if (!fp) return set_error(TARA_ERR_ARGS, "cannot open " + path + " for writing");
   const size_t items = 2 + fields.size(), rec = items * kItem + 1;
   // blocks of whole x columns (ny records each), formatted in parallel into
   // their final offsets, then written in order; about 64 MB of text per block
   const int cols = std::max(1, (int)std::min<size_t>((size_t)nx, (64u << 20) / (rec * (size_t)ny)));
-  std::vector<char> buf(rec * (size_t)ny * cols);
+  std::vector<char> buf;
+  try {
+    buf.resize(rec * (size_t)ny * cols);
+  } catch (const std::bad_alloc&) {
+    return set_error(TARA_ERR_NOMEM, "write_grid_records: no host memory for the text buffer");
+  }
+  FILE* fp = std::fopen(path.c_str(), "w");
+  if (!fp) return set_error(TARA_ERR_ARGS, "cannot open " + path + " for writing");
   const int hw = (int)std::thread::hardware_concurrency();
   const int nthreads = std::max(1, std::min(hw > 0 ? hw : 1, 64));
   int rc = TARA_OK;
@@ -356,7 +363,12 @@ int write_grid_records(const std::string& path, int nx, int ny, const double* xs
     };
     const int nt = std::min(nthreads, ncol);
     std::vector<std::thread> pool;
-    for (int t = 1; t < nt; ++t) pool.emplace_back(work, t);
+    int started = 1;
+    try {
+      for (; started < nt; ++started) pool.emplace_back(work, started);
+    } catch (const std::exception&) {  // no more threads: this one takes the rest
+    }
+    for (int t = started; t < nt; ++t) work(t);
     work(0);
     for (std::thread& th : pool) th.join();
     const size_t bytes = rec * (size_t)ny * ncol;
