@@ -3,6 +3,8 @@
 // src/main2coh.f95, src/main2com.f95, src/main3com.f95), with their output files.  Host code over the C ABI; every
 // transform and update runs in libtara's kernels.
 #include <cmath>
+#include <exception>
+#include <new>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -486,7 +488,24 @@ void say(const char* line) {
 
 }  // namespace
 
+namespace {
+int run_ini(const char* ini_path, const char* out_dir, int max_steps);
+}
+
+// No C++ exception leaves the C ABI: a host allocation that fails (the field
+// buffers of a large grid) is reported as TARA_ERR_NOMEM.
 extern "C" int tara_run_ini(const char* ini_path, const char* out_dir, int max_steps) {
+  try {
+    return run_ini(ini_path, out_dir, max_steps);
+  } catch (const std::bad_alloc&) {
+    return set_error(TARA_ERR_NOMEM, "tara_run_ini: host allocation failed");
+  } catch (const std::exception& e) {
+    return set_error(TARA_ERR_ARGS, std::string("tara_run_ini: ") + e.what());
+  }
+}
+
+namespace {
+int run_ini(const char* ini_path, const char* out_dir, int max_steps) {
   Reader R;
   if (!ini_path) return set_error(TARA_ERR_ARGS, "null ini path");
   if (!ini_parse_file(ini_path, R.ini, R.err)) return set_error(TARA_ERR_INI, R.err);
@@ -528,3 +547,4 @@ extern "C" int tara_run_ini(const char* ini_path, const char* out_dir, int max_s
   say(" Incompatible Input file. Please check TARA user-manual.\n");
   return set_error(TARA_ERR_INI, "incompatible input file");
 }
+}  // namespace
