@@ -67,7 +67,12 @@ struct Out {
   ~Out() {
     if (f) std::fclose(f);
   }
+  // the refusal to return when the file could not be opened
+  int open_error(const std::string& path) const {
+    return f ? TARA_OK : set_error(TARA_ERR_ARGS, "cannot open " + path + " for writing");
+  }
   void rec(std::initializer_list<double> v) {
+    if (!f) return;
     std::vector<double> a(v);
     const std::string r = fortran_list_record(a.data(), (int)a.size());
     std::fprintf(f, "%s\n", r.c_str());
@@ -224,6 +229,7 @@ int run_2d(Reader& R, const std::string& out, int max_steps, bool screened) {
     if (tara_particles_create(h, kPi, lx, ly, np, xp.data(), yp.data(), &parts)) return fail_rc();
   }
   Out energy(out + "/Energy.dat");  // written every step by the screened driver only
+  if (int rc = energy.open_error(out + "/Energy.dat")) return rc;
   const tara2d_diag_params dp = {kPi, lx, ly, screened ? lambda : 0.0, screened ? 1 : 0};
   const long n = trip_count(tmin, tmax, dt);
   const long steps = (max_steps > 0 && max_steps < n) ? max_steps : n;
@@ -255,6 +261,7 @@ int run_2d(Reader& R, const std::string& out, int max_steps, bool screened) {
         if (t % every == 0) {  // fort.(t+105): one "xp yp" record per particle
           if (tara_particles_get(parts, xp.data(), yp.data())) return fail_rc();
           Out pf(fort_name(out, t + 105));
+          if (int rc = pf.open_error(fort_name(out, t + 105))) return rc;
           for (int i = 0; i < np; ++i) pf.rec({xp[i], yp[i]});
         }
       }
@@ -329,6 +336,7 @@ int run_3d(Reader& R, const std::string& out, int max_steps) {
   if (tara3d_set_state_real(h, real.data())) return fail_rc();
   mkdir(out.c_str(), 0755);
   Out energy(out + "/Energy.dat");
+  if (int rc = energy.open_error(out + "/Energy.dat")) return rc;
   const long n = trip_count(tmin, tmax, dt);
   const long steps = (max_steps > 0 && max_steps < n) ? max_steps : n;
   double time = tmin;
@@ -387,6 +395,7 @@ int run_coh(Reader& R, const std::string& out, int max_steps) {
   int rc;
   if ((rc = snapshot(out + "/Initial_Grid_Data_Reproduced.dat"))) return rc;  // (:214-238)
   Out energy(out + "/Energy.dat");
+  if (int rc = energy.open_error(out + "/Energy.dat")) return rc;
   const long n = trip_count(tmin, tmax, dt);
   const long steps = (max_steps > 0 && max_steps < n) ? max_steps : n;
   const double every = 1.0 / (10.0 * dt);  // mod(float(t),1.0d0/(10.0d0*dt)) == 0.0 (:407)
@@ -451,6 +460,7 @@ int run_com(Reader& R, const std::string& out, int max_steps) {
   for (int i = 0; i < nx; ++i) xs[i] = 0.0 + (double)(float)i * dx;
   for (int j = 0; j < ny; ++j) ys[j] = 0.0 + (double)(float)j * dy;
   Out energy(out + "/Energy.dat");
+  if (int rc = energy.open_error(out + "/Energy.dat")) return rc;
   const long n = trip_count(tmin, tmax, dt);
   const long steps = (max_steps > 0 && max_steps < n) ? max_steps : n;
   double time = tmin;
